@@ -1,0 +1,235 @@
+// Test-infrastructure only: a small driver around the UNMODIFIED qTorch
+// headers (compiled from the reference source tree by oracle/Makefile, never
+// copied into this repository).  It is used to generate golden vectors that
+// pin the CPU oracle port and the CUDA path.  Nothing in the product links or
+// runs it.
+//
+// Sub-commands (all results go to stdout; the reference's own chatter on
+// std::cout is discarded):
+//   stoch  <qasm> <measure> <threads>       stochastic contraction (ContractionTools.h:219-388)
+//                                           -> value, flop counter, recorded mCreatedFrom sequence
+//   seq    <qasm> <measure> <seqfile>       ContractGivenSequence replay (ContractionTools.h:392-411)
+//   lg     <qasm> <measure> <qbbfile>       LineGraph::LGContract replay of a qbb.out ordering (LineGraph.h:357-376)
+//   lgwires <qasm> <measure>                wire ids assigned by the LineGraph constructor (LineGraph.h:92-171)
+//   gates                                   every gate tensor of Node.h for a fixed set of parameters
+//   pair   <in.bin> <out.bin>               one ContractIndices call (Network.h:876-971) on raw tensors
+//   qaoa   <dgf> <p> <b_1..b_p g_1..g_p>    per-edge light-cone QASM text exactly as maxcut.cpp:166-190 writes it
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include <vector>
+#include <string>
+
+#include "maxcut.h"   // pulls in ContractionTools.h, Network.h, Node.h, LineGraph.h, preprocess.h
+
+using namespace qtorch;
+
+static std::ofstream g_null;
+
+static void print_value(const std::complex<double> &v) {
+    std::printf("value %.17g %.17g\n", v.real(), v.imag());
+}
+
+static void print_sequence(const std::shared_ptr<Network> &net) {
+    // the same walk preprocess.h:41-46 makes over mAllNodes
+    std::printf("sequence");
+    for (const auto &n : net->GetAllNodes()) {
+        if (!(n->mCreatedFrom.first == 0 && n->mCreatedFrom.second == 0)) {
+            std::printf(" %d %d", n->mCreatedFrom.first, n->mCreatedFrom.second);
+        }
+    }
+    std::printf("\n");
+}
+
+// Exposes the protected ContractIndices of the reference Network.
+class PairHarness : public Network {
+public:
+    void run(std::shared_ptr<Node> a, std::shared_ptr<Node> b, std::shared_ptr<Node> c,
+             const std::vector<std::pair<bool, int>> &freeIdx, const std::vector<std::pair<int, int>> &sumIdx) {
+        std::vector<int> ia(a->mRank), ib(b->mRank);
+        ContractIndices(freeIdx, sumIdx, ia, ib, a, b, c);
+    }
+};
+
+static int cmd_pair(const char *inPath, const char *outPath) {
+    // binary layout (int32 little endian then float64):
+    // rankA rankB nFree [fromA idx]*nFree nSum [ia ib]*nSum  A(2*4^rA doubles) B(2*4^rB doubles)
+    FILE *f = std::fopen(inPath, "rb");
+    if (!f) return 2;
+    int32_t rA, rB, nF, nS;
+    if (std::fread(&rA, 4, 1, f) != 1 || std::fread(&rB, 4, 1, f) != 1 || std::fread(&nF, 4, 1, f) != 1) return 3;
+    std::vector<std::pair<bool, int>> freeIdx;
+    for (int i = 0; i < nF; i++) {
+        int32_t fa, idx;
+        if (std::fread(&fa, 4, 1, f) != 1 || std::fread(&idx, 4, 1, f) != 1) return 3;
+        freeIdx.push_back({fa != 0, idx});
+    }
+    if (std::fread(&nS, 4, 1, f) != 1) return 3;
+    std::vector<std::pair<int, int>> sumIdx;
+    for (int i = 0; i < nS; i++) {
+        int32_t ia, ib;
+        if (std::fread(&ia, 4, 1, f) != 1 || std::fread(&ib, 4, 1, f) != 1) return 3;
+        sumIdx.push_back({ia, ib});
+    }
+    auto a = std::make_shared<Node>(rA);
+    auto b = std::make_shared<Node>(rB);
+    auto c = std::make_shared<Node>(nF);
+    if (std::fread(a->GetTensorVals().data(), 16, a->GetTensorVals().size(), f) != a->GetTensorVals().size()) return 3;
+    if (std::fread(b->GetTensorVals().data(), 16, b->GetTensorVals().size(), f) != b->GetTensorVals().size()) return 3;
+    std::fclose(f);
+    PairHarness h;
+    h.SetNumThreads(1);
+    h.run(a, b, c, freeIdx, sumIdx);
+    FILE *o = std::fopen(outPath, "wb");
+    if (!o) return 2;
+    std::fwrite(c->GetTensorVals().data(), 16, c->GetTensorVals().size(), o);
+    std::fclose(o);
+    return 0;
+}
+
+static void dump_node(const char *name, Node &n) {
+    std::printf("gate %s %d", name, n.mRank);
+    for (const auto &v : n.GetTensorVals()) std::printf(" %.17g %.17g", v.real(), v.imag());
+    std::printf("\n");
+}
+
+static int cmd_gates(const char *gateDir) {
+    const double angles[] = {0.1, -0.1, 0.785399, 2.5, -3.0, 1e-3};
+    for (double th : angles) {
+        char nm[64];
+        float thf = (float) th;  // the parser narrows angles through std::stof (Network.h:342)
+        std::snprintf(nm, sizeof nm, "Rx:%.17g", (double) thf); { RxNode n(thf); dump_node(nm, n); }
+        std::snprintf(nm, sizeof nm, "Ry:%.17g", (double) thf); { RyNode n(thf); dump_node(nm, n); }
+        std::snprintf(nm, sizeof nm, "Rz:%.17g", (double) thf); { RzNode n(thf); dump_node(nm, n); }
+        std::snprintf(nm, sizeof nm, "PHASE:%.17g", (double) thf); { PhaseNode n(thf); dump_node(nm, n); }
+        std::snprintf(nm, sizeof nm, "CPHASE:%.17g", th); { CPhaseNode n(th); dump_node(nm, n); }
+    }
+    for (int k = 0; k < 6; k++) {
+        char nm[32];
+        std::snprintf(nm, sizeof nm, "CRk:%d", k);
+        CRkNode n(k);
+        dump_node(nm, n);
+    }
+    { HNode n; dump_node("H", n); }
+    { XNode n; dump_node("X", n); }
+    { YNode n; dump_node("Y", n); }
+    { ZNode n; dump_node("Z", n); }
+    { CNOTNode n; dump_node("CNOT", n); }
+    { CZNode n; dump_node("CZ", n); }
+    { SwapNode n; dump_node("SWAP", n); }
+    { ZeroStateNode n; dump_node("INIT", n); }
+    { TraceNode n; dump_node("T", n); }
+    { XMeasure n; dump_node("MX", n); }
+    { YMeasure n; dump_node("MY", n); }
+    { ZMeasure n; dump_node("MZ", n); }
+    { ProjectZero n; dump_node("M0", n); }
+    { ProjectOne n; dump_node("M1", n); }
+    if (gateDir) {
+        std::string d(gateDir);
+        { ArbitraryOneQubitNode n(d + "/../s.gate", "s"); dump_node("ARB1:s.gate", n); }
+        { ArbitraryOneQubitNode n(d + "/../t.gate", "t"); dump_node("ARB1:t.gate", n); }
+        { ArbitraryOneQubitNode n(d + "/../tdagger.gate", "td"); dump_node("ARB1:tdagger.gate", n); }
+        { ArbitraryOneQubitNode n(d + "/../zee.gate", "z"); dump_node("ARB1:zee.gate", n); }
+        for (int i = 0; i < 3; i++) {
+            char nm[64];
+            std::snprintf(nm, sizeof nm, "ARB2:matrix%d.gate", i);
+            ArbitraryTwoQubitNode n(d + "/matrix" + std::to_string(i) + ".gate", "m");
+            dump_node(nm, n);
+        }
+    }
+    return 0;
+}
+
+static int cmd_qaoa(int argc, char **argv) {
+    // argv: dgf p betas.. gammas..
+    int p = std::atoi(argv[1]);
+    std::vector<double> bg;
+    for (int i = 0; i < 2 * p; i++) bg.push_back(std::atof(argv[2 + i]));
+    ExtraData e(p, argv[0]);
+    for (size_t counter = 0; counter < e.pairs.size(); counter++) {
+        // the body of F_p (maxcut.cpp:166-190), writing to a string instead of input/tempMaxCut.qasm
+        std::string path = "/tmp/qt_ref_harness_term.qasm";
+        std::ofstream q(path);
+        int numQubits = e.qubitsNeeded[counter];
+        q << numQubits << std::endl;
+        outputInitialPlusStateToFile(q, numQubits);
+        applyU_CsThenU_Bs(e.realIterations[counter], e.p, bg, numQubits, q);
+        q.close();
+        std::ifstream r(path);
+        std::stringstream ss;
+        ss << r.rdbuf();
+        std::string text = ss.str();
+        std::printf("term %zu %d %d %d\n", counter, e.pairs[counter].first, e.pairs[counter].second, numQubits);
+        std::printf("%s", text.c_str());
+        std::printf("endterm\n");
+        std::remove(path.c_str());
+    }
+    return 0;
+}
+
+int main(int argc, char **argv) {
+    if (argc < 2) {
+        std::fprintf(stderr, "usage: %s stoch|seq|lg|lgwires|gates|pair|qaoa ...\n", argv[0]);
+        return 1;
+    }
+    g_null.open("/dev/null");
+    std::streambuf *orig = std::cout.rdbuf(g_null.rdbuf());
+    std::string cmd(argv[1]);
+    int rc = 0;
+    try {
+        if (cmd == "stoch" && argc >= 5) {
+            ContractionTools t(argv[2], argv[3], std::atoi(argv[4]));
+            auto net = t.Contract(Stochastic);
+            print_value(t.GetFinalVal());
+            std::printf("flops %lld\n", net->getNumFloatOps());
+            print_sequence(net);
+        } else if (cmd == "seq" && argc >= 5) {
+            std::vector<std::pair<int, int>> seq;
+            std::ifstream s(argv[4]);
+            int a, b;
+            while (s >> a >> b) seq.push_back({a, b});
+            ContractionTools t(argv[2], argv[3], 1);
+            auto net = t.ContractGivenSequence(seq);
+            print_value(t.GetFinalVal());
+            std::printf("flops %lld\n", net->getNumFloatOps());
+        } else if (cmd == "lg" && argc >= 5) {
+            auto net = std::make_shared<Network>(argv[2], argv[3]);
+            net->SetNumThreads(1);
+            LineGraph lg(net);
+            lg.SetQBBOutFiles("/dev/null", argv[4], "/dev/null");
+            lg.LGContract();
+            print_value(net->GetFinalValue());
+            auto rem = net->GetUncontractedNodes();
+            print_value(rem[0]->GetTensorVals()[0]);
+            std::printf("flops %lld\n", net->getNumFloatOps());
+            print_sequence(net);
+        } else if (cmd == "lgwires" && argc >= 4) {
+            auto net = std::make_shared<Network>(argv[2], argv[3]);
+            LineGraph lg(net);
+            for (const auto &n : net->GetUncontractedNodes()) {
+                std::printf("node %d", n->mID);
+                for (const auto &w : n->GetWires()) {
+                    std::printf(" %d:%d:%d", w->GetWireID(), w->GetNodeA().lock()->mID, w->GetNodeB().lock()->mID);
+                }
+                std::printf("\n");
+            }
+        } else if (cmd == "gates") {
+            rc = cmd_gates(argc >= 3 ? argv[2] : nullptr);
+        } else if (cmd == "pair" && argc >= 4) {
+            rc = cmd_pair(argv[2], argv[3]);
+        } else if (cmd == "qaoa" && argc >= 4) {
+            rc = cmd_qaoa(argc - 2, argv + 2);
+        } else {
+            std::fprintf(stderr, "bad command\n");
+            rc = 1;
+        }
+    } catch (std::exception &e) {
+        std::printf("exception %s\n", e.what());
+        rc = 4;
+    }
+    std::cout.rdbuf(orig);
+    return rc;
+}
