@@ -1,0 +1,244 @@
+/*
+ * qtorch_gb300 — C ABI of the GB300 (sm_103a) contraction engine for
+ * qTorch-style density-matrix tensor networks.
+ *
+ * Tensors follow qTorch's layout: every wire has dimension 4 (s = 2r + c of a
+ * one-qubit density matrix), a rank-r tensor holds 4^r complex values and the
+ * flat index is sum_i idx_i * 4^i (src/Node.h:112-113, 168-186).
+ *
+ * All entry points return a qt_status; none throws.  Errors map one to one onto
+ * the reference's exception types (src/Exceptions.h:24-59).  A context owns one
+ * CUDA stream and a caching device allocator; calls on one context are
+ * serialised by an internal lock and may come from any thread.
+ */
+#ifndef QTORCH_GB300_H
+#define QTORCH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum qt_status {
+    QT_OK = 0,
+    QT_ERR_INVALID_ARGUMENT = 1,        /* a bad pointer, size or index map */
+    QT_ERR_INVALID_FILE = 2,            /* InvalidFile (Exceptions.h:24) */
+    QT_ERR_INVALID_FILE_FORMAT = 3,     /* InvalidFileFormat (Exceptions.h:28) */
+    QT_ERR_CONTRACTION_FAILURE = 4,     /* ContractionFailure (Exceptions.h:36) */
+    QT_ERR_INVALID_USER_SEQUENCE = 5,   /* InvalidUserContractionSequence (Exceptions.h:40) */
+    QT_ERR_INVALID_FUNCTION_INPUT = 6,  /* InvalidFunctionInput (Exceptions.h:44) */
+    QT_ERR_INVALID_CONTRACTION_METHOD = 7, /* InvalidContractionMethod (Exceptions.h:52) */
+    QT_ERR_REFUSED = 8,                 /* ContractNodes returned nullptr (Network.h:719-723, 772-777) */
+    QT_ERR_OUT_OF_MEMORY = 9,           /* device allocation or memory budget exceeded */
+    QT_ERR_CUDA = 10,                   /* a CUDA runtime error; see qt_last_error */
+    QT_ERR_DEADLINE = 11,               /* the context deadline expired (the reference's maxTime, Network.h:51) */
+    QT_ERR_NO_DEVICE = 12,              /* no usable sm_103 device */
+    QT_ERR_BUSY = 13                    /* admission refused: not enough free budget right now */
+} qt_status;
+
+typedef enum qt_dtype {
+    QT_C128 = 0,   /* complex128: interleaved double (re, im) */
+    QT_C64 = 1     /* complex64:  interleaved float (re, im) */
+} qt_dtype;
+
+typedef enum qt_precision {
+    QT_PREC_FP64 = 0,   /* complex128 throughout, each product rounded as the reference's loop */
+    QT_PREC_MIXED = 1   /* complex64 storage, FP32 accumulation, power-of-two scaling, FP64 tail */
+} qt_precision;
+
+typedef struct qt_ctx qt_ctx;
+typedef struct qt_tensor qt_tensor;
+typedef struct qt_network qt_network;
+typedef struct qt_plan qt_plan;
+typedef struct qt_batch qt_batch;
+typedef struct qt_server qt_server;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* stream: a cudaStream_t to launch on, or NULL for a context-owned stream. */
+qt_status qt_ctx_create(int device, void *stream, qt_ctx **out);
+qt_status qt_ctx_destroy(qt_ctx *ctx);
+qt_status qt_ctx_synchronize(qt_ctx *ctx);
+const char *qt_status_string(qt_status s);
+/* last error text of this context (thread-safe copy into buf). */
+size_t qt_last_error(qt_ctx *ctx, char *buf, size_t cap);
+/* Device memory budget for plans and requests (bytes, 0 = no limit). */
+qt_status qt_ctx_set_memory_budget(qt_ctx *ctx, uint64_t bytes);
+/* Cooperative deadline in seconds from now (<= 0 clears it).  Mirrors the
+ * reference's totTimer/maxTime polling (Network.h:50-51, 899-910): long
+ * contractions stop at the deadline and report QT_ERR_DEADLINE. */
+qt_status qt_ctx_set_deadline(qt_ctx *ctx, double seconds_from_now);
+/* Number of kernels this library launched on the context (for accounting). */
+uint64_t qt_ctx_kernel_launches(const qt_ctx *ctx);
+
+/* ---- tensors ---------------------------------------------------------- */
+
+qt_status qt_tensor_create(qt_ctx *ctx, int rank, qt_dtype dtype, qt_tensor **out);  /* zero-filled */
+qt_status qt_tensor_free(qt_ctx *ctx, qt_tensor *t);
+qt_status qt_tensor_upload(qt_ctx *ctx, qt_tensor *t, const void *host, size_t bytes);
+qt_status qt_tensor_download(qt_ctx *ctx, const qt_tensor *t, void *host, size_t bytes);
+int qt_tensor_rank(const qt_tensor *t);
+qt_dtype qt_tensor_dtype(const qt_tensor *t);
+void *qt_tensor_device_ptr(const qt_tensor *t);
+
+/* ---- the pairwise contraction (the drop-in for ContractIndices) --------
+ *
+ * Replaces Network::ContractIndices (src/Network.h:112-118, 876-971), called
+ * from Network::ContractNodes (src/Network.h:837):
+ *   C[c] = sum_k A[a(c,k)] * B[b(c,k)]
+ * free_from_a[i], free_idx[i]  = toNotSumOn[i]: digit i of C is wire free_idx[i]
+ *                                of A (free_from_a[i] != 0) or of B;
+ * sum_a[j], sum_b[j]           = toSumOn[j]: wire sum_a[j] of A is summed
+ *                                against wire sum_b[j] of B.
+ * Summation runs over k in the reference's order (digit i of k <-> pair
+ * n_sum-1-i), one output element per accumulator, so the QT_C128 result equals
+ * the reference's bit for bit.  *c_out receives a new tensor of rank n_free.
+ */
+qt_status qt_contract_pair(qt_ctx *ctx, const qt_tensor *a, const qt_tensor *b,
+                           int n_free, const uint8_t *free_from_a, const int32_t *free_idx,
+                           int n_sum, const int32_t *sum_a, const int32_t *sum_b,
+                           qt_tensor **c_out);
+
+/* The same on caller-owned device buffers (complex128, flat base-4 layout).
+ * c must hold 4^n_free elements; it is overwritten.  Asynchronous on the
+ * context stream. */
+qt_status qt_contract_pair_device(qt_ctx *ctx, const void *a, int rank_a, const void *b, int rank_b,
+                                  int n_free, const uint8_t *free_from_a, const int32_t *free_idx,
+                                  int n_sum, const int32_t *sum_a, const int32_t *sum_b, void *c);
+
+/* The same on host buffers: copies A and B in, contracts, copies C out (synchronous). */
+qt_status qt_contract_pair_host(qt_ctx *ctx, const double *a, int rank_a, const double *b, int rank_b,
+                                int n_free, const uint8_t *free_from_a, const int32_t *free_idx,
+                                int n_sum, const int32_t *sum_a, const int32_t *sum_b, double *c);
+
+/* ---- networks (Network / ContractionTools / LineGraph) ------------------ */
+
+typedef enum qt_ordering {
+    QT_ORDER_STOCHASTIC = 0,   /* ContractionTools::ParallelContract (ContractionTools.h:219-388), seeded */
+    QT_ORDER_LINEGRAPH = 1,    /* LineGraph + min-fill elimination order (LineGraph.h:92-171, 357-376) */
+    QT_ORDER_SEQUENCE = 2      /* ContractGivenSequence (ContractionTools.h:392-411) */
+} qt_ordering;
+
+/* Network(qasm, measure) from text (Network.h:148-151, 246-304).  gate_dir
+ * resolves relative def1/def2 paths (NULL = current directory).  With ctx ==
+ * NULL the network is symbolic: it tracks ranks and wires only (for planning). */
+qt_status qt_network_create(qt_ctx *ctx, const char *qasm_text, const char *measure_text,
+                            const char *gate_dir, qt_network **out);
+qt_status qt_network_create_from_files(qt_ctx *ctx, const char *qasm_path, const char *measure_path,
+                                       qt_network **out);
+qt_status qt_network_free(qt_network *net);
+qt_status qt_network_reset(qt_network *net);                       /* Network::Reset (Network.h:154-171) */
+int qt_network_num_qubits(const qt_network *net);
+int qt_network_num_nodes(const qt_network *net);                   /* size of GetAllNodes() */
+int qt_network_num_uncontracted(const qt_network *net);
+int qt_network_node_rank(const qt_network *net, int node_id);
+int qt_network_is_done(const qt_network *net);
+/* ContractNodes(allNodes[a], allNodes[b], threshold) (Network.h:715-864).
+ * *new_id = id of the new node, or -1 when the call returned nullptr. */
+qt_status qt_network_contract_nodes(qt_network *net, int node_a, int node_b, int threshold, int *new_id);
+/* ContractGivenSequence: pairs[2*i], pairs[2*i+1] index GetAllNodes(). */
+qt_status qt_network_contract_sequence(qt_network *net, const int32_t *pairs, int n_pairs);
+/* ContractUserDefinedSequenceOfWires (ContractionTools.h:155-214) from text "a b\n..." */
+qt_status qt_network_contract_user_sequence(qt_network *net, const char *sequence_text);
+/* Stochastic ordering with a fixed seed (the reference seeds from random_device). */
+qt_status qt_network_contract_stochastic(qt_network *net, uint64_t seed);
+/* Line-graph ordering: min-fill elimination over the line graph, then the LGContract walk. */
+qt_status qt_network_contract_linegraph(qt_network *net);
+/* LGContract over a caller-given 1-based wire order (the content of a qbb.out). */
+qt_status qt_network_contract_wire_order(qt_network *net, const int32_t *order_1based, int n);
+/* ReduceCircuit (Network.h:1015-1118). */
+qt_status qt_network_reduce(qt_network *net);
+qt_status qt_network_final_value(const qt_network *net, double *re_im);
+int64_t qt_network_flops(const qt_network *net);                   /* getNumFloatOps (Network.h:91) */
+/* The recorded mCreatedFrom pairs (the walk of preprocess.h:41-46); returns the count. */
+int qt_network_created_from(const qt_network *net, int32_t *pairs, int cap_pairs);
+/* Values of node `node_id` (complex128) if it still holds data; returns count or -1. */
+int64_t qt_network_node_values(qt_network *net, int node_id, double *out, int64_t cap_complex);
+/* Line-graph wire order chosen by the min-fill heuristic (1-based, qbb.out order). */
+int qt_network_linegraph_order(qt_network *net, int32_t *order_1based, int cap);
+
+/* ---- plans: an ordering lowered once, executed many times ---------------
+ *
+ * A plan is built by running the ordering over a symbolic copy of the network
+ * (same bookkeeping as ContractNodes, no data) and recording every step.  The
+ * leaves (gate / state / measurement tensors) are bound separately, so one
+ * plan serves every parameter point of the same circuit structure.
+ */
+qt_status qt_plan_build(qt_ctx *ctx, const char *qasm_text, const char *measure_text, const char *gate_dir,
+                        qt_ordering ordering, uint64_t seed, const int32_t *sequence_pairs, int n_pairs,
+                        qt_plan **out);
+qt_status qt_plan_free(qt_plan *plan);
+int qt_plan_num_steps(const qt_plan *plan);
+int qt_plan_num_leaves(const qt_plan *plan);
+int qt_plan_peak_rank(const qt_plan *plan);
+uint64_t qt_plan_workspace_bytes(const qt_plan *plan, qt_precision prec);
+int64_t qt_plan_flops(const qt_plan *plan);                         /* sum of 4^(free+summed) */
+/* recorded node-id pairs (replayable through QT_ORDER_SEQUENCE / the oracle) */
+int qt_plan_sequence(const qt_plan *plan, int32_t *pairs, int cap_pairs);
+/* Leaf tensors of the plan's own circuit, complex128, concatenated in leaf order. */
+uint64_t qt_plan_leaf_elems(const qt_plan *plan);
+qt_status qt_plan_leaf_values(const qt_plan *plan, double *out, uint64_t cap_complex);
+/* One network value (synchronous, host in / host out). */
+qt_status qt_plan_execute(qt_ctx *ctx, qt_plan *plan, qt_precision prec, double *re_im);
+
+/* ---- batches: many plan instances in one persistent grouped launch ------ */
+
+/* A batch holds instances (plan, leaf values).  Leaves are complex128 on the
+ * host; the batch converts them to the execution precision on upload. */
+qt_status qt_batch_create(qt_ctx *ctx, qt_batch **out);
+qt_status qt_batch_free(qt_batch *b);
+/* leaves = NULL uses the plan's own leaf values. Returns the instance index. */
+qt_status qt_batch_add(qt_batch *b, qt_plan *plan, const double *leaves, int *index);
+int qt_batch_size(const qt_batch *b);
+/* Upload leaves, launch, download values (synchronous). values: 2 doubles per instance. */
+qt_status qt_batch_execute(qt_batch *b, qt_precision prec, double *values);
+/* Device-resident variants for timing: prepare uploads everything once, run
+ * launches only (async on the context stream), fetch copies values back. */
+qt_status qt_batch_prepare(qt_batch *b, qt_precision prec);
+qt_status qt_batch_run(qt_batch *b);
+qt_status qt_batch_fetch(qt_batch *b, double *values);
+/* Replace the leaf values of instance i (host complex128) for the next run. */
+qt_status qt_batch_set_leaves(qt_batch *b, int index, const double *leaves);
+/* Upload all leaf values again from the host copies (async; part of an end-to-end step). */
+qt_status qt_batch_upload(qt_batch *b);
+/* Capture qt_batch_run into a CUDA graph and replay it (0 disables). */
+qt_status qt_batch_use_graph(qt_batch *b, int enable);
+uint64_t qt_batch_h2d_bytes(const qt_batch *b);
+uint64_t qt_batch_d2h_bytes(const qt_batch *b);
+/* kernels launched by one qt_batch_run */
+int qt_batch_launches_per_run(const qt_batch *b);
+
+/* ---- QAOA MaxCut term generator (src/maxcut.h:31-233, maxcut.cpp:166-190) --- */
+
+/* Light-cone QASM + measurement text of edge `edge` of a .dgf graph, as the
+ * reference writes it (angles with 6 significant digits).  Returns the number
+ * of bytes needed (including the NUL); text is truncated to cap. */
+int64_t qt_qaoa_term_text(const char *dgf_text, int p, const double *betas_gammas, int edge,
+                          char *qasm_out, int64_t qasm_cap, char *measure_out, int64_t measure_cap);
+int qt_qaoa_num_edges(const char *dgf_text);
+/* Seeded x-regular random graph in .dgf text (the XregGraphGen algorithm with
+ * std::mt19937(seed), retried until every vertex reaches degree x). */
+int64_t qt_random_regular_graph(int num_nodes, int degree, uint64_t seed, char *dgf_out, int64_t cap);
+
+/* ---- serving: continuous batching of contraction requests --------------- */
+
+/* A server admits requests while their plan's workspace fits the context's
+ * memory budget and a slot is free, and runs every admitted request in grouped
+ * launches; requests that arrive while others run join the next launch. */
+qt_status qt_server_create(qt_ctx *ctx, int max_inflight, qt_precision prec, qt_server **out);
+qt_status qt_server_free(qt_server *s);
+/* Submit (non-blocking).  *ticket identifies the request. */
+qt_status qt_server_submit(qt_server *s, qt_plan *plan, const double *leaves, int64_t *ticket);
+/* Poll: 1 = done (value written), 0 = pending, <0 = error (status negated). */
+int qt_server_poll(qt_server *s, int64_t ticket, double *re_im, double *latency_s);
+/* Block until every submitted request has finished. */
+qt_status qt_server_drain(qt_server *s);
+/* p50/p99 latency in seconds and completed count since creation. */
+qt_status qt_server_stats(qt_server *s, double *p50, double *p99, int64_t *completed, int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,565 @@
+"""qtorch_gb300 — qTorch's tensor-network contraction engine on GB300 (sm_103a).
+
+Python mirror of the C ABI (include/qtorch_gb300.h).  Every entry point runs on
+the GPU through libqtorch_gb300.so; there is no CPU fallback: without the
+library or without an sm_103 device, creating a context raises.
+
+Names follow the reference API (src/Network.h, src/ContractionTools.h,
+src/LineGraph.h) so that code written against qTorch reads the same:
+
+    tools = ContractionTools("circuit.qasm", "measure.txt")
+    tools.Contract(Stochastic, seed=7)
+    value = tools.GetFinalVal()
+"""
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import _capi
+
+__all__ = [
+    "QtError", "InvalidFile", "InvalidFileFormat", "ContractionFailure", "InvalidUserContractionSequence",
+    "InvalidFunctionInput", "InvalidContractionMethod", "Refused", "DeadlineExpired", "OutOfMemory",
+    "Context", "default_context", "contract_pair", "contract_pair_device", "Network", "ContractionTools",
+    "LineGraph", "Plan", "Batch", "Server", "Stochastic", "FP64", "MIXED", "qaoa_term_text", "qaoa_num_edges",
+    "random_regular_graph", "library_path",
+]
+
+FP64 = 0
+MIXED = 1
+Stochastic = 0
+ORDER_STOCHASTIC, ORDER_LINEGRAPH, ORDER_SEQUENCE = 0, 1, 2
+
+
+class QtError(RuntimeError):
+    status = -1
+
+    def __init__(self, status, detail=""):
+        self.status = status
+        lib = _capi.load()
+        msg = lib.qt_status_string(status).decode()
+        super().__init__(f"{msg}{': ' + detail if detail else ''} (status {status})")
+
+
+class InvalidFile(QtError):
+    pass
+
+
+class InvalidFileFormat(QtError):
+    pass
+
+
+class ContractionFailure(QtError):
+    pass
+
+
+class InvalidUserContractionSequence(QtError):
+    pass
+
+
+class InvalidFunctionInput(QtError):
+    pass
+
+
+class InvalidContractionMethod(QtError):
+    pass
+
+
+class Refused(QtError):
+    pass
+
+
+class OutOfMemory(QtError):
+    pass
+
+
+class DeadlineExpired(QtError):
+    pass
+
+
+_ERRORS = {2: InvalidFile, 3: InvalidFileFormat, 4: ContractionFailure, 5: InvalidUserContractionSequence,
+           6: InvalidFunctionInput, 7: InvalidContractionMethod, 8: Refused, 9: OutOfMemory, 11: DeadlineExpired}
+
+
+def library_path():
+    return _capi.LIB_PATH
+
+
+def _lib():
+    return _capi.load()
+
+
+def _check(status, ctx=None):
+    if status != 0:
+        detail = ""
+        if ctx is not None and ctx.handle:
+            buf = ctypes.create_string_buffer(512)
+            _lib().qt_last_error(ctx.handle, buf, 512)
+            detail = buf.value.decode(errors="replace")
+        raise _ERRORS.get(status, QtError)(status, detail)
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+class Context:
+    """One device, one CUDA stream (``stream``: a cudaStream_t as int, or None)."""
+
+    def __init__(self, device=0, stream=None):
+        self.handle = None
+        h = ctypes.c_void_p()
+        _check(_lib().qt_ctx_create(device, ctypes.c_void_p(stream) if stream else None, ctypes.byref(h)))
+        self.handle = h.value
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            _lib().qt_ctx_destroy(self.handle)
+            self.handle = None
+
+    def synchronize(self):
+        _check(_lib().qt_ctx_synchronize(self.handle), self)
+
+    def set_memory_budget(self, nbytes):
+        _check(_lib().qt_ctx_set_memory_budget(self.handle, int(nbytes)), self)
+
+    def set_deadline(self, seconds):
+        _check(_lib().qt_ctx_set_deadline(self.handle, float(seconds)), self)
+
+    @property
+    def kernel_launches(self):
+        return int(_lib().qt_ctx_kernel_launches(self.handle))
+
+    @property
+    def last_error(self):
+        buf = ctypes.create_string_buffer(512)
+        _lib().qt_last_error(self.handle, buf, 512)
+        return buf.value.decode(errors="replace")
+
+
+_default = None
+_default_lock = threading.Lock()
+
+
+def default_context():
+    global _default
+    with _default_lock:
+        if _default is None:
+            _default = Context(0)
+        return _default
+
+
+def _index_maps(free_from_a, free_idx, sum_a, sum_b):
+    ffa = np.ascontiguousarray(np.asarray(free_from_a, dtype=np.uint8))
+    fi = np.ascontiguousarray(np.asarray(free_idx, dtype=np.int32))
+    sa = np.ascontiguousarray(np.asarray(sum_a, dtype=np.int32))
+    sb = np.ascontiguousarray(np.asarray(sum_b, dtype=np.int32))
+    return ffa, fi, sa, sb
+
+
+def _rank_of(n):
+    r = 0
+    while (1 << (2 * r)) < n:
+        r += 1
+    if (1 << (2 * r)) != n:
+        raise ValueError(f"tensor of {n} elements is not 4^rank")
+    return r
+
+
+def contract_pair(a, b, free_from_a, free_idx, sum_a, sum_b, ctx=None):
+    """ContractIndices (src/Network.h:876-971) of two host complex128 tensors on the GPU."""
+    ctx = ctx or default_context()
+    a = np.ascontiguousarray(a, dtype=np.complex128).reshape(-1)
+    b = np.ascontiguousarray(b, dtype=np.complex128).reshape(-1)
+    ffa, fi, sa, sb = _index_maps(free_from_a, free_idx, sum_a, sum_b)
+    c = np.zeros(4 ** len(fi), dtype=np.complex128)
+    _check(_lib().qt_contract_pair_host(
+        ctx.handle, _dp(a.view(np.float64)), _rank_of(a.size), _dp(b.view(np.float64)), _rank_of(b.size), len(fi),
+        ffa.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), _ip(fi), len(sa), _ip(sa), _ip(sb),
+        _dp(c.view(np.float64))), ctx)
+    return c
+
+
+def contract_pair_device(a_ptr, rank_a, b_ptr, rank_b, free_from_a, free_idx, sum_a, sum_b, c_ptr, ctx=None):
+    """ContractIndices on caller-owned device buffers (complex128), asynchronous on ctx's stream."""
+    ctx = ctx or default_context()
+    ffa, fi, sa, sb = _index_maps(free_from_a, free_idx, sum_a, sum_b)
+    _check(_lib().qt_contract_pair_device(
+        ctx.handle, ctypes.c_void_p(a_ptr), rank_a, ctypes.c_void_p(b_ptr), rank_b, len(fi),
+        ffa.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), _ip(fi), len(sa), _ip(sa), _ip(sb),
+        ctypes.c_void_p(c_ptr)), ctx)
+
+
+class Network:
+    """Network (src/Network.h:54-140): parse, ContractNodes on the GPU, final value."""
+
+    def __init__(self, qasm_text, measure_text="", gate_dir=None, ctx=None, symbolic=False):
+        self.ctx = None if symbolic else (ctx or default_context())
+        h = ctypes.c_void_p()
+        _check(_lib().qt_network_create(self.ctx.handle if self.ctx else None, qasm_text.encode(),
+                                        (measure_text or "").encode(), gate_dir.encode() if gate_dir else None,
+                                        ctypes.byref(h)), self.ctx)
+        self.handle = h.value
+
+    @classmethod
+    def from_files(cls, qasm_path, measure_path, ctx=None):
+        with open(qasm_path) as f:
+            q = f.read()
+        try:
+            with open(measure_path) as f:
+                m = f.read()
+        except OSError:
+            m = ""   # every qubit traced out, as Network.h:286-288
+        return cls(q, m, gate_dir=None, ctx=ctx)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            _lib().qt_network_free(h)
+            self.handle = None
+
+    def reset(self):
+        _check(_lib().qt_network_reset(self.handle), self.ctx)
+
+    @property
+    def num_qubits(self):
+        return _lib().qt_network_num_qubits(self.handle)
+
+    @property
+    def num_nodes(self):
+        return _lib().qt_network_num_nodes(self.handle)
+
+    @property
+    def num_uncontracted(self):
+        return _lib().qt_network_num_uncontracted(self.handle)
+
+    def node_rank(self, i):
+        return _lib().qt_network_node_rank(self.handle, i)
+
+    @property
+    def is_done(self):
+        return bool(_lib().qt_network_is_done(self.handle))
+
+    def contract_nodes(self, a, b, threshold):
+        out = ctypes.c_int(-1)
+        _check(_lib().qt_network_contract_nodes(self.handle, a, b, threshold, ctypes.byref(out)), self.ctx)
+        return None if out.value < 0 else out.value
+
+    def contract_sequence(self, pairs):
+        arr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1))
+        _check(_lib().qt_network_contract_sequence(self.handle, _ip(arr), arr.size // 2), self.ctx)
+
+    def contract_user_sequence(self, text):
+        _check(_lib().qt_network_contract_user_sequence(self.handle, text.encode()), self.ctx)
+
+    def contract_stochastic(self, seed):
+        _check(_lib().qt_network_contract_stochastic(self.handle, int(seed)), self.ctx)
+
+    def contract_linegraph(self):
+        _check(_lib().qt_network_contract_linegraph(self.handle), self.ctx)
+
+    def contract_wire_order(self, order_1based):
+        arr = np.ascontiguousarray(np.asarray(order_1based, dtype=np.int32))
+        _check(_lib().qt_network_contract_wire_order(self.handle, _ip(arr), arr.size), self.ctx)
+
+    def linegraph_order(self):
+        n = _lib().qt_network_linegraph_order(self.handle, None, 0)
+        arr = np.zeros(max(n, 1), dtype=np.int32)
+        _lib().qt_network_linegraph_order(self.handle, _ip(arr), n)
+        return [int(x) for x in arr[:n]]
+
+    def reduce(self):
+        _check(_lib().qt_network_reduce(self.handle), self.ctx)
+
+    @property
+    def final_value(self):
+        v = np.zeros(2)
+        _check(_lib().qt_network_final_value(self.handle, _dp(v)), self.ctx)
+        return complex(v[0], v[1])
+
+    @property
+    def flops(self):
+        return int(_lib().qt_network_flops(self.handle))
+
+    def created_from(self):
+        n = _lib().qt_network_created_from(self.handle, None, 0)
+        arr = np.zeros(2 * max(n, 1), dtype=np.int32)
+        _lib().qt_network_created_from(self.handle, _ip(arr), n)
+        return [(int(arr[2 * i]), int(arr[2 * i + 1])) for i in range(n)]
+
+    def node_values(self, i):
+        n = _lib().qt_network_node_values(self.handle, i, None, 0)
+        if n < 0:
+            return None
+        out = np.zeros(n, dtype=np.complex128)
+        _lib().qt_network_node_values(self.handle, i, _dp(out.view(np.float64)), n)
+        return out
+
+
+class ContractionTools:
+    """ContractionTools (src/ContractionTools.h:52-123) over a GPU-backed Network."""
+
+    def __init__(self, qasm_or_network, measure_path=None, ctx=None):
+        if isinstance(qasm_or_network, Network):
+            self._net = qasm_or_network
+            self._paths = None
+        else:
+            self._net = None
+            self._paths = (qasm_or_network, measure_path)
+        self._ctx = ctx
+        self._final = 0j
+
+    def _acquire(self):
+        if self._net is None:
+            self._net = Network.from_files(*self._paths, ctx=self._ctx)
+        return self._net
+
+    def Contract(self, kind=Stochastic, seed=None):
+        if kind != Stochastic:
+            raise InvalidContractionMethod(7)
+        net = self._acquire()
+        net.contract_stochastic(np.random.SeedSequence().entropy % (1 << 63) if seed is None else seed)
+        self._final = net.final_value
+        return net
+
+    def ContractGivenSequence(self, sequence):
+        net = self._acquire()
+        net.contract_sequence(sequence)
+        self._final = net.final_value
+        return net
+
+    def ContractUserDefinedSequenceOfWires(self, path):
+        with open(path) as f:
+            text = f.read()
+        net = self._acquire()
+        net.contract_user_sequence(text)
+        self._final = net.final_value
+        return net
+
+    def GetFinalVal(self):
+        return self._final
+
+
+class LineGraph:
+    """LineGraph (src/LineGraph.h): min-fill elimination order of the line graph, then LGContract."""
+
+    def __init__(self, network):
+        self._net = network
+
+    def ordering(self):
+        return self._net.linegraph_order()
+
+    def LGContract(self, order_1based=None):
+        if order_1based is None:
+            self._net.contract_linegraph()
+        else:
+            self._net.contract_wire_order(order_1based)
+        return True
+
+
+_ORDER_NAMES = {"stochastic": ORDER_STOCHASTIC, "linegraph": ORDER_LINEGRAPH, "sequence": ORDER_SEQUENCE}
+
+
+class Plan:
+    """An ordering lowered once; executed for many leaf bindings (see qt_plan_build)."""
+
+    def __init__(self, qasm_text, measure_text="", ordering="linegraph", seed=0, sequence=None, gate_dir=None,
+                 ctx=None, symbolic=False):
+        # symbolic plans need no device: they can be inspected but not executed
+        self.ctx = None if symbolic else (ctx or default_context())
+        h = ctypes.c_void_p()
+        seq = np.ascontiguousarray(np.asarray(sequence if sequence is not None else [], dtype=np.int32).reshape(-1))
+        _check(_lib().qt_plan_build(self.ctx.handle if self.ctx else None, qasm_text.encode(),
+                                    (measure_text or "").encode(),
+                                    gate_dir.encode() if gate_dir else None, _ORDER_NAMES[ordering], int(seed),
+                                    _ip(seq) if seq.size else None, seq.size // 2, ctypes.byref(h)), self.ctx)
+        self.handle = h.value
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            _lib().qt_plan_free(h)
+            self.handle = None
+
+    @property
+    def num_steps(self):
+        return _lib().qt_plan_num_steps(self.handle)
+
+    @property
+    def num_leaves(self):
+        return _lib().qt_plan_num_leaves(self.handle)
+
+    @property
+    def peak_rank(self):
+        return _lib().qt_plan_peak_rank(self.handle)
+
+    def workspace_bytes(self, precision=FP64):
+        return int(_lib().qt_plan_workspace_bytes(self.handle, precision))
+
+    @property
+    def flops(self):
+        return int(_lib().qt_plan_flops(self.handle))
+
+    def sequence(self):
+        n = _lib().qt_plan_sequence(self.handle, None, 0)
+        arr = np.zeros(2 * max(n, 1), dtype=np.int32)
+        _lib().qt_plan_sequence(self.handle, _ip(arr), n)
+        return [(int(arr[2 * i]), int(arr[2 * i + 1])) for i in range(n)]
+
+    def leaf_values(self):
+        n = int(_lib().qt_plan_leaf_elems(self.handle))
+        out = np.zeros(n, dtype=np.complex128)
+        _check(_lib().qt_plan_leaf_values(self.handle, _dp(out.view(np.float64)), n), self.ctx)
+        return out
+
+    def execute(self, precision=FP64):
+        v = np.zeros(2)
+        _check(_lib().qt_plan_execute(self.ctx.handle, self.handle, precision, _dp(v)), self.ctx)
+        return complex(v[0], v[1])
+
+
+class Batch:
+    """Many plan instances in one persistent grouped launch."""
+
+    def __init__(self, ctx=None):
+        self.ctx = ctx or default_context()
+        h = ctypes.c_void_p()
+        _check(_lib().qt_batch_create(self.ctx.handle, ctypes.byref(h)), self.ctx)
+        self.handle = h.value
+        self._plans = []
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            _lib().qt_batch_free(h)
+            self.handle = None
+
+    def add(self, plan, leaves=None):
+        idx = ctypes.c_int(-1)
+        if leaves is not None:
+            leaves = np.ascontiguousarray(leaves, dtype=np.complex128)
+        _check(_lib().qt_batch_add(self.handle, plan.handle,
+                                   _dp(leaves.view(np.float64)) if leaves is not None else None,
+                                   ctypes.byref(idx)), self.ctx)
+        self._plans.append(plan)
+        return idx.value
+
+    def __len__(self):
+        return _lib().qt_batch_size(self.handle)
+
+    def execute(self, precision=FP64):
+        out = np.zeros(2 * len(self))
+        _check(_lib().qt_batch_execute(self.handle, precision, _dp(out)), self.ctx)
+        return out.view(np.complex128).copy()
+
+    def prepare(self, precision=FP64):
+        _check(_lib().qt_batch_prepare(self.handle, precision), self.ctx)
+
+    def run(self):
+        _check(_lib().qt_batch_run(self.handle), self.ctx)
+
+    def fetch(self):
+        out = np.zeros(2 * len(self))
+        _check(_lib().qt_batch_fetch(self.handle, _dp(out)), self.ctx)
+        return out.view(np.complex128).copy()
+
+    def set_leaves(self, index, leaves):
+        leaves = np.ascontiguousarray(leaves, dtype=np.complex128)
+        _check(_lib().qt_batch_set_leaves(self.handle, index, _dp(leaves.view(np.float64))), self.ctx)
+
+    def upload(self):
+        _check(_lib().qt_batch_upload(self.handle), self.ctx)
+
+    def use_graph(self, enable=True):
+        _check(_lib().qt_batch_use_graph(self.handle, 1 if enable else 0), self.ctx)
+
+    @property
+    def h2d_bytes(self):
+        return int(_lib().qt_batch_h2d_bytes(self.handle))
+
+    @property
+    def d2h_bytes(self):
+        return int(_lib().qt_batch_d2h_bytes(self.handle))
+
+    @property
+    def launches_per_run(self):
+        return int(_lib().qt_batch_launches_per_run(self.handle))
+
+
+class Server:
+    """Continuous-batching request loop (qt_server_*)."""
+
+    def __init__(self, max_inflight=64, precision=FP64, ctx=None):
+        self.ctx = ctx or default_context()
+        h = ctypes.c_void_p()
+        _check(_lib().qt_server_create(self.ctx.handle, max_inflight, precision, ctypes.byref(h)), self.ctx)
+        self.handle = h.value
+        self._keep = []
+
+    def close(self):
+        if self.handle:
+            _lib().qt_server_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        self.close()
+
+    def submit(self, plan, leaves=None):
+        t = ctypes.c_int64(-1)
+        if leaves is not None:
+            leaves = np.ascontiguousarray(leaves, dtype=np.complex128)
+        self._keep.append(plan)
+        _check(_lib().qt_server_submit(self.handle, plan.handle,
+                                       _dp(leaves.view(np.float64)) if leaves is not None else None,
+                                       ctypes.byref(t)), self.ctx)
+        return t.value
+
+    def poll(self, ticket):
+        v = np.zeros(2)
+        lat = ctypes.c_double(0)
+        st = _lib().qt_server_poll(self.handle, ticket, _dp(v), ctypes.byref(lat))
+        if st < 0:
+            raise _ERRORS.get(-st, QtError)(-st)
+        return (complex(v[0], v[1]), lat.value) if st == 1 else None
+
+    def drain(self):
+        _check(_lib().qt_server_drain(self.handle), self.ctx)
+
+    def stats(self):
+        p50, p99 = ctypes.c_double(0), ctypes.c_double(0)
+        done, launches = ctypes.c_int64(0), ctypes.c_int64(0)
+        _check(_lib().qt_server_stats(self.handle, ctypes.byref(p50), ctypes.byref(p99), ctypes.byref(done),
+                                      ctypes.byref(launches)), self.ctx)
+        return {"p50_s": p50.value, "p99_s": p99.value, "completed": done.value, "launches": launches.value}
+
+
+def qaoa_num_edges(dgf_text):
+    return _lib().qt_qaoa_num_edges(dgf_text.encode())
+
+
+def qaoa_term_text(dgf_text, p, betas_gammas, edge):
+    """(qasm, measure) of one MaxCut light-cone term, as src/maxcut.cpp:166-190 writes it."""
+    bg = np.ascontiguousarray(np.asarray(betas_gammas, dtype=np.float64))
+    n = _lib().qt_qaoa_term_text(dgf_text.encode(), p, _dp(bg), edge, None, 0, None, 0)
+    if n < 0:
+        raise ValueError("bad graph, p or edge")
+    q = ctypes.create_string_buffer(int(n))
+    m = ctypes.create_string_buffer(4096)
+    _lib().qt_qaoa_term_text(dgf_text.encode(), p, _dp(bg), edge, q, int(n), m, 4096)
+    return q.value.decode(), m.value.decode()
+
+
+def random_regular_graph(num_nodes, degree, seed):
+    n = _lib().qt_random_regular_graph(num_nodes, degree, int(seed), None, 0)
+    if n < 0:
+        raise ValueError("no regular graph for these parameters")
+    buf = ctypes.create_string_buffer(int(n))
+    _lib().qt_random_regular_graph(num_nodes, degree, int(seed), buf, int(n))
+    return buf.value.decode()

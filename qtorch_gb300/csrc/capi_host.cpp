@@ -1,0 +1,579 @@
+// C ABI over the host library: networks (Network / ContractionTools /
+// LineGraph), plans and batches.
+#include <cstring>
+#include <fstream>
+#include <new>
+#include <sstream>
+
+#include "kernels.h"
+#include "plan.h"
+
+using namespace qtg;
+
+struct qt_network {
+    qt_ctx *ctx = nullptr;
+    std::string qasm, measure, gate_dir;
+    std::shared_ptr<qtorch::Network> net;
+};
+
+// exceptions of the host library -> status codes
+template <typename F>
+static qt_status guard(qt_ctx *ctx, F &&f) {
+    try {
+        return f();
+    } catch (const qtorch::InvalidFile &) {
+        return set_error(ctx, QT_ERR_INVALID_FILE, "invalid file");
+    } catch (const qtorch::InvalidFileFormat &) {
+        return set_error(ctx, QT_ERR_INVALID_FILE_FORMAT, "invalid file format");
+    } catch (const qtorch::ContractionFailure &) {
+        return set_error(ctx, QT_ERR_CONTRACTION_FAILURE, "contraction failed");
+    } catch (const qtorch::InvalidUserContractionSequence &) {
+        return set_error(ctx, QT_ERR_INVALID_USER_SEQUENCE, "invalid user contraction sequence");
+    } catch (const qtorch::InvalidFunctionInput &) {
+        return set_error(ctx, QT_ERR_INVALID_FUNCTION_INPUT, "invalid function input");
+    } catch (const qtorch::InvalidContractionMethod &) {
+        return set_error(ctx, QT_ERR_INVALID_CONTRACTION_METHOD, "invalid contraction method");
+    } catch (const qtorch::QbbFailure &) {
+        return set_error(ctx, QT_ERR_CONTRACTION_FAILURE, "line graph ordering failure");
+    } catch (const qtorch::EngineFailure &e) {
+        return e.status();
+    } catch (const std::bad_alloc &) {
+        return set_error(ctx, QT_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (const std::exception &e) {
+        return set_error(ctx, QT_ERR_INVALID_ARGUMENT, e.what());
+    }
+}
+
+static bool slurp(const char *path, std::string &out) {
+    std::ifstream in(path, std::ios::binary);
+    if (!in.is_open()) return false;
+    std::stringstream ss;
+    ss << in.rdbuf();
+    out = ss.str();
+    return true;
+}
+
+extern "C" {
+
+// ---------------------------------------------------------------------------
+// networks
+
+qt_status qt_network_create(qt_ctx *ctx, const char *qasm_text, const char *measure_text, const char *gate_dir,
+                            qt_network **out) {
+    if (!qasm_text || !out) return QT_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&]() {
+        auto *n = new qt_network();
+        n->ctx = ctx;
+        n->qasm = qasm_text;
+        n->measure = measure_text ? measure_text : "";
+        n->gate_dir = gate_dir ? gate_dir : "";
+        try {
+            n->net = qtorch::Network::FromText(n->qasm, n->measure, n->gate_dir, ctx);
+        } catch (...) {
+            delete n;
+            throw;
+        }
+        *out = n;
+        return QT_OK;
+    });
+}
+
+qt_status qt_network_create_from_files(qt_ctx *ctx, const char *qasm_path, const char *measure_path, qt_network **out) {
+    if (!qasm_path || !out) return QT_ERR_INVALID_ARGUMENT;
+    std::string q, m;
+    if (!slurp(qasm_path, q)) return set_error(ctx, QT_ERR_INVALID_FILE, "cannot open QASM file");
+    if (measure_path) slurp(measure_path, m);   // unreadable: every qubit is traced out
+    return qt_network_create(ctx, q.c_str(), m.c_str(), nullptr, out);
+}
+
+qt_status qt_network_free(qt_network *n) {
+    if (!n) return QT_ERR_INVALID_ARGUMENT;
+    delete n;
+    return QT_OK;
+}
+
+qt_status qt_network_reset(qt_network *n) {
+    if (!n) return QT_ERR_INVALID_ARGUMENT;
+    return guard(n->ctx, [&]() {
+        n->net = qtorch::Network::FromText(n->qasm, n->measure, n->gate_dir, n->ctx);
+        return QT_OK;
+    });
+}
+
+int qt_network_num_qubits(const qt_network *n) { return n ? n->net->GetNumQubits() : -1; }
+int qt_network_num_nodes(const qt_network *n) { return n ? (int) n->net->GetAllNodes().size() : -1; }
+int qt_network_num_uncontracted(const qt_network *n) { return n ? (int) n->net->GetUncontractedNodes().size() : -1; }
+
+int qt_network_node_rank(const qt_network *n, int id) {
+    if (!n || id < 0 || id >= (int) n->net->GetAllNodes().size()) return -1;
+    return n->net->GetAllNodes()[id]->mRank;
+}
+
+int qt_network_is_done(const qt_network *n) { return n && n->net->IsDone() ? 1 : 0; }
+
+qt_status qt_network_contract_nodes(qt_network *n, int a, int b, int threshold, int *new_id) {
+    if (!n) return QT_ERR_INVALID_ARGUMENT;
+    const int cnt = (int) n->net->GetAllNodes().size();
+    if (a < 0 || b < 0 || a >= cnt || b >= cnt) return QT_ERR_INVALID_ARGUMENT;
+    return guard(n->ctx, [&]() {
+        auto r = n->net->ContractNodes(n->net->GetAllNodes()[a], n->net->GetAllNodes()[b], threshold);
+        if (new_id) *new_id = r ? r->mID : -1;
+        return QT_OK;
+    });
+}
+
+qt_status qt_network_contract_sequence(qt_network *n, const int32_t *pairs, int n_pairs) {
+    if (!n || (n_pairs && !pairs) || n_pairs < 0) return QT_ERR_INVALID_ARGUMENT;
+    return guard(n->ctx, [&]() {
+        std::vector<std::pair<int, int>> seq(n_pairs);
+        for (int i = 0; i < n_pairs; i++) seq[i] = {pairs[2 * i], pairs[2 * i + 1]};
+        qtorch::ContractionTools t(n->net);
+        t.ContractGivenSequence(seq);
+        return QT_OK;
+    });
+}
+
+qt_status qt_network_contract_user_sequence(qt_network *n, const char *text) {
+    if (!n || !text) return QT_ERR_INVALID_ARGUMENT;
+    return guard(n->ctx, [&]() {
+        qtorch::ContractionTools t(n->net);
+        t.ContractUserDefinedSequenceText(text);
+        return QT_OK;
+    });
+}
+
+qt_status qt_network_contract_stochastic(qt_network *n, uint64_t seed) {
+    if (!n) return QT_ERR_INVALID_ARGUMENT;
+    return guard(n->ctx, [&]() {
+        qtorch::ContractionTools t(n->net);
+        t.Seed(seed);
+        t.Contract(qtorch::Stochastic);
+        return QT_OK;
+    });
+}
+
+qt_status qt_network_contract_linegraph(qt_network *n) {
+    if (!n) return QT_ERR_INVALID_ARGUMENT;
+    return guard(n->ctx, [&]() {
+        qtorch::LineGraph lg(n->net);
+        lg.LGContract();
+        return QT_OK;
+    });
+}
+
+qt_status qt_network_contract_wire_order(qt_network *n, const int32_t *order, int cnt) {
+    if (!n || (cnt && !order) || cnt < 0) return QT_ERR_INVALID_ARGUMENT;
+    return guard(n->ctx, [&]() {
+        qtorch::LineGraph lg(n->net);
+        lg.LGContract(std::vector<int>(order, order + cnt));
+        return QT_OK;
+    });
+}
+
+int qt_network_linegraph_order(qt_network *n, int32_t *order, int cap) {
+    if (!n) return -1;
+    try {
+        qtorch::LineGraph lg(n->net);
+        const auto &o = lg.MinFillOrdering();
+        for (int i = 0; i < (int) o.size() && i < cap; i++) order[i] = o[i];
+        return (int) o.size();
+    } catch (...) {
+        return -1;
+    }
+}
+
+qt_status qt_network_reduce(qt_network *n) {
+    if (!n) return QT_ERR_INVALID_ARGUMENT;
+    return guard(n->ctx, [&]() {
+        n->net->ReduceCircuit();
+        return QT_OK;
+    });
+}
+
+qt_status qt_network_final_value(const qt_network *n, double *v) {
+    if (!n || !v) return QT_ERR_INVALID_ARGUMENT;
+    v[0] = n->net->GetFinalValue().real();
+    v[1] = n->net->GetFinalValue().imag();
+    return QT_OK;
+}
+
+int64_t qt_network_flops(const qt_network *n) { return n ? n->net->getNumFloatOps() : -1; }
+
+int qt_network_created_from(const qt_network *n, int32_t *pairs, int cap) {
+    if (!n) return -1;
+    int k = 0;
+    for (const auto &node : n->net->GetAllNodes()) {
+        if (node->mCreatedFrom.first == 0 && node->mCreatedFrom.second == 0) continue;
+        if (k < cap && pairs) {
+            pairs[2 * k] = node->mCreatedFrom.first;
+            pairs[2 * k + 1] = node->mCreatedFrom.second;
+        }
+        k++;
+    }
+    return k;
+}
+
+int64_t qt_network_node_values(qt_network *n, int id, double *out, int64_t cap) {
+    if (!n || id < 0 || id >= (int) n->net->GetAllNodes().size()) return -1;
+    auto &node = n->net->GetAllNodes()[id];
+    if (!node->HasData()) return -1;
+    try {
+        auto &v = node->GetTensorVals();
+        const int64_t cnt = (int64_t) v.size();
+        if (out) std::memcpy(out, v.data(), sizeof(double) * 2 * (size_t) std::min(cnt, cap));
+        return cnt;
+    } catch (...) {
+        return -1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// plans
+
+qt_status qt_plan_build(qt_ctx *ctx, const char *qasm_text, const char *measure_text, const char *gate_dir,
+                        qt_ordering ordering, uint64_t seed, const int32_t *pairs, int n_pairs, qt_plan **out) {
+    // ctx may be NULL: the plan can then be inspected (sequence, sizes) but not executed
+    if (!qasm_text || !out) return QT_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&]() {
+        auto *p = new qt_plan();
+        p->ctx = ctx;
+        p->qasm = qasm_text;
+        p->measure = measure_text ? measure_text : "";
+        p->gate_dir = gate_dir ? gate_dir : "";
+        std::unique_ptr<qt_plan> owner(p);
+        auto net = qtorch::Network::FromText(p->qasm, p->measure, p->gate_dir, nullptr);
+        for (const auto &leaf : net->Leaves()) {
+            p->leaf_rank.push_back(leaf->mRank);
+            const auto &v = leaf->GetTensorVals();
+            p->leaf_values.insert(p->leaf_values.end(), v.begin(), v.end());
+        }
+        if (ordering == QT_ORDER_STOCHASTIC) {
+            qtorch::ContractionTools t(net);
+            t.Seed(seed);
+            t.Contract(qtorch::Stochastic);
+        } else if (ordering == QT_ORDER_LINEGRAPH) {
+            qtorch::LineGraph lg(net);
+            lg.LGContract();
+        } else if (ordering == QT_ORDER_SEQUENCE) {
+            if (n_pairs < 0 || (n_pairs && !pairs)) return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "sequence");
+            std::vector<std::pair<int, int>> seq(n_pairs);
+            for (int i = 0; i < n_pairs; i++) seq[i] = {pairs[2 * i], pairs[2 * i + 1]};
+            qtorch::ContractionTools t(net);
+            t.ContractGivenSequence(seq);
+        } else {
+            return set_error(ctx, QT_ERR_INVALID_CONTRACTION_METHOD, "unknown ordering");
+        }
+        if (!net->IsDone()) return set_error(ctx, QT_ERR_CONTRACTION_FAILURE, "ordering did not finish the network");
+        for (const auto &node : net->GetAllNodes()) {
+            if (node->mCreatedFrom.first == 0 && node->mCreatedFrom.second == 0) continue;
+            p->sequence.push_back(node->mCreatedFrom.first);
+            p->sequence.push_back(node->mCreatedFrom.second);
+        }
+        qt_status s = lower_plan(p, *net);
+        if (s != QT_OK) return s;
+        *out = owner.release();
+        return QT_OK;
+    });
+}
+
+qt_status qt_plan_free(qt_plan *p) {
+    if (!p) return QT_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < 2; i++)
+        if (p->dev[i] && p->ctx) dev_free(p->ctx, p->dev[i]);
+    delete p;
+    return QT_OK;
+}
+
+int qt_plan_num_steps(const qt_plan *p) { return p ? p->n_steps : -1; }
+int qt_plan_num_leaves(const qt_plan *p) { return p ? (int) p->leaf_rank.size() : -1; }
+int qt_plan_peak_rank(const qt_plan *p) { return p ? p->peak_rank : -1; }
+uint64_t qt_plan_workspace_bytes(const qt_plan *p, qt_precision prec) {
+    return p && (prec == QT_PREC_FP64 || prec == QT_PREC_MIXED) ? p->ws_bytes[prec] : 0;
+}
+int64_t qt_plan_flops(const qt_plan *p) { return p ? p->flops : -1; }
+
+int qt_plan_sequence(const qt_plan *p, int32_t *pairs, int cap) {
+    if (!p) return -1;
+    const int n = (int) p->sequence.size() / 2;
+    for (int i = 0; i < n && i < cap; i++) {
+        pairs[2 * i] = p->sequence[2 * i];
+        pairs[2 * i + 1] = p->sequence[2 * i + 1];
+    }
+    return n;
+}
+
+uint64_t qt_plan_leaf_elems(const qt_plan *p) { return p ? p->leaf_values.size() : 0; }
+
+qt_status qt_plan_leaf_values(const qt_plan *p, double *out, uint64_t cap) {
+    if (!p || !out || cap < p->leaf_values.size()) return QT_ERR_INVALID_ARGUMENT;
+    std::memcpy(out, p->leaf_values.data(), p->leaf_values.size() * sizeof(std::complex<double>));
+    return QT_OK;
+}
+
+qt_status qt_plan_execute(qt_ctx *ctx, qt_plan *p, qt_precision prec, double *v) {
+    if (!ctx || !p || !p->ctx || !v || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return QT_ERR_INVALID_ARGUMENT;
+    if (!p->grouped) return execute_stepwise(p, prec, p->leaf_values.data(), v);
+    qt_batch *b = nullptr;
+    qt_status s = qt_batch_create(ctx, &b);
+    if (s != QT_OK) return s;
+    int idx;
+    s = qt_batch_add(b, p, nullptr, &idx);
+    if (s == QT_OK) s = qt_batch_execute(b, prec, v);
+    qt_batch_free(b);
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// batches
+
+static void batch_release(qt_batch *b) {
+    qt_ctx *ctx = b->ctx;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    dev_free(ctx, b->d_leaves);
+    dev_free(ctx, b->d_inst);
+    dev_free(ctx, b->d_values);
+    dev_free(ctx, b->d_ws);
+    dev_free(ctx, b->d_exps);
+    b->d_leaves = b->d_inst = b->d_values = b->d_ws = b->d_exps = nullptr;
+    if (b->h_leaves) cudaFreeHost(b->h_leaves);
+    if (b->h_values) cudaFreeHost(b->h_values);
+    b->h_leaves = b->h_values = nullptr;
+    b->prepared_prec = -1;
+}
+
+qt_status qt_batch_create(qt_ctx *ctx, qt_batch **out) {
+    if (!ctx || !out) return QT_ERR_INVALID_ARGUMENT;
+    *out = new (std::nothrow) qt_batch();
+    if (!*out) return QT_ERR_OUT_OF_MEMORY;
+    (*out)->ctx = ctx;
+    return QT_OK;
+}
+
+qt_status qt_batch_free(qt_batch *b) {
+    if (!b) return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::recursive_mutex> g(b->ctx->lock);
+    cudaStreamSynchronize(b->ctx->stream);
+    batch_release(b);
+    delete b;
+    return QT_OK;
+}
+
+qt_status qt_batch_add(qt_batch *b, qt_plan *p, const double *leaves, int *index) {
+    // plans may come from another context on the same device (the server's lanes)
+    if (!b || !p || !p->ctx || p->ctx->device != b->ctx->device) return QT_ERR_INVALID_ARGUMENT;
+    b->plans.push_back(p);
+    if (leaves) {
+        const auto *c = reinterpret_cast<const std::complex<double> *>(leaves);
+        b->leaves.emplace_back(c, c + p->leaf_values.size());
+    } else {
+        b->leaves.push_back(p->leaf_values);
+    }
+    b->dirty = true;
+    if (index) *index = (int) b->plans.size() - 1;
+    return QT_OK;
+}
+
+int qt_batch_size(const qt_batch *b) { return b ? (int) b->plans.size() : -1; }
+
+qt_status qt_batch_set_leaves(qt_batch *b, int i, const double *leaves) {
+    if (!b || !leaves || i < 0 || i >= (int) b->plans.size()) return QT_ERR_INVALID_ARGUMENT;
+    const auto *c = reinterpret_cast<const std::complex<double> *>(leaves);
+    std::copy(c, c + b->leaves[i].size(), b->leaves[i].begin());
+    return QT_OK;
+}
+
+static qt_status batch_pack(qt_batch *b) {
+    const int prec = b->prepared_prec;
+    for (size_t i = 0; i < b->plans.size(); i++) {
+        if (!b->plans[i]->grouped) continue;
+        pack_leaves(b->plans[i], prec, b->leaves[i].data(), (char *) b->h_leaves + b->inst_leaf_off[i]);
+    }
+    return QT_OK;
+}
+
+qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
+    if (!b || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return QT_ERR_INVALID_ARGUMENT;
+    qt_ctx *ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    cudaStreamSynchronize(ctx->stream);
+    batch_release(b);
+    b->prepared_prec = prec;
+    const int n = (int) b->plans.size();
+    b->stepwise.clear();
+    b->inst_leaf_off.assign(n, 0);
+    uint64_t off = 0, ws = 0, ex = 0;
+    int n_grouped = 0;
+    for (int i = 0; i < n; i++) {
+        qt_plan *p = b->plans[i];
+        if (!p->grouped) {
+            b->stepwise.push_back(i);
+            continue;
+        }
+        qt_status s = upload_plan(p, prec);
+        if (s != QT_OK) return s;
+        b->inst_leaf_off[i] = off;
+        off += (p->leaf_bytes[prec] + 255) / 256 * 256;
+        ws = std::max<uint64_t>(ws, p->ws_bytes[prec]);
+        ex = std::max<uint64_t>(ex, (uint64_t) p->n_steps);
+        n_grouped++;
+    }
+    b->leaf_bytes = off;
+    b->ws_stride = (ws + 255) / 256 * 256;
+    b->exps_stride = (ex + 63) / 64 * 64;
+    b->grid = std::min(n_grouped, plan_max_grid());
+    qt_status s = QT_OK;
+    auto chk = [&](cudaError_t e, const char *w) {
+        if (s == QT_OK && e != cudaSuccess) s = cuda_error(ctx, e, w);
+    };
+    if (off) {
+        chk(cudaMallocHost(&b->h_leaves, off), "cudaMallocHost");
+        if (s == QT_OK) s = dev_alloc(ctx, off, &b->d_leaves);
+    }
+    if (s == QT_OK && n) {
+        chk(cudaMallocHost(&b->h_values, sizeof(double) * 2 * n), "cudaMallocHost");
+        if (s == QT_OK) s = dev_alloc(ctx, sizeof(double) * 2 * n, &b->d_values);
+    }
+    if (s == QT_OK && b->grid > 0) {
+        s = dev_alloc(ctx, b->ws_stride * b->grid, &b->d_ws);
+        if (s == QT_OK && prec == QT_PREC_MIXED) s = dev_alloc(ctx, sizeof(int32_t) * b->exps_stride * b->grid, &b->d_exps);
+    }
+    if (s != QT_OK) {
+        batch_release(b);
+        return s;
+    }
+    // instance descriptors (grouped instances only, packed)
+    std::vector<InstanceDesc> inst;
+    for (int i = 0; i < n; i++) {
+        qt_plan *p = b->plans[i];
+        if (!p->grouped) continue;
+        InstanceDesc d;
+        d.plan = reinterpret_cast<const PlanDesc *>(p->dev[prec]);
+        d.leaves = (const char *) b->d_leaves + b->inst_leaf_off[i];
+        d.value = (double *) b->d_values + 2 * i;
+        inst.push_back(d);
+    }
+    if (!inst.empty()) {
+        s = dev_alloc(ctx, sizeof(InstanceDesc) * inst.size(), &b->d_inst);
+        if (s == QT_OK) {
+            chk(cudaMemcpyAsync(b->d_inst, inst.data(), sizeof(InstanceDesc) * inst.size(), cudaMemcpyHostToDevice,
+                                ctx->stream),
+                "instance upload");
+            chk(cudaStreamSynchronize(ctx->stream), "sync");
+        }
+    }
+    if (s == QT_OK) {
+        batch_pack(b);
+        s = qt_batch_upload(b);
+    }
+    if (s == QT_OK) chk(cudaStreamSynchronize(ctx->stream), "sync");
+    if (s != QT_OK) batch_release(b);
+    b->dirty = false;
+    return s;
+}
+
+qt_status qt_batch_upload(qt_batch *b) {
+    if (!b || b->prepared_prec < 0) return QT_ERR_INVALID_ARGUMENT;
+    qt_ctx *ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    batch_pack(b);
+    if (!b->leaf_bytes) return QT_OK;
+    return cuda_error(ctx, cudaMemcpyAsync(b->d_leaves, b->h_leaves, b->leaf_bytes, cudaMemcpyHostToDevice, ctx->stream),
+                      "leaf upload");
+}
+
+static qt_status batch_launch(qt_batch *b) {
+    qt_ctx *ctx = b->ctx;
+    const int n_grouped = (int) b->plans.size() - (int) b->stepwise.size();
+    if (n_grouped <= 0) return QT_OK;
+    cudaError_t e = launch_plan((const InstanceDesc *) b->d_inst, n_grouped, b->prepared_prec == QT_PREC_MIXED,
+                                b->grid, (char *) b->d_ws, b->ws_stride, (int32_t *) b->d_exps, b->exps_stride,
+                                ctx->stream);
+    ctx->launches++;
+    return cuda_error(ctx, e, "plan kernel launch");
+}
+
+qt_status qt_batch_run(qt_batch *b) {
+    if (!b || b->prepared_prec < 0) return QT_ERR_INVALID_ARGUMENT;
+    qt_ctx *ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    if (deadline_passed(ctx)) return set_error(ctx, QT_ERR_DEADLINE, "deadline expired");
+    if (b->use_graph && !b->graph && b->stepwise.empty()) {
+        cudaGraph_t graph;
+        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "begin capture");
+        qt_status s = batch_launch(b);
+        e = cudaStreamEndCapture(ctx->stream, &graph);
+        if (s != QT_OK) return s;
+        if (e != cudaSuccess) return cuda_error(ctx, e, "end capture");
+        e = cudaGraphInstantiate(&b->graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "graph instantiate");
+    }
+    qt_status s;
+    if (b->graph) {
+        s = cuda_error(ctx, cudaGraphLaunch(b->graph, ctx->stream), "graph launch");
+        ctx->launches++;
+    } else {
+        s = batch_launch(b);
+    }
+    if (s != QT_OK) return s;
+    // plans too large for one CTA run step by step
+    for (int i : b->stepwise) {
+        double v[2];
+        s = execute_stepwise(b->plans[i], b->prepared_prec, b->leaves[i].data(), v);
+        if (s != QT_OK) return s;
+        cudaMemcpyAsync((double *) b->d_values + 2 * i, v, 16, cudaMemcpyHostToDevice, ctx->stream);
+    }
+    return QT_OK;
+}
+
+qt_status qt_batch_fetch(qt_batch *b, double *values) {
+    if (!b || !values || b->prepared_prec < 0) return QT_ERR_INVALID_ARGUMENT;
+    qt_ctx *ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    const size_t bytes = sizeof(double) * 2 * b->plans.size();
+    if (!bytes) return QT_OK;
+    cudaError_t e = cudaMemcpyAsync(b->h_values, b->d_values, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "value download");
+    std::memcpy(values, b->h_values, bytes);
+    return QT_OK;
+}
+
+qt_status qt_batch_execute(qt_batch *b, qt_precision prec, double *values) {
+    if (!b || !values) return QT_ERR_INVALID_ARGUMENT;
+    qt_status s = QT_OK;
+    if (b->dirty || b->prepared_prec != (int) prec) s = qt_batch_prepare(b, prec);
+    else s = qt_batch_upload(b);
+    if (s == QT_OK) s = qt_batch_run(b);
+    if (s == QT_OK) s = qt_batch_fetch(b, values);
+    return s;
+}
+
+qt_status qt_batch_use_graph(qt_batch *b, int enable) {
+    if (!b) return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::recursive_mutex> g(b->ctx->lock);
+    b->use_graph = enable != 0;
+    if (!b->use_graph && b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return QT_OK;
+}
+
+uint64_t qt_batch_h2d_bytes(const qt_batch *b) { return b ? b->leaf_bytes : 0; }
+uint64_t qt_batch_d2h_bytes(const qt_batch *b) { return b ? sizeof(double) * 2 * b->plans.size() : 0; }
+
+int qt_batch_launches_per_run(const qt_batch *b) {
+    if (!b) return 0;
+    int n = ((int) b->plans.size() - (int) b->stepwise.size()) > 0 ? 1 : 0;
+    for (int i : b->stepwise) n += b->plans[i]->n_steps;
+    return n;
+}
+
+}  // extern "C"

@@ -1,0 +1,375 @@
+// C ABI: contexts, the caching device allocator, tensors and the pairwise
+// contraction entry points (the drop-in for Network::ContractIndices,
+// src/Network.h:876-971).
+#include "core.h"
+
+#include <cstring>
+#include <new>
+
+#include "kernels.h"
+
+namespace qtg {
+
+qt_status set_error(qt_ctx *ctx, qt_status s, const std::string &msg) {
+    if (ctx) {
+        std::lock_guard<std::mutex> g(ctx->err_lock);
+        ctx->last_error = msg;
+    }
+    return s;
+}
+
+qt_status cuda_error(qt_ctx *ctx, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return QT_OK;
+    std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return set_error(ctx, QT_ERR_OUT_OF_MEMORY, msg);
+    return set_error(ctx, QT_ERR_CUDA, msg);
+}
+
+static size_t size_class(size_t bytes) {
+    size_t c = 256;
+    while (c < bytes) c <<= 1;
+    return c;
+}
+
+qt_status dev_alloc(qt_ctx *ctx, size_t bytes, void **out) {
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    const size_t cls = size_class(bytes ? bytes : 1);
+    auto it = ctx->free_blocks.find(cls);
+    if (it != ctx->free_blocks.end() && !it->second.empty()) {
+        *out = it->second.back();
+        it->second.pop_back();
+        ctx->bytes_cached -= cls;
+        ctx->bytes_in_use += cls;
+        return QT_OK;
+    }
+    if (ctx->memory_budget && ctx->bytes_in_use + cls > ctx->memory_budget)
+        return set_error(ctx, QT_ERR_OUT_OF_MEMORY, "device memory budget exceeded");
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, cls);
+    if (e == cudaErrorMemoryAllocation) {
+        // give the cached blocks back and retry once
+        cudaGetLastError();
+        for (auto &kv : ctx->free_blocks)
+            for (void *q : kv.second) {
+                cudaFree(q);
+                ctx->block_size.erase(q);
+            }
+        ctx->free_blocks.clear();
+        ctx->bytes_cached = 0;
+        e = cudaMalloc(&p, cls);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_error(ctx, e, "cudaMalloc");
+    }
+    ctx->block_size[p] = cls;
+    ctx->bytes_in_use += cls;
+    *out = p;
+    return QT_OK;
+}
+
+void dev_free(qt_ctx *ctx, void *p) {
+    if (!p) return;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    auto it = ctx->block_size.find(p);
+    if (it == ctx->block_size.end()) return;
+    ctx->free_blocks[it->second].push_back(p);
+    ctx->bytes_in_use -= it->second;
+    ctx->bytes_cached += it->second;
+}
+
+qt_status ensure_pinned(qt_ctx *ctx, size_t bytes) {
+    if (ctx->pinned_bytes >= bytes) return QT_OK;
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    ctx->pinned = nullptr;
+    ctx->pinned_bytes = 0;
+    size_t want = 1 << 20;
+    while (want < bytes) want <<= 1;
+    cudaError_t e = cudaMallocHost(&ctx->pinned, want);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "cudaMallocHost");
+    ctx->pinned_bytes = want;
+    return QT_OK;
+}
+
+bool deadline_passed(qt_ctx *ctx) {
+    return ctx->has_deadline && std::chrono::steady_clock::now() > ctx->deadline;
+}
+
+qt_status make_step(int rank_a, int rank_b, int n_free, const uint8_t *free_from_a, const int32_t *free_idx,
+                    int n_sum, const int32_t *sum_a, const int32_t *sum_b, StepDesc *d) {
+    if (rank_a < 0 || rank_b < 0 || rank_a > kMaxWires || rank_b > kMaxWires || n_free < 0 || n_sum < 0 ||
+        n_free > kMaxWires || n_sum > kMaxWires)
+        return QT_ERR_INVALID_ARGUMENT;
+    if (n_free + 2 * n_sum != rank_a + rank_b) return QT_ERR_INVALID_ARGUMENT;
+    std::memset(d, 0, sizeof(*d));
+    d->rA = (uint8_t) rank_a;
+    d->rB = (uint8_t) rank_b;
+    d->nFree = (uint8_t) n_free;
+    d->nSum = (uint8_t) n_sum;
+    int seenA[kMaxWires] = {0}, seenB[kMaxWires] = {0};
+    int fa = 0, fb = 0;
+    for (int i = 0; i < n_free; i++) {
+        const int w = free_idx[i];
+        if (free_from_a[i]) {
+            if (w < 0 || w >= rank_a || seenA[w]++) return QT_ERR_INVALID_ARGUMENT;
+            d->cA[i] = (uint8_t) w;
+            d->cB[i] = kNoWire;
+            fa++;
+        } else {
+            if (w < 0 || w >= rank_b || seenB[w]++) return QT_ERR_INVALID_ARGUMENT;
+            d->cB[i] = (uint8_t) w;
+            d->cA[i] = kNoWire;
+            fb++;
+        }
+    }
+    for (int j = 0; j < n_sum; j++) {
+        const int wa = sum_a[j], wb = sum_b[j];
+        if (wa < 0 || wa >= rank_a || seenA[wa]++) return QT_ERR_INVALID_ARGUMENT;
+        if (wb < 0 || wb >= rank_b || seenB[wb]++) return QT_ERR_INVALID_ARGUMENT;
+        // digit i of k <-> pair n_sum-1-i (src/Network.h:912-916)
+        d->posAs[n_sum - 1 - j] = (uint8_t) wa;
+        d->posBs[n_sum - 1 - j] = (uint8_t) wb;
+    }
+    d->fA = (uint8_t) fa;
+    d->fB = (uint8_t) fb;
+    d->a_step = d->b_step = -1;
+    return QT_OK;
+}
+
+}  // namespace qtg
+
+using namespace qtg;
+
+extern "C" {
+
+const char *qt_status_string(qt_status s) {
+    switch (s) {
+        case QT_OK: return "ok";
+        case QT_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case QT_ERR_INVALID_FILE: return "Invalid Input or Output File Path";
+        case QT_ERR_INVALID_FILE_FORMAT: return "Invalid File Format.";
+        case QT_ERR_CONTRACTION_FAILURE: return "Contraction Failed.";
+        case QT_ERR_INVALID_USER_SEQUENCE: return "Invalid User Defined Contraction Sequence.";
+        case QT_ERR_INVALID_FUNCTION_INPUT: return "Input to Function Invalid.";
+        case QT_ERR_INVALID_CONTRACTION_METHOD: return "Invalid Contraction Method.";
+        case QT_ERR_REFUSED: return "contraction refused";
+        case QT_ERR_OUT_OF_MEMORY: return "out of device memory or over the memory budget";
+        case QT_ERR_CUDA: return "CUDA error";
+        case QT_ERR_DEADLINE: return "deadline expired";
+        case QT_ERR_NO_DEVICE: return "no usable CUDA device";
+        case QT_ERR_BUSY: return "not enough free budget right now";
+    }
+    return "unknown status";
+}
+
+qt_status qt_ctx_create(int device, void *stream, qt_ctx **out) {
+    if (!out) return QT_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) {
+        cudaGetLastError();
+        return QT_ERR_NO_DEVICE;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return QT_ERR_NO_DEVICE;
+    // the kernels are built for sm_103a only
+    if (prop.major != 10 || prop.minor != 3) return QT_ERR_NO_DEVICE;
+    if (cudaSetDevice(device) != cudaSuccess) return QT_ERR_NO_DEVICE;
+    qt_ctx *ctx = new (std::nothrow) qt_ctx();
+    if (!ctx) return QT_ERR_OUT_OF_MEMORY;
+    ctx->device = device;
+    if (stream) {
+        ctx->stream = (cudaStream_t) stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete ctx;
+            return QT_ERR_CUDA;
+        }
+        ctx->own_stream = true;
+    }
+    *out = ctx;
+    return QT_OK;
+}
+
+qt_status qt_ctx_destroy(qt_ctx *ctx) {
+    if (!ctx) return QT_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto &kv : ctx->free_blocks)
+        for (void *p : kv.second) cudaFree(p);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return QT_OK;
+}
+
+qt_status qt_ctx_synchronize(qt_ctx *ctx) {
+    if (!ctx) return QT_ERR_INVALID_ARGUMENT;
+    return cuda_error(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+}
+
+size_t qt_last_error(qt_ctx *ctx, char *buf, size_t cap) {
+    if (!ctx) return 0;
+    std::lock_guard<std::mutex> g(ctx->err_lock);
+    if (buf && cap) {
+        size_t n = ctx->last_error.size() < cap - 1 ? ctx->last_error.size() : cap - 1;
+        std::memcpy(buf, ctx->last_error.data(), n);
+        buf[n] = 0;
+    }
+    return ctx->last_error.size();
+}
+
+qt_status qt_ctx_set_memory_budget(qt_ctx *ctx, uint64_t bytes) {
+    if (!ctx) return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    ctx->memory_budget = bytes;
+    return QT_OK;
+}
+
+qt_status qt_ctx_set_deadline(qt_ctx *ctx, double seconds) {
+    if (!ctx) return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    if (seconds <= 0) {
+        ctx->has_deadline = false;
+    } else {
+        ctx->has_deadline = true;
+        ctx->deadline = std::chrono::steady_clock::now() +
+                        std::chrono::duration_cast<std::chrono::steady_clock::duration>(std::chrono::duration<double>(seconds));
+    }
+    return QT_OK;
+}
+
+uint64_t qt_ctx_kernel_launches(const qt_ctx *ctx) { return ctx ? ctx->launches.load() : 0; }
+
+qt_status qt_tensor_create(qt_ctx *ctx, int rank, qt_dtype dtype, qt_tensor **out) {
+    if (!ctx || !out || rank < 0 || rank > kMaxWires || (dtype != QT_C128 && dtype != QT_C64)) return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    qt_tensor *t = new (std::nothrow) qt_tensor();
+    if (!t) return QT_ERR_OUT_OF_MEMORY;
+    t->rank = rank;
+    t->dtype = dtype;
+    t->bytes = (size_t) elem_bytes(dtype) << (2 * rank);
+    qt_status s = dev_alloc(ctx, t->bytes, &t->ptr);
+    if (s != QT_OK) {
+        delete t;
+        return s;
+    }
+    cudaError_t e = cudaMemsetAsync(t->ptr, 0, t->bytes, ctx->stream);
+    if (e != cudaSuccess) {
+        dev_free(ctx, t->ptr);
+        delete t;
+        return cuda_error(ctx, e, "cudaMemsetAsync");
+    }
+    *out = t;
+    return QT_OK;
+}
+
+qt_status qt_tensor_free(qt_ctx *ctx, qt_tensor *t) {
+    if (!ctx || !t) return QT_ERR_INVALID_ARGUMENT;
+    // blocks go back to the cache; stream order keeps later reuse safe
+    dev_free(ctx, t->ptr);
+    delete t;
+    return QT_OK;
+}
+
+qt_status qt_tensor_upload(qt_ctx *ctx, qt_tensor *t, const void *host, size_t bytes) {
+    if (!ctx || !t || !host || bytes != t->bytes) return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    cudaError_t e = cudaMemcpyAsync(t->ptr, host, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return cuda_error(ctx, e, "upload");
+}
+
+qt_status qt_tensor_download(qt_ctx *ctx, const qt_tensor *t, void *host, size_t bytes) {
+    if (!ctx || !t || !host || bytes != t->bytes) return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    cudaError_t e = cudaMemcpyAsync(host, t->ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return cuda_error(ctx, e, "download");
+}
+
+int qt_tensor_rank(const qt_tensor *t) { return t ? t->rank : -1; }
+qt_dtype qt_tensor_dtype(const qt_tensor *t) { return t ? t->dtype : QT_C128; }
+void *qt_tensor_device_ptr(const qt_tensor *t) { return t ? t->ptr : nullptr; }
+
+qt_status qt_contract_pair_device(qt_ctx *ctx, const void *a, int rank_a, const void *b, int rank_b, int n_free,
+                                  const uint8_t *free_from_a, const int32_t *free_idx, int n_sum,
+                                  const int32_t *sum_a, const int32_t *sum_b, void *c) {
+    if (!ctx || !a || !b || !c) return QT_ERR_INVALID_ARGUMENT;
+    if ((n_free && (!free_from_a || !free_idx)) || (n_sum && (!sum_a || !sum_b))) return QT_ERR_INVALID_ARGUMENT;
+    StepDesc d;
+    qt_status s = make_step(rank_a, rank_b, n_free, free_from_a, free_idx, n_sum, sum_a, sum_b, &d);
+    if (s != QT_OK) return set_error(ctx, s, "index maps do not describe a contraction of these ranks");
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    if (deadline_passed(ctx)) return set_error(ctx, QT_ERR_DEADLINE, "deadline expired");
+    cudaError_t e = launch_pair(d, a, b, c, true, ctx->stream);
+    ctx->launches++;
+    return cuda_error(ctx, e, "pair kernel launch");
+}
+
+qt_status qt_contract_pair(qt_ctx *ctx, const qt_tensor *a, const qt_tensor *b, int n_free,
+                           const uint8_t *free_from_a, const int32_t *free_idx, int n_sum,
+                           const int32_t *sum_a, const int32_t *sum_b, qt_tensor **c_out) {
+    if (!ctx || !a || !b || !c_out) return QT_ERR_INVALID_ARGUMENT;
+    // an operand without data is the reference's InvalidFunctionInput (Network.h:938-940)
+    if (!a->ptr || !b->ptr) return set_error(ctx, QT_ERR_INVALID_FUNCTION_INPUT, "operand holds no data");
+    if (a->dtype != b->dtype) return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "operand dtypes differ");
+    if ((n_free && (!free_from_a || !free_idx)) || (n_sum && (!sum_a || !sum_b))) return QT_ERR_INVALID_ARGUMENT;
+    StepDesc d;
+    qt_status s = make_step(a->rank, b->rank, n_free, free_from_a, free_idx, n_sum, sum_a, sum_b, &d);
+    if (s != QT_OK) return set_error(ctx, s, "index maps do not describe a contraction of these ranks");
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    if (deadline_passed(ctx)) return set_error(ctx, QT_ERR_DEADLINE, "deadline expired");
+    qt_tensor *c = new (std::nothrow) qt_tensor();
+    if (!c) return QT_ERR_OUT_OF_MEMORY;
+    c->rank = n_free;
+    c->dtype = a->dtype;
+    c->bytes = (size_t) elem_bytes(c->dtype) << (2 * n_free);
+    s = dev_alloc(ctx, c->bytes, &c->ptr);
+    if (s != QT_OK) {
+        delete c;
+        return s;
+    }
+    // every output element is written by the kernel; no zero fill needed
+    cudaError_t e = launch_pair(d, a->ptr, b->ptr, c->ptr, a->dtype == QT_C128, ctx->stream);
+    ctx->launches++;
+    if (e != cudaSuccess) {
+        dev_free(ctx, c->ptr);
+        delete c;
+        return cuda_error(ctx, e, "pair kernel launch");
+    }
+    *c_out = c;
+    return QT_OK;
+}
+
+qt_status qt_contract_pair_host(qt_ctx *ctx, const double *a, int rank_a, const double *b, int rank_b, int n_free,
+                                const uint8_t *free_from_a, const int32_t *free_idx, int n_sum, const int32_t *sum_a,
+                                const int32_t *sum_b, double *c) {
+    if (!ctx || !a || !b || !c) return QT_ERR_INVALID_ARGUMENT;
+    if (rank_a < 0 || rank_b < 0 || n_free < 0 || rank_a > kMaxWires || rank_b > kMaxWires || n_free > kMaxWires)
+        return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    const size_t ba = (size_t) 16 << (2 * rank_a), bb = (size_t) 16 << (2 * rank_b), bc = (size_t) 16 << (2 * n_free);
+    void *da = nullptr, *db = nullptr, *dc = nullptr;
+    qt_status s = dev_alloc(ctx, ba, &da);
+    if (s == QT_OK) s = dev_alloc(ctx, bb, &db);
+    if (s == QT_OK) s = dev_alloc(ctx, bc, &dc);
+    if (s == QT_OK) {
+        cudaError_t e = cudaMemcpyAsync(da, a, ba, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(db, b, bb, cudaMemcpyHostToDevice, ctx->stream);
+        s = cuda_error(ctx, e, "upload");
+    }
+    if (s == QT_OK)
+        s = qt_contract_pair_device(ctx, da, rank_a, db, rank_b, n_free, free_from_a, free_idx, n_sum, sum_a, sum_b, dc);
+    if (s == QT_OK) {
+        cudaError_t e = cudaMemcpyAsync(c, dc, bc, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        s = cuda_error(ctx, e, "download");
+    }
+    dev_free(ctx, da);
+    dev_free(ctx, db);
+    dev_free(ctx, dc);
+    return s;
+}
+
+}  // extern "C"

@@ -1,0 +1,59 @@
+// Internal structures of the C ABI: context, caching device allocator, tensors.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <chrono>
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/qtorch_gb300.h"
+#include "engine.cuh"
+
+struct qt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::recursive_mutex lock;
+    std::string last_error;
+    std::mutex err_lock;
+    // caching allocator: size class (bytes, power of two >= 256) -> free blocks
+    std::map<size_t, std::vector<void *>> free_blocks;
+    std::map<void *, size_t> block_size;
+    uint64_t bytes_in_use = 0;
+    uint64_t bytes_cached = 0;
+    uint64_t memory_budget = 0;          // 0 = unlimited
+    std::atomic<uint64_t> launches{0};
+    bool has_deadline = false;
+    std::chrono::steady_clock::time_point deadline;
+    // pinned staging buffer for small host<->device transfers
+    void *pinned = nullptr;
+    size_t pinned_bytes = 0;
+};
+
+struct qt_tensor {
+    void *ptr = nullptr;
+    int rank = 0;
+    qt_dtype dtype = QT_C128;
+    size_t bytes = 0;
+};
+
+namespace qtg {
+
+qt_status set_error(qt_ctx *ctx, qt_status s, const std::string &msg);
+qt_status cuda_error(qt_ctx *ctx, cudaError_t e, const char *what);
+// allocate from the context cache (bytes rounded up to a size class)
+qt_status dev_alloc(qt_ctx *ctx, size_t bytes, void **out);
+void dev_free(qt_ctx *ctx, void *p);
+qt_status ensure_pinned(qt_ctx *ctx, size_t bytes);
+bool deadline_passed(qt_ctx *ctx);
+inline size_t elem_bytes(qt_dtype d) { return d == QT_C128 ? 16 : 8; }
+
+// Fill a StepDesc from the reference's index lists (toNotSumOn, toSumOn).
+qt_status make_step(int rank_a, int rank_b, int n_free, const uint8_t *free_from_a, const int32_t *free_idx,
+                    int n_sum, const int32_t *sum_a, const int32_t *sum_b, StepDesc *d);
+
+}  // namespace qtg

@@ -1,0 +1,88 @@
+// Device-side data structures shared by the host planner and the kernels.
+//
+// A contraction step computes C[c] = sum_k A[a(c,k)] * B[b(c,k)] (the
+// reference's ContractIndices, src/Network.h:876-971).  Digit i of C's flat
+// index c is wire cA[i] of A or wire cB[i] of B (the other entry is kNoWire),
+// as toNotSumOn says; ContractNodes lists A's free wires first
+// (src/Network.h:738-769).  So
+//   a(c,k) = sum_{i: cA[i] set} digit_i(c) 4^cA[i] + scatter(k, posAs)
+//   b(c,k) = sum_{i: cB[i] set} digit_i(c) 4^cB[i] + scatter(k, posBs)
+// where scatter(x, pos) places base-4 digit i of x at wire pos[i].  posAs/posBs
+// are stored in the reference's inner-loop digit order (digit i of k <-> pair
+// nSum-1-i, Network.h:912-916) so that k itself walks the reference's order.
+#pragma once
+#include <cstdint>
+
+namespace qtg {
+
+constexpr int kMaxWires = 24;      // rank limit of one operand (4^24 elements is far beyond HBM)
+constexpr uint8_t kNoWire = 0xff;
+
+enum StepFlags : uint32_t {
+    kALeaf = 1u << 0,        // A is read from the leaf buffer (else workspace)
+    kBLeaf = 1u << 1,
+    kAF64 = 1u << 2,         // A stored as complex128 (mixed plans only; FP64 plans are all complex128)
+    kBF64 = 1u << 3,
+    kCF64 = 1u << 4,         // C computed with FP64 accumulation and stored as complex128
+    kOutRank0 = 1u << 5,     // C has rank 0: it takes part in the final-value rule
+    kBothRank0 = 1u << 6,    // A and B both rank 0 (Network.h:963)
+};
+
+struct StepDesc {
+    int64_t a_off;           // byte offset into the leaf buffer or the workspace
+    int64_t b_off;
+    int64_t c_off;           // byte offset into the workspace
+    int32_t a_step;          // step that produced A (-1 for a leaf): its scale exponent applies
+    int32_t b_step;
+    uint32_t flags;
+    uint8_t rA, rB, nFree, nSum, fA, fB, pad0, pad1;
+    uint8_t cA[kMaxWires];       // C digit -> A wire (kNoWire if the digit belongs to B)
+    uint8_t cB[kMaxWires];       // C digit -> B wire (kNoWire if the digit belongs to A)
+    uint8_t posAs[kMaxWires];
+    uint8_t posBs[kMaxWires];
+};
+static_assert(sizeof(StepDesc) % 8 == 0, "StepDesc alignment");
+
+// One executable plan in device memory.
+struct PlanDesc {
+    const StepDesc *steps;       // sorted by level
+    const int32_t *level_start;  // n_levels + 1 entries
+    const int32_t *rank0_steps;  // steps with a rank-0 output, in contraction (sequence) order
+    int32_t n_steps;
+    int32_t n_levels;
+    int32_t n_rank0;
+    int32_t pad;
+};
+
+// One instance of a batch: a plan with its own leaves.  Intermediates live in
+// the workspace of the CTA that runs the instance.
+struct InstanceDesc {
+    const PlanDesc *plan;        // device pointer
+    const char *leaves;          // leaf buffer of this instance (complex128, or complex64 in mixed mode)
+    double *value;               // 2 doubles out
+};
+
+// What one CTA works with while it interprets an instance.
+struct CtaScratch {
+    char *workspace;             // intermediate tensors
+    int32_t *exps;               // per-step power-of-two exponent (mixed precision)
+};
+
+__host__ __device__ inline uint64_t scatter_digits(uint64_t x, const uint8_t *pos, int n) {
+    uint64_t off = 0;
+    for (int i = 0; i < n; i++) off += ((x >> (2 * i)) & 3ull) << (2 * pos[i]);
+    return off;
+}
+
+// Offsets of output element c inside A and B.
+__host__ __device__ inline void scatter_c(uint64_t c, const StepDesc &d, uint64_t &oa, uint64_t &ob) {
+    oa = 0;
+    ob = 0;
+    for (int i = 0; i < d.nFree; i++) {
+        const uint64_t dig = (c >> (2 * i)) & 3ull;
+        if (d.cA[i] != kNoWire) oa += dig << (2 * d.cA[i]);
+        else ob += dig << (2 * d.cB[i]);
+    }
+}
+
+}  // namespace qtg

@@ -1,0 +1,372 @@
+// Contraction orderings on top of Network::ContractNodes.
+//
+//   ContractionTools::ParallelContract   src/ContractionTools.h:219-388, 1261-1279
+//   ContractionTools::ContractGivenSequence                  :392-411
+//   ContractionTools::ContractUserDefinedSequenceOfWires     :155-214
+//   LineGraph (wire numbering, line-graph edges)     src/LineGraph.h:92-171
+//   LineGraph::LGContract walk                       src/LineGraph.h:357-376
+//   Network::ReduceCircuit                           src/Network.h:1015-1118
+//
+// Differences from the reference, on purpose:
+//  * the stochastic ordering draws from one std::mt19937 with a caller-given
+//    seed and runs the two partition loops one after the other, so an ordering
+//    is reproducible (the reference seeds from std::random_device and lets two
+//    threads share one generator);
+//  * the line-graph elimination order comes from a min-fill heuristic computed
+//    here instead of the external QuickBB binary (which the reference calls
+//    with --min-fill-ordering).
+#include <algorithm>
+#include <cmath>
+#include <fstream>
+#include <set>
+#include <sstream>
+
+#include "../../include/qtorch/qtorch.hpp"
+
+namespace qtorch {
+
+// ===========================================================================
+// ContractionTools
+
+ContractionTools::ContractionTools(const std::string &inputFile, const std::string &measureFile, int numThreads)
+    : mString(inputFile), mMeasureFile(measureFile), mRandGen(std::random_device()()), mCopyCreated(false),
+      mNumThreadsInNetwork(numThreads) {}
+
+ContractionTools::ContractionTools(std::shared_ptr<Network> network)
+    : mNetwork(network), mRandGen(std::random_device()()), mCopyCreated(true) {}
+
+void ContractionTools::Reset() {
+    mNetwork = nullptr;
+    mCopyCreated = false;
+}
+
+void ContractionTools::Reset(const std::string &inputFile, const std::string &measureFile, int numThreads) {
+    mNetwork = nullptr;
+    mCopyCreated = false;
+    mString = inputFile;
+    mMeasureFile = measureFile;
+    mNumThreadsInNetwork = numThreads;
+}
+
+std::shared_ptr<Network> ContractionTools::Acquire() {
+    if (!mCopyCreated) {
+        mNetwork = std::make_shared<Network>(mString, mMeasureFile);
+        mNetwork->SetNumThreads(mNumThreadsInNetwork);
+    }
+    return mNetwork;
+}
+
+std::shared_ptr<Network> ContractionTools::Contract(ContractionType type, int, int) {
+    if (type == Stochastic) return ParallelContract(mRandGen);
+    throw InvalidContractionMethod();
+}
+
+std::shared_ptr<Network> ContractionTools::ParallelContract(std::mt19937 &gen) {
+    std::shared_ptr<Network> net = Acquire();
+    if (net->HasFailed()) return nullptr;
+    // CreateChunksOfNodes: partitions of size n/2, the remainder last (ContractionTools.h:1261-1279)
+    const std::vector<std::shared_ptr<Node>> &all = net->GetUncontractedNodes();
+    std::vector<std::vector<std::shared_ptr<Node>>> parts;
+    {
+        const int size = (int) all.size();
+        int skip = size / 2, counter = 0;
+        size_t it = 0;
+        while (it < all.size() && skip > 0) {
+            parts.emplace_back(all.begin() + it, all.begin() + it + skip);
+            it += skip;
+            counter += skip;
+            if (size - counter < skip) skip = size - counter;
+        }
+        if (it < all.size()) parts.emplace_back(all.begin() + it, all.end());
+    }
+    auto remove_pair = [](std::vector<std::shared_ptr<Node>> &v, int one, int two) {
+        if (two == (int) v.size() - 1) {
+            v[two] = v.back();
+            v.pop_back();
+            v[one] = v.back();
+            v.pop_back();
+        } else {
+            v[one] = v.back();
+            v.pop_back();
+            v[two] = v.back();
+            v.pop_back();
+        }
+    };
+    // contractPieceFunction (ContractionTools.h:248-305), threshold 1
+    for (auto &part : parts) {
+        int failures = 0;
+        while (part.size() != 1 && failures < (int) std::pow(part.size(), 2)) {
+            std::uniform_int_distribution<> dist(0, (int) part.size() - 1);
+            const int one = dist(gen), two = dist(gen);
+            if (one == two) continue;
+            auto r = net->ContractNodes(part[one], part[two], 1);
+            if (r) {
+                remove_pair(part, one, two);
+                failures = 0;
+                part.push_back(r);
+            } else if (!net->IsDone()) {
+                failures++;
+            } else {
+                break;
+            }
+        }
+    }
+    // contractNodesLeftFunction (ContractionTools.h:309-356), adaptive threshold from -1
+    std::vector<std::shared_ptr<Node>> left;
+    for (auto &part : parts) left.insert(left.end(), part.begin(), part.end());
+    int threshold = -1, fails = 0;
+    while (!net->IsDone()) {
+        if (fails > std::pow(left.size(), 2)) {
+            threshold++;
+            fails = 0;
+        }
+        std::uniform_int_distribution<> dist(0, (int) left.size() - 1);
+        const int one = dist(gen), two = dist(gen);
+        if (one == two || left[one]->mContracted || left[two]->mContracted) continue;
+        auto r = net->ContractNodes(left[one], left[two], threshold);
+        if (r) {
+            remove_pair(left, one, two);
+            left.push_back(r);
+            fails = 0;
+            threshold = -1;
+        } else {
+            fails++;
+        }
+    }
+    mFinalVal = net->GetFinalValue();
+    return net;
+}
+
+std::shared_ptr<Network> ContractionTools::ContractGivenSequence(const std::vector<std::pair<int, int>> &sequence) {
+    std::shared_ptr<Network> net = Acquire();
+    if (net->HasFailed()) return nullptr;
+    for (const auto &p : sequence) {
+        const auto &all = net->GetAllNodes();
+        if (p.first < 0 || p.second < 0 || p.first >= (int) all.size() || p.second >= (int) all.size())
+            throw ContractionFailure();
+        net->ContractNodes(all[p.first], all[p.second], 100);
+    }
+    if (!net->IsDone()) throw ContractionFailure();
+    mFinalVal = net->GetFinalValue();
+    return net;
+}
+
+std::shared_ptr<Network> ContractionTools::ContractUserDefinedSequenceOfWires(const std::string &path) {
+    std::ifstream in(path);
+    if (!in) throw InvalidFile();
+    std::stringstream ss;
+    ss << in.rdbuf();
+    return ContractUserDefinedSequenceText(ss.str());
+}
+
+std::shared_ptr<Network> ContractionTools::ContractUserDefinedSequenceText(const std::string &text) {
+    std::shared_ptr<Network> net = Acquire();
+    if (net->HasFailed()) return nullptr;
+    // one "a b" pair per line, every line read (ContractionTools.h:168-186)
+    std::vector<std::pair<int, int>> order;
+    std::istringstream in(text);
+    std::string line;
+    const int n = (int) net->GetAllNodes().size();
+    while (std::getline(in, line)) {
+        std::istringstream ls(line);
+        int a, b;
+        if (!(ls >> a >> b)) continue;
+        if (a < 0 || a > n || b < 0 || b > n) throw InvalidFileFormat();
+        order.push_back({a, b});
+    }
+    std::vector<int> map(net->GetAllNodes().size());
+    for (size_t i = 0; i < map.size(); i++) map[i] = (int) i;
+    for (const auto &p : order) {
+        if (p.first >= (int) map.size() || p.second >= (int) map.size()) throw InvalidUserContractionSequence();
+        const auto &all = net->GetAllNodes();
+        auto a = all[map[p.first]], b = all[map[p.second]];
+        if (a->mContracted || b->mContracted) continue;
+        net->ContractNodes(a, b, 10000);
+        map[p.first] = (int) net->GetAllNodes().size() - 1;
+        map[p.second] = (int) net->GetAllNodes().size() - 1;
+    }
+    if (!net->IsDone()) throw InvalidUserContractionSequence();
+    mFinalVal = net->GetFinalValue();
+    return net;
+}
+
+// ===========================================================================
+// LineGraph
+
+LineGraph::LineGraph(std::shared_ptr<Network> network) : mNetwork(network) { Build(); }
+
+void LineGraph::Reset(std::shared_ptr<Network> network) {
+    if (!network) {
+        mNetwork->Reset();
+    } else {
+        mNetwork = network;
+    }
+    Build();
+}
+
+void LineGraph::Build() {
+    mGraphWires.clear();
+    mEdges.clear();
+    mOrder.clear();
+    // wire ids in first-seen order over the uncontracted nodes; every pair of
+    // wires of one node is a line-graph edge (LineGraph.h:92-130)
+    for (const auto &n : mNetwork->GetUncontractedNodes()) {
+        auto &ws = n->GetWires();
+        for (size_t w = 0; w < ws.size(); w++) {
+            auto &wire = ws[w];
+            if (std::find(mGraphWires.begin(), mGraphWires.end(), wire) == mGraphWires.end()) {
+                wire->SetWireID((int) mGraphWires.size());
+                mGraphWires.push_back(wire);
+            }
+            for (size_t w2 = 0; w2 < w; w2++) mEdges.push_back({ws[w2]->GetWireID(), wire->GetWireID()});
+        }
+    }
+}
+
+const std::vector<int> &LineGraph::MinFillOrdering() {
+    if (!mOrder.empty() || mGraphWires.empty()) return mOrder;
+    const int n = (int) mGraphWires.size();
+    std::vector<std::set<int>> adj(n);
+    for (auto &e : mEdges) {
+        if (e[0] == e[1]) continue;
+        adj[e[0]].insert(e[1]);
+        adj[e[1]].insert(e[0]);
+    }
+    std::vector<char> gone(n, 0);
+    auto fill_of = [&](int v) {
+        long long fill = 0;
+        for (auto i = adj[v].begin(); i != adj[v].end(); ++i) {
+            auto j = i;
+            for (++j; j != adj[v].end(); ++j)
+                if (!adj[*i].count(*j)) fill++;
+        }
+        return fill;
+    };
+    // greedy min-fill: fewest added edges, then smallest degree, then smallest id
+    for (int step = 0; step < n; step++) {
+        int best = -1;
+        long long bestFill = 0;
+        size_t bestDeg = 0;
+        for (int v = 0; v < n; v++) {
+            if (gone[v]) continue;
+            const long long f = fill_of(v);
+            if (best < 0 || f < bestFill || (f == bestFill && adj[v].size() < bestDeg)) {
+                best = v;
+                bestFill = f;
+                bestDeg = adj[v].size();
+            }
+        }
+        gone[best] = 1;
+        mOrder.push_back(best + 1);
+        std::vector<int> nb(adj[best].begin(), adj[best].end());
+        for (size_t i = 0; i < nb.size(); i++)
+            for (size_t j = i + 1; j < nb.size(); j++) {
+                adj[nb[i]].insert(nb[j]);
+                adj[nb[j]].insert(nb[i]);
+            }
+        for (int u : nb) adj[u].erase(best);
+        adj[best].clear();
+    }
+    return mOrder;
+}
+
+bool LineGraph::LGContract() { return LGContract(MinFillOrdering()); }
+
+bool LineGraph::LGContract(const std::vector<int> &order) {
+    // contract both endpoints of each not yet contracted wire, threshold 100 (LineGraph.h:357-376)
+    for (int id1 : order) {
+        if (id1 < 1 || id1 > (int) mGraphWires.size()) throw QbbFailure();
+        auto &w = mGraphWires[id1 - 1];
+        if (w->IsContracted()) continue;
+        auto a = w->GetNodeA().lock(), b = w->GetNodeB().lock();
+        if (!a || !b) continue;
+        mNetwork->ContractNodes(a, b, 100);
+    }
+    const auto &rem = mNetwork->GetUncontractedNodes();
+    if (rem.size() != 1) throw ContractionFailure();
+    if (rem[0]->mRank != 0) throw ContractionFailure();
+    return true;
+}
+
+// ===========================================================================
+// ReduceCircuit (src/Network.h:1015-1118): fold rank-2 gates into their
+// predecessor on the wire, then merge consecutive two-qubit gates on the same
+// pair of wires.
+
+void Network::ReduceCircuit() {
+    std::vector<std::vector<std::shared_ptr<Node>>> holder(mNumberOfQubits);
+    for (int i = 0; i < mNumberOfQubits; i++) {
+        for (auto &node : mNodesByWire[i]) {
+            if (node->mRank == 2) {
+                std::shared_ptr<Node> prev = holder[i].back();
+                std::shared_ptr<Node> t = ContractNodes(prev, node, 0);
+                if (!t) throw ContractionFailure();
+                auto in0 = node->GetWires()[0]->GetNodeA().lock();
+                t->AddWireNumber(in0->GetWireNumber()[0]);
+                if (in0->mRank > 2) t->AddWireNumber(in0->GetWireNumber()[1]);
+                if (prev->GetTypeOfNode() == GateType::INITSTATE) {
+                    t->SetTypeOfNode(GateType::INITSTATE);
+                    t->SetTypeOfNodeString("INITSTATE(Manipulated)");
+                }
+                FindAndReplace(mNodesByWire, prev, t);
+                FindAndReplace(holder, prev, t);
+            } else {
+                holder[i].push_back(node);
+            }
+        }
+    }
+    mNodesByWire = std::move(holder);
+
+    std::vector<std::vector<std::shared_ptr<Node>>> next(mNumberOfQubits);
+    std::vector<std::shared_ptr<Node>> current(mNumberOfQubits);
+    std::vector<int> idx(mNumberOfQubits, 0);
+    std::vector<bool> updated(mNumberOfQubits, false);
+    bool finished = false, found = false;
+    while (!finished) {
+        for (int j = 0; j < mNumberOfQubits; j++) {
+            if (idx[j] >= (int) mNodesByWire[j].size() || updated[j]) continue;
+            std::shared_ptr<Node> t = mNodesByWire[j][idx[j]];
+            if (t->mRank == 1) {
+                current[j] = t;
+                updated[j] = true;
+                idx[j]++;
+                continue;
+            }
+            const int w0 = t->GetWireNumber()[0], w1 = t->GetWireNumber()[1];
+            if (!updated[w1] && !updated[w0]) {
+                if (idx[w0] < (int) mNodesByWire[w0].size() && idx[w1] < (int) mNodesByWire[w1].size() &&
+                    mNodesByWire[w0][idx[w0]] == mNodesByWire[w1][idx[w1]]) {
+                    if (current[w0] == current[w1] && current[w0]) {
+                        current[w0] = ContractNodes(t, current[w0], 0);
+                        if (!current[w0]) throw ContractionFailure();
+                        current[w1] = current[w0];
+                        current[w0]->AddWireNumber(w0);
+                        current[w0]->AddWireNumber(w1);
+                        found = true;
+                    } else {
+                        current[w0] = t;
+                        current[w1] = t;
+                    }
+                    idx[w0]++;
+                    idx[w1]++;
+                    updated[w0] = true;
+                    updated[w1] = true;
+                }
+            }
+        }
+        for (int j = 0; j < mNumberOfQubits; j++) {
+            if (updated[j]) {
+                if (found && !next[j].empty()) next[j].back() = current[j];
+                else next[j].push_back(current[j]);
+            } else if (idx[j] < (int) mNodesByWire[j].size() && !found) {
+                next[j].push_back(nullptr);
+            }
+        }
+        if (std::all_of(updated.begin(), updated.end(), [](bool b) { return !b; })) finished = true;
+        std::fill(updated.begin(), updated.end(), false);
+        found = false;
+    }
+    mNodesByWire = std::move(next);
+}
+
+}  // namespace qtorch

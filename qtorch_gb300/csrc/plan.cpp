@@ -1,0 +1,380 @@
+// Plans and batches: an ordering is run once over a symbolic copy of the
+// network (the same ContractNodes bookkeeping, no data), every contraction is
+// recorded, and the record is lowered to device step descriptors:
+//   * steps are grouped into dependency levels (all steps of a level are
+//     independent and run concurrently inside one CTA);
+//   * intermediates get workspace offsets from a first-fit allocator driven by
+//     liveness across levels;
+//   * leaves (state, gate and measurement tensors) are bound per instance, so
+//     one plan serves every parameter point of a circuit structure.
+// Small plans run in the grouped interpreter (one CTA per instance, one launch
+// for a whole batch); plans with large intermediates run step by step with the
+// whole-GPU pairwise kernel.
+#include "plan.h"
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <new>
+
+#include "kernels.h"
+
+namespace qtg {
+
+static uint64_t align_up(uint64_t x, uint64_t a) { return (x + a - 1) / a * a; }
+
+// first-fit allocator over a linear workspace
+class OffsetAllocator {
+public:
+    uint64_t alloc(uint64_t bytes) {
+        bytes = align_up(bytes ? bytes : 1, 256);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= bytes) {
+                const uint64_t off = it->first, sz = it->second;
+                free_.erase(it);
+                if (sz > bytes) free_[off + bytes] = sz - bytes;
+                return off;
+            }
+        }
+        const uint64_t off = top_;
+        top_ += bytes;
+        return off;
+    }
+    void release(uint64_t off, uint64_t bytes) {
+        bytes = align_up(bytes ? bytes : 1, 256);
+        auto it = free_.emplace(off, bytes).first;
+        // coalesce with the next and the previous block
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    uint64_t high_water() const { return top_; }
+private:
+    std::map<uint64_t, uint64_t> free_;
+    uint64_t top_ = 0;
+};
+
+qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
+    const auto &leaves = net.Leaves();
+    const auto &rec = net.Steps();
+    const int L = (int) leaves.size();
+    const int S = (int) rec.size();
+    // tensor ids: leaves 0..L-1, then one per step in creation order
+    std::map<int64_t, int> producer;   // tensor id -> step (contraction order)
+    for (int s = 0; s < S; s++) producer[rec[s].c] = s;
+    std::vector<int> level(S, 0);
+    int n_levels = 0;
+    for (int s = 0; s < S; s++) {
+        int la = 0, lb = 0;
+        auto ia = producer.find(rec[s].a), ib = producer.find(rec[s].b);
+        if (ia != producer.end()) la = level[ia->second];
+        if (ib != producer.end()) lb = level[ib->second];
+        level[s] = 1 + std::max(la, lb);
+        n_levels = std::max(n_levels, level[s]);
+    }
+    std::vector<int> order(S);
+    for (int s = 0; s < S; s++) order[s] = s;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return level[x] < level[y]; });
+    std::vector<int> sorted_of(S);
+    for (int i = 0; i < S; i++) sorted_of[order[i]] = i;
+    // consumer level of every intermediate tensor
+    std::map<int64_t, int> consumer_level;
+    for (int s = 0; s < S; s++) {
+        consumer_level[rec[s].a] = level[s];
+        consumer_level[rec[s].b] = level[s];
+    }
+    p->level_start.assign(n_levels + 1, 0);
+    for (int i = 0, L0 = 1; L0 <= n_levels; L0++) {
+        p->level_start[L0 - 1] = i;
+        while (i < S && level[order[i]] == L0) i++;
+        p->level_start[L0] = i;
+    }
+    p->rank0_steps.clear();
+    for (int s = 0; s < S; s++)
+        if (rec[s].freeIdx.empty()) p->rank0_steps.push_back(sorted_of[s]);
+
+    p->peak_rank = 0;
+    p->flops = 0;
+    p->max_step_out = 0;
+    p->max_step_k = 0;
+    for (int s = 0; s < S; s++) {
+        p->peak_rank = std::max<int>(p->peak_rank, (int) rec[s].freeIdx.size());
+        p->flops += (int64_t) 1 << (2 * (rec[s].freeIdx.size() + rec[s].sumIdx.size()));
+        p->max_step_out = std::max<int>(p->max_step_out, (int) rec[s].freeIdx.size());
+        p->max_step_k = std::max<int>(p->max_step_k, (int) rec[s].sumIdx.size());
+    }
+    for (int i = 0; i < L; i++) p->peak_rank = std::max(p->peak_rank, leaves[i]->mRank);
+
+    for (int prec = 0; prec < 2; prec++) {
+        const bool mixed = prec == QT_PREC_MIXED;
+        // leaf layout
+        uint64_t loff = 0;
+        std::vector<uint64_t> leaf_off(L);
+        for (int i = 0; i < L; i++) {
+            leaf_off[i] = loff;
+            loff = align_up(loff + ((uint64_t) (mixed ? 8 : 16) << (2 * leaves[i]->mRank)), 16);
+        }
+        p->leaf_bytes[prec] = loff;
+        p->leaf_off[prec] = leaf_off;
+        // workspace layout, level by level
+        OffsetAllocator alloc;
+        std::map<int64_t, std::pair<uint64_t, uint64_t>> live;   // tensor id -> (offset, bytes)
+        std::vector<uint64_t> c_off(S), c_bytes(S);
+        std::vector<bool> c_f64(S);
+        for (int L0 = 1; L0 <= n_levels; L0++) {
+            for (auto it = live.begin(); it != live.end();) {
+                auto cl = consumer_level.find(it->first);
+                // rank-0 outputs stay: the final-value rule reads all of them at the end
+                const bool keep = it->second.second <= 16;
+                if (!keep && cl != consumer_level.end() && cl->second < L0) {
+                    alloc.release(it->second.first, it->second.second);
+                    it = live.erase(it);
+                } else {
+                    ++it;
+                }
+            }
+            for (int i = p->level_start[L0 - 1]; i < p->level_start[L0]; i++) {
+                const int s = order[i];
+                const int nf = (int) rec[s].freeIdx.size();
+                // mixed plans keep the expectation-value reductions (outputs of rank <= 1) in FP64
+                const bool f64 = !mixed || nf <= kMixedTailRank;
+                const uint64_t bytes = (uint64_t) (f64 ? 16 : 8) << (2 * nf);
+                c_off[s] = alloc.alloc(bytes);
+                c_bytes[s] = bytes;
+                c_f64[s] = f64;
+                live[rec[s].c] = {c_off[s], bytes};
+            }
+        }
+        p->ws_bytes[prec] = align_up(alloc.high_water(), 256);
+        // descriptors in sorted order
+        std::vector<StepDesc> &steps = p->steps[prec];
+        steps.assign(S, StepDesc());
+        p->a_leaf.assign(S, -1);
+        p->b_leaf.assign(S, -1);
+        for (int i = 0; i < S; i++) {
+            const int s = order[i];
+            const auto &r = rec[s];
+            std::vector<uint8_t> ffa(r.freeIdx.size());
+            std::vector<int32_t> fi(r.freeIdx.size()), sa(r.sumIdx.size()), sb(r.sumIdx.size());
+            for (size_t k = 0; k < r.freeIdx.size(); k++) {
+                ffa[k] = r.freeIdx[k].first;
+                fi[k] = r.freeIdx[k].second;
+            }
+            for (size_t k = 0; k < r.sumIdx.size(); k++) {
+                sa[k] = r.sumIdx[k].first;
+                sb[k] = r.sumIdx[k].second;
+            }
+            StepDesc &d = steps[i];
+            qt_status st = make_step(r.rankA, r.rankB, (int) ffa.size(), ffa.data(), fi.data(), (int) sa.size(),
+                                     sa.data(), sb.data(), &d);
+            if (st != QT_OK) return st;
+            auto ia = producer.find(r.a), ib = producer.find(r.b);
+            d.flags = 0;
+            if (ia == producer.end()) {
+                d.flags |= kALeaf;
+                d.a_off = (int64_t) leaf_off[r.a];
+                p->a_leaf[i] = (int) r.a;
+                d.a_step = -1;
+                if (!mixed) d.flags |= kAF64;
+            } else {
+                d.a_off = (int64_t) c_off[ia->second];
+                d.a_step = sorted_of[ia->second];
+                if (c_f64[ia->second]) d.flags |= kAF64;
+            }
+            if (ib == producer.end()) {
+                d.flags |= kBLeaf;
+                d.b_off = (int64_t) leaf_off[r.b];
+                p->b_leaf[i] = (int) r.b;
+                d.b_step = -1;
+                if (!mixed) d.flags |= kBF64;
+            } else {
+                d.b_off = (int64_t) c_off[ib->second];
+                d.b_step = sorted_of[ib->second];
+                if (c_f64[ib->second]) d.flags |= kBF64;
+            }
+            d.c_off = (int64_t) c_off[s];
+            if (c_f64[s]) d.flags |= kCF64;
+            if (r.freeIdx.empty()) d.flags |= kOutRank0;
+            if (r.rankA == 0 && r.rankB == 0) d.flags |= kBothRank0;
+        }
+    }
+    p->n_steps = S;
+    p->n_levels = n_levels;
+    p->grouped = p->max_step_out <= kGroupedMaxRank && p->max_step_k <= kGroupedMaxSum &&
+                 p->ws_bytes[QT_PREC_FP64] <= kGroupedMaxWorkspace;
+    for (int i = 0; i < L; i++) p->peak_rank = std::max(p->peak_rank, leaves[i]->mRank);
+    return QT_OK;
+}
+
+qt_status upload_plan(qt_plan *p, int prec) {
+    qt_ctx *ctx = p->ctx;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    if (p->dev[prec]) return QT_OK;
+    const size_t steps_bytes = sizeof(StepDesc) * p->steps[prec].size();
+    const size_t lvl_bytes = sizeof(int32_t) * p->level_start.size();
+    const size_t r0_bytes = sizeof(int32_t) * (p->rank0_steps.size() + 1);
+    const size_t off_steps = align_up(sizeof(PlanDesc), 256);
+    const size_t off_lvl = align_up(off_steps + steps_bytes, 256);
+    const size_t off_r0 = align_up(off_lvl + lvl_bytes, 256);
+    const size_t total = off_r0 + r0_bytes;
+    void *d = nullptr;
+    qt_status s = dev_alloc(ctx, total, &d);
+    if (s != QT_OK) return s;
+    std::vector<char> host(total, 0);
+    PlanDesc pd;
+    pd.steps = reinterpret_cast<const StepDesc *>((char *) d + off_steps);
+    pd.level_start = reinterpret_cast<const int32_t *>((char *) d + off_lvl);
+    pd.rank0_steps = reinterpret_cast<const int32_t *>((char *) d + off_r0);
+    pd.n_steps = p->n_steps;
+    pd.n_levels = p->n_levels;
+    pd.n_rank0 = (int32_t) p->rank0_steps.size();
+    pd.pad = 0;
+    std::memcpy(host.data(), &pd, sizeof(pd));
+    if (steps_bytes) std::memcpy(host.data() + off_steps, p->steps[prec].data(), steps_bytes);
+    if (lvl_bytes) std::memcpy(host.data() + off_lvl, p->level_start.data(), lvl_bytes);
+    if (!p->rank0_steps.empty()) std::memcpy(host.data() + off_r0, p->rank0_steps.data(), r0_bytes - sizeof(int32_t));
+    cudaError_t e = cudaMemcpyAsync(d, host.data(), total, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        dev_free(ctx, d);
+        return cuda_error(ctx, e, "plan upload");
+    }
+    p->dev[prec] = d;
+    p->dev_bytes[prec] = total;
+    return QT_OK;
+}
+
+// leaves of one instance in the execution precision, written at dst
+void pack_leaves(const qt_plan *p, int prec, const std::complex<double> *src, char *dst) {
+    const bool mixed = prec == QT_PREC_MIXED;
+    uint64_t e = 0;
+    for (size_t i = 0; i < p->leaf_rank.size(); i++) {
+        const uint64_t n = 1ull << (2 * p->leaf_rank[i]);
+        char *o = dst + p->leaf_off[prec][i];
+        if (mixed) {
+            float *f = reinterpret_cast<float *>(o);
+            for (uint64_t j = 0; j < n; j++) {
+                f[2 * j] = (float) src[e + j].real();
+                f[2 * j + 1] = (float) src[e + j].imag();
+            }
+        } else {
+            std::memcpy(o, src + e, n * sizeof(std::complex<double>));
+        }
+        e += n;
+    }
+}
+
+// Step-by-step execution with the whole-GPU pairwise kernel (plans whose
+// intermediates are too large for one CTA).  Mixed precision runs every step
+// in complex64 and reads the final value back as FP64.
+qt_status execute_stepwise(qt_plan *p, int prec, const std::complex<double> *leaves, double *value) {
+    qt_ctx *ctx = p->ctx;
+    const bool mixed = prec == QT_PREC_MIXED;
+    const size_t es = mixed ? 8 : 16;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    // leaf buffer in the uniform precision of this mode
+    uint64_t loff = 0;
+    std::vector<uint64_t> leaf_off(p->leaf_rank.size());
+    for (size_t i = 0; i < p->leaf_rank.size(); i++) {
+        leaf_off[i] = loff;
+        loff = align_up(loff + (es << (2 * p->leaf_rank[i])), 256);
+    }
+    std::vector<char> host(loff);
+    uint64_t e = 0;
+    for (size_t i = 0; i < p->leaf_rank.size(); i++) {
+        const uint64_t n = 1ull << (2 * p->leaf_rank[i]);
+        if (mixed) {
+            float *f = reinterpret_cast<float *>(host.data() + leaf_off[i]);
+            for (uint64_t j = 0; j < n; j++) {
+                f[2 * j] = (float) leaves[e + j].real();
+                f[2 * j + 1] = (float) leaves[e + j].imag();
+            }
+        } else {
+            std::memcpy(host.data() + leaf_off[i], leaves + e, n * 16);
+        }
+        e += n;
+    }
+    void *dleaf = nullptr;
+    qt_status s = dev_alloc(ctx, loff ? loff : 256, &dleaf);
+    if (s != QT_OK) return s;
+    cudaError_t ce = cudaMemcpyAsync(dleaf, host.data(), loff, cudaMemcpyHostToDevice, ctx->stream);
+    if (ce != cudaSuccess) {
+        dev_free(ctx, dleaf);
+        return cuda_error(ctx, ce, "leaf upload");
+    }
+    // intermediates: one device buffer per step output, released when consumed
+    const auto &steps = p->steps[QT_PREC_FP64];   // index maps are precision independent
+    std::vector<void *> outs(steps.size(), nullptr);
+    std::vector<int> uses(steps.size(), 0);
+    for (const auto &d : steps) {
+        if (d.a_step >= 0) uses[d.a_step]++;
+        if (d.b_step >= 0) uses[d.b_step]++;
+    }
+    s = QT_OK;
+    for (size_t i = 0; i < steps.size() && s == QT_OK; i++) {
+        if (deadline_passed(ctx)) {
+            s = set_error(ctx, QT_ERR_DEADLINE, "deadline expired");
+            break;
+        }
+        const StepDesc &d = steps[i];
+        const void *A = (d.flags & kALeaf) ? (const char *) dleaf + leaf_off[p->a_leaf[i]] : outs[d.a_step];
+        const void *B = (d.flags & kBLeaf) ? (const char *) dleaf + leaf_off[p->b_leaf[i]] : outs[d.b_step];
+        s = dev_alloc(ctx, es << (2 * d.nFree), &outs[i]);
+        if (s != QT_OK) break;
+        ce = launch_pair(d, A, B, outs[i], !mixed, ctx->stream);
+        ctx->launches++;
+        if (ce != cudaSuccess) {
+            s = cuda_error(ctx, ce, "pair kernel launch");
+            break;
+        }
+        if (d.a_step >= 0 && --uses[d.a_step] == 0 && !(steps[d.a_step].flags & kOutRank0)) {
+            dev_free(ctx, outs[d.a_step]);
+            outs[d.a_step] = nullptr;
+        }
+        if (d.b_step >= 0 && --uses[d.b_step] == 0 && !(steps[d.b_step].flags & kOutRank0)) {
+            dev_free(ctx, outs[d.b_step]);
+            outs[d.b_step] = nullptr;
+        }
+    }
+    if (s == QT_OK) {
+        // final-value rule over the rank-0 outputs in contraction order (Network.h:961-965)
+        double fre = 0.0, fim = 0.0;
+        for (int r : p->rank0_steps) {
+            double v[2];
+            if (mixed) {
+                float f[2];
+                ce = cudaMemcpyAsync(f, outs[r], 8, cudaMemcpyDeviceToHost, ctx->stream);
+                if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+                v[0] = f[0];
+                v[1] = f[1];
+            } else {
+                ce = cudaMemcpyAsync(v, outs[r], 16, cudaMemcpyDeviceToHost, ctx->stream);
+                if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+            }
+            if (ce != cudaSuccess) {
+                s = cuda_error(ctx, ce, "value download");
+                break;
+            }
+            if ((std::fabs(fre) <= 1.0e-30 && std::fabs(fim) <= 1.0e-30) || (steps[r].flags & kBothRank0)) {
+                fre = v[0];
+                fim = v[1];
+            }
+        }
+        value[0] = fre;
+        value[1] = fim;
+    }
+    for (void *o : outs) dev_free(ctx, o);
+    dev_free(ctx, dleaf);
+    return s;
+}
+
+}  // namespace qtg

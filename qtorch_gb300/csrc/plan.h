@@ -1,0 +1,71 @@
+// Host-side plan and batch objects of the C ABI.
+#pragma once
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "../../include/qtorch/qtorch.hpp"
+#include "core.h"
+
+namespace qtg {
+
+// mixed plans compute outputs of rank <= this in FP64 (the expectation-value reductions)
+constexpr int kMixedTailRank = 1;
+// limits of the grouped interpreter (one CTA per instance)
+constexpr int kGroupedMaxRank = 11;
+constexpr int kGroupedMaxSum = 8;
+constexpr uint64_t kGroupedMaxWorkspace = 96ull << 20;
+
+}  // namespace qtg
+
+struct qt_plan {
+    qt_ctx *ctx = nullptr;
+    std::string qasm, measure, gate_dir;
+    std::vector<int> leaf_rank;
+    std::vector<std::complex<double>> leaf_values;   // the plan's own circuit, complex128
+    std::vector<int32_t> sequence;                    // recorded (idA, idB) pairs
+    std::vector<qtg::StepDesc> steps[2];              // per precision, sorted by level
+    std::vector<int> a_leaf, b_leaf;                  // leaf index of each operand or -1
+    std::vector<int32_t> level_start;
+    std::vector<int32_t> rank0_steps;
+    std::vector<uint64_t> leaf_off[2];
+    uint64_t leaf_bytes[2] = {0, 0};
+    uint64_t ws_bytes[2] = {0, 0};
+    int n_steps = 0, n_levels = 0;
+    int peak_rank = 0, max_step_out = 0, max_step_k = 0;
+    int64_t flops = 0;
+    bool grouped = false;
+    void *dev[2] = {nullptr, nullptr};
+    size_t dev_bytes[2] = {0, 0};
+};
+
+struct qt_batch {
+    qt_ctx *ctx = nullptr;
+    std::vector<qt_plan *> plans;                     // per instance
+    std::vector<std::vector<std::complex<double>>> leaves;   // per instance, complex128
+    int prepared_prec = -1;
+    bool dirty = true;
+    // device state
+    void *d_leaves = nullptr;
+    uint64_t leaf_bytes = 0;
+    std::vector<uint64_t> inst_leaf_off;
+    void *d_inst = nullptr;
+    void *d_values = nullptr;
+    void *d_ws = nullptr;
+    void *d_exps = nullptr;
+    uint64_t ws_stride = 0, exps_stride = 0;
+    int grid = 0;
+    void *h_leaves = nullptr;                         // pinned staging of the leaf image
+    void *h_values = nullptr;                         // pinned values
+    bool use_graph = false;
+    cudaGraphExec_t graph = nullptr;
+    bool all_grouped = true;
+    std::vector<int> stepwise;                        // instances run step by step
+};
+
+namespace qtg {
+qt_status lower_plan(qt_plan *p, const qtorch::Network &net);
+qt_status upload_plan(qt_plan *p, int prec);
+void pack_leaves(const qt_plan *p, int prec, const std::complex<double> *src, char *dst);
+qt_status execute_stepwise(qt_plan *p, int prec, const std::complex<double> *leaves, double *value);
+}  // namespace qtg

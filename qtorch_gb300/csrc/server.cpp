@@ -1,0 +1,252 @@
+// Continuous-batching request server.
+//
+// Requests (a plan plus its leaf values) are admitted in arrival order while
+// their device footprint (plan workspace + leaves, per precision) fits the
+// memory budget and an in-flight slot is free.  Admitted requests are grouped
+// into waves; every wave runs as one batch (one grouped launch, or step by step
+// for plans too large for a CTA) on one of several lanes, each lane with its
+// own CUDA stream, so a wave formed from requests that arrived while another
+// wave is on the GPU runs concurrently with it.  Each request's result is
+// independent of what it was batched with: an instance only ever touches its
+// own leaves and its CTA's workspace.
+#include <algorithm>
+#include <condition_variable>
+#include <deque>
+#include <thread>
+#include <unordered_map>
+
+#include "plan.h"
+
+using namespace qtg;
+
+namespace {
+
+struct Request {
+    int64_t ticket;
+    qt_plan *plan;
+    std::vector<double> leaves;
+    std::chrono::steady_clock::time_point t_submit;
+    uint64_t footprint;
+};
+
+struct Result {
+    int state = 0;   // 0 pending, 1 done, <0 -status
+    double v[2] = {0, 0};
+    double latency = 0;
+};
+
+}  // namespace
+
+struct qt_server {
+    qt_ctx *ctx = nullptr;                 // the caller's context (device, budget)
+    int max_inflight = 64;
+    qt_precision prec = QT_PREC_FP64;
+    std::mutex m;
+    std::condition_variable cv;            // new work or a lane became free
+    std::condition_variable done_cv;       // a request finished
+    std::deque<Request> pending;
+    std::unordered_map<int64_t, Result> results;
+    int64_t next_ticket = 0;
+    int inflight = 0;
+    uint64_t inflight_bytes = 0;
+    bool stop = false;
+    std::vector<double> latencies;
+    int64_t completed = 0;
+    int64_t launches = 0;
+    struct Lane {
+        qt_ctx *ctx = nullptr;
+        std::thread th;
+        std::vector<Request> wave;
+        bool busy = false;
+    };
+    std::vector<Lane> lanes;
+    std::thread dispatcher;
+};
+
+static uint64_t footprint(const qt_plan *p, qt_precision prec) {
+    return p->ws_bytes[prec] + p->leaf_bytes[prec] + 4096;
+}
+
+static void lane_main(qt_server *s, int li) {
+    auto &lane = s->lanes[li];
+    for (;;) {
+        std::vector<Request> wave;
+        {
+            std::unique_lock<std::mutex> g(s->m);
+            s->cv.wait(g, [&] { return s->stop || (lane.busy && !lane.wave.empty()); });
+            if (s->stop && lane.wave.empty()) return;
+            wave.swap(lane.wave);
+        }
+        std::vector<double> vals(2 * wave.size(), 0.0);
+        qt_batch *b = nullptr;
+        qt_status st = qt_batch_create(lane.ctx, &b);
+        for (auto &r : wave)
+            if (st == QT_OK) st = qt_batch_add(b, r.plan, r.leaves.empty() ? nullptr : r.leaves.data(), nullptr);
+        if (st == QT_OK) st = qt_batch_execute(b, s->prec, vals.data());
+        int nl = b ? qt_batch_launches_per_run(b) : 0;
+        if (b) qt_batch_free(b);
+        const auto now = std::chrono::steady_clock::now();
+        {
+            std::lock_guard<std::mutex> g(s->m);
+            for (size_t i = 0; i < wave.size(); i++) {
+                Result &res = s->results[wave[i].ticket];
+                if (st == QT_OK) {
+                    res.state = 1;
+                    res.v[0] = vals[2 * i];
+                    res.v[1] = vals[2 * i + 1];
+                } else {
+                    res.state = -(int) st;
+                }
+                res.latency = std::chrono::duration<double>(now - wave[i].t_submit).count();
+                s->latencies.push_back(res.latency);
+                s->completed++;
+                s->inflight--;
+                s->inflight_bytes -= wave[i].footprint;
+            }
+            s->launches += nl;
+            lane.busy = false;
+        }
+        s->cv.notify_all();
+        s->done_cv.notify_all();
+    }
+}
+
+static void dispatcher_main(qt_server *s) {
+    std::unique_lock<std::mutex> g(s->m);
+    for (;;) {
+        s->cv.wait(g, [&] {
+            if (s->stop) return true;
+            if (s->pending.empty()) return false;
+            for (auto &l : s->lanes)
+                if (!l.busy) return true;
+            return false;
+        });
+        if (s->stop) return;
+        int li = -1;
+        for (int i = 0; i < (int) s->lanes.size(); i++)
+            if (!s->lanes[i].busy) {
+                li = i;
+                break;
+            }
+        if (li < 0) continue;
+        // admission: arrival order, bounded by slots and the memory budget
+        std::vector<Request> wave;
+        const uint64_t budget = s->ctx->memory_budget;
+        while (!s->pending.empty() && s->inflight < s->max_inflight) {
+            Request &r = s->pending.front();
+            if (budget && s->inflight_bytes + r.footprint > budget && s->inflight > 0) break;
+            s->inflight++;
+            s->inflight_bytes += r.footprint;
+            wave.push_back(std::move(r));
+            s->pending.pop_front();
+        }
+        if (wave.empty()) {
+            // nothing admissible until a running wave returns its memory
+            s->cv.wait(g, [&] { return s->stop || s->inflight == 0; });
+            continue;
+        }
+        s->lanes[li].wave = std::move(wave);
+        s->lanes[li].busy = true;
+        s->cv.notify_all();
+    }
+}
+
+extern "C" {
+
+qt_status qt_server_create(qt_ctx *ctx, int max_inflight, qt_precision prec, qt_server **out) {
+    if (!ctx || !out || max_inflight < 1 || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return QT_ERR_INVALID_ARGUMENT;
+    auto *s = new qt_server();
+    s->ctx = ctx;
+    s->max_inflight = max_inflight;
+    s->prec = prec;
+    const int n_lanes = 2;
+    s->lanes.resize(n_lanes);
+    for (int i = 0; i < n_lanes; i++) {
+        qt_status st = qt_ctx_create(ctx->device, nullptr, &s->lanes[i].ctx);
+        if (st != QT_OK) {
+            for (int j = 0; j < i; j++) qt_ctx_destroy(s->lanes[j].ctx);
+            delete s;
+            return st;
+        }
+    }
+    for (int i = 0; i < n_lanes; i++) s->lanes[i].th = std::thread(lane_main, s, i);
+    s->dispatcher = std::thread(dispatcher_main, s);
+    *out = s;
+    return QT_OK;
+}
+
+qt_status qt_server_free(qt_server *s) {
+    if (!s) return QT_ERR_INVALID_ARGUMENT;
+    qt_server_drain(s);
+    {
+        std::lock_guard<std::mutex> g(s->m);
+        s->stop = true;
+    }
+    s->cv.notify_all();
+    s->dispatcher.join();
+    for (auto &l : s->lanes) l.th.join();
+    for (auto &l : s->lanes) qt_ctx_destroy(l.ctx);
+    delete s;
+    return QT_OK;
+}
+
+qt_status qt_server_submit(qt_server *s, qt_plan *plan, const double *leaves, int64_t *ticket) {
+    if (!s || !plan || !ticket) return QT_ERR_INVALID_ARGUMENT;
+    Request r;
+    r.plan = plan;
+    if (leaves) r.leaves.assign(leaves, leaves + 2 * plan->leaf_values.size());
+    r.t_submit = std::chrono::steady_clock::now();
+    r.footprint = footprint(plan, s->prec);
+    {
+        std::lock_guard<std::mutex> g(s->m);
+        const uint64_t budget = s->ctx->memory_budget;
+        if (budget && r.footprint > budget) return set_error(s->ctx, QT_ERR_OUT_OF_MEMORY, "request larger than the budget");
+        r.ticket = s->next_ticket++;
+        s->results[r.ticket] = Result();
+        *ticket = r.ticket;
+        s->pending.push_back(std::move(r));
+    }
+    s->cv.notify_all();
+    return QT_OK;
+}
+
+int qt_server_poll(qt_server *s, int64_t ticket, double *v, double *latency) {
+    if (!s) return -(int) QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->m);
+    auto it = s->results.find(ticket);
+    if (it == s->results.end()) return -(int) QT_ERR_INVALID_ARGUMENT;
+    if (it->second.state == 1) {
+        if (v) {
+            v[0] = it->second.v[0];
+            v[1] = it->second.v[1];
+        }
+        if (latency) *latency = it->second.latency;
+    }
+    return it->second.state;
+}
+
+qt_status qt_server_drain(qt_server *s) {
+    if (!s) return QT_ERR_INVALID_ARGUMENT;
+    std::unique_lock<std::mutex> g(s->m);
+    s->done_cv.wait(g, [&] { return s->pending.empty() && s->inflight == 0; });
+    return QT_OK;
+}
+
+qt_status qt_server_stats(qt_server *s, double *p50, double *p99, int64_t *completed, int64_t *launches) {
+    if (!s) return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->m);
+    std::vector<double> l = s->latencies;
+    std::sort(l.begin(), l.end());
+    auto q = [&](double f) {
+        if (l.empty()) return 0.0;
+        size_t i = (size_t) std::min<double>((double) l.size() - 1, std::ceil(f * (double) l.size()) - 1);
+        return l[i];
+    };
+    if (p50) *p50 = q(0.50);
+    if (p99) *p99 = q(0.99);
+    if (completed) *completed = s->completed;
+    if (launches) *launches = s->launches;
+    return QT_OK;
+}
+
+}  // extern "C"
