@@ -1,0 +1,405 @@
+"""Benchmark: MaxCut QAOA <Z_i Z_j> terms/s on one GB300.
+
+Workload (the reference's QAOA objective, src/maxcut.cpp:162-204): a seeded
+random 4-regular graph with 30 vertices (60 edges), QAOA depth p=1, every edge
+term's light-cone circuit as src/maxcut.h:105-233 writes it, contracted under
+this build's line-graph (min-fill) ordering.  One step evaluates all 60 terms
+at one (gamma, beta) point.
+
+  value      mixed-precision terms/s with the inputs resident in HBM (one grouped
+             launch per step, per-step CUDA events on the launching stream, L2
+             flushed between steps)
+  e2e        the same through the public API with host buffers: every step sets
+             the rotation angles of a new (gamma, beta) point on the host, uploads
+             the leaf tensors from pinned memory, runs, and reads the 60 values back
+  fp64       the plain complex128 path (bit-exact with the reference) for the
+             mixed/FP64 ratio; error = |mixed - fp64| per term
+  cpu_baseline / --impl reference: the CPU oracle port (a C restatement of the
+             reference's ContractIndices loop, QASM parse included per term, as
+             the reference pays it) on the host cores
+
+python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "QAOA <ZZ> terms/s (mixed vs FP64 GPU, err<=1e-6); serve p50/p99 latency"
+NODES, DEGREE, P = 30, 4, 1
+WORKLOAD = "MaxCut QAOA p=1, seeded random 4-regular graph, 30 nodes, 60 edge terms, line-graph (min-fill) ordering"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def max_over_ranks(values, world, device):
+    """Element-wise max of per-rank timings (the slowest rank sets the job time)."""
+    if world <= 1:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def angle_points(seed, n):
+    rng = np.random.default_rng(seed)
+    return [list(rng.uniform(0.0, math.pi, 2)) for _ in range(n)]   # [beta, gamma], U[0, pi)
+
+
+def term_rotation_angles(qasm_text):
+    """Angles of the rotation gates of a term in node order, as the parser reads them."""
+    out = []
+    for line in qasm_text.split("\n"):
+        t = line.split(" ")
+        if t and t[0] in ("Rx", "Rz"):
+            out.append(float(t[1]))
+    return out
+
+
+def build_terms(dgf, point):
+    import qtorch_gb300 as qg
+    n = qg.qaoa_num_edges(dgf)
+    return [qg.qaoa_term_text(dgf, P, point, e) for e in range(n)]
+
+
+# ---------------------------------------------------------------------------
+# CPU side (oracle port): the checker / baseline, never the product
+
+def _cpu_worker(job):
+    from oracle import port
+    qasm, meas, seq = job
+    t0 = time.perf_counter()
+    v, _ = port.replay_value(qasm, meas, seq)
+    return v, time.perf_counter() - t0
+
+
+def cpu_terms_per_s(jobs, workers, min_seconds=0.0):
+    """Oracle port over (qasm, measure, sequence) jobs on `workers` processes (spawn)."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers) as pool:
+        pool.map(_cpu_worker, jobs[:workers])          # warm the workers
+        done, t0 = 0, time.perf_counter()
+        while True:
+            pool.map(_cpu_worker, jobs)
+            done += len(jobs)
+            el = time.perf_counter() - t0
+            if el >= min_seconds:
+                break
+    return done / el, done, el
+
+
+def sequences_for(terms):
+    """Line-graph orderings of the terms (computed by the host planner, no GPU)."""
+    import qtorch_gb300 as qg
+    return [qg.Plan(q, m, ordering="linegraph", symbolic=True).sequence() for q, m in terms]
+
+
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.rows = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+                for n, v in zip(names, r[3:7]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d["hbm_gbs"], "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of the grouped kernel from the committed ncu summary, if any."""
+    path = os.path.join(HERE, "profiles", "plan_kernel_mixed_qaoa_p1_30node.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_launch"):
+                    return float(line.split("=")[1].split()[0])
+    except (OSError, ValueError, IndexError):
+        pass
+    return None
+
+
+def time_steps(run, steps, warmup, stream, flush):
+    """Per-step CUDA events on the launching stream; L2 flushed between steps."""
+    import torch
+    for _ in range(warmup):
+        run()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        flush()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        run()
+        e.record(stream)
+        e.synchronize()
+        times.append(s.elapsed_time(e) / 1e3)
+    torch.cuda.synchronize()
+    return times
+
+
+def run_engine(args):
+    import torch
+
+    import qtorch_gb300 as qg
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream()
+    ctx = qg.Context(local, stream=stream.cuda_stream)
+
+    dgf = qg.random_regular_graph(NODES, DEGREE, seed=args.graph_seed)
+    points = angle_points(1000 + rank, args.warmup + args.steps + 1)
+    terms = build_terms(dgf, points[0])
+    plans = [qg.Plan(q, m, ordering="linegraph", ctx=ctx) for q, m in terms]
+    n_terms = len(plans)
+
+    batches = {}
+    for prec in (qg.FP64, qg.MIXED):
+        b = qg.Batch(ctx)
+        for p in plans:
+            b.add(p)
+        b.prepare(prec)
+        b.use_graph(True)
+        batches[prec] = b
+
+    flush_buf = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    def flush():
+        flush_buf.fill_(1)
+
+    # accuracy of the mixed form against the FP64 form at the first point
+    v64 = batches[qg.FP64].execute(qg.FP64)
+    vmx = batches[qg.MIXED].execute(qg.MIXED)
+    err = np.abs(vmx - v64)
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.kernel_launches
+    with ClockSampler(local) as clk:
+        t_mixed = time_steps(batches[qg.MIXED].run, args.steps, args.warmup, stream, flush)
+    launches_mixed = ctx.kernel_launches - launches0
+    t_fp64 = time_steps(batches[qg.FP64].run, args.steps, args.warmup, stream, flush)
+
+    # end to end through the public API: new angles -> H2D -> run -> D2H, every step
+    rot = [term_rotation_angles(q) for q, _ in terms]
+    n_rot = [len(r) for r in rot]
+    for p, n in zip(plans, n_rot):
+        assert p.num_rotations == n
+
+    def angles_for(point):
+        # Rz(-gamma) per light-cone edge, then Rx(2 beta) per qubit (maxcut.h:205-233), 6 significant digits
+        beta, gamma = point
+        out = []
+        for q, _ in terms:
+            for line in q.split("\n"):
+                t = line.split(" ")
+                if t[0] == "Rz":
+                    out.append(float("%g" % -gamma))
+                elif t[0] == "Rx":
+                    out.append(float("%g" % (beta * 2.0)))
+        return np.array(out)
+
+    bm = batches[qg.MIXED]
+    bm.use_graph(False)
+    e2e_times = []
+    for j in range(args.warmup + args.steps):
+        a = angles_for(points[1 + (j % (len(points) - 1))])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        bm.set_rotations(a)
+        bm.upload()
+        bm.run()
+        vals = bm.fetch()
+        t1 = time.perf_counter()
+        if j >= args.warmup:
+            e2e_times.append(t1 - t0)
+    assert np.all(np.isfinite(vals))
+
+    sum_mixed, sum_fp64, sum_e2e = max_over_ranks([sum(t_mixed), sum(t_fp64), sum(e2e_times)], world, "cuda")
+    total_terms = n_terms * args.steps * world
+    value = total_terms / sum_mixed
+    fp64_value = total_terms / sum_fp64
+    e2e_value = total_terms / sum_e2e
+
+    peak, peak_kind = measured_peaks()
+    alg_bytes = sum(p.algorithmic_bytes(qg.MIXED) for p in plans)
+    achieved = alg_bytes / (sum_mixed / args.steps) / 1e9
+    cmacs = sum(p.flops for p in plans)
+    traffic = profiled_traffic()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "terms/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sum_mixed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "complex64/fp32 (fp64 rank<=1 reductions)",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "graph_seed": args.graph_seed, "terms_per_step": n_terms,
+                   "angles": "beta,gamma ~ U[0,pi) seeded per rank", "precision": "mixed",
+                   "l2": "flushed between steps (256 MiB write), per-step CUDA events",
+                   "parallelism": f"weak: each rank evaluates its own {n_terms} terms per step"},
+        "fp64": {"value": fp64_value, "unit": "terms/s", "ms_per_step": 1e3 * sum_fp64 / args.steps,
+                 "parity": "bit-exact with the reference CPU loop under the same ordering"},
+        "mixed_over_fp64": value / fp64_value,
+        "error_vs_fp64": {"max_abs": float(err.max()), "mean_abs": float(err.mean()), "bound": 1e-6},
+        "e2e": {"value": e2e_value, "unit": "terms/s", "h2d_bytes_per_step": bm.h2d_bytes,
+                "d2h_bytes_per_step": bm.d2h_bytes, "ms_per_step": 1e3 * sum_e2e / args.steps},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_kind, "kernel": "plan_kernel<mixed>",
+                     "algorithmic_bytes_per_launch": alg_bytes, "complex_macs_per_launch": cmacs},
+        "gpu_launches": int(launches_mixed),
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        seqs = sequences_for(terms)
+        jobs = [(q, m, s) for (q, m), s in zip(terms, seqs)]
+        cores = os.cpu_count() or 1
+        rate, done, el = cpu_terms_per_s(jobs, cores, min_seconds=args.cpu_seconds)
+        line["cpu_baseline"] = {"value": rate, "unit": "terms/s", "cores": cores, "kind": "port",
+                                "sample": f"{done} terms ({done // n_terms} x the 60-term step) in {el:.1f} s, "
+                                          "QASM parse + recorded line-graph replay per term"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    del batches, plans
+    ctx.close()
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import qtorch_gb300 as qg   # host planner only (orderings), no device
+    from oracle import qaoa_terms
+
+    dgf = qg.random_regular_graph(NODES, DEGREE, seed=args.graph_seed)
+    points = angle_points(1000, args.warmup + args.steps + 1)
+    seqs = sequences_for(build_terms(dgf, points[0]))
+    cores = os.cpu_count() or 1
+    import multiprocessing as mp
+    pool = mp.get_context("spawn").Pool(cores)
+    times = []
+    n_terms = len(seqs)
+    for j in range(args.warmup + args.steps):
+        pt = points[j % len(points)]
+        t0 = time.perf_counter()
+        # the reference's own per-step work: write each term's QASM text, parse it, contract it
+        terms = qaoa_terms.all_terms(dgf, P, [pt[0], pt[1]])
+        jobs = [(q, m, s) for (_, q, m), s in zip(terms, seqs)]
+        pool.map(_cpu_worker, jobs)
+        if j >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    pool.close()
+    value = n_terms * args.steps / sum(times)
+    line = {
+        "metric": METRIC, "value": value, "unit": "terms/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "complex128", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "graph_seed": args.graph_seed, "terms_per_step": n_terms},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "terms/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} steps of {n_terms} terms: term text + QASM parse + "
+                                   "ContractIndices loop (C restatement of src/Network.h:876-971)"},
+        "e2e": {"value": value, "unit": "terms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--graph-seed", type=int, default=1)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    from qtorch_gb300 import build as qbuild
+    qbuild.build()
+    from oracle import port
+    port.build()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_engine(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -155,6 +155,8 @@ private:
 // gate tensors built on the host with the reference's expressions
 std::shared_ptr<Node> MakeGateNode(const std::string &kind, double param);
 std::shared_ptr<Node> MakeArbitraryNode(const std::string &path, const std::string &name, bool twoQubit);
+// the angle a rotation gate node was built with (0 for other nodes)
+double GateAngle(const Node &n);
 
 // ---- one recorded contraction (what the planner lowers) -------------------
 struct StepRecord {

@@ -175,6 +175,9 @@ int qt_plan_num_leaves(const qt_plan *plan);
 int qt_plan_peak_rank(const qt_plan *plan);
 uint64_t qt_plan_workspace_bytes(const qt_plan *plan, qt_precision prec);
 int64_t qt_plan_flops(const qt_plan *plan);                         /* sum of 4^(free+summed) */
+/* Algorithmic bytes of one execution: sum over steps of the element size times
+ * (4^rank_a + 4^rank_b + 4^rank_c) in the given precision's storage types. */
+uint64_t qt_plan_algorithmic_bytes(const qt_plan *plan, qt_precision prec);
 /* recorded node-id pairs (replayable through QT_ORDER_SEQUENCE / the oracle) */
 int qt_plan_sequence(const qt_plan *plan, int32_t *pairs, int cap_pairs);
 /* Leaf tensors of the plan's own circuit, complex128, concatenated in leaf order. */
@@ -182,6 +185,10 @@ uint64_t qt_plan_leaf_elems(const qt_plan *plan);
 qt_status qt_plan_leaf_values(const qt_plan *plan, double *out, uint64_t cap_complex);
 /* One network value (synchronous, host in / host out). */
 qt_status qt_plan_execute(qt_ctx *ctx, qt_plan *plan, qt_precision prec, double *re_im);
+/* Parametrised rotation leaves (Rx, Ry, Rz, PHASE, CPHASE) of the plan, in leaf
+ * order: their count, and the angles the plan's own circuit gives them. */
+int qt_plan_num_rotations(const qt_plan *plan);
+qt_status qt_plan_rotation_angles(const qt_plan *plan, double *angles, int cap);
 
 /* ---- batches: many plan instances in one persistent grouped launch ------ */
 
@@ -201,6 +208,13 @@ qt_status qt_batch_run(qt_batch *b);
 qt_status qt_batch_fetch(qt_batch *b, double *values);
 /* Replace the leaf values of instance i (host complex128) for the next run. */
 qt_status qt_batch_set_leaves(qt_batch *b, int index, const double *leaves);
+/* New angles for the rotation leaves of every instance, concatenated in
+ * instance order (qt_plan_num_rotations angles per instance).  The leaf tensors
+ * are rebuilt on the host with the reference's expressions (angles narrowed to
+ * float as its parser does) and go to the device with the next upload.  This is
+ * how an optimiser moves a batch of QAOA terms to a new (gamma, beta) point
+ * without re-planning. */
+qt_status qt_batch_set_rotations(qt_batch *b, const double *angles, int64_t n_angles);
 /* Upload all leaf values again from the host copies (async; part of an end-to-end step). */
 qt_status qt_batch_upload(qt_batch *b);
 /* Capture qt_batch_run into a CUDA graph and replay it (0 disables). */

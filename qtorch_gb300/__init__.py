@@ -407,6 +407,9 @@ class Plan:
     def flops(self):
         return int(_lib().qt_plan_flops(self.handle))
 
+    def algorithmic_bytes(self, precision=FP64):
+        return int(_lib().qt_plan_algorithmic_bytes(self.handle, precision))
+
     def sequence(self):
         n = _lib().qt_plan_sequence(self.handle, None, 0)
         arr = np.zeros(2 * max(n, 1), dtype=np.int32)
@@ -423,6 +426,16 @@ class Plan:
         v = np.zeros(2)
         _check(_lib().qt_plan_execute(self.ctx.handle, self.handle, precision, _dp(v)), self.ctx)
         return complex(v[0], v[1])
+
+    @property
+    def num_rotations(self):
+        return _lib().qt_plan_num_rotations(self.handle)
+
+    def rotation_angles(self):
+        n = self.num_rotations
+        out = np.zeros(max(n, 1))
+        _check(_lib().qt_plan_rotation_angles(self.handle, _dp(out), n), self.ctx)
+        return out[:n].copy()
 
 
 class Batch:
@@ -473,6 +486,10 @@ class Batch:
     def set_leaves(self, index, leaves):
         leaves = np.ascontiguousarray(leaves, dtype=np.complex128)
         _check(_lib().qt_batch_set_leaves(self.handle, index, _dp(leaves.view(np.float64))), self.ctx)
+
+    def set_rotations(self, angles):
+        a = np.ascontiguousarray(np.asarray(angles, dtype=np.float64))
+        _check(_lib().qt_batch_set_rotations(self.handle, _dp(a), a.size), self.ctx)
 
     def upload(self):
         _check(_lib().qt_batch_upload(self.handle), self.ctx)

@@ -63,10 +63,14 @@ SIGNATURES = [
     ("qt_plan_peak_rank", c_int, [c_void_p]),
     ("qt_plan_workspace_bytes", c_uint64, [c_void_p, c_int]),
     ("qt_plan_flops", c_int64, [c_void_p]),
+    ("qt_plan_algorithmic_bytes", c_uint64, [c_void_p, c_int]),
     ("qt_plan_sequence", c_int, [c_void_p, P(c_int32), c_int]),
     ("qt_plan_leaf_elems", c_uint64, [c_void_p]),
     ("qt_plan_leaf_values", c_int, [c_void_p, P(c_double), c_uint64]),
     ("qt_plan_execute", c_int, [c_void_p, c_void_p, c_int, P(c_double)]),
+    ("qt_plan_num_rotations", c_int, [c_void_p]),
+    ("qt_plan_rotation_angles", c_int, [c_void_p, P(c_double), c_int]),
+    ("qt_batch_set_rotations", c_int, [c_void_p, P(c_double), c_int64]),
     ("qt_batch_create", c_int, [c_void_p, P(c_void_p)]),
     ("qt_batch_free", c_int, [c_void_p]),
     ("qt_batch_add", c_int, [c_void_p, c_void_p, P(c_double), P(c_int)]),

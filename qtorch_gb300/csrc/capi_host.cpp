@@ -247,6 +247,20 @@ qt_status qt_plan_build(qt_ctx *ctx, const char *qasm_text, const char *measure_
         for (const auto &leaf : net->Leaves()) {
             p->leaf_rank.push_back(leaf->mRank);
             const auto &v = leaf->GetTensorVals();
+            const char *kind = nullptr;
+            switch (leaf->GetTypeOfNode()) {
+                case qtorch::GateType::RX: kind = "Rx"; break;
+                case qtorch::GateType::RY: kind = "Ry"; break;
+                case qtorch::GateType::RZ: kind = "Rz"; break;
+                case qtorch::GateType::PHASE: kind = "PHASE"; break;
+                case qtorch::GateType::CPHASE: kind = "CPHASE"; break;
+                default: break;
+            }
+            if (kind) {
+                p->rot_kind.push_back(kind);
+                p->rot_angle.push_back(qtorch::GateAngle(*leaf));
+                p->rot_elem.push_back(p->leaf_values.size());
+            }
             p->leaf_values.insert(p->leaf_values.end(), v.begin(), v.end());
         }
         if (ordering == QT_ORDER_STOCHASTIC) {
@@ -294,6 +308,16 @@ uint64_t qt_plan_workspace_bytes(const qt_plan *p, qt_precision prec) {
 }
 int64_t qt_plan_flops(const qt_plan *p) { return p ? p->flops : -1; }
 
+uint64_t qt_plan_algorithmic_bytes(const qt_plan *p, qt_precision prec) {
+    if (!p || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return 0;
+    uint64_t total = 0;
+    for (const auto &d : p->steps[prec]) {
+        const uint64_t ea = (d.flags & kAF64) ? 16 : 8, eb = (d.flags & kBF64) ? 16 : 8, ec = (d.flags & kCF64) ? 16 : 8;
+        total += (ea << (2 * d.rA)) + (eb << (2 * d.rB)) + (ec << (2 * d.nFree));
+    }
+    return total;
+}
+
 int qt_plan_sequence(const qt_plan *p, int32_t *pairs, int cap) {
     if (!p) return -1;
     const int n = (int) p->sequence.size() / 2;
@@ -305,6 +329,14 @@ int qt_plan_sequence(const qt_plan *p, int32_t *pairs, int cap) {
 }
 
 uint64_t qt_plan_leaf_elems(const qt_plan *p) { return p ? p->leaf_values.size() : 0; }
+
+int qt_plan_num_rotations(const qt_plan *p) { return p ? (int) p->rot_kind.size() : -1; }
+
+qt_status qt_plan_rotation_angles(const qt_plan *p, double *angles, int cap) {
+    if (!p || (!angles && cap)) return QT_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < (int) p->rot_angle.size() && i < cap; i++) angles[i] = p->rot_angle[i];
+    return QT_OK;
+}
 
 qt_status qt_plan_leaf_values(const qt_plan *p, double *out, uint64_t cap) {
     if (!p || !out || cap < p->leaf_values.size()) return QT_ERR_INVALID_ARGUMENT;
@@ -385,6 +417,25 @@ qt_status qt_batch_set_leaves(qt_batch *b, int i, const double *leaves) {
     const auto *c = reinterpret_cast<const std::complex<double> *>(leaves);
     std::copy(c, c + b->leaves[i].size(), b->leaves[i].begin());
     return QT_OK;
+}
+
+qt_status qt_batch_set_rotations(qt_batch *b, const double *angles, int64_t n_angles) {
+    if (!b || (n_angles && !angles)) return QT_ERR_INVALID_ARGUMENT;
+    int64_t need = 0;
+    for (auto *p : b->plans) need += (int64_t) p->rot_kind.size();
+    if (need != n_angles) return set_error(b->ctx, QT_ERR_INVALID_ARGUMENT, "angle count does not match the batch");
+    return guard(b->ctx, [&]() {
+        int64_t k = 0;
+        for (size_t i = 0; i < b->plans.size(); i++) {
+            const qt_plan *p = b->plans[i];
+            for (size_t r = 0; r < p->rot_kind.size(); r++, k++) {
+                auto g = qtorch::MakeGateNode(p->rot_kind[r], angles[k]);
+                const auto &v = g->GetTensorVals();
+                std::copy(v.begin(), v.end(), b->leaves[i].begin() + p->rot_elem[r]);
+            }
+        }
+        return QT_OK;
+    });
 }
 
 static qt_status batch_pack(qt_batch *b) {

@@ -59,11 +59,12 @@ inline void fold_negative_zero(std::vector<std::complex<double>> &v) {
 
 class GateNode : public Node {
 public:
-    GateNode(int rank, GateType type, const std::string &name) : Node(rank) {
+    GateNode(int rank, GateType type, const std::string &name, double angle = 0.0) : Node(rank), mAngle(angle) {
         mType = type;
         mStringType = name;
     }
     std::vector<std::complex<double>> &Vals() { return mVals; }
+    double mAngle;
 };
 
 void set1(std::vector<std::complex<double>> &t, int in, int out, std::complex<double> v) { t[in + 4 * out] = v; }
@@ -94,7 +95,7 @@ std::shared_ptr<Node> MakeGateNode(const std::string &kind, double param) {
         const double cc = std::pow(std::cos(th / 2.0), 2);
         const double ss = std::pow(std::sin(th / 2.0), 2);
         const double sh = std::sin(th) / 2.0;
-        auto n = std::make_shared<GateNode>(2, kind == "Rx" ? GateType::RX : GateType::RY, kind);
+        auto n = std::make_shared<GateNode>(2, kind == "Rx" ? GateType::RX : GateType::RY, kind, param);
         auto &t = n->Vals();
         set1(t, 0, 0, cc); set1(t, 1, 1, cc); set1(t, 2, 2, cc); set1(t, 3, 3, cc);
         if (kind == "Rx") {
@@ -113,7 +114,8 @@ std::shared_ptr<Node> MakeGateNode(const std::string &kind, double param) {
     }
     if (kind == "Rz" || kind == "PHASE") {
         const double th = (double) (float) param;
-        auto n = std::make_shared<GateNode>(2, kind == "Rz" ? GateType::RZ : GateType::PHASE, kind == "Rz" ? "Rz" : "Phase");
+        auto n = std::make_shared<GateNode>(2, kind == "Rz" ? GateType::RZ : GateType::PHASE, kind == "Rz" ? "Rz" : "Phase",
+                                            param);
         auto &t = n->Vals();
         set1(t, 0, 0, 1.0);
         set1(t, 3, 3, 1.0);
@@ -160,7 +162,8 @@ std::shared_ptr<Node> MakeGateNode(const std::string &kind, double param) {
             em = std::exp(2.0 * kPi * C(0, -1) / std::pow(2, param + 1.0));
             ep = std::exp(2.0 * kPi * C(0, 1) / std::pow(2, param + 1.0));
         }
-        auto n = std::make_shared<GateNode>(4, kind == "CPHASE" ? GateType::CPHASE : GateType::CRK, kind == "CPHASE" ? "CPhase" : "CRk");
+        auto n = std::make_shared<GateNode>(4, kind == "CPHASE" ? GateType::CPHASE : GateType::CRK,
+                                            kind == "CPHASE" ? "CPhase" : "CRk", param);
         auto &t = n->Vals();
         for (int i1 = 0; i1 < 4; i1++)
             for (int i2 = 0; i2 < 4; i2++) {
@@ -173,6 +176,11 @@ std::shared_ptr<Node> MakeGateNode(const std::string &kind, double param) {
         return n;
     }
     throw InvalidFileFormat();
+}
+
+double GateAngle(const Node &n) {
+    const auto *g = dynamic_cast<const GateNode *>(&n);
+    return g ? g->mAngle : 0.0;
 }
 
 std::shared_ptr<Node> MakeArbitraryNode(const std::string &path, const std::string &name, bool twoQubit) {

@@ -24,6 +24,10 @@ struct qt_plan {
     std::vector<int> leaf_rank;
     std::vector<std::complex<double>> leaf_values;   // the plan's own circuit, complex128
     std::vector<int32_t> sequence;                    // recorded (idA, idB) pairs
+    // rotation leaves in leaf order: kind ("Rx", "Ry", "Rz", "PHASE", "CPHASE"), angle, first element
+    std::vector<std::string> rot_kind;
+    std::vector<double> rot_angle;
+    std::vector<uint64_t> rot_elem;
     std::vector<qtg::StepDesc> steps[2];              // per precision, sorted by level
     std::vector<int> a_leaf, b_leaf;                  // leaf index of each operand or -1
     std::vector<int32_t> level_start;
