@@ -216,7 +216,9 @@ def run_engine(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    stream = torch.cuda.current_stream()
+    # a non-default stream: the engine captures its launches into a CUDA graph there
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx = qg.Context(local, stream=stream.cuda_stream)
 
     dgf = qg.random_regular_graph(NODES, DEGREE, seed=args.graph_seed)
