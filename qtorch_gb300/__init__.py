@@ -14,6 +14,7 @@ src/LineGraph.h) so that code written against qTorch reads the same:
 import ctypes
 import os
 import threading
+import weakref
 
 import numpy as np
 
@@ -109,11 +110,32 @@ def _ip(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
 
 
+class _Owned:
+    """A native object tied to a context: the context frees it before it goes away."""
+
+    _free_name = None
+    _release_rank = 9   # lower ranks are freed first when the context closes
+
+    def _register(self, ctx):
+        if ctx is not None:
+            ctx._deps.add(self)
+
+    def _release(self):
+        h = getattr(self, "handle", None)
+        if h:
+            self.handle = None
+            getattr(_lib(), self._free_name)(h)
+
+    def __del__(self):
+        self._release()
+
+
 class Context:
     """One device, one CUDA stream (``stream``: a cudaStream_t as int, or None)."""
 
     def __init__(self, device=0, stream=None):
         self.handle = None
+        self._deps = weakref.WeakSet()
         h = ctypes.c_void_p()
         _check(_lib().qt_ctx_create(device, ctypes.c_void_p(stream) if stream else None, ctypes.byref(h)))
         self.handle = h.value
@@ -121,8 +143,14 @@ class Context:
 
     def close(self):
         if self.handle:
+            # servers, batches, networks and plans on this context go first
+            for dep in sorted(list(self._deps), key=lambda d: d._release_rank):
+                dep._release()
             _lib().qt_ctx_destroy(self.handle)
             self.handle = None
+
+    def __del__(self):
+        self.close()
 
     def synchronize(self):
         _check(_lib().qt_ctx_synchronize(self.handle), self)
@@ -197,8 +225,11 @@ def contract_pair_device(a_ptr, rank_a, b_ptr, rank_b, free_from_a, free_idx, su
         ctypes.c_void_p(c_ptr)), ctx)
 
 
-class Network:
+class Network(_Owned):
     """Network (src/Network.h:54-140): parse, ContractNodes on the GPU, final value."""
+
+    _free_name = "qt_network_free"
+    _release_rank = 2
 
     def __init__(self, qasm_text, measure_text="", gate_dir=None, ctx=None, symbolic=False):
         self.ctx = None if symbolic else (ctx or default_context())
@@ -207,6 +238,7 @@ class Network:
                                         (measure_text or "").encode(), gate_dir.encode() if gate_dir else None,
                                         ctypes.byref(h)), self.ctx)
         self.handle = h.value
+        self._register(self.ctx)
 
     @classmethod
     def from_files(cls, qasm_path, measure_path, ctx=None):
@@ -218,12 +250,6 @@ class Network:
         except OSError:
             m = ""   # every qubit traced out, as Network.h:286-288
         return cls(q, m, gate_dir=None, ctx=ctx)
-
-    def __del__(self):
-        h = getattr(self, "handle", None)
-        if h:
-            _lib().qt_network_free(h)
-            self.handle = None
 
     def reset(self):
         _check(_lib().qt_network_reset(self.handle), self.ctx)
@@ -367,8 +393,11 @@ class LineGraph:
 _ORDER_NAMES = {"stochastic": ORDER_STOCHASTIC, "linegraph": ORDER_LINEGRAPH, "sequence": ORDER_SEQUENCE}
 
 
-class Plan:
+class Plan(_Owned):
     """An ordering lowered once; executed for many leaf bindings (see qt_plan_build)."""
+
+    _free_name = "qt_plan_free"
+    _release_rank = 3
 
     def __init__(self, qasm_text, measure_text="", ordering="linegraph", seed=0, sequence=None, gate_dir=None,
                  ctx=None, symbolic=False):
@@ -381,12 +410,7 @@ class Plan:
                                     gate_dir.encode() if gate_dir else None, _ORDER_NAMES[ordering], int(seed),
                                     _ip(seq) if seq.size else None, seq.size // 2, ctypes.byref(h)), self.ctx)
         self.handle = h.value
-
-    def __del__(self):
-        h = getattr(self, "handle", None)
-        if h:
-            _lib().qt_plan_free(h)
-            self.handle = None
+        self._register(self.ctx)
 
     @property
     def num_steps(self):
@@ -438,8 +462,11 @@ class Plan:
         return out[:n].copy()
 
 
-class Batch:
+class Batch(_Owned):
     """Many plan instances in one persistent grouped launch."""
+
+    _free_name = "qt_batch_free"
+    _release_rank = 1
 
     def __init__(self, ctx=None):
         self.ctx = ctx or default_context()
@@ -447,12 +474,7 @@ class Batch:
         _check(_lib().qt_batch_create(self.ctx.handle, ctypes.byref(h)), self.ctx)
         self.handle = h.value
         self._plans = []
-
-    def __del__(self):
-        h = getattr(self, "handle", None)
-        if h:
-            _lib().qt_batch_free(h)
-            self.handle = None
+        self._register(self.ctx)
 
     def add(self, plan, leaves=None):
         idx = ctypes.c_int(-1)
@@ -510,8 +532,11 @@ class Batch:
         return int(_lib().qt_batch_launches_per_run(self.handle))
 
 
-class Server:
+class Server(_Owned):
     """Continuous-batching request loop (qt_server_*)."""
+
+    _free_name = "qt_server_free"
+    _release_rank = 0
 
     def __init__(self, max_inflight=64, precision=FP64, ctx=None):
         self.ctx = ctx or default_context()
@@ -519,14 +544,10 @@ class Server:
         _check(_lib().qt_server_create(self.ctx.handle, max_inflight, precision, ctypes.byref(h)), self.ctx)
         self.handle = h.value
         self._keep = []
+        self._register(self.ctx)
 
     def close(self):
-        if self.handle:
-            _lib().qt_server_free(self.handle)
-            self.handle = None
-
-    def __del__(self):
-        self.close()
+        self._release()
 
     def submit(self, plan, leaves=None):
         t = ctypes.c_int64(-1)

@@ -476,7 +476,9 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
     b->leaf_bytes = off;
     b->ws_stride = (ws + 255) / 256 * 256;
     b->exps_stride = (ex + 63) / 64 * 64;
-    b->grid = std::min(n_grouped, plan_max_grid());
+    // small workspaces live in shared memory, the rest in per-CTA global scratch
+    b->ws_in_smem = b->ws_stride <= kSmemWorkspaceMax;
+    b->grid = std::min(n_grouped, plan_max_grid(kPlanHeaderBytes + (b->ws_in_smem ? b->ws_stride : 0)));
     qt_status s = QT_OK;
     auto chk = [&](cudaError_t e, const char *w) {
         if (s == QT_OK && e != cudaSuccess) s = cuda_error(ctx, e, w);
@@ -489,10 +491,7 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
         chk(cudaMallocHost(&b->h_values, sizeof(double) * 2 * n), "cudaMallocHost");
         if (s == QT_OK) s = dev_alloc(ctx, sizeof(double) * 2 * n, &b->d_values);
     }
-    if (s == QT_OK && b->grid > 0) {
-        s = dev_alloc(ctx, b->ws_stride * b->grid, &b->d_ws);
-        if (s == QT_OK && prec == QT_PREC_MIXED) s = dev_alloc(ctx, sizeof(int32_t) * b->exps_stride * b->grid, &b->d_exps);
-    }
+    if (s == QT_OK && b->grid > 0 && !b->ws_in_smem) s = dev_alloc(ctx, b->ws_stride * b->grid, &b->d_ws);
     if (s != QT_OK) {
         batch_release(b);
         return s;
@@ -542,8 +541,7 @@ static qt_status batch_launch(qt_batch *b) {
     const int n_grouped = (int) b->plans.size() - (int) b->stepwise.size();
     if (n_grouped <= 0) return QT_OK;
     cudaError_t e = launch_plan((const InstanceDesc *) b->d_inst, n_grouped, b->prepared_prec == QT_PREC_MIXED,
-                                b->grid, (char *) b->d_ws, b->ws_stride, (int32_t *) b->d_exps, b->exps_stride,
-                                ctx->stream);
+                                b->grid, (char *) b->d_ws, b->ws_stride, b->ws_in_smem, ctx->stream);
     ctx->launches++;
     return cuda_error(ctx, e, "plan kernel launch");
 }

@@ -17,6 +17,9 @@ namespace qtg {
 
 constexpr int kMaxWires = 24;      // rank limit of one operand (4^24 elements is far beyond HBM)
 constexpr uint8_t kNoWire = 0xff;
+constexpr int kPlanThreads = 256;              // threads of one interpreter CTA
+constexpr int kPlanMaxSteps = 1024;            // steps of a plan the interpreter takes
+constexpr int kPlanHeaderBytes = 8 * kPlanMaxSteps;   // per-step scale bookkeeping in shared memory
 
 enum StepFlags : uint32_t {
     kALeaf = 1u << 0,        // A is read from the leaf buffer (else workspace)
@@ -35,11 +38,14 @@ struct StepDesc {
     int32_t a_step;          // step that produced A (-1 for a leaf): its scale exponent applies
     int32_t b_step;
     uint32_t flags;
-    uint8_t rA, rB, nFree, nSum, fA, fB, pad0, pad1;
+    uint8_t rA, rB, nFree, nSum, fA, fB;
+    uint8_t group;               // interpreter: lanes that share one output's k loop (power of two)
+    uint8_t pad1;
     uint8_t cA[kMaxWires];       // C digit -> A wire (kNoWire if the digit belongs to B)
     uint8_t cB[kMaxWires];       // C digit -> B wire (kNoWire if the digit belongs to A)
     uint8_t posAs[kMaxWires];
     uint8_t posBs[kMaxWires];
+    uint32_t item_start;         // interpreter: first work item of this step inside its level
 };
 static_assert(sizeof(StepDesc) % 8 == 0, "StepDesc alignment");
 
@@ -48,6 +54,7 @@ struct PlanDesc {
     const StepDesc *steps;       // sorted by level
     const int32_t *level_start;  // n_levels + 1 entries
     const int32_t *rank0_steps;  // steps with a rank-0 output, in contraction (sequence) order
+    const uint32_t *level_items; // work items of each level (n_levels entries)
     int32_t n_steps;
     int32_t n_levels;
     int32_t n_rank0;

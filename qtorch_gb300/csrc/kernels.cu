@@ -106,98 +106,58 @@ pair_kernel(const typename Vec2<T>::type *__restrict__ A, const typename Vec2<T>
 // ---------------------------------------------------------------------------
 // Grouped plan interpreter.
 
-constexpr int kPlanThreads = 256;
-constexpr int kMaxLevelSteps = 64;      // steps of one level staged in shared memory per sub-batch
-constexpr int kTableEntries = 4096;     // shared k-offset table entries per sub-batch
+// The schedule of a level is precomputed on the host: every step carries the
+// first work item it owns (item_start, relative to its level) and its lane
+// group size, so a thread finds its step with a binary search and the CTA
+// needs one barrier per level.
+//
+// Mixed precision keeps each intermediate as stored values S with a true value
+// S * 2^E.  A step loads its operands as they are, scales the accumulated sum
+// by 2^-(mA+mB) (m = the exponent of the producer's largest |S|, tracked with a
+// shared-memory atomicMax while the producer ran) and records
+// E_C = E_A + E_B + mA + mB.  Every stored tensor thus stays within a factor 4^K
+// of 1 (no overflow, no underflow drift) without a separate normalisation pass.
 
-struct PlanShared {
-    StepDesc steps[kMaxLevelSteps];        // descriptors of the sub-batch
-    uint32_t prefix[kMaxLevelSteps + 1];   // first work item of each step (aligned to its lane group)
-    uint32_t tbl_start[kMaxLevelSteps];    // start of each step's k table (or kNoTable)
-    int32_t group[kMaxLevelSteps];         // lanes per output (power of two, <= 16)
-    uint32_t maxbits[kMaxLevelSteps];      // max |C| bits per step (mixed)
-    uint32_t tbl_a[kTableEntries];
-    uint32_t tbl_b[kTableEntries];
+struct PlanSmemHeader {
+    uint32_t maxbits[kPlanMaxSteps];   // float bits of max |S| of each step's output
+    int32_t expo[kPlanMaxSteps];       // E of each step's output
 };
 
-constexpr uint32_t kNoTable = 0xffffffffu;
+__device__ __forceinline__ int step_scale(const PlanSmemHeader &h, int step) {
+    if (step < 0) return 0;
+    const float mx = __uint_as_float(h.maxbits[step]);
+    int e = 0;
+    if (mx > 0.f && isfinite(mx)) frexpf(mx, &e);
+    return e;
+}
 
 template <bool kMixed>
-__device__ void plan_level(const PlanDesc &P, const InstanceDesc &I, const CtaScratch &W, int s_begin, int s_end,
-                           PlanShared &sh) {
+__device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, uint32_t total, const char *leaves,
+                           char *ws, PlanSmemHeader &h) {
     const int tid = threadIdx.x;
-    const int ns = s_end - s_begin;
-    // ---- stage descriptors
-    {
-        const uint64_t *src = reinterpret_cast<const uint64_t *>(P.steps + s_begin);
-        uint64_t *dst = reinterpret_cast<uint64_t *>(sh.steps);
-        const int words = ns * (int) (sizeof(StepDesc) / 8);
-        for (int w = tid; w < words; w += blockDim.x) dst[w] = src[w];
-    }
-    __syncthreads();
-    // ---- per-step work sizes, lane groups, table layout
-    if (tid == 0) {
-        uint32_t acc = 0, tacc = 0;
-        for (int i = 0; i < ns; i++) {
-            const StepDesc &d = sh.steps[i];
-            const uint32_t n_out = 1u << (2 * d.nFree);
-            const uint32_t K = 1u << (2 * d.nSum);
-            uint32_t g = 1;
-            if (kMixed && !(d.flags & kCF64)) {
-                // split the k loop of tiny outputs across up to 16 lanes
-                while (g < 16 && g * 2 <= K && n_out * g * 2 <= (uint32_t) blockDim.x) g *= 2;
-            }
-            acc = (acc + g - 1) / g * g;   // lane groups start on a multiple of their size
-            sh.group[i] = (int) g;
-            sh.prefix[i] = acc;
-            acc += n_out * g;
-            if (tacc + K <= (uint32_t) kTableEntries) {
-                sh.tbl_start[i] = tacc;
-                tacc += K;
-            } else {
-                sh.tbl_start[i] = kNoTable;
-            }
-            sh.maxbits[i] = 0;
-        }
-        sh.prefix[ns] = acc;
-    }
-    __syncthreads();
-    // ---- k-offset tables (element offsets; interpreter tensors are < 4^16 elements)
-    for (int i = 0; i < ns; i++) {
-        const uint32_t t0 = sh.tbl_start[i];
-        if (t0 == kNoTable) continue;
-        const StepDesc &d = sh.steps[i];
-        const uint32_t K = 1u << (2 * d.nSum);
-        for (uint32_t k = tid; k < K; k += blockDim.x) {
-            sh.tbl_a[t0 + k] = (uint32_t) scatter_digits(k, d.posAs, d.nSum);
-            sh.tbl_b[t0 + k] = (uint32_t) scatter_digits(k, d.posBs, d.nSum);
-        }
-    }
-    __syncthreads();
-    // ---- compute
-    const uint32_t total = sh.prefix[ns];
     for (uint32_t base = 0; base < total; base += blockDim.x) {
         const uint32_t item = base + tid;
-        int si = 0;
+        int si = s0;
         if (item < total) {
-            int lo = 0, hi = ns - 1;   // last step whose first item is <= item
+            int lo = s0, hi = s1 - 1;   // last step whose first item is <= item
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
-                if (sh.prefix[mid] <= item) lo = mid; else hi = mid - 1;
+                if (steps[mid].item_start <= item) lo = mid; else hi = mid - 1;
             }
             si = lo;
         }
-        const StepDesc &d = sh.steps[si];
-        const uint32_t g = (uint32_t) sh.group[si];
-        const uint32_t local = item - sh.prefix[si];
+        const StepDesc &d = steps[si];
+        const uint32_t g = d.group;
+        const uint32_t local = item - d.item_start;
         const uint32_t c = local / g;
         const uint32_t lane_k = local % g;
-        const uint32_t n_out = 1u << (2 * d.nFree);
+        const int nFree = d.nFree, nSum = d.nSum;
+        const uint32_t n_out = 1u << (2 * nFree);
         const bool valid = item < total && c < n_out;
-        const uint32_t K = 1u << (2 * d.nSum);
+        const uint32_t K = 1u << (2 * nSum);
         const uint32_t flags = d.flags;
-        const char *abase = ((flags & kALeaf) ? I.leaves : W.workspace) + d.a_off;
-        const char *bbase = ((flags & kBLeaf) ? I.leaves : W.workspace) + d.b_off;
+        const char *abase = ((flags & kALeaf) ? leaves : ws) + d.a_off;
+        const char *bbase = ((flags & kBLeaf) ? leaves : ws) + d.b_off;
         uint32_t oa0 = 0, ob0 = 0;
         if (valid) {
             uint64_t oa, ob;
@@ -205,19 +165,17 @@ __device__ void plan_level(const PlanDesc &P, const InstanceDesc &I, const CtaSc
             oa0 = (uint32_t) oa;
             ob0 = (uint32_t) ob;
         }
-        const uint32_t t0 = sh.tbl_start[si];
-        if (!kMixed) {
-            const double2 *A = reinterpret_cast<const double2 *>(abase);
-            const double2 *B = reinterpret_cast<const double2 *>(bbase);
+        if constexpr (!kMixed) {
             if (valid) {
+                const double2 *A = reinterpret_cast<const double2 *>(abase);
+                const double2 *B = reinterpret_cast<const double2 *>(bbase);
                 double cre = 0.0, cim = 0.0;
                 for (uint32_t k = 0; k < K; k++) {
-                    uint32_t ka, kb;
-                    if (t0 != kNoTable) { ka = sh.tbl_a[t0 + k]; kb = sh.tbl_b[t0 + k]; }
-                    else { ka = (uint32_t) scatter_digits(k, d.posAs, d.nSum); kb = (uint32_t) scatter_digits(k, d.posBs, d.nSum); }
+                    const uint32_t ka = (uint32_t) scatter_digits(k, d.posAs, nSum);
+                    const uint32_t kb = (uint32_t) scatter_digits(k, d.posBs, nSum);
                     cmac_exact(cre, cim, A[oa0 + ka], B[ob0 + kb]);
                 }
-                reinterpret_cast<double2 *>(W.workspace + d.c_off)[c] = make_double2(cre, cim);
+                reinterpret_cast<double2 *>(ws + d.c_off)[c] = make_double2(cre, cim);
             }
         } else {
             const bool f64 = (flags & kCF64) != 0;
@@ -226,9 +184,8 @@ __device__ void plan_level(const PlanDesc &P, const InstanceDesc &I, const CtaSc
             float fre = 0.f, fim = 0.f;
             if (valid) {
                 for (uint32_t k = lane_k; k < K; k += g) {
-                    uint32_t ka, kb;
-                    if (t0 != kNoTable) { ka = sh.tbl_a[t0 + k]; kb = sh.tbl_b[t0 + k]; }
-                    else { ka = (uint32_t) scatter_digits(k, d.posAs, d.nSum); kb = (uint32_t) scatter_digits(k, d.posBs, d.nSum); }
+                    const uint32_t ka = (uint32_t) scatter_digits(k, d.posAs, nSum);
+                    const uint32_t kb = (uint32_t) scatter_digits(k, d.posBs, nSum);
                     if (f64) {
                         double2 a, b;
                         if (a64) a = reinterpret_cast<const double2 *>(abase)[oa0 + ka];
@@ -253,87 +210,70 @@ __device__ void plan_level(const PlanDesc &P, const InstanceDesc &I, const CtaSc
                 if ((uint32_t) off < g) { fre += ore; fim += oim; }
             }
             if (valid && lane_k == 0) {
+                const int ma = step_scale(h, d.a_step), mb = step_scale(h, d.b_step);
+                const int shift = -(ma + mb);
                 float mag;
                 if (f64) {
-                    reinterpret_cast<double2 *>(W.workspace + d.c_off)[c] = make_double2(dre, dim);
+                    dre = ldexp(dre, shift);
+                    dim = ldexp(dim, shift);
+                    reinterpret_cast<double2 *>(ws + d.c_off)[c] = make_double2(dre, dim);
                     mag = (float) fmax(fabs(dre), fabs(dim));
                 } else {
-                    reinterpret_cast<float2 *>(W.workspace + d.c_off)[c] = make_float2(fre, fim);
+                    fre = ldexpf(fre, shift);
+                    fim = ldexpf(fim, shift);
+                    reinterpret_cast<float2 *>(ws + d.c_off)[c] = make_float2(fre, fim);
                     mag = fmaxf(fabsf(fre), fabsf(fim));
                 }
-                atomicMax(&sh.maxbits[si], __float_as_uint(mag));
-            }
-        }
-    }
-    __syncthreads();
-    if constexpr (!kMixed) return;
-    // ---- power-of-two normalisation of every C of this sub-batch
-    for (int i = 0; i < ns; i++) {
-        const StepDesc &d = sh.steps[i];
-        const float mx = __uint_as_float(sh.maxbits[i]);
-        int e = 0;
-        if (mx > 0.f && isfinite(mx)) frexpf(mx, &e);
-        const uint32_t n_out = 1u << (2 * d.nFree);
-        if (e != 0) {
-            if (d.flags & kCF64) {
-                double2 *Cp = reinterpret_cast<double2 *>(W.workspace + d.c_off);
-                for (uint32_t c = tid; c < n_out; c += blockDim.x) {
-                    const double2 v = Cp[c];
-                    Cp[c] = make_double2(ldexp(v.x, -e), ldexp(v.y, -e));
-                }
-            } else {
-                float2 *Cp = reinterpret_cast<float2 *>(W.workspace + d.c_off);
-                for (uint32_t c = tid; c < n_out; c += blockDim.x) {
-                    const float2 v = Cp[c];
-                    Cp[c] = make_float2(ldexpf(v.x, -e), ldexpf(v.y, -e));
+                atomicMax(&h.maxbits[si], __float_as_uint(mag));
+                if (c == 0) {
+                    const int ea = d.a_step >= 0 ? h.expo[d.a_step] : 0;
+                    const int eb = d.b_step >= 0 ? h.expo[d.b_step] : 0;
+                    h.expo[si] = ea + eb + ma + mb;
                 }
             }
         }
-        if (tid == 0) {
-            const int ea = d.a_step >= 0 ? W.exps[d.a_step] : 0;
-            const int eb = d.b_step >= 0 ? W.exps[d.b_step] : 0;
-            W.exps[s_begin + i] = ea + eb + e;
-        }
     }
-    __syncthreads();
 }
 
 template <bool kMixed>
 __global__ void __launch_bounds__(kPlanThreads)
 plan_kernel(const InstanceDesc *__restrict__ instances, int n_instances, char *ws_base, uint64_t ws_stride,
-            int32_t *exps_base, uint64_t exps_stride) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    PlanShared &sh = *reinterpret_cast<PlanShared *>(smem_raw);
-    CtaScratch W;
-    W.workspace = ws_base + (uint64_t) blockIdx.x * ws_stride;
-    W.exps = exps_base ? exps_base + (uint64_t) blockIdx.x * exps_stride : nullptr;
+            int ws_in_smem) {
+    extern __shared__ __align__(256) unsigned char smem_raw[];
+    PlanSmemHeader &h = *reinterpret_cast<PlanSmemHeader *>(smem_raw);
+    char *ws = ws_in_smem ? reinterpret_cast<char *>(smem_raw) + kPlanHeaderBytes
+                          : ws_base + (uint64_t) blockIdx.x * ws_stride;
     for (int inst = blockIdx.x; inst < n_instances; inst += gridDim.x) {
         const InstanceDesc I = instances[inst];
         const PlanDesc P = *I.plan;
-        for (int L = 0; L < P.n_levels; L++) {
-            const int s0 = P.level_start[L], s1 = P.level_start[L + 1];
-            for (int sb = s0; sb < s1; sb += kMaxLevelSteps) {
-                const int se = (s1 - sb) < kMaxLevelSteps ? s1 : sb + kMaxLevelSteps;
-                plan_level<kMixed>(P, I, W, sb, se, sh);
+        if (kMixed) {
+            for (int s = threadIdx.x; s < P.n_steps; s += blockDim.x) {
+                h.maxbits[s] = 0;
+                h.expo[s] = 0;
             }
+            __syncthreads();
+        }
+        for (int L = 0; L < P.n_levels; L++) {
+            plan_level<kMixed>(P.steps, P.level_start[L], P.level_start[L + 1], P.level_items[L], I.leaves, ws, h);
+            __syncthreads();
         }
         // final-value rule of src/Network.h:961-965, applied in contraction order
         if (threadIdx.x == 0) {
             double fre = 0.0, fim = 0.0;
             for (int r = 0; r < P.n_rank0; r++) {
-                const StepDesc &d = P.steps[P.rank0_steps[r]];
+                const int s = P.rank0_steps[r];
+                const StepDesc &d = P.steps[s];
                 double vre, vim;
                 if (!kMixed || (d.flags & kCF64)) {
-                    const double2 v = *reinterpret_cast<const double2 *>(W.workspace + d.c_off);
+                    const double2 v = *reinterpret_cast<const double2 *>(ws + d.c_off);
                     vre = v.x; vim = v.y;
                 } else {
-                    const float2 v = *reinterpret_cast<const float2 *>(W.workspace + d.c_off);
+                    const float2 v = *reinterpret_cast<const float2 *>(ws + d.c_off);
                     vre = v.x; vim = v.y;
                 }
                 if (kMixed) {
-                    const int e = W.exps[P.rank0_steps[r]];
-                    vre = ldexp(vre, e);
-                    vim = ldexp(vim, e);
+                    vre = ldexp(vre, h.expo[s]);
+                    vim = ldexp(vim, h.expo[s]);
                 }
                 if ((fabs(fre) <= 1.0e-30 && fabs(fim) <= 1.0e-30) || (d.flags & kBothRank0)) {
                     fre = vre;
@@ -378,27 +318,24 @@ cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C
     return cudaGetLastError();
 }
 
-size_t plan_smem_bytes() { return sizeof(PlanShared); }
-
-int plan_max_grid() {
-    // resident CTAs: 256 threads and ~41 KB of shared memory each
-    return num_sms() * 4;
+int plan_max_grid(size_t smem_bytes) {
+    int dev = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, plan_kernel<true>, kPlanThreads, smem_bytes);
+    if (per_sm < 1) per_sm = 1;
+    return num_sms() * per_sm;
 }
 
 cudaError_t launch_plan(const InstanceDesc *instances, int n_instances, bool mixed, int grid, char *ws_base,
-                        uint64_t ws_stride, int32_t *exps_base, uint64_t exps_stride, cudaStream_t stream) {
+                        uint64_t ws_stride, bool ws_in_smem, cudaStream_t stream) {
     if (n_instances <= 0) return cudaSuccess;
-    const size_t smem = sizeof(PlanShared);
-    static bool attr_done[2] = {false, false};
-    if (!attr_done[mixed]) {
-        cudaError_t e = mixed ? cudaFuncSetAttribute(plan_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)
-                              : cudaFuncSetAttribute(plan_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-        if (e != cudaSuccess) return e;
-        attr_done[mixed] = true;
-    }
+    const size_t smem = kPlanHeaderBytes + (ws_in_smem ? ws_stride : 0);
+    cudaError_t e = mixed ? cudaFuncSetAttribute(plan_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)
+                          : cudaFuncSetAttribute(plan_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    if (e != cudaSuccess) return e;
     if (grid <= 0 || grid > n_instances) grid = n_instances;
-    if (mixed) plan_kernel<true><<<grid, kPlanThreads, smem, stream>>>(instances, n_instances, ws_base, ws_stride, exps_base, exps_stride);
-    else plan_kernel<false><<<grid, kPlanThreads, smem, stream>>>(instances, n_instances, ws_base, ws_stride, exps_base, exps_stride);
+    if (mixed) plan_kernel<true><<<grid, kPlanThreads, smem, stream>>>(instances, n_instances, ws_base, ws_stride, ws_in_smem ? 1 : 0);
+    else plan_kernel<false><<<grid, kPlanThreads, smem, stream>>>(instances, n_instances, ws_base, ws_stride, ws_in_smem ? 1 : 0);
     return cudaGetLastError();
 }
 

@@ -9,12 +9,12 @@ namespace qtg {
 // rounding; otherwise complex64 with FP32 FMA.
 cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C, bool f64, cudaStream_t stream);
 
-// Grouped interpreter over plan instances; workspace and exponent buffers are
-// per CTA (ws_base + blockIdx.x * ws_stride).
-cudaError_t launch_plan(const InstanceDesc *instances, int n_instances, bool mixed, int grid,
-                        char *ws_base, uint64_t ws_stride, int32_t *exps_base, uint64_t exps_stride,
-                        cudaStream_t stream);
-size_t plan_smem_bytes();
-int plan_max_grid();
+// Grouped interpreter over plan instances.  The workspace of a CTA is either
+// its shared memory (ws_in_smem; ws_stride bytes after the header) or
+// ws_base + blockIdx.x * ws_stride in global memory.
+cudaError_t launch_plan(const InstanceDesc *instances, int n_instances, bool mixed, int grid, char *ws_base,
+                        uint64_t ws_stride, bool ws_in_smem, cudaStream_t stream);
+// resident CTAs of the interpreter for a given dynamic shared memory size
+int plan_max_grid(size_t smem_bytes);
 
 }  // namespace qtg

@@ -206,11 +206,30 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
             if (r.freeIdx.empty()) d.flags |= kOutRank0;
             if (r.rankA == 0 && r.rankB == 0) d.flags |= kBothRank0;
         }
+        // interpreter schedule: work items of each level, lane groups for tiny outputs
+        // (mixed form only; FP64 keeps one accumulator per output element)
+        p->level_items[prec].assign(n_levels, 0);
+        for (int L0 = 0; L0 < n_levels; L0++) {
+            uint32_t acc = 0;
+            for (int i = p->level_start[L0]; i < p->level_start[L0 + 1]; i++) {
+                StepDesc &d = steps[i];
+                const uint64_t n_out = 1ull << (2 * d.nFree), K = 1ull << (2 * d.nSum);
+                uint32_t g = 1;
+                if (mixed && !(d.flags & kCF64))
+                    while (g < 16 && g * 2 <= K && n_out * g * 2 <= (uint64_t) kPlanThreads) g *= 2;
+                acc = (acc + g - 1) / g * g;   // a lane group starts on a multiple of its size
+                d.group = (uint8_t) g;
+                d.item_start = acc;
+                const uint64_t next = acc + n_out * g;
+                acc = next > 0xffffffffull ? 0xffffffffu : (uint32_t) next;
+            }
+            p->level_items[prec][L0] = acc;
+        }
     }
     p->n_steps = S;
     p->n_levels = n_levels;
     p->grouped = p->max_step_out <= kGroupedMaxRank && p->max_step_k <= kGroupedMaxSum &&
-                 p->ws_bytes[QT_PREC_FP64] <= kGroupedMaxWorkspace;
+                 p->ws_bytes[QT_PREC_FP64] <= kGroupedMaxWorkspace && S <= kPlanMaxSteps;
     for (int i = 0; i < L; i++) p->peak_rank = std::max(p->peak_rank, leaves[i]->mRank);
     return QT_OK;
 }
@@ -222,10 +241,12 @@ qt_status upload_plan(qt_plan *p, int prec) {
     const size_t steps_bytes = sizeof(StepDesc) * p->steps[prec].size();
     const size_t lvl_bytes = sizeof(int32_t) * p->level_start.size();
     const size_t r0_bytes = sizeof(int32_t) * (p->rank0_steps.size() + 1);
+    const size_t items_bytes = sizeof(uint32_t) * (p->level_items[prec].size() + 1);
     const size_t off_steps = align_up(sizeof(PlanDesc), 256);
     const size_t off_lvl = align_up(off_steps + steps_bytes, 256);
     const size_t off_r0 = align_up(off_lvl + lvl_bytes, 256);
-    const size_t total = off_r0 + r0_bytes;
+    const size_t off_items = align_up(off_r0 + r0_bytes, 256);
+    const size_t total = off_items + items_bytes;
     void *d = nullptr;
     qt_status s = dev_alloc(ctx, total, &d);
     if (s != QT_OK) return s;
@@ -234,6 +255,7 @@ qt_status upload_plan(qt_plan *p, int prec) {
     pd.steps = reinterpret_cast<const StepDesc *>((char *) d + off_steps);
     pd.level_start = reinterpret_cast<const int32_t *>((char *) d + off_lvl);
     pd.rank0_steps = reinterpret_cast<const int32_t *>((char *) d + off_r0);
+    pd.level_items = reinterpret_cast<const uint32_t *>((char *) d + off_items);
     pd.n_steps = p->n_steps;
     pd.n_levels = p->n_levels;
     pd.n_rank0 = (int32_t) p->rank0_steps.size();
@@ -242,6 +264,8 @@ qt_status upload_plan(qt_plan *p, int prec) {
     if (steps_bytes) std::memcpy(host.data() + off_steps, p->steps[prec].data(), steps_bytes);
     if (lvl_bytes) std::memcpy(host.data() + off_lvl, p->level_start.data(), lvl_bytes);
     if (!p->rank0_steps.empty()) std::memcpy(host.data() + off_r0, p->rank0_steps.data(), r0_bytes - sizeof(int32_t));
+    if (!p->level_items[prec].empty())
+        std::memcpy(host.data() + off_items, p->level_items[prec].data(), items_bytes - sizeof(uint32_t));
     cudaError_t e = cudaMemcpyAsync(d, host.data(), total, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {

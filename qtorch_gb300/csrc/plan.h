@@ -15,6 +15,8 @@ constexpr int kMixedTailRank = 1;
 constexpr int kGroupedMaxRank = 11;
 constexpr int kGroupedMaxSum = 8;
 constexpr uint64_t kGroupedMaxWorkspace = 96ull << 20;
+// a batch whose largest workspace is at most this keeps it in shared memory
+constexpr uint64_t kSmemWorkspaceMax = 96ull << 10;
 
 }  // namespace qtg
 
@@ -32,6 +34,7 @@ struct qt_plan {
     std::vector<int> a_leaf, b_leaf;                  // leaf index of each operand or -1
     std::vector<int32_t> level_start;
     std::vector<int32_t> rank0_steps;
+    std::vector<uint32_t> level_items[2];             // interpreter work items per level, per precision
     std::vector<uint64_t> leaf_off[2];
     uint64_t leaf_bytes[2] = {0, 0};
     uint64_t ws_bytes[2] = {0, 0};
@@ -58,6 +61,7 @@ struct qt_batch {
     void *d_ws = nullptr;
     void *d_exps = nullptr;
     uint64_t ws_stride = 0, exps_stride = 0;
+    bool ws_in_smem = false;
     int grid = 0;
     void *h_leaves = nullptr;                         // pinned staging of the leaf image
     void *h_values = nullptr;                         // pinned values

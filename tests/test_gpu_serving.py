@@ -1,0 +1,80 @@
+"""Serving: continuous batching with memory admission.  Each request's result
+is the same alone and in the mix (bit for bit in FP64, within 1e-6 in the
+mixed form)."""
+import time
+
+import numpy as np
+import pytest
+
+import qtorch_gb300 as qg
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def request_mix(ctx):
+    """QAOA terms at several points plus a few golden sample circuits."""
+    plans = []
+    dgf = qg.random_regular_graph(20, 3, seed=9)
+    rng = np.random.default_rng(3)
+    for e in range(0, qg.qaoa_num_edges(dgf), 3):
+        bg = list(rng.uniform(0, np.pi, 2))
+        q, m = qg.qaoa_term_text(dgf, 1, bg, e)
+        plans.append(qg.Plan(q, m, ordering="linegraph", ctx=ctx))
+    for case in load_golden("networks.json"):
+        if case["gate_files"]:
+            continue
+        plans.append(qg.Plan(case["qasm"], case["measure"], ordering="sequence", sequence=case["sequence"], ctx=ctx))
+    return plans
+
+
+@pytest.mark.parametrize("prec", [qg.FP64, qg.MIXED])
+def test_alone_equals_in_the_mix(ctx, prec):
+    plans = request_mix(ctx)
+    alone = [p.execute(prec) for p in plans]
+    srv = qg.Server(max_inflight=8, precision=prec, ctx=ctx)
+    try:
+        tickets = []
+        for i, p in enumerate(plans):
+            tickets.append(srv.submit(p))
+            if i % 4 == 0:
+                time.sleep(0.001)    # arrivals while earlier requests run
+        srv.drain()
+        mixed = [srv.poll(t) for t in tickets]
+        stats = srv.stats()
+    finally:
+        srv.close()
+    assert all(m is not None for m in mixed)
+    for a, (v, lat) in zip(alone, mixed):
+        if prec == qg.FP64:
+            assert v == a
+        else:
+            assert abs(v - a) <= 1e-6
+        assert lat >= 0
+    assert stats["completed"] == len(plans)
+    assert 0 < stats["p50_s"] <= stats["p99_s"]
+
+
+def test_admission_respects_memory_budget():
+    c = qg.Context(0)
+    try:
+        plans = request_mix(c)[:6]
+        need = max(p.workspace_bytes(qg.FP64) for p in plans) + 64 * 1024
+        c.set_memory_budget(need * 3)
+        srv = qg.Server(max_inflight=64, precision=qg.FP64, ctx=c)
+        try:
+            tickets = [srv.submit(p) for p in plans]
+            srv.drain()
+            assert all(srv.poll(t) is not None for t in tickets)
+        finally:
+            srv.close()
+        # a request larger than the whole budget is refused at submission
+        c.set_memory_budget(1024)
+        srv = qg.Server(max_inflight=4, precision=qg.FP64, ctx=c)
+        try:
+            with pytest.raises(qg.OutOfMemory):
+                srv.submit(plans[0])
+        finally:
+            srv.close()
+    finally:
+        c.close()
