@@ -159,6 +159,13 @@ int64_t qt_network_node_values(qt_network *net, int node_id, double *out, int64_
 /* Line-graph wire order chosen by the min-fill heuristic (1-based, qbb.out order). */
 int qt_network_linegraph_order(qt_network *net, int32_t *order_1based, int cap);
 
+/* Run an .inp script (src/leviParser.hpp:41-104, the flow of src/main.cpp:42-309):
+ * parse the QASM and measurement files it names, ReduceCircuit, contract with
+ * its contractmethod (linegraph-qbb | simple-stoch | user-defined; qbbonly /
+ * readqbbresonly use output/qbb.out in QuickBB's format) and write its output
+ * file.  ctx == NULL runs the bookkeeping only (value 0).  value: 2 doubles. */
+qt_status qt_run_inp(qt_ctx *ctx, const char *inp_path, double *value, int64_t *flops);
+
 /* ---- plans: an ordering lowered once, executed many times ---------------
  *
  * A plan is built by running the ordering over a symbolic copy of the network

@@ -206,6 +206,17 @@ int main(int argc, char **argv) {
             print_value(rem[0]->GetTensorVals()[0]);
             std::printf("flops %lld\n", net->getNumFloatOps());
             print_sequence(net);
+        } else if (cmd == "reduce" && argc >= 4) {
+            // ReduceCircuit (Network.h:1015-1118), then a stochastic contraction
+            auto net = std::make_shared<Network>(argv[2], argv[3]);
+            net->SetNumThreads(1);
+            net->ReduceCircuit();
+            std::printf("reduced_nodes %zu %zu\n", net->GetAllNodes().size(), net->GetUncontractedNodes().size());
+            print_sequence(net);
+            ContractionTools t(net);
+            t.Contract(Stochastic);
+            print_value(t.GetFinalVal());
+            print_sequence(net);
         } else if (cmd == "lgwires" && argc >= 4) {
             auto net = std::make_shared<Network>(argv[2], argv[3]);
             LineGraph lg(net);

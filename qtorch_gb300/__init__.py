@@ -601,3 +601,12 @@ def random_regular_graph(num_nodes, degree, seed):
     buf = ctypes.create_string_buffer(int(n))
     _lib().qt_random_regular_graph(num_nodes, degree, int(seed), buf, int(n))
     return buf.value.decode()
+
+
+def run_inp(path, ctx=None, symbolic=False):
+    """Run an .inp script (src/main.cpp flow): returns (value, flop counter)."""
+    c = None if symbolic else (ctx or default_context())
+    v = np.zeros(2)
+    fl = ctypes.c_int64(0)
+    _check(_lib().qt_run_inp(c.handle if c else None, path.encode(), _dp(v), ctypes.byref(fl)), c)
+    return complex(v[0], v[1]), fl.value

@@ -55,6 +55,7 @@ SIGNATURES = [
     ("qt_network_created_from", c_int, [c_void_p, P(c_int32), c_int]),
     ("qt_network_node_values", c_int64, [c_void_p, c_int, P(c_double), c_int64]),
     ("qt_network_linegraph_order", c_int, [c_void_p, P(c_int32), c_int]),
+    ("qt_run_inp", c_int, [c_void_p, c_char_p, P(c_double), P(c_int64)]),
     ("qt_plan_build", c_int, [c_void_p, c_char_p, c_char_p, c_char_p, c_int, c_uint64, P(c_int32), c_int,
                               P(c_void_p)]),
     ("qt_plan_free", c_int, [c_void_p]),

@@ -319,9 +319,10 @@ cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C
 }
 
 int plan_max_grid(size_t smem_bytes) {
-    int dev = 0, per_sm = 0;
-    cudaGetDevice(&dev);
+    int per_sm = 0;
+    cudaFuncSetAttribute(plan_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_bytes);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, plan_kernel<true>, kPlanThreads, smem_bytes);
+    cudaGetLastError();
     if (per_sm < 1) per_sm = 1;
     return num_sms() * per_sm;
 }

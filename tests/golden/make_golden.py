@@ -206,20 +206,42 @@ def gen_linegraph(ref_root, cwd):
     return out
 
 
+def gen_reduce(ref_root, cwd):
+    """ReduceCircuit's contractions, then a stochastic finish (main.cpp:112 path)."""
+    out = []
+    for qasm, meas in (("test_JW.qasm", "Z T T T"), ("rand-nq6-cn2-d10_rxyz.qasm", "Z T Z T Z T"),
+                       ("qft4.qasm", "X Y Z 0"), ("catStateEightQubits.qasm", "Z Z T T T T T T")):
+        mpath = "/tmp/qt_golden_reduce_meas.txt"
+        with open(mpath, "w") as f:
+            f.write(meas)
+        d = parse_kv(run(["reduce", os.path.join("Samples", qasm), mpath], cwd))
+        red = [int(x) for x in d["sequence"][0]]
+        full = [int(x) for x in d["sequence"][1]]
+        out.append({"name": qasm, "qasm": open(os.path.join(ref_root, "Samples", qasm)).read(), "measure": meas,
+                    "reduced_nodes": [int(x) for x in d["reduced_nodes"][0]],
+                    "reduce_sequence": [[red[i], red[i + 1]] for i in range(0, len(red), 2)],
+                    "sequence": [[full[i], full[i + 1]] for i in range(0, len(full), 2)],
+                    "value": [float(d["value"][0][0]), float(d["value"][0][1])]})
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-root", default="/root/reference")
+    ap.add_argument("--only", nargs="*", help="regenerate only these fixtures (the stochastic ones change every run)")
     args = ap.parse_args()
     src = os.path.join(args.ref_root, "src")
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", f"REF_SRC={src}"], check=True)
     cwd = args.ref_root
-    fixtures = {
-        "gates.json": gen_gates(cwd),
-        "pairs.json": gen_pairs(cwd),
-        "networks.json": gen_networks(args.ref_root, cwd),
-        "qaoa.json": gen_qaoa(args.ref_root, cwd),
-        "linegraph.json": gen_linegraph(args.ref_root, cwd),
+    makers = {
+        "gates.json": lambda: gen_gates(cwd),
+        "pairs.json": lambda: gen_pairs(cwd),
+        "networks.json": lambda: gen_networks(args.ref_root, cwd),
+        "qaoa.json": lambda: gen_qaoa(args.ref_root, cwd),
+        "linegraph.json": lambda: gen_linegraph(args.ref_root, cwd),
+        "reduce.json": lambda: gen_reduce(args.ref_root, cwd),
     }
+    fixtures = {k: f() for k, f in makers.items() if not args.only or k in args.only}
     for name, data in fixtures.items():
         with open(os.path.join(HERE, name), "w") as f:
             json.dump(data, f, indent=0)

@@ -192,3 +192,17 @@ def test_reduce_circuit_then_contract():
     assert n.num_uncontracted < before
     n.contract_stochastic(5)
     assert n.is_done
+
+
+@pytest.mark.parametrize("case", load_golden("reduce.json"), ids=lambda c: c["name"])
+def test_reduce_circuit_matches_reference(case):
+    """ReduceCircuit makes the reference's contractions in the reference's order (Network.h:1015-1118)."""
+    n = qg.Network(case["qasm"], case["measure"], symbolic=True)
+    n.reduce()
+    assert [list(p) for p in n.created_from()] == case["reduce_sequence"]
+    assert [n.num_nodes, n.num_uncontracted] == case["reduced_nodes"]
+    rest = case["sequence"][len(case["reduce_sequence"]):]
+    n.contract_sequence(rest)
+    assert n.is_done
+    v, _ = port.replay_value(case["qasm"], case["measure"], case["sequence"])
+    assert v == complex(*case["value"])
