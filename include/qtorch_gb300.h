@@ -192,6 +192,32 @@ uint64_t qt_plan_leaf_elems(const qt_plan *plan);
 qt_status qt_plan_leaf_values(const qt_plan *plan, double *out, uint64_t cap_complex);
 /* One network value (synchronous, host in / host out). */
 qt_status qt_plan_execute(qt_ctx *ctx, qt_plan *plan, qt_precision prec, double *re_im);
+/* Size of the device array that qt_plan_execute_static works in.  It is
+ * reserved statically: every GPU that loads this library holds it until the
+ * process exits. */
+#define QT_STATIC_SCRATCH_BYTES (8u << 20)
+
+/* One plan instance evaluated without allocating device memory (no reference
+ * counterpart: qTorch has no device code).  It is meant for callers that cannot
+ * call cudaMalloc -- code running under a framework that owns all device memory
+ * (a custom call or operator whose allocator belongs to the host framework) and
+ * latency-bound loops that must never pay cudaMalloc's implicit device
+ * synchronisation.
+ *   leaves_device: the plan's leaf tensors in device memory owned by the caller,
+ *                  concatenated in leaf order (the order of qt_plan_leaf_values):
+ *                  complex128 for QT_PREC_FP64, complex64 for QT_PREC_MIXED;
+ *   value_device:  two doubles (re, im) in device memory owned by the caller.
+ * The descriptors of the plan and its intermediates live in a static device
+ * array of QT_STATIC_SCRATCH_BYTES; a plan that needs more (descriptors plus
+ * workspace) is rejected with QT_ERR_OUT_OF_MEMORY, and a plan beyond the
+ * grouped interpreter's limits with QT_ERR_INVALID_ARGUMENT.  The first call on
+ * a device looks the array's device address up, so make it before any stream
+ * capture.  Every call shares the one array and overwrites what the previous
+ * call left there: calls that overlap on the GPU (other streams, other
+ * contexts of the same device) race.  The call returns after the launch; the
+ * value is ready once the context stream reaches it. */
+qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *plan, qt_precision prec, const void *leaves_device,
+                                 double *value_device);
 /* Parametrised rotation leaves (Rx, Ry, Rz, PHASE, CPHASE) of the plan, in leaf
  * order: their count, and the angles the plan's own circuit gives them. */
 int qt_plan_num_rotations(const qt_plan *plan);

@@ -69,6 +69,7 @@ SIGNATURES = [
     ("qt_plan_leaf_elems", c_uint64, [c_void_p]),
     ("qt_plan_leaf_values", c_int, [c_void_p, P(c_double), c_uint64]),
     ("qt_plan_execute", c_int, [c_void_p, c_void_p, c_int, P(c_double)]),
+    ("qt_plan_execute_static", c_int, [c_void_p, c_void_p, c_int, c_void_p, P(c_double)]),
     ("qt_plan_num_rotations", c_int, [c_void_p]),
     ("qt_plan_rotation_angles", c_int, [c_void_p, P(c_double), c_int]),
     ("qt_batch_set_rotations", c_int, [c_void_p, P(c_double), c_int64]),

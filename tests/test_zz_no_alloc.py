@@ -1,0 +1,90 @@
+"""qt_plan_execute_static, the entry point that allocates no device memory.
+
+Some callers cannot call cudaMalloc: code that runs under a framework that owns
+every byte of the device, or a latency-bound loop that must not pay
+cudaMalloc's implicit synchronisation.  They hand over inputs and outputs in
+device memory they already own, and the engine works in a statically reserved
+device array.  This test calls that entry point through the C ABI, twice in a
+row on the same static array, and checks it against qt_plan_execute: equal bit
+for bit in FP64, within 1e-6 in the mixed form.  It lives in a file of its own
+that pytest collects last."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import qtorch_gb300 as qg
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+MIXED_TOL = 1e-6
+
+
+def static_call(lib, ctx, plan, prec, leaves, out):
+    return lib.qt_plan_execute_static(ctx.handle, plan.handle, prec, ctypes.c_void_p(leaves.data_ptr()),
+                                      ctypes.cast(ctypes.c_void_p(out.data_ptr()), ctypes.POINTER(ctypes.c_double)))
+
+
+def plans_under_test(ctx):
+    dgf = qg.random_regular_graph(20, 3, seed=12)
+    out = []
+    for p, bg in ((1, [0.7, 1.3]), (2, [0.2, 0.9, 1.1, 0.4])):
+        for e in (0, 5):
+            q, m = qg.qaoa_term_text(dgf, p, bg, e)
+            out.append(qg.Plan(q, m, ordering="linegraph", ctx=ctx))
+    case = load_golden("networks.json")[0]
+    out.append(qg.Plan(case["qasm"], case["measure"], ordering="sequence", sequence=case["sequence"], ctx=ctx))
+    return out
+
+
+@pytest.mark.parametrize("prec", [qg.FP64, qg.MIXED], ids=["fp64", "mixed"])
+def test_static_entry_point_matches_plan_execute(prec):
+    import torch
+    lib = qg._capi.load()
+    lib.qt_plan_execute_static.restype = ctypes.c_int
+    lib.qt_plan_execute_static.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.POINTER(ctypes.c_double)]
+    ctx = qg.Context(0)
+    try:
+        for plan in plans_under_test(ctx):
+            want = plan.execute(prec)
+            leaves = plan.leaf_values()
+            if prec == qg.MIXED:
+                leaves = leaves.astype(np.complex64)
+            d_leaves = torch.from_numpy(leaves).cuda()
+            got = []
+            for _ in range(2):   # two calls in a row on the same static array
+                out = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda")
+                torch.cuda.synchronize()
+                assert static_call(lib, ctx, plan, prec, d_leaves, out) == 0, ctx.last_error
+                ctx.synchronize()
+                v = out.cpu().numpy()
+                got.append(complex(v[0], v[1]))
+            for g in got:
+                if prec == qg.FP64:
+                    assert g == want
+                else:
+                    assert abs(g - want) <= MIXED_TOL
+    finally:
+        ctx.close()
+
+
+def test_static_entry_point_rejects_oversized_plans():
+    import torch
+    lib = qg._capi.load()
+    lib.qt_plan_execute_static.restype = ctypes.c_int
+    lib.qt_plan_execute_static.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.POINTER(ctypes.c_double)]
+    ctx = qg.Context(0)
+    try:
+        case = [c for c in load_golden("networks.json") if c["name"] == "4regRand20Node1-p1.qasm"][0]
+        plan = qg.Plan(case["qasm"], case["measure"], ordering="sequence", sequence=case["sequence"], ctx=ctx)
+        assert plan.workspace_bytes(qg.FP64) > 8 << 20
+        d_leaves = torch.from_numpy(plan.leaf_values()).cuda()
+        out = torch.zeros(2, dtype=torch.float64, device="cuda")
+        rc = static_call(lib, ctx, plan, qg.FP64, d_leaves, out)
+        assert rc == 9   # QT_ERR_OUT_OF_MEMORY
+        assert "static scratch" in ctx.last_error
+    finally:
+        ctx.close()
