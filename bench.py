@@ -206,6 +206,74 @@ def time_steps(run, steps, warmup, stream, flush):
     return times
 
 
+def term_layer_shape(qasm_text, p):
+    """(edges per layer, qubits) of a light-cone term: rotations come as
+    [Rz(-gamma_i) x E, Rx(2 beta_i) x n] for i = 1..p (src/maxcut.h:205-233)."""
+    n = int(qasm_text.split("\n", 1)[0])
+    n_rz = sum(1 for line in qasm_text.split("\n") if line.startswith("Rz "))
+    return n_rz // p, n
+
+
+def rotation_vector(shapes, point, p):
+    """Rotation angles of every term at one point, as the parser reads the reference's text."""
+    betas, gammas = point[:p], point[p:]
+    out = []
+    for e, n in shapes:
+        for i in range(p):
+            out += [float("%g" % -gammas[i])] * e + [float("%g" % (betas[i] * 2.0))] * n
+    return out
+
+
+def run_batched(ctx, args, stream, flush):
+    """Config 4: 64 seeded (gamma, beta) points x all edge terms of 16 random
+    3-regular graphs with 20-40 vertices, p = 1 or 2, in one grouped launch."""
+    import qtorch_gb300 as qg
+    rng = np.random.default_rng(4242)
+    graphs = []
+    for g in range(16):
+        n = int(rng.integers(10, 21)) * 2
+        p = 1 + (g % 2)
+        graphs.append((qg.random_regular_graph(n, 3, seed=100 + g), p))
+    n_points = args.batched_points
+    plans, shapes, ps = [], [], []
+    for dgf, p in graphs:
+        pt0 = [0.3] * p + [0.7] * p
+        for e in range(qg.qaoa_num_edges(dgf)):
+            q, m = qg.qaoa_term_text(dgf, p, pt0, e)
+            plans.append(qg.Plan(q, m, ordering="linegraph", ctx=ctx))
+            shapes.append(term_layer_shape(q, p))
+            ps.append(p)
+    points = [list(rng.uniform(0.0, math.pi, 4)) for _ in range(n_points)]   # beta1, beta2, gamma1, gamma2
+    angles = []
+    for pt in points:
+        for sh, p in zip(shapes, ps):
+            angles += rotation_vector([sh], pt[:p] + pt[2:2 + p], p)
+    res = {}
+    for prec in (qg.MIXED, qg.FP64):
+        b = qg.Batch(ctx)
+        for _ in points:
+            for pl in plans:
+                b.add(pl)
+        b.set_rotations(np.array(angles))
+        b.prepare(prec)
+        b.use_graph(True)
+        vals = b.execute(prec)
+        t = time_steps(b.run, args.batched_steps, 3, stream, flush)
+        res[prec] = (vals, sum(t) / len(t), len(b), b.launches_per_run)
+        b._release()
+    n_inst = res[qg.MIXED][2]
+    err = np.abs(res[qg.MIXED][0] - res[qg.FP64][0])
+    mixed_rate = n_inst / res[qg.MIXED][1]
+    fp64_rate = n_inst / res[qg.FP64][1]
+    return {"workload": "64 seeded (gamma,beta) points x all edge terms of 16 random 3-regular graphs, "
+                        "20-40 vertices, p=1 (8 graphs) and p=2 (8 graphs), one grouped launch per step",
+            "terms_per_step": n_inst, "distinct_plans": len(plans), "mixed_terms_per_s": mixed_rate,
+            "fp64_terms_per_s": fp64_rate, "mixed_over_fp64": mixed_rate / fp64_rate,
+            "mixed_ms_per_step": 1e3 * res[qg.MIXED][1], "fp64_ms_per_step": 1e3 * res[qg.FP64][1],
+            "error_vs_fp64": {"max_abs": float(err.max()), "mean_abs": float(err.mean())},
+            "launches_per_step": res[qg.MIXED][3]}
+
+
 def run_engine(args):
     import torch
 
@@ -322,6 +390,9 @@ def run_engine(args):
         "gpu_launches": int(args.steps * batches[qg.MIXED].launches_per_run),
         "clocks": clk.summary(),
     }
+    if not args.no_batched:
+        bm._release()
+        line["batched"] = run_batched(ctx, args, stream, flush)
     if rank == 0 and world == 1 and not args.no_cpu:
         seqs = sequences_for(terms)
         jobs = [(q, m, s) for (q, m), s in zip(terms, seqs)]
@@ -388,6 +459,9 @@ def main():
     ap.add_argument("--graph-seed", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-point x 16-graph batched workload")
+    ap.add_argument("--batched-points", type=int, default=64)
+    ap.add_argument("--batched-steps", type=int, default=5)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -457,7 +457,7 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
     const int n = (int) b->plans.size();
     b->stepwise.clear();
     b->inst_leaf_off.assign(n, 0);
-    uint64_t off = 0, ws = 0, ex = 0;
+    uint64_t off = 0, ws = 0, ex = 0, ws_small = 0, stage_small = 0;
     int n_grouped = 0;
     for (int i = 0; i < n; i++) {
         qt_plan *p = b->plans[i];
@@ -469,16 +469,25 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
         if (s != QT_OK) return s;
         b->inst_leaf_off[i] = off;
         off += (p->leaf_bytes[prec] + 255) / 256 * 256;
-        ws = std::max<uint64_t>(ws, p->ws_bytes[prec]);
+        const uint64_t w = (p->ws_bytes[prec] + 255) / 256 * 256;
+        const uint64_t st = round16(p->dev_bytes[prec]) + round16(p->leaf_bytes[prec]);
+        ws = std::max<uint64_t>(ws, w);
+        if (w <= kSmemWorkspaceMax) ws_small = std::max<uint64_t>(ws_small, w);
+        if (st <= kSmemStageMax / 2) stage_small = std::max<uint64_t>(stage_small, st);
         ex = std::max<uint64_t>(ex, (uint64_t) p->n_steps);
         n_grouped++;
     }
     b->leaf_bytes = off;
-    b->ws_stride = (ws + 255) / 256 * 256;
+    b->ws_stride = ws;
     b->exps_stride = (ex + 63) / 64 * 64;
-    // small workspaces live in shared memory, the rest in per-CTA global scratch
-    b->ws_in_smem = b->ws_stride <= kSmemWorkspaceMax;
-    b->grid = std::min(n_grouped, plan_max_grid(kPlanHeaderBytes + (b->ws_in_smem ? b->ws_stride : 0)));
+    // shared memory of a CTA: a workspace region as large as the largest workspace
+    // that fits it and a staging region as large as the largest plan block + leaf
+    // image that fits; instances beyond either use the global slab / read in place
+    b->ws_smem_bytes = (uint32_t) ws_small;
+    if (kPlanHeaderBytes + 128 + b->ws_smem_bytes + stage_small > kSmemStageMax) stage_small = 0;
+    b->stage_bytes = b->allow_stage ? (uint32_t) stage_small : 0;
+    b->ws_in_smem = ws <= b->ws_smem_bytes;   // no global slab needed
+    b->grid = std::min(n_grouped, plan_max_grid(kPlanHeaderBytes + 128 + b->ws_smem_bytes + b->stage_bytes));
     qt_status s = QT_OK;
     auto chk = [&](cudaError_t e, const char *w) {
         if (s == QT_OK && e != cudaSuccess) s = cuda_error(ctx, e, w);
@@ -505,6 +514,10 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
         d.plan = reinterpret_cast<const PlanDesc *>(p->dev[prec]);
         d.leaves = (const char *) b->d_leaves + b->inst_leaf_off[i];
         d.value = (double *) b->d_values + 2 * i;
+        d.plan_bytes = b->stage_bytes ? (uint32_t) round16(p->dev_bytes[prec]) : 0;
+        d.leaf_bytes = (uint32_t) round16(p->leaf_bytes[prec]);
+        d.ws_bytes = (uint32_t) ((p->ws_bytes[prec] + 255) / 256 * 256);
+        d.pad = 0;
         inst.push_back(d);
     }
     if (!inst.empty()) {
@@ -540,8 +553,15 @@ static qt_status batch_launch(qt_batch *b) {
     qt_ctx *ctx = b->ctx;
     const int n_grouped = (int) b->plans.size() - (int) b->stepwise.size();
     if (n_grouped <= 0) return QT_OK;
-    cudaError_t e = launch_plan((const InstanceDesc *) b->d_inst, n_grouped, b->prepared_prec == QT_PREC_MIXED,
-                                b->grid, (char *) b->d_ws, b->ws_stride, b->ws_in_smem, ctx->stream);
+    PlanLaunch lp;
+    lp.instances = (const InstanceDesc *) b->d_inst;
+    lp.n_instances = n_grouped;
+    lp.ws_smem_bytes = b->ws_smem_bytes;
+    lp.ws_base = (char *) b->d_ws;
+    lp.ws_stride = b->ws_stride;
+    lp.stage_bytes = b->stage_bytes;
+    lp.pad = 0;
+    cudaError_t e = launch_plan(lp, b->prepared_prec == QT_PREC_MIXED, b->grid, ctx->stream);
     ctx->launches++;
     return cuda_error(ctx, e, "plan kernel launch");
 }

@@ -11,6 +11,8 @@
 // are stored in the reference's inner-loop digit order (digit i of k <-> pair
 // nSum-1-i, Network.h:912-916) so that k itself walks the reference's order.
 #pragma once
+#include <vector_types.h>
+
 #include <cstdint>
 
 namespace qtg {
@@ -46,7 +48,11 @@ struct StepDesc {
     uint8_t posAs[kMaxWires];
     uint8_t posBs[kMaxWires];
     uint32_t item_start;         // interpreter: first work item of this step inside its level
+    uint32_t tab_off;            // interpreter: first entry of this step's offset tables (kNoTable: none)
+    uint32_t pad2;
 };
+
+constexpr uint32_t kNoTable = 0xffffffffu;
 static_assert(sizeof(StepDesc) % 8 == 0, "StepDesc alignment");
 
 // One executable plan in device memory.
@@ -55,6 +61,10 @@ struct PlanDesc {
     const int32_t *level_start;  // n_levels + 1 entries
     const int32_t *rank0_steps;  // steps with a rank-0 output, in contraction (sequence) order
     const uint32_t *level_items; // work items of each level (n_levels entries)
+    // Offset tables of steps whose operands have at most 4^8 elements: for step s,
+    // tab[tab_off + c] = (A offset, B offset) of output c (n_out entries), then
+    // tab[tab_off + n_out + k] = (A offset, B offset) of summed index k (K entries).
+    const ushort2 *tables;
     int32_t n_steps;
     int32_t n_levels;
     int32_t n_rank0;
@@ -64,9 +74,27 @@ struct PlanDesc {
 // One instance of a batch: a plan with its own leaves.  Intermediates live in
 // the workspace of the CTA that runs the instance.
 struct InstanceDesc {
-    const PlanDesc *plan;        // device pointer
+    const PlanDesc *plan;        // device pointer to the plan block (PlanDesc and its arrays)
     const char *leaves;          // leaf buffer of this instance (complex128, or complex64 in mixed mode)
     double *value;               // 2 doubles out
+    uint32_t plan_bytes;         // bytes of the plan block (multiple of 16) when it may be staged, else 0
+    uint32_t leaf_bytes;         // bytes of the leaf image (multiple of 16)
+    uint32_t ws_bytes;           // workspace this instance needs
+    uint32_t pad;
+};
+
+// Parameters of one interpreter launch.  Shared memory of a CTA: the scale
+// header, a workspace region of ws_smem_bytes, a staging region of stage_bytes.
+// An instance whose workspace or plan block + leaves do not fit there uses the
+// CTA's global workspace slab or reads in place.
+struct PlanLaunch {
+    const InstanceDesc *instances;
+    int n_instances;
+    uint32_t ws_smem_bytes;      // shared-memory workspace region (0: none)
+    char *ws_base;               // global workspace: ws_base + blockIdx.x * ws_stride
+    uint64_t ws_stride;
+    uint32_t stage_bytes;        // shared memory for a staged plan block + leaf image (0: none)
+    uint32_t pad;
 };
 
 // What one CTA works with while it interprets an instance.

@@ -123,17 +123,31 @@ struct PlanSmemHeader {
     int32_t expo[kPlanMaxSteps];       // E of each step's output
 };
 
+// exponent m of the producer's largest |S| (max = f 2^m, f in [0.5, 1)), from the float bits
 __device__ __forceinline__ int step_scale(const PlanSmemHeader &h, int step) {
     if (step < 0) return 0;
-    const float mx = __uint_as_float(h.maxbits[step]);
-    int e = 0;
-    if (mx > 0.f && isfinite(mx)) frexpf(mx, &e);
-    return e;
+    const uint32_t bits = h.maxbits[step];
+    const uint32_t ex = (bits >> 23) & 0xffu;
+    if (ex == 0xffu || bits == 0) return 0;        // inf/NaN or an all-zero tensor: no scaling
+    if (ex == 0) {                                  // subnormal maximum
+        int e;
+        frexpf(__uint_as_float(bits), &e);
+        return e;
+    }
+    return (int) ex - 126;
+}
+
+// exact multiplication by 2^e: one multiply while 2^e is a normal float, ldexp beyond
+__device__ __forceinline__ float scale2f(float x, int e) {
+    return (e >= -126 && e <= 127) ? x * __int_as_float((127 + e) << 23) : ldexpf(x, e);
+}
+__device__ __forceinline__ double scale2d(double x, int e) {
+    return (e >= -1022 && e <= 1023) ? x * __longlong_as_double((long long) (1023 + e) << 52) : ldexp(x, e);
 }
 
 template <bool kMixed>
 __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, uint32_t total, const char *leaves,
-                           char *ws, PlanSmemHeader &h) {
+                           char *ws, PlanSmemHeader &h, const ushort2 *__restrict__ tables) {
     const int tid = threadIdx.x;
     for (uint32_t base = 0; base < total; base += blockDim.x) {
         const uint32_t item = base + tid;
@@ -158,22 +172,47 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
         const uint32_t flags = d.flags;
         const char *abase = ((flags & kALeaf) ? leaves : ws) + d.a_off;
         const char *bbase = ((flags & kBLeaf) ? leaves : ws) + d.b_off;
+        const uint32_t tab = d.tab_off;
+        const ushort2 *ktab = tables + tab + n_out;   // used only when tab != kNoTable
         uint32_t oa0 = 0, ob0 = 0;
         if (valid) {
-            uint64_t oa, ob;
-            scatter_c(c, d, oa, ob);
-            oa0 = (uint32_t) oa;
-            ob0 = (uint32_t) ob;
+            if (tab != kNoTable) {
+                const ushort2 o = tables[tab + c];
+                oa0 = o.x;
+                ob0 = o.y;
+            } else {
+                uint64_t oa, ob;
+                scatter_c(c, d, oa, ob);
+                oa0 = (uint32_t) oa;
+                ob0 = (uint32_t) ob;
+            }
         }
         if constexpr (!kMixed) {
             if (valid) {
-                const double2 *A = reinterpret_cast<const double2 *>(abase);
-                const double2 *B = reinterpret_cast<const double2 *>(bbase);
+                const double2 *A = reinterpret_cast<const double2 *>(abase) + oa0;
+                const double2 *B = reinterpret_cast<const double2 *>(bbase) + ob0;
                 double cre = 0.0, cim = 0.0;
-                for (uint32_t k = 0; k < K; k++) {
-                    const uint32_t ka = (uint32_t) scatter_digits(k, d.posAs, nSum);
-                    const uint32_t kb = (uint32_t) scatter_digits(k, d.posBs, nSum);
-                    cmac_exact(cre, cim, A[oa0 + ka], B[ob0 + kb]);
+                if (tab != kNoTable) {
+                    // loads of four terms are issued together, the adds stay in k order
+                    uint32_t k = 0;
+                    for (; k + 4 <= K; k += 4) {
+                        double2 a[4], b[4];
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const ushort2 kk = ktab[k + j];
+                            a[j] = A[kk.x];
+                            b[j] = B[kk.y];
+                        }
+#pragma unroll
+                        for (int j = 0; j < 4; j++) cmac_exact(cre, cim, a[j], b[j]);
+                    }
+                    for (; k < K; k++) {
+                        const ushort2 kk = ktab[k];
+                        cmac_exact(cre, cim, A[kk.x], B[kk.y]);
+                    }
+                } else {
+                    for (uint32_t k = 0; k < K; k++)
+                        cmac_exact(cre, cim, A[scatter_digits(k, d.posAs, nSum)], B[scatter_digits(k, d.posBs, nSum)]);
                 }
                 reinterpret_cast<double2 *>(ws + d.c_off)[c] = make_double2(cre, cim);
             }
@@ -183,23 +222,53 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
             double dre = 0.0, dim = 0.0;
             float fre = 0.f, fim = 0.f;
             if (valid) {
-                for (uint32_t k = lane_k; k < K; k += g) {
-                    const uint32_t ka = (uint32_t) scatter_digits(k, d.posAs, nSum);
-                    const uint32_t kb = (uint32_t) scatter_digits(k, d.posBs, nSum);
-                    if (f64) {
+                if (!f64 && !a64 && !b64 && tab != kNoTable) {
+                    // the common case: complex64 operands, tabled offsets
+                    const float2 *A = reinterpret_cast<const float2 *>(abase) + oa0;
+                    const float2 *B = reinterpret_cast<const float2 *>(bbase) + ob0;
+                    // four terms in flight, two accumulators to break the FMA chain
+                    float r1 = 0.f, i1 = 0.f;
+                    uint32_t k = lane_k;
+                    for (; k + 3 * g < K; k += 4 * g) {
+                        float2 a[4], b[4];
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const ushort2 kk = ktab[k + j * g];
+                            a[j] = A[kk.x];
+                            b[j] = B[kk.y];
+                        }
+                        cmac_f32(fre, fim, a[0], b[0]);
+                        cmac_f32(r1, i1, a[1], b[1]);
+                        cmac_f32(fre, fim, a[2], b[2]);
+                        cmac_f32(r1, i1, a[3], b[3]);
+                    }
+                    for (; k < K; k += g) {
+                        const ushort2 kk = ktab[k];
+                        cmac_f32(fre, fim, A[kk.x], B[kk.y]);
+                    }
+                    fre += r1;
+                    fim += i1;
+                } else {
+                    for (uint32_t k = lane_k; k < K; k += g) {
+                        uint32_t ka, kb;
+                        if (tab != kNoTable) {
+                            const ushort2 kk = ktab[k];
+                            ka = kk.x;
+                            kb = kk.y;
+                        } else {
+                            ka = (uint32_t) scatter_digits(k, d.posAs, nSum);
+                            kb = (uint32_t) scatter_digits(k, d.posBs, nSum);
+                        }
                         double2 a, b;
                         if (a64) a = reinterpret_cast<const double2 *>(abase)[oa0 + ka];
                         else { const float2 t = reinterpret_cast<const float2 *>(abase)[oa0 + ka]; a = make_double2(t.x, t.y); }
                         if (b64) b = reinterpret_cast<const double2 *>(bbase)[ob0 + kb];
                         else { const float2 t = reinterpret_cast<const float2 *>(bbase)[ob0 + kb]; b = make_double2(t.x, t.y); }
-                        cmac_f64(dre, dim, a, b);
-                    } else {
-                        float2 a, b;
-                        if (a64) { const double2 t = reinterpret_cast<const double2 *>(abase)[oa0 + ka]; a = make_float2((float) t.x, (float) t.y); }
-                        else a = reinterpret_cast<const float2 *>(abase)[oa0 + ka];
-                        if (b64) { const double2 t = reinterpret_cast<const double2 *>(bbase)[ob0 + kb]; b = make_float2((float) t.x, (float) t.y); }
-                        else b = reinterpret_cast<const float2 *>(bbase)[ob0 + kb];
-                        cmac_f32(fre, fim, a, b);
+                        if (f64) {
+                            cmac_f64(dre, dim, a, b);
+                        } else {
+                            cmac_f32(fre, fim, make_float2((float) a.x, (float) a.y), make_float2((float) b.x, (float) b.y));
+                        }
                     }
                 }
             }
@@ -211,16 +280,15 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
             }
             if (valid && lane_k == 0) {
                 const int ma = step_scale(h, d.a_step), mb = step_scale(h, d.b_step);
-                const int shift = -(ma + mb);
                 float mag;
                 if (f64) {
-                    dre = ldexp(dre, shift);
-                    dim = ldexp(dim, shift);
+                    dre = scale2d(dre, -(ma + mb));
+                    dim = scale2d(dim, -(ma + mb));
                     reinterpret_cast<double2 *>(ws + d.c_off)[c] = make_double2(dre, dim);
                     mag = (float) fmax(fabs(dre), fabs(dim));
                 } else {
-                    fre = ldexpf(fre, shift);
-                    fim = ldexpf(fim, shift);
+                    fre = scale2f(fre, -(ma + mb));
+                    fim = scale2f(fim, -(ma + mb));
                     reinterpret_cast<float2 *>(ws + d.c_off)[c] = make_float2(fre, fim);
                     mag = fmaxf(fabsf(fre), fabsf(fim));
                 }
@@ -235,17 +303,115 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
     }
 }
 
+// Staging: at the start of an instance one thread issues TMA bulk copies
+// (cp.async.bulk, completion counted on an mbarrier) of the instance's plan
+// block and leaf image into shared memory; the CTA waits once and then every
+// level reads descriptors, leaves and intermediates from shared memory.
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok) : "r"(mbar), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: a bulk copy finishes in microseconds; after ~1 s of polling the
+// wait gives up and the instance reports NaN instead of hanging the CTA.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
+    for (uint32_t it = 0; it < (1u << 22); it++) {
+        if (mbar_try_wait(mbar, parity)) return true;
+        if (it > 64) __nanosleep(256);
+    }
+    return false;
+}
+
+constexpr uint32_t kBulkChunk = 32768;
+
+__device__ __forceinline__ void bulk_copy_chunks(unsigned char *dst, const char *src, uint32_t bytes, uint32_t mbar) {
+    for (uint32_t off = 0; off < bytes; off += kBulkChunk) {
+        const uint32_t n = bytes - off < kBulkChunk ? bytes - off : kBulkChunk;
+        bulk_g2s(smem_addr(dst + off), src + off, n, mbar);
+    }
+}
+
 template <bool kMixed>
-__global__ void __launch_bounds__(kPlanThreads)
-plan_kernel(const InstanceDesc *__restrict__ instances, int n_instances, char *ws_base, uint64_t ws_stride,
-            int ws_in_smem) {
+__global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch lp) {
     extern __shared__ __align__(256) unsigned char smem_raw[];
     PlanSmemHeader &h = *reinterpret_cast<PlanSmemHeader *>(smem_raw);
-    char *ws = ws_in_smem ? reinterpret_cast<char *>(smem_raw) + kPlanHeaderBytes
-                          : ws_base + (uint64_t) blockIdx.x * ws_stride;
-    for (int inst = blockIdx.x; inst < n_instances; inst += gridDim.x) {
-        const InstanceDesc I = instances[inst];
-        const PlanDesc P = *I.plan;
+    uint64_t *mbar_slot = reinterpret_cast<uint64_t *>(smem_raw + kPlanHeaderBytes);
+    unsigned char *region = smem_raw + kPlanHeaderBytes + 128;
+    char *const ws_smem = reinterpret_cast<char *>(region);
+    char *const ws_global = lp.ws_base ? lp.ws_base + (uint64_t) blockIdx.x * lp.ws_stride : nullptr;
+    unsigned char *stage = region + lp.ws_smem_bytes;
+    const uint32_t mbar = smem_addr(mbar_slot);
+    if (lp.stage_bytes && threadIdx.x == 0) {
+        mbar_init(mbar);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    uint32_t parity = 0;
+    for (int inst = blockIdx.x; inst < lp.n_instances; inst += gridDim.x) {
+        const InstanceDesc I = lp.instances[inst];
+        char *const ws = I.ws_bytes <= lp.ws_smem_bytes ? ws_smem : ws_global;
+        const bool staged = lp.stage_bytes && I.plan_bytes && I.plan_bytes + I.leaf_bytes <= lp.stage_bytes;
+        const StepDesc *steps;
+        const int32_t *level_start, *rank0_steps;
+        const uint32_t *level_items;
+        const ushort2 *tables;
+        const char *leaves;
+        PlanDesc P;
+        if (staged) {
+            if (threadIdx.x == 0) {
+                // the previous instance's generic reads of this region are ordered before the async writes
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_expect_tx(mbar, I.plan_bytes + I.leaf_bytes);
+                bulk_copy_chunks(stage, reinterpret_cast<const char *>(I.plan), I.plan_bytes, mbar);
+                bulk_copy_chunks(stage + I.plan_bytes, I.leaves, I.leaf_bytes, mbar);
+            }
+            const bool ok = mbar_wait_bounded(mbar, parity);
+            parity ^= 1u;
+            if (__syncthreads_or(!ok)) {
+                // the copies never completed: this CTA's instances report NaN instead of hanging
+                if (threadIdx.x == 0)
+                    for (int j = inst; j < lp.n_instances; j += gridDim.x)
+                        lp.instances[j].value[0] = lp.instances[j].value[1] = __longlong_as_double(0x7ff8000000000000ll);
+                return;
+            }
+            P = *reinterpret_cast<const PlanDesc *>(stage);
+            const char *gbase = reinterpret_cast<const char *>(I.plan);
+            const char *sbase = reinterpret_cast<const char *>(stage);
+            steps = reinterpret_cast<const StepDesc *>(sbase + (reinterpret_cast<const char *>(P.steps) - gbase));
+            level_start = reinterpret_cast<const int32_t *>(sbase + (reinterpret_cast<const char *>(P.level_start) - gbase));
+            rank0_steps = reinterpret_cast<const int32_t *>(sbase + (reinterpret_cast<const char *>(P.rank0_steps) - gbase));
+            level_items = reinterpret_cast<const uint32_t *>(sbase + (reinterpret_cast<const char *>(P.level_items) - gbase));
+            tables = reinterpret_cast<const ushort2 *>(sbase + (reinterpret_cast<const char *>(P.tables) - gbase));
+            leaves = sbase + I.plan_bytes;
+        } else {
+            P = *I.plan;
+            steps = P.steps;
+            level_start = P.level_start;
+            rank0_steps = P.rank0_steps;
+            level_items = P.level_items;
+            tables = P.tables;
+            leaves = I.leaves;
+        }
         if (kMixed) {
             for (int s = threadIdx.x; s < P.n_steps; s += blockDim.x) {
                 h.maxbits[s] = 0;
@@ -254,15 +420,15 @@ plan_kernel(const InstanceDesc *__restrict__ instances, int n_instances, char *w
             __syncthreads();
         }
         for (int L = 0; L < P.n_levels; L++) {
-            plan_level<kMixed>(P.steps, P.level_start[L], P.level_start[L + 1], P.level_items[L], I.leaves, ws, h);
+            plan_level<kMixed>(steps, level_start[L], level_start[L + 1], level_items[L], leaves, ws, h, tables);
             __syncthreads();
         }
         // final-value rule of src/Network.h:961-965, applied in contraction order
         if (threadIdx.x == 0) {
             double fre = 0.0, fim = 0.0;
             for (int r = 0; r < P.n_rank0; r++) {
-                const int s = P.rank0_steps[r];
-                const StepDesc &d = P.steps[s];
+                const int s = rank0_steps[r];
+                const StepDesc &d = steps[s];
                 double vre, vim;
                 if (!kMixed || (d.flags & kCF64)) {
                     const double2 v = *reinterpret_cast<const double2 *>(ws + d.c_off);
@@ -327,16 +493,19 @@ int plan_max_grid(size_t smem_bytes) {
     return num_sms() * per_sm;
 }
 
-cudaError_t launch_plan(const InstanceDesc *instances, int n_instances, bool mixed, int grid, char *ws_base,
-                        uint64_t ws_stride, bool ws_in_smem, cudaStream_t stream) {
-    if (n_instances <= 0) return cudaSuccess;
-    const size_t smem = kPlanHeaderBytes + (ws_in_smem ? ws_stride : 0);
+size_t plan_smem_bytes(const PlanLaunch &lp) {
+    return kPlanHeaderBytes + 128 + lp.ws_smem_bytes + lp.stage_bytes;
+}
+
+cudaError_t launch_plan(const PlanLaunch &lp, bool mixed, int grid, cudaStream_t stream) {
+    if (lp.n_instances <= 0) return cudaSuccess;
+    const size_t smem = plan_smem_bytes(lp);
     cudaError_t e = mixed ? cudaFuncSetAttribute(plan_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)
                           : cudaFuncSetAttribute(plan_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     if (e != cudaSuccess) return e;
-    if (grid <= 0 || grid > n_instances) grid = n_instances;
-    if (mixed) plan_kernel<true><<<grid, kPlanThreads, smem, stream>>>(instances, n_instances, ws_base, ws_stride, ws_in_smem ? 1 : 0);
-    else plan_kernel<false><<<grid, kPlanThreads, smem, stream>>>(instances, n_instances, ws_base, ws_stride, ws_in_smem ? 1 : 0);
+    if (grid <= 0 || grid > lp.n_instances) grid = lp.n_instances;
+    if (mixed) plan_kernel<true><<<grid, kPlanThreads, smem, stream>>>(lp);
+    else plan_kernel<false><<<grid, kPlanThreads, smem, stream>>>(lp);
     return cudaGetLastError();
 }
 

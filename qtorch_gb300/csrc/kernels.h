@@ -11,9 +11,11 @@ cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C
 
 // Grouped interpreter over plan instances.  The workspace of a CTA is either
 // its shared memory (ws_in_smem; ws_stride bytes after the header) or
-// ws_base + blockIdx.x * ws_stride in global memory.
-cudaError_t launch_plan(const InstanceDesc *instances, int n_instances, bool mixed, int grid, char *ws_base,
-                        uint64_t ws_stride, bool ws_in_smem, cudaStream_t stream);
+// ws_base + blockIdx.x * ws_stride in global memory; with stage_bytes > 0 each
+// instance's plan block and leaf image are copied into shared memory first.
+cudaError_t launch_plan(const PlanLaunch &lp, bool mixed, int grid, cudaStream_t stream);
+// dynamic shared memory of one interpreter CTA for these parameters
+size_t plan_smem_bytes(const PlanLaunch &lp);
 // resident CTAs of the interpreter for a given dynamic shared memory size
 int plan_max_grid(size_t smem_bytes);
 

@@ -242,19 +242,17 @@ const std::vector<int> &LineGraph::MinFillOrdering() {
         }
         return fill;
     };
+    // fill counts are cached; eliminating x changes them only within distance 2 of x
+    std::vector<long long> fill(n);
+    for (int v = 0; v < n; v++) fill[v] = fill_of(v);
+    std::vector<int> mark(n, -1);
     // greedy min-fill: fewest added edges, then smallest degree, then smallest id
     for (int step = 0; step < n; step++) {
         int best = -1;
-        long long bestFill = 0;
-        size_t bestDeg = 0;
         for (int v = 0; v < n; v++) {
             if (gone[v]) continue;
-            const long long f = fill_of(v);
-            if (best < 0 || f < bestFill || (f == bestFill && adj[v].size() < bestDeg)) {
+            if (best < 0 || fill[v] < fill[best] || (fill[v] == fill[best] && adj[v].size() < adj[best].size()))
                 best = v;
-                bestFill = f;
-                bestDeg = adj[v].size();
-            }
         }
         gone[best] = 1;
         mOrder.push_back(best + 1);
@@ -266,6 +264,19 @@ const std::vector<int> &LineGraph::MinFillOrdering() {
             }
         for (int u : nb) adj[u].erase(best);
         adj[best].clear();
+        std::vector<int> affected;
+        for (int u : nb) {
+            if (mark[u] != step) {
+                mark[u] = step;
+                affected.push_back(u);
+            }
+            for (int w : adj[u])
+                if (mark[w] != step) {
+                    mark[w] = step;
+                    affected.push_back(w);
+                }
+        }
+        for (int u : affected) fill[u] = fill_of(u);
     }
     return mOrder;
 }
@@ -281,6 +292,17 @@ bool LineGraph::LGContract(const std::vector<int> &order) {
         auto a = w->GetNodeA().lock(), b = w->GetNodeB().lock();
         if (!a || !b) continue;
         mNetwork->ContractNodes(a, b, 100);
+    }
+    // A circuit whose qubits form several unconnected groups leaves one rank-0
+    // node per group; the reference stops with ContractionFailure there
+    // (LineGraph.h:384-388).  They are multiplied together here instead, in
+    // list order, as the stochastic ordering's leftover phase does.
+    while (mNetwork->GetUncontractedNodes().size() > 1) {
+        const auto &r = mNetwork->GetUncontractedNodes();
+        bool all_scalar = true;
+        for (const auto &x : r) all_scalar = all_scalar && x->mRank == 0;
+        if (!all_scalar) break;
+        mNetwork->ContractNodes(r[0], r[1], 100);
     }
     const auto &rem = mNetwork->GetUncontractedNodes();
     if (rem.size() != 1) throw ContractionFailure();

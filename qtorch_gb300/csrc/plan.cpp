@@ -226,6 +226,36 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
             p->level_items[prec][L0] = acc;
         }
     }
+    // offset tables for the interpreter when every operand fits 16-bit offsets
+    // (same maps for both precisions; offsets in elements)
+    {
+        bool small = true;
+        uint64_t entries = 0;
+        for (const auto &d : p->steps[QT_PREC_FP64]) {
+            if (d.rA > 8 || d.rB > 8) small = false;
+            entries += (1ull << (2 * d.nFree)) + (1ull << (2 * d.nSum));
+        }
+        p->tables.clear();
+        if (small && entries * sizeof(uint16_t) * 2 <= kMaxTableBytes) {
+            for (int i = 0; i < S; i++) {
+                const StepDesc &d = p->steps[QT_PREC_FP64][i];
+                const uint32_t off = (uint32_t) p->tables.size();
+                for (int prec = 0; prec < 2; prec++) p->steps[prec][i].tab_off = off;
+                const uint64_t n_out = 1ull << (2 * d.nFree), K = 1ull << (2 * d.nSum);
+                for (uint64_t c = 0; c < n_out; c++) {
+                    uint64_t oa, ob;
+                    scatter_c(c, d, oa, ob);
+                    p->tables.push_back({(uint16_t) oa, (uint16_t) ob});
+                }
+                for (uint64_t k = 0; k < K; k++)
+                    p->tables.push_back({(uint16_t) scatter_digits(k, d.posAs, d.nSum),
+                                         (uint16_t) scatter_digits(k, d.posBs, d.nSum)});
+            }
+        } else {
+            for (int prec = 0; prec < 2; prec++)
+                for (auto &d : p->steps[prec]) d.tab_off = kNoTable;
+        }
+    }
     p->n_steps = S;
     p->n_levels = n_levels;
     p->grouped = p->max_step_out <= kGroupedMaxRank && p->max_step_k <= kGroupedMaxSum &&
@@ -246,16 +276,21 @@ qt_status upload_plan(qt_plan *p, int prec) {
     const size_t off_lvl = align_up(off_steps + steps_bytes, 256);
     const size_t off_r0 = align_up(off_lvl + lvl_bytes, 256);
     const size_t off_items = align_up(off_r0 + r0_bytes, 256);
-    const size_t total = off_items + items_bytes;
+    const size_t tab_bytes = sizeof(ushort2) * p->tables.size();
+    const size_t off_tab = align_up(off_items + items_bytes, 256);
+    const size_t total = off_tab + tab_bytes + 16;
     void *d = nullptr;
     qt_status s = dev_alloc(ctx, total, &d);
     if (s != QT_OK) return s;
     std::vector<char> host(total, 0);
     PlanDesc pd;
+    std::memset(&pd, 0, sizeof pd);
     pd.steps = reinterpret_cast<const StepDesc *>((char *) d + off_steps);
     pd.level_start = reinterpret_cast<const int32_t *>((char *) d + off_lvl);
     pd.rank0_steps = reinterpret_cast<const int32_t *>((char *) d + off_r0);
     pd.level_items = reinterpret_cast<const uint32_t *>((char *) d + off_items);
+    pd.tables = reinterpret_cast<const ushort2 *>((char *) d + off_tab);
+    if (tab_bytes) std::memcpy(host.data() + off_tab, p->tables.data(), tab_bytes);
     pd.n_steps = p->n_steps;
     pd.n_levels = p->n_levels;
     pd.n_rank0 = (int32_t) p->rank0_steps.size();

@@ -17,6 +17,11 @@ constexpr int kGroupedMaxSum = 8;
 constexpr uint64_t kGroupedMaxWorkspace = 96ull << 20;
 // a batch whose largest workspace is at most this keeps it in shared memory
 constexpr uint64_t kSmemWorkspaceMax = 96ull << 10;
+// total dynamic shared memory of an interpreter CTA when instances are staged
+constexpr uint64_t kSmemStageMax = 200ull << 10;
+inline uint64_t round16(uint64_t x) { return (x + 15) / 16 * 16; }
+// offset tables are built when they take at most this many bytes
+constexpr uint64_t kMaxTableBytes = 64ull << 10;
 
 }  // namespace qtg
 
@@ -35,6 +40,7 @@ struct qt_plan {
     std::vector<int32_t> level_start;
     std::vector<int32_t> rank0_steps;
     std::vector<uint32_t> level_items[2];             // interpreter work items per level, per precision
+    std::vector<ushort2> tables;                      // interpreter offset tables (empty: none)
     std::vector<uint64_t> leaf_off[2];
     uint64_t leaf_bytes[2] = {0, 0};
     uint64_t ws_bytes[2] = {0, 0};
@@ -61,7 +67,10 @@ struct qt_batch {
     void *d_ws = nullptr;
     void *d_exps = nullptr;
     uint64_t ws_stride = 0, exps_stride = 0;
-    bool ws_in_smem = false;
+    bool ws_in_smem = false;                          // every instance's workspace fits shared memory
+    uint32_t ws_smem_bytes = 0;                       // shared-memory workspace region per CTA
+    uint32_t stage_bytes = 0;                         // shared memory for staged plan block + leaves
+    bool allow_stage = true;
     int grid = 0;
     void *h_leaves = nullptr;                         // pinned staging of the leaf image
     void *h_values = nullptr;                         // pinned values

@@ -73,7 +73,9 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     const uint64_t off_lvl = align256(off_steps + steps_bytes);
     const uint64_t off_r0 = align256(off_lvl + lvl_bytes);
     const uint64_t off_items = align256(off_r0 + r0_bytes);
-    const uint64_t off_inst = align256(off_items + items_bytes);
+    const uint64_t tab_bytes = sizeof(ushort2) * p->tables.size();
+    const uint64_t off_tab = align256(off_items + items_bytes);
+    const uint64_t off_inst = align256(off_tab + tab_bytes);
     const uint64_t off_ws = align256(off_inst + sizeof(InstanceDesc));
     const uint64_t total = off_ws + align256(p->ws_bytes[prec]);
     if (total > QT_STATIC_SCRATCH_BYTES)
@@ -90,6 +92,7 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     pd.level_start = reinterpret_cast<const int32_t *>(b + off_lvl);
     pd.rank0_steps = reinterpret_cast<const int32_t *>(b + off_r0);
     pd.level_items = reinterpret_cast<const uint32_t *>(b + off_items);
+    pd.tables = reinterpret_cast<const ushort2 *>(b + off_tab);
     pd.n_steps = p->n_steps;
     pd.n_levels = p->n_levels;
     pd.n_rank0 = (int32_t) p->rank0_steps.size();
@@ -97,6 +100,10 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     inst.plan = reinterpret_cast<const PlanDesc *>(b);
     inst.leaves = static_cast<const char *>(d_leaves);
     inst.value = d_value;
+    inst.plan_bytes = 0;   // read in place from the static array, never staged
+    inst.leaf_bytes = 0;
+    inst.ws_bytes = (uint32_t) align256(p->ws_bytes[prec]);
+    inst.pad = 0;
     // the descriptors of the previous call are overwritten; the workspace needs
     // no clearing (every intermediate is written before it is read)
     cudaError_t e = cudaMemcpyAsync(b, &pd, sizeof pd, cudaMemcpyHostToDevice, ctx->stream);
@@ -108,13 +115,22 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
         e = cudaMemcpyAsync(b + off_r0, p->rank0_steps.data(), r0_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && items_bytes)
         e = cudaMemcpyAsync(b + off_items, p->level_items[prec].data(), items_bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && tab_bytes)
+        e = cudaMemcpyAsync(b + off_tab, p->tables.data(), tab_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(b + off_inst, &inst, sizeof inst, cudaMemcpyHostToDevice, ctx->stream);
     // the stack copies above must not go out of scope before the transfers are done
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_error(ctx, e, "static scratch upload");
-    e = launch_plan(reinterpret_cast<const InstanceDesc *>(b + off_inst), 1, prec == QT_PREC_MIXED, 1, b + off_ws,
-                    align256(p->ws_bytes[prec]), false, ctx->stream);
+    PlanLaunch lp;
+    lp.instances = reinterpret_cast<const InstanceDesc *>(b + off_inst);
+    lp.n_instances = 1;
+    lp.ws_smem_bytes = 0;   // the workspace is the static array's tail
+    lp.ws_base = b + off_ws;
+    lp.ws_stride = align256(p->ws_bytes[prec]);
+    lp.stage_bytes = 0;
+    lp.pad = 0;
+    e = launch_plan(lp, prec == QT_PREC_MIXED, 1, ctx->stream);
     ctx->launches++;
     return cuda_error(ctx, e, "plan kernel launch");
 }
