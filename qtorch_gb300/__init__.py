@@ -215,6 +215,31 @@ def contract_pair(a, b, free_from_a, free_idx, sum_a, sum_b, ctx=None):
     return c
 
 
+def contract_pair_c64(a, b, free_from_a, free_idx, sum_a, sum_b, ctx=None):
+    """The same contraction in complex64 through device tensors (qt_tensor_* and
+    qt_contract_pair); GEMM-shaped steps run on the tcgen05 tensor cores."""
+    ctx = ctx or default_context()
+    lib = _lib()
+    a = np.ascontiguousarray(a, dtype=np.complex64).reshape(-1)
+    b = np.ascontiguousarray(b, dtype=np.complex64).reshape(-1)
+    ffa, fi, sa, sb = _index_maps(free_from_a, free_idx, sum_a, sum_b)
+    ta, tb, tc = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    try:
+        _check(lib.qt_tensor_create(ctx.handle, _rank_of(a.size), 1, ctypes.byref(ta)), ctx)
+        _check(lib.qt_tensor_create(ctx.handle, _rank_of(b.size), 1, ctypes.byref(tb)), ctx)
+        _check(lib.qt_tensor_upload(ctx.handle, ta, a.ctypes.data_as(ctypes.c_void_p), a.nbytes), ctx)
+        _check(lib.qt_tensor_upload(ctx.handle, tb, b.ctypes.data_as(ctypes.c_void_p), b.nbytes), ctx)
+        _check(lib.qt_contract_pair(ctx.handle, ta, tb, len(fi), ffa.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                    _ip(fi), len(sa), _ip(sa), _ip(sb), ctypes.byref(tc)), ctx)
+        c = np.zeros(4 ** len(fi), dtype=np.complex64)
+        _check(lib.qt_tensor_download(ctx.handle, tc, c.ctypes.data_as(ctypes.c_void_p), c.nbytes), ctx)
+        return c
+    finally:
+        for t in (ta, tb, tc):
+            if t.value:
+                lib.qt_tensor_free(ctx.handle, t)
+
+
 def contract_pair_device(a_ptr, rank_a, b_ptr, rank_b, free_from_a, free_idx, sum_a, sum_b, c_ptr, ctx=None):
     """ContractIndices on caller-owned device buffers (complex128), asynchronous on ctx's stream."""
     ctx = ctx or default_context()

@@ -473,7 +473,7 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
         const uint64_t st = round16(p->dev_bytes[prec]) + round16(p->leaf_bytes[prec]);
         ws = std::max<uint64_t>(ws, w);
         if (w <= kSmemWorkspaceMax) ws_small = std::max<uint64_t>(ws_small, w);
-        if (st <= kSmemStageMax / 2) stage_small = std::max<uint64_t>(stage_small, st);
+        if (st <= kSmemStageMax) stage_small = std::max<uint64_t>(stage_small, st);
         ex = std::max<uint64_t>(ex, (uint64_t) p->n_steps);
         n_grouped++;
     }
@@ -484,7 +484,6 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
     // that fits it and a staging region as large as the largest plan block + leaf
     // image that fits; instances beyond either use the global slab / read in place
     b->ws_smem_bytes = (uint32_t) ws_small;
-    if (kPlanHeaderBytes + 128 + b->ws_smem_bytes + stage_small > kSmemStageMax) stage_small = 0;
     b->stage_bytes = b->allow_stage ? (uint32_t) stage_small : 0;
     b->ws_in_smem = ws <= b->ws_smem_bytes;   // no global slab needed
     b->grid = std::min(n_grouped, plan_max_grid(kPlanHeaderBytes + 128 + b->ws_smem_bytes + b->stage_bytes));

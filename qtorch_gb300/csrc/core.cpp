@@ -3,9 +3,11 @@
 // src/Network.h:876-971).
 #include "core.h"
 
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
+#include "gemm_tc.h"
 #include "kernels.h"
 
 namespace qtg {
@@ -93,6 +95,40 @@ qt_status ensure_pinned(qt_ctx *ctx, size_t bytes) {
 
 bool deadline_passed(qt_ctx *ctx) {
     return ctx->has_deadline && std::chrono::steady_clock::now() > ctx->deadline;
+}
+
+bool tensor_cores_enabled() {
+    static const bool on = [] {
+        const char *v = std::getenv("QT_DISABLE_TCGEN05");
+        return !(v && v[0] == '1');
+    }();
+    return on;
+}
+
+qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const void *B, void *C, bool f64) {
+    if (!f64 && tensor_cores_enabled() && gemm_eligible(d)) {
+        void *scratch = nullptr, *flag = nullptr;
+        qt_status s = dev_alloc(ctx, sizeof(float) * gemm_scratch_floats(d), &scratch);
+        if (s == QT_OK) s = dev_alloc(ctx, 256, &flag);
+        if (s == QT_OK) {
+            cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream);
+            if (e == cudaSuccess)
+                e = launch_gemm_step(d, (const float2 *) A, (const float2 *) B, (float2 *) C, (float *) scratch,
+                                     (int *) flag, ctx->stream);
+            ctx->launches += 3;
+            int h = 0;
+            if (e == cudaSuccess) e = cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+            s = cuda_error(ctx, e, "tensor-core contraction");
+            if (s == QT_OK && h) s = set_error(ctx, QT_ERR_CUDA, "tensor-core pipeline wait timed out");
+        }
+        dev_free(ctx, scratch);
+        dev_free(ctx, flag);
+        return s;
+    }
+    cudaError_t e = launch_pair(d, A, B, C, f64, ctx->stream);
+    ctx->launches++;
+    return cuda_error(ctx, e, "pair kernel launch");
 }
 
 qt_status make_step(int rank_a, int rank_b, int n_free, const uint8_t *free_from_a, const int32_t *free_idx,
@@ -331,12 +367,11 @@ qt_status qt_contract_pair(qt_ctx *ctx, const qt_tensor *a, const qt_tensor *b, 
         return s;
     }
     // every output element is written by the kernel; no zero fill needed
-    cudaError_t e = launch_pair(d, a->ptr, b->ptr, c->ptr, a->dtype == QT_C128, ctx->stream);
-    ctx->launches++;
-    if (e != cudaSuccess) {
+    s = run_contraction(ctx, d, a->ptr, b->ptr, c->ptr, a->dtype == QT_C128);
+    if (s != QT_OK) {
         dev_free(ctx, c->ptr);
         delete c;
-        return cuda_error(ctx, e, "pair kernel launch");
+        return s;
     }
     *c_out = c;
     return QT_OK;

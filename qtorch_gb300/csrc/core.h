@@ -52,6 +52,13 @@ qt_status ensure_pinned(qt_ctx *ctx, size_t bytes);
 bool deadline_passed(qt_ctx *ctx);
 inline size_t elem_bytes(qt_dtype d) { return d == QT_C128 ? 16 : 8; }
 
+// One contraction step over the whole GPU: complex128 with the reference's
+// rounding, or complex64 -- through the tcgen05 tensor-core GEMM when the step
+// is GEMM-shaped and large (gemm_tc.cu), else the SIMT pair kernel.
+qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const void *B, void *C, bool f64);
+// whether complex64 steps may use the tensor cores (QT_DISABLE_TCGEN05=1 turns it off)
+bool tensor_cores_enabled();
+
 // Fill a StepDesc from the reference's index lists (toNotSumOn, toSumOn).
 qt_status make_step(int rank_a, int rank_b, int n_free, const uint8_t *free_from_a, const int32_t *free_idx,
                     int n_sum, const int32_t *sum_a, const int32_t *sum_b, StepDesc *d);

@@ -1,0 +1,288 @@
+// Tensor-core (tcgen05) path for contraction steps dense enough to be a GEMM.
+//
+// A step C[m + M n] = sum_k A[a(m,k)] B[b(n,k)] in complex64 becomes one real
+// GEMM  D = X Y^T  with
+//   X (M x 2K)  = [Ar | Ai]                       row m, K contiguous
+//   Y (2N x 2K) row 2n   = [Br_n | -Bi_n]          -> D[m][2n]   = Re C
+//               row 2n+1 = [Bi_n |  Br_n]          -> D[m][2n+1] = Im C
+// computed with three TF32 products per term (x_hi y_hi + x_hi y_lo + x_lo y_hi,
+// FP32 accumulation in tensor memory), which carries ~21 bits per product.
+//
+// pack_operand writes X and Y (hi and lo planes) already in the UMMA canonical
+// K-major layout without swizzle, tile by tile (128 rows x 32 columns, 16 KB),
+// so every shared-memory stage is filled by one TMA bulk copy per plane.
+// Inside a tile the 8x4 "core matrices" (8 rows x 16 bytes) are stored row
+// group major: byte offset of (r, k) = ((r/8)*8 + k/4)*128 + (r%8)*16 + (k%4)*4,
+// i.e. LBO (next core matrix along K) = 128 B, SBO (next 8-row group) = 1024 B.
+//
+// gemm_tf32x3: one CTA per 128x128 tile of D, 128 threads.  Thread 0 runs the
+// pipeline (bulk copies into 3 stages, 12 tcgen05.mma per stage, tcgen05.commit
+// to release a stage); all four warps read the accumulator with tcgen05.ld and
+// store complex pairs.  Every mbarrier wait is bounded; on a timeout the CTA
+// raises an error flag, frees its tensor memory and returns.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "engine.cuh"
+#include "gemm_tc.h"
+
+namespace qtg {
+
+constexpr int kTileM = 128;          // rows of X per tile (UMMA M)
+constexpr int kTileN = 128;          // rows of Y per tile (UMMA N, real columns of D)
+constexpr int kTileK = 32;           // tf32 elements of K per stage (128 bytes)
+constexpr int kTileBytes = kTileM * kTileK * 4;   // 16 KB, same for X and Y tiles
+constexpr int kStages = 3;
+constexpr int kGemmThreads = 128;
+constexpr uint32_t kTmemCols = 128;
+
+__host__ __device__ inline uint64_t tiled_offset(uint64_t r, uint64_t k, uint64_t k_tiles) {
+    // tiles ordered [row tile][k tile]; canonical core-matrix layout inside a tile
+    const uint64_t tile = (r / kTileM) * k_tiles + k / kTileK;
+    const uint64_t rr = r % kTileM, kk = k % kTileK;
+    return tile * (kTileBytes / 4) + ((rr / 8) * 8 + kk / 4) * 32 + (rr % 8) * 4 + (kk % 4);
+}
+
+__device__ __forceinline__ void split_tf32(float x, float &hi, float &lo) {
+    // hi keeps the top 10 mantissa bits (what a TF32 operand holds), lo the next ones
+    hi = __uint_as_float(__float_as_uint(x) & 0xffffe000u);
+    lo = x - hi;
+}
+
+// X: rows m < M, columns j < 2K; Y: rows i < 2N, columns j < 2K (see the file comment).
+__global__ void pack_operand(const float2 *__restrict__ src, const StepDesc d, int which, uint64_t rows,
+                             uint64_t rows_padded, uint64_t K, uint64_t k_tiles, float *__restrict__ hi,
+                             float *__restrict__ lo) {
+    const uint64_t cols_padded = k_tiles * kTileK;
+    const uint64_t total = rows_padded * cols_padded;
+    const uint64_t M = 1ull << (2 * d.fA);
+    for (uint64_t t = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (uint64_t) gridDim.x * blockDim.x) {
+        const uint64_t r = t / cols_padded, j = t % cols_padded;
+        float v = 0.f;
+        if (r < rows && j < 2 * K) {
+            const uint64_t k = j < K ? j : j - K;
+            const bool second = j >= K;
+            if (which == 0) {
+                // X row m: free digits of A, then the summed digits
+                uint64_t oa, ob;
+                scatter_c(r, d, oa, ob);   // r < M: only A digits are non-zero
+                const float2 a = src[oa + scatter_digits(k, d.posAs, d.nSum)];
+                v = second ? a.y : a.x;
+            } else {
+                const uint64_t n = r >> 1;
+                uint64_t oa, ob;
+                scatter_c(n * M, d, oa, ob);   // the B digits of output column n
+                const float2 b = src[ob + scatter_digits(k, d.posBs, d.nSum)];
+                if ((r & 1) == 0) v = second ? -b.y : b.x;
+                else v = second ? b.x : b.y;
+            }
+        }
+        float h, l;
+        split_tf32(v, h, l);
+        const uint64_t o = tiled_offset(r, j, k_tiles);
+        hi[o] = h;
+        lo[o] = l;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// PTX wrappers
+
+__device__ __forceinline__ uint32_t sm_addr(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void mbar_init1(uint32_t mbar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    for (uint32_t it = 0; it < (1u << 24); it++) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok) : "r"(mbar), "r"(parity) : "memory");
+        if (ok) return true;
+        if (it > 128) __nanosleep(64);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(mbar) : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, no swizzle, LBO 128 B, SBO 1024 B
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t) ((addr >> 4) & 0x3fff);
+    d |= (uint64_t) ((128 >> 4) & 0x3fff) << 16;
+    d |= (uint64_t) ((1024 >> 4) & 0x3fff) << 32;
+    d |= (uint64_t) 1 << 46;   // descriptor version of tcgen05
+    return d;                  // base offset 0, layout type 0 = no swizzle
+}
+
+// instruction descriptor: kind::tf32, D = F32, A = B = TF32, both K-major, M = 128, N = 128
+constexpr uint32_t kInstrDesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t) (kTileN >> 3) << 17) |
+                                ((uint32_t) (kTileM >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+                 ::"r"(tmem_d), "l"(a), "l"(b), "r"(kInstrDesc), "r"(accumulate) : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+__global__ void __launch_bounds__(kGemmThreads, 1)
+gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, const float *__restrict__ y_hi,
+            const float *__restrict__ y_lo, uint64_t k_tiles, uint64_t M, uint64_t N2, float2 *__restrict__ C,
+            int *__restrict__ error_flag) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    // [stages x (x_hi, x_lo, y_hi, y_lo) tiles][full[stages], empty[stages], done][tmem address]
+    unsigned char *tiles = smem;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kStages * 4 * kTileBytes);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kStages + 1);
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const uint64_t tm = blockIdx.x, tn = blockIdx.y;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(sm_addr(tmem_slot)), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 2 * kStages + 1; i++) mbar_init1(sm_addr(&bars[i]));
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    bool ok = true;
+    if (threadIdx.x == 0) {
+        const uint64_t tile_floats = kTileBytes / 4;
+        auto stage_ptr = [&](int s, int plane) { return tiles + (s * 4 + plane) * kTileBytes; };
+        auto issue = [&](uint64_t kt, int s) {
+            const uint32_t full = sm_addr(&bars[s]);
+            mbar_arrive_tx(full, 4 * kTileBytes);
+            const uint64_t xt = (tm * k_tiles + kt) * tile_floats, yt = (tn * k_tiles + kt) * tile_floats;
+            bulk_load(sm_addr(stage_ptr(s, 0)), x_hi + xt, kTileBytes, full);
+            bulk_load(sm_addr(stage_ptr(s, 1)), x_lo + xt, kTileBytes, full);
+            bulk_load(sm_addr(stage_ptr(s, 2)), y_hi + yt, kTileBytes, full);
+            bulk_load(sm_addr(stage_ptr(s, 3)), y_lo + yt, kTileBytes, full);
+        };
+        uint32_t full_phase[kStages] = {0, 0, 0}, empty_phase[kStages] = {0, 0, 0};
+        for (uint64_t i = 0; i < (uint64_t) kStages && i < k_tiles; i++) issue(i, (int) i);
+        for (uint64_t kt = 0; kt < k_tiles && ok; kt++) {
+            const int s = (int) (kt % kStages);
+            if (!mbar_wait(sm_addr(&bars[s]), full_phase[s])) { ok = false; break; }
+            full_phase[s] ^= 1u;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t xh = sm_addr(stage_ptr(s, 0)), xl = sm_addr(stage_ptr(s, 1));
+            const uint32_t yh = sm_addr(stage_ptr(s, 2)), yl = sm_addr(stage_ptr(s, 3));
+            for (int j = 0; j < kTileK / 8; j++) {
+                // 8 tf32 of K per instruction = two core matrices = 256 bytes along K
+                const uint32_t o = (uint32_t) j * 256;
+                const uint32_t acc = (kt > 0 || j > 0) ? 1u : 0u;
+                mma_tf32(tmem, smem_desc(xh + o), smem_desc(yh + o), acc);
+                mma_tf32(tmem, smem_desc(xh + o), smem_desc(yl + o), 1u);
+                mma_tf32(tmem, smem_desc(xl + o), smem_desc(yh + o), 1u);
+            }
+            mma_commit(sm_addr(&bars[kStages + s]));
+            const uint64_t next = kt + kStages;
+            if (next < k_tiles) {
+                if (!mbar_wait(sm_addr(&bars[kStages + s]), empty_phase[s])) { ok = false; break; }
+                empty_phase[s] ^= 1u;
+                issue(next, s);
+            }
+        }
+        mma_commit(sm_addr(&bars[2 * kStages]));
+    }
+    // every thread waits for the accumulator (bounded)
+    ok = __syncthreads_and(ok) != 0;
+    bool done = ok && mbar_wait(sm_addr(&bars[2 * kStages]), 0);
+    done = __syncthreads_and(done) != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (done) {
+        const uint64_t m = tm * kTileM + (uint64_t) warp * 32 + lane;
+        for (int c0 = 0; c0 < kTileN; c0 += 16) {
+            uint32_t r[16];
+            const uint32_t taddr = tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) c0;
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                           "=r"(r[14]), "=r"(r[15])
+                         : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (m < M) {
+#pragma unroll
+                for (int j = 0; j < 16; j += 2) {
+                    const uint64_t col = tn * kTileN + (uint64_t) (c0 + j);   // even: Re, odd: Im
+                    if (col + 1 < N2 + 1 && col < N2)
+                        C[m + M * (col >> 1)] = make_float2(__uint_as_float(r[j]), __uint_as_float(r[j + 1]));
+                }
+            }
+        }
+    } else if (threadIdx.x == 0) {
+        atomicExch(error_flag, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+
+bool gemm_eligible(const StepDesc &d) {
+    // A's free digits must be C's low digits and B's the high ones (what ContractNodes produces)
+    for (int i = 0; i < d.nFree; i++) {
+        const bool from_a = d.cA[i] != kNoWire;
+        if (from_a != (i < d.fA)) return false;
+    }
+    const uint64_t M = 1ull << (2 * d.fA), N = 1ull << (2 * d.fB), K = 1ull << (2 * d.nSum);
+    return M >= (uint64_t) kTileM && 2 * N >= 64 && 2 * K >= (uint64_t) kTileK && M * N * K >= (1ull << 26);
+}
+
+GemmSizes gemm_sizes(const StepDesc &d) {
+    GemmSizes s;
+    s.M = 1ull << (2 * d.fA);
+    s.N2 = 2ull << (2 * d.fB);
+    s.K = 1ull << (2 * d.nSum);
+    s.k_tiles = (2 * s.K + kTileK - 1) / kTileK;
+    s.m_tiles = (s.M + kTileM - 1) / kTileM;
+    s.n_tiles = (s.N2 + kTileN - 1) / kTileN;
+    s.x_floats = s.m_tiles * kTileM * s.k_tiles * kTileK;
+    s.y_floats = s.n_tiles * kTileN * s.k_tiles * kTileK;
+    return s;
+}
+
+size_t gemm_smem_bytes() { return (size_t) kStages * 4 * kTileBytes + (2 * kStages + 1) * 8 + 16; }
+
+cudaError_t launch_gemm_step(const StepDesc &d, const float2 *A, const float2 *B, float2 *C, float *scratch,
+                             int *error_flag, cudaStream_t stream) {
+    const GemmSizes s = gemm_sizes(d);
+    float *xh = scratch, *xl = xh + s.x_floats, *yh = xl + s.x_floats, *yl = yh + s.y_floats;
+    const int threads = 256;
+    const uint64_t xt = s.m_tiles * kTileM * s.k_tiles * kTileK, yt = s.n_tiles * kTileN * s.k_tiles * kTileK;
+    const unsigned gx = (unsigned) ((xt + threads - 1) / threads < 65535 * 8 ? (xt + threads - 1) / threads : 65535 * 8);
+    const unsigned gy = (unsigned) ((yt + threads - 1) / threads < 65535 * 8 ? (yt + threads - 1) / threads : 65535 * 8);
+    pack_operand<<<gx, threads, 0, stream>>>(A, d, 0, s.M, s.m_tiles * kTileM, s.K, s.k_tiles, xh, xl);
+    pack_operand<<<gy, threads, 0, stream>>>(B, d, 1, s.N2, s.n_tiles * kTileN, s.K, s.k_tiles, yh, yl);
+    const size_t smem = gemm_smem_bytes();
+    cudaError_t e = cudaFuncSetAttribute(gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned) s.m_tiles, (unsigned) s.n_tiles);
+    gemm_tf32x3<<<grid, kGemmThreads, smem, stream>>>(xh, xl, yh, yl, s.k_tiles, s.M, s.N2, C, error_flag);
+    return cudaGetLastError();
+}
+
+}  // namespace qtg

@@ -1,0 +1,29 @@
+// Tensor-core path (gemm_tc.cu) for GEMM-shaped contraction steps in complex64.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "engine.cuh"
+
+namespace qtg {
+
+struct GemmSizes {
+    uint64_t M, N2, K;              // rows of X, rows of Y (2 x complex columns), summed range
+    uint64_t k_tiles, m_tiles, n_tiles;
+    uint64_t x_floats, y_floats;    // one plane of packed X / Y
+};
+
+// A step qualifies when A's free wires are C's low digits (as ContractNodes
+// orders them) and the GEMM is large enough to fill 128x128 tiles.
+bool gemm_eligible(const StepDesc &d);
+GemmSizes gemm_sizes(const StepDesc &d);
+inline uint64_t gemm_scratch_floats(const StepDesc &d) {
+    const GemmSizes s = gemm_sizes(d);
+    return 2 * (s.x_floats + s.y_floats);
+}
+size_t gemm_smem_bytes();
+// pack X and Y (hi/lo TF32 planes) into scratch, then the tcgen05 GEMM writes C.
+// error_flag (device int, zero on entry) becomes 1 if a pipeline wait timed out.
+cudaError_t launch_gemm_step(const StepDesc &d, const float2 *A, const float2 *B, float2 *C, float *scratch,
+                             int *error_flag, cudaStream_t stream);
+
+}  // namespace qtg

@@ -272,11 +272,19 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
                     }
                 }
             }
-            // lane groups are aligned inside a warp; every lane takes part in the shuffles
-            for (int off = 8; off >= 1; off >>= 1) {
-                const float ore = __shfl_xor_sync(0xffffffffu, fre, off);
-                const float oim = __shfl_xor_sync(0xffffffffu, fim, off);
-                if ((uint32_t) off < g) { fre += ore; fim += oim; }
+            // lane groups are aligned inside a warp; every lane takes part in the shuffles,
+            // which run only as far as the widest group of the warp needs
+            const uint32_t gmax = __reduce_max_sync(0xffffffffu, valid ? g : 1u);
+            const bool dbl = __any_sync(0xffffffffu, valid && f64 && g > 1);
+            for (uint32_t off = gmax >> 1; off >= 1; off >>= 1) {
+                const float ore = __shfl_xor_sync(0xffffffffu, fre, (int) off);
+                const float oim = __shfl_xor_sync(0xffffffffu, fim, (int) off);
+                if (off < g) { fre += ore; fim += oim; }
+                if (dbl) {
+                    const double dro = __shfl_xor_sync(0xffffffffu, dre, (int) off);
+                    const double dio = __shfl_xor_sync(0xffffffffu, dim, (int) off);
+                    if (off < g) { dre += dro; dim += dio; }
+                }
             }
             if (valid && lane_k == 0) {
                 const int ma = step_scale(h, d.a_step), mb = step_scale(h, d.b_step);

@@ -215,8 +215,10 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
                 StepDesc &d = steps[i];
                 const uint64_t n_out = 1ull << (2 * d.nFree), K = 1ull << (2 * d.nSum);
                 uint32_t g = 1;
-                if (mixed && !(d.flags & kCF64))
-                    while (g < 16 && g * 2 <= K && n_out * g * 2 <= (uint64_t) kPlanThreads) g *= 2;
+                // mixed form: small outputs share their k loop among up to a warp of lanes
+                // (FP64-accumulated reductions too; the FP64 form keeps the reference's order)
+                if (mixed)
+                    while (g < 32 && g * 2 <= K && n_out * g * 2 <= (uint64_t) kPlanThreads) g *= 2;
                 acc = (acc + g - 1) / g * g;   // a lane group starts on a multiple of its size
                 d.group = (uint8_t) g;
                 d.item_start = acc;
@@ -389,12 +391,8 @@ qt_status execute_stepwise(qt_plan *p, int prec, const std::complex<double> *lea
         const void *B = (d.flags & kBLeaf) ? (const char *) dleaf + leaf_off[p->b_leaf[i]] : outs[d.b_step];
         s = dev_alloc(ctx, es << (2 * d.nFree), &outs[i]);
         if (s != QT_OK) break;
-        ce = launch_pair(d, A, B, outs[i], !mixed, ctx->stream);
-        ctx->launches++;
-        if (ce != cudaSuccess) {
-            s = cuda_error(ctx, ce, "pair kernel launch");
-            break;
-        }
+        s = run_contraction(ctx, d, A, B, outs[i], !mixed);
+        if (s != QT_OK) break;
         if (d.a_step >= 0 && --uses[d.a_step] == 0 && !(steps[d.a_step].flags & kOutRank0)) {
             dev_free(ctx, outs[d.a_step]);
             outs[d.a_step] = nullptr;

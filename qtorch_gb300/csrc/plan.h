@@ -15,10 +15,12 @@ constexpr int kMixedTailRank = 1;
 constexpr int kGroupedMaxRank = 11;
 constexpr int kGroupedMaxSum = 8;
 constexpr uint64_t kGroupedMaxWorkspace = 96ull << 20;
-// a batch whose largest workspace is at most this keeps it in shared memory
-constexpr uint64_t kSmemWorkspaceMax = 96ull << 10;
-// total dynamic shared memory of an interpreter CTA when instances are staged
-constexpr uint64_t kSmemStageMax = 200ull << 10;
+// Shared memory of an interpreter CTA: instances whose workspace is at most
+// kSmemWorkspaceMax keep it in shared memory, those whose plan block + leaves
+// are at most kSmemStageMax are staged there.  The caps keep two CTAs per SM
+// (the register budget allows two), larger instances run from global memory.
+constexpr uint64_t kSmemWorkspaceMax = 32ull << 10;
+constexpr uint64_t kSmemStageMax = 64ull << 10;
 inline uint64_t round16(uint64_t x) { return (x + 15) / 16 * 16; }
 // offset tables are built when they take at most this many bytes
 constexpr uint64_t kMaxTableBytes = 64ull << 10;
