@@ -222,6 +222,13 @@ qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *plan, qt_precision 
  * order: their count, and the angles the plan's own circuit gives them. */
 int qt_plan_num_rotations(const qt_plan *plan);
 qt_status qt_plan_rotation_angles(const qt_plan *plan, double *angles, int cap);
+/* The plan's schedule as the grouped interpreter runs it (no reference
+ * counterpart), QT_STEP_INFO_FIELDS int32 per step in execution order:
+ * dependency level, rank of A, rank of B, output rank, summed wires, lane-group
+ * size, flags (bit 0/1: A/B is a leaf, bit 4: FP64 accumulation), and 1 when the
+ * step has offset tables.  Returns the number of steps, -1 on a bad argument. */
+#define QT_STEP_INFO_FIELDS 8
+int qt_plan_step_info(const qt_plan *plan, qt_precision prec, int32_t *out, int cap_steps);
 
 /* ---- batches: many plan instances in one persistent grouped launch ------ */
 

@@ -486,6 +486,19 @@ class Plan(_Owned):
         _check(_lib().qt_plan_rotation_angles(self.handle, _dp(out), n), self.ctx)
         return out[:n].copy()
 
+    STEP_INFO_FIELDS = ("level", "rank_a", "rank_b", "rank_c", "summed", "group", "flags", "table")
+
+    def step_info(self, precision=FP64):
+        """The interpreter schedule: one row per step in execution order with the
+        columns of STEP_INFO_FIELDS."""
+        n = self.num_steps
+        out = np.zeros((max(n, 1), len(self.STEP_INFO_FIELDS)), dtype=np.int32)
+        got = _lib().qt_plan_step_info(self.handle, precision,
+                                       out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), n)
+        if got < 0:
+            raise InvalidFunctionInput("qt_plan_step_info")
+        return out[:n].copy()
+
 
 class Batch(_Owned):
     """Many plan instances in one persistent grouped launch."""

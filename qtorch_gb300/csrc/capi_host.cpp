@@ -338,6 +338,26 @@ qt_status qt_plan_rotation_angles(const qt_plan *p, double *angles, int cap) {
     return QT_OK;
 }
 
+int qt_plan_step_info(const qt_plan *p, qt_precision prec, int32_t *out, int cap) {
+    if (!p || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED) || (!out && cap)) return -1;
+    const auto &steps = p->steps[prec];
+    for (int L = 0; L < p->n_levels; L++) {
+        for (int i = p->level_start[L]; i < p->level_start[L + 1] && i < cap; i++) {
+            const qtg::StepDesc &d = steps[i];
+            int32_t *o = out + (size_t) i * QT_STEP_INFO_FIELDS;
+            o[0] = L;
+            o[1] = d.rA;
+            o[2] = d.rB;
+            o[3] = d.nFree;
+            o[4] = d.nSum;
+            o[5] = d.group;
+            o[6] = (int32_t) d.flags;
+            o[7] = d.tab_off != qtg::kNoTable ? 1 : 0;
+        }
+    }
+    return p->n_steps;
+}
+
 qt_status qt_plan_leaf_values(const qt_plan *p, double *out, uint64_t cap) {
     if (!p || !out || cap < p->leaf_values.size()) return QT_ERR_INVALID_ARGUMENT;
     std::memcpy(out, p->leaf_values.data(), p->leaf_values.size() * sizeof(std::complex<double>));
