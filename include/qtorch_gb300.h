@@ -45,7 +45,7 @@ typedef enum qt_dtype {
 
 typedef enum qt_precision {
     QT_PREC_FP64 = 0,   /* complex128 throughout, each product rounded as the reference's loop */
-    QT_PREC_MIXED = 1   /* complex64 storage, FP32 accumulation, power-of-two scaling, FP64 tail */
+    QT_PREC_MIXED = 1   /* complex64 storage, FP32 accumulation, power-of-two scaling, compensated (twice-FP32) final reductions */
 } qt_precision;
 
 typedef struct qt_ctx qt_ctx;
@@ -225,7 +225,7 @@ qt_status qt_plan_rotation_angles(const qt_plan *plan, double *angles, int cap);
 /* The plan's schedule as the grouped interpreter runs it (no reference
  * counterpart), QT_STEP_INFO_FIELDS int32 per step in execution order:
  * dependency level, rank of A, rank of B, output rank, summed wires, lane-group
- * size, flags (bit 0/1: A/B is a leaf, bit 4: FP64 accumulation), and 1 when the
+ * size, flags (bit 0/1: A/B is a leaf, bit 4: complex128 output), and 1 when the
  * step has offset tables.  Returns the number of steps, -1 on a bad argument. */
 #define QT_STEP_INFO_FIELDS 8
 int qt_plan_step_info(const qt_plan *plan, qt_precision prec, int32_t *out, int cap_steps);
@@ -255,6 +255,15 @@ qt_status qt_batch_set_leaves(qt_batch *b, int index, const double *leaves);
  * how an optimiser moves a batch of QAOA terms to a new (gamma, beta) point
  * without re-planning. */
 qt_status qt_batch_set_rotations(qt_batch *b, const double *angles, int64_t n_angles);
+/* The same, with the gate tensors built on the device (no reference
+ * counterpart): only the angles travel (8 bytes each, one asynchronous copy
+ * from pinned memory on the context stream), and every following qt_batch_run
+ * rebuilds the rotation leaves inside the interpreter before contracting --
+ * Rx/Ry/Rz narrowed to float like the reference's parser, the trigonometry in
+ * FP64, each entry rounded to complex64.  Batches prepared for QT_PREC_MIXED
+ * only; instances run step by step get their leaves on the host.  A later
+ * qt_batch_set_rotations or qt_batch_set_leaves switches back to host leaves. */
+qt_status qt_batch_set_rotations_device(qt_batch *b, const double *angles, int64_t n_angles);
 /* Upload all leaf values again from the host copies (async; part of an end-to-end step). */
 qt_status qt_batch_upload(qt_batch *b);
 /* Capture qt_batch_run into a CUDA graph and replay it (0 disables). */

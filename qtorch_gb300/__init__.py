@@ -551,6 +551,12 @@ class Batch(_Owned):
         a = np.ascontiguousarray(np.asarray(angles, dtype=np.float64))
         _check(_lib().qt_batch_set_rotations(self.handle, _dp(a), a.size), self.ctx)
 
+    def set_rotations_device(self, angles):
+        """New rotation angles whose gate tensors are built on the device at the
+        next run (batches prepared for MIXED); only the angles are copied."""
+        a = np.ascontiguousarray(np.asarray(angles, dtype=np.float64))
+        _check(_lib().qt_batch_set_rotations_device(self.handle, _dp(a), a.size), self.ctx)
+
     def upload(self):
         _check(_lib().qt_batch_upload(self.handle), self.ctx)
 

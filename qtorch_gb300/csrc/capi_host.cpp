@@ -1,5 +1,6 @@
 // C ABI over the host library: networks (Network / ContractionTools /
 // LineGraph), plans and batches.
+#include <algorithm>
 #include <cstring>
 #include <fstream>
 #include <new>
@@ -260,6 +261,7 @@ qt_status qt_plan_build(qt_ctx *ctx, const char *qasm_text, const char *measure_
                 p->rot_kind.push_back(kind);
                 p->rot_angle.push_back(qtorch::GateAngle(*leaf));
                 p->rot_elem.push_back(p->leaf_values.size());
+                p->rot_leaf.push_back((int) p->leaf_rank.size() - 1);
             }
             p->leaf_values.insert(p->leaf_values.end(), v.begin(), v.end());
         }
@@ -380,6 +382,8 @@ qt_status qt_plan_execute(qt_ctx *ctx, qt_plan *p, qt_precision prec, double *v)
 // ---------------------------------------------------------------------------
 // batches
 
+static qt_status batch_device_rotations(qt_batch *b, bool on);
+
 static void batch_release(qt_batch *b) {
     qt_ctx *ctx = b->ctx;
     if (b->graph) {
@@ -390,8 +394,15 @@ static void batch_release(qt_batch *b) {
     dev_free(ctx, b->d_inst);
     dev_free(ctx, b->d_values);
     dev_free(ctx, b->d_ws);
-    dev_free(ctx, b->d_exps);
-    b->d_leaves = b->d_inst = b->d_values = b->d_ws = b->d_exps = nullptr;
+    dev_free(ctx, b->d_next);
+    dev_free(ctx, b->d_angles);
+    b->d_leaves = b->d_inst = b->d_values = b->d_ws = b->d_next = b->d_angles = nullptr;
+    b->tile_bytes = 0;
+    if (b->h_angles) cudaFreeHost(b->h_angles);
+    b->h_angles = nullptr;
+    if (b->angles_done) cudaEventDestroy(b->angles_done);
+    b->angles_done = nullptr;
+    b->dev_rot = false;
     if (b->h_leaves) cudaFreeHost(b->h_leaves);
     if (b->h_values) cudaFreeHost(b->h_values);
     b->h_leaves = b->h_values = nullptr;
@@ -434,13 +445,87 @@ int qt_batch_size(const qt_batch *b) { return b ? (int) b->plans.size() : -1; }
 
 qt_status qt_batch_set_leaves(qt_batch *b, int i, const double *leaves) {
     if (!b || !leaves || i < 0 || i >= (int) b->plans.size()) return QT_ERR_INVALID_ARGUMENT;
+    {
+        std::lock_guard<std::recursive_mutex> g(b->ctx->lock);
+        qt_status s = batch_device_rotations(b, false);
+        if (s != QT_OK) return s;
+    }
     const auto *c = reinterpret_cast<const std::complex<double> *>(leaves);
     std::copy(c, c + b->leaves[i].size(), b->leaves[i].begin());
     return QT_OK;
 }
 
+// Device rotations on/off: the descriptors carry the angle pointers or null.
+static qt_status batch_device_rotations(qt_batch *b, bool on) {
+    if (b->dev_rot == on || b->inst_desc.empty()) {
+        b->dev_rot = on;
+        return QT_OK;
+    }
+    qt_ctx *ctx = b->ctx;
+    for (size_t j = 0; j < b->inst_desc.size(); j++) {
+        const int i = b->inst_index[j];
+        b->inst_desc[j].angles = on && !b->plans[i]->rot_kind.empty()
+                                     ? static_cast<const double *>(b->d_angles) + b->inst_angle_off[i]
+                                     : nullptr;
+    }
+    cudaError_t e = cudaMemcpyAsync(b->d_inst, b->inst_desc.data(), sizeof(InstanceDesc) * b->inst_desc.size(),
+                                    cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);   // the host copy may change again
+    if (e != cudaSuccess) return cuda_error(ctx, e, "instance descriptor upload");
+    b->dev_rot = on;
+    return QT_OK;
+}
+
+qt_status qt_batch_set_rotations_device(qt_batch *b, const double *angles, int64_t n_angles) {
+    if (!b || (n_angles && !angles)) return QT_ERR_INVALID_ARGUMENT;
+    qt_ctx *ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    if (b->prepared_prec != QT_PREC_MIXED)
+        return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "device rotations need a batch prepared for QT_PREC_MIXED");
+    if (n_angles != b->n_angles) return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "angle count does not match the batch");
+    if (!n_angles) return QT_OK;
+    qt_status s = QT_OK;
+    if (!b->d_angles) {
+        cudaError_t e = cudaMallocHost((void **) &b->h_angles, sizeof(double) * n_angles);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->angles_done, cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "angle staging");
+        s = dev_alloc(ctx, sizeof(double) * n_angles, &b->d_angles);
+        if (s != QT_OK) return s;
+    } else {
+        // the previous upload must have read the pinned copy before it is overwritten
+        cudaError_t e = cudaEventSynchronize(b->angles_done);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "angle staging");
+    }
+    std::memcpy(b->h_angles, angles, sizeof(double) * n_angles);
+    cudaError_t e = cudaMemcpyAsync(b->d_angles, b->h_angles, sizeof(double) * n_angles, cudaMemcpyHostToDevice,
+                                    ctx->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b->angles_done, ctx->stream);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "angle upload");
+    // instances run step by step take their leaves from the host
+    if (!b->stepwise.empty()) {
+        s = guard(ctx, [&]() {
+            for (int i : b->stepwise) {
+                const qt_plan *p = b->plans[i];
+                for (size_t r = 0; r < p->rot_kind.size(); r++) {
+                    auto gt = qtorch::MakeGateNode(p->rot_kind[r], angles[b->inst_angle_off[i] + (int64_t) r]);
+                    const auto &v = gt->GetTensorVals();
+                    std::copy(v.begin(), v.end(), b->leaves[i].begin() + p->rot_elem[r]);
+                }
+            }
+            return QT_OK;
+        });
+        if (s != QT_OK) return s;
+    }
+    return batch_device_rotations(b, true);
+}
+
 qt_status qt_batch_set_rotations(qt_batch *b, const double *angles, int64_t n_angles) {
     if (!b || (n_angles && !angles)) return QT_ERR_INVALID_ARGUMENT;
+    {
+        std::lock_guard<std::recursive_mutex> g(b->ctx->lock);
+        qt_status s = batch_device_rotations(b, false);
+        if (s != QT_OK) return s;
+    }
     int64_t need = 0;
     for (auto *p : b->plans) need += (int64_t) p->rot_kind.size();
     if (need != n_angles) return set_error(b->ctx, QT_ERR_INVALID_ARGUMENT, "angle count does not match the batch");
@@ -477,8 +562,9 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
     const int n = (int) b->plans.size();
     b->stepwise.clear();
     b->inst_leaf_off.assign(n, 0);
-    uint64_t off = 0, ws = 0, ex = 0, ws_small = 0, stage_small = 0;
+    uint64_t off = 0, ws = 0, ws_small = 0;
     int n_grouped = 0;
+    bool any_tiled = false;
     for (int i = 0; i < n; i++) {
         qt_plan *p = b->plans[i];
         if (!p->grouped) {
@@ -490,23 +576,30 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
         b->inst_leaf_off[i] = off;
         off += (p->leaf_bytes[prec] + 255) / 256 * 256;
         const uint64_t w = (p->ws_bytes[prec] + 255) / 256 * 256;
-        const uint64_t st = round16(p->dev_bytes[prec]) + round16(p->leaf_bytes[prec]);
         ws = std::max<uint64_t>(ws, w);
         if (w <= kSmemWorkspaceMax) ws_small = std::max<uint64_t>(ws_small, w);
-        if (st <= kSmemStageMax) stage_small = std::max<uint64_t>(stage_small, st);
-        ex = std::max<uint64_t>(ex, (uint64_t) p->n_steps);
+        any_tiled = any_tiled || p->n_tiled > 0;
         n_grouped++;
+    }
+    // shared memory of a CTA: a workspace region as large as the largest workspace
+    // that fits it, a staging region as large as the largest plan block + leaf
+    // image that fits, and the tile buffers when an instance has CTA-tiled steps;
+    // instances beyond either region use the global slab / read in place
+    const uint64_t stage_cap = any_tiled ? kSmemStageMaxTiled : kSmemStageMax;
+    uint64_t stage_small = 0;
+    for (int i = 0; i < n; i++) {
+        const qt_plan *p = b->plans[i];
+        if (!p->grouped) continue;
+        const uint64_t st = round16(p->dev_bytes[prec]) + round16(p->leaf_bytes[prec]);
+        if (st <= stage_cap) stage_small = std::max<uint64_t>(stage_small, st);
     }
     b->leaf_bytes = off;
     b->ws_stride = ws;
-    b->exps_stride = (ex + 63) / 64 * 64;
-    // shared memory of a CTA: a workspace region as large as the largest workspace
-    // that fits it and a staging region as large as the largest plan block + leaf
-    // image that fits; instances beyond either use the global slab / read in place
     b->ws_smem_bytes = (uint32_t) ws_small;
     b->stage_bytes = b->allow_stage ? (uint32_t) stage_small : 0;
+    b->tile_bytes = any_tiled ? kCtaTileBytes : 0;
     b->ws_in_smem = ws <= b->ws_smem_bytes;   // no global slab needed
-    b->grid = std::min(n_grouped, plan_max_grid(kPlanHeaderBytes + 128 + b->ws_smem_bytes + b->stage_bytes));
+    b->grid = std::min(n_grouped, plan_max_grid(kPlanHeaderBytes + 128 + b->ws_smem_bytes + b->stage_bytes + b->tile_bytes));
     qt_status s = QT_OK;
     auto chk = [&](cudaError_t e, const char *w) {
         if (s == QT_OK && e != cudaSuccess) s = cuda_error(ctx, e, w);
@@ -520,16 +613,29 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
         if (s == QT_OK) s = dev_alloc(ctx, sizeof(double) * 2 * n, &b->d_values);
     }
     if (s == QT_OK && b->grid > 0 && !b->ws_in_smem) s = dev_alloc(ctx, b->ws_stride * b->grid, &b->d_ws);
+    // more instances than CTAs: a dynamic schedule over the instances sorted by
+    // estimated cost, longest first
+    if (s == QT_OK && n_grouped > b->grid) s = dev_alloc(ctx, 256, &b->d_next);
     if (s != QT_OK) {
         batch_release(b);
         return s;
     }
-    // instance descriptors (grouped instances only, packed)
+    // instance descriptors (grouped instances only, packed; longest first under
+    // the dynamic schedule)
+    std::vector<int> inst_order;
+    for (int i = 0; i < n; i++)
+        if (b->plans[i]->grouped) inst_order.push_back(i);
+    if (b->d_next) {
+        auto cost = [&](int i) {
+            const qt_plan *p = b->plans[i];
+            return (double) p->flops + 2048.0 * p->n_levels;   // MACs plus a per-level latency term
+        };
+        std::stable_sort(inst_order.begin(), inst_order.end(), [&](int x, int y) { return cost(x) > cost(y); });
+    }
     std::vector<InstanceDesc> inst;
-    for (int i = 0; i < n; i++) {
+    for (int i : inst_order) {
         qt_plan *p = b->plans[i];
-        if (!p->grouped) continue;
-        InstanceDesc d;
+        InstanceDesc d{};
         d.plan = reinterpret_cast<const PlanDesc *>(p->dev[prec]);
         d.leaves = (const char *) b->d_leaves + b->inst_leaf_off[i];
         d.value = (double *) b->d_values + 2 * i;
@@ -537,7 +643,16 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
         d.leaf_bytes = (uint32_t) round16(p->leaf_bytes[prec]);
         d.ws_bytes = (uint32_t) ((p->ws_bytes[prec] + 255) / 256 * 256);
         d.pad = 0;
+        d.angles = nullptr;
         inst.push_back(d);
+    }
+    b->inst_desc = inst;
+    b->inst_index = inst_order;
+    b->inst_angle_off.assign(n, 0);
+    b->n_angles = 0;
+    for (int i = 0; i < n; i++) {
+        b->inst_angle_off[i] = b->n_angles;
+        b->n_angles += (int64_t) b->plans[i]->rot_kind.size();
     }
     if (!inst.empty()) {
         s = dev_alloc(ctx, sizeof(InstanceDesc) * inst.size(), &b->d_inst);
@@ -572,15 +687,18 @@ static qt_status batch_launch(qt_batch *b) {
     qt_ctx *ctx = b->ctx;
     const int n_grouped = (int) b->plans.size() - (int) b->stepwise.size();
     if (n_grouped <= 0) return QT_OK;
-    PlanLaunch lp;
+    PlanLaunch lp{};
     lp.instances = (const InstanceDesc *) b->d_inst;
     lp.n_instances = n_grouped;
     lp.ws_smem_bytes = b->ws_smem_bytes;
     lp.ws_base = (char *) b->d_ws;
     lp.ws_stride = b->ws_stride;
     lp.stage_bytes = b->stage_bytes;
-    lp.pad = 0;
-    cudaError_t e = launch_plan(lp, b->prepared_prec == QT_PREC_MIXED, b->grid, ctx->stream);
+    lp.tile_bytes = b->tile_bytes;
+    lp.next = (uint32_t *) b->d_next;
+    cudaError_t e = cudaSuccess;
+    if (lp.next) e = cudaMemsetAsync(lp.next, 0, sizeof(uint32_t), ctx->stream);
+    if (e == cudaSuccess) e = launch_plan(lp, b->prepared_prec == QT_PREC_MIXED, b->grid, ctx->stream);
     ctx->launches++;
     return cuda_error(ctx, e, "plan kernel launch");
 }
@@ -654,7 +772,10 @@ qt_status qt_batch_use_graph(qt_batch *b, int enable) {
     return QT_OK;
 }
 
-uint64_t qt_batch_h2d_bytes(const qt_batch *b) { return b ? b->leaf_bytes : 0; }
+uint64_t qt_batch_h2d_bytes(const qt_batch *b) {
+    if (!b) return 0;
+    return b->dev_rot ? sizeof(double) * (uint64_t) b->n_angles : b->leaf_bytes;
+}
 uint64_t qt_batch_d2h_bytes(const qt_batch *b) { return b ? sizeof(double) * 2 * b->plans.size() : 0; }
 
 int qt_batch_launches_per_run(const qt_batch *b) {

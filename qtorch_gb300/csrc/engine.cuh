@@ -28,10 +28,19 @@ enum StepFlags : uint32_t {
     kBLeaf = 1u << 1,
     kAF64 = 1u << 2,         // A stored as complex128 (mixed plans only; FP64 plans are all complex128)
     kBF64 = 1u << 3,
-    kCF64 = 1u << 4,         // C computed with FP64 accumulation and stored as complex128
+    kCF64 = 1u << 4,         // C stored as complex128; mixed plans accumulate it with compensated FP32 (Dot2)
     kOutRank0 = 1u << 5,     // C has rank 0: it takes part in the final-value rule
     kBothRank0 = 1u << 6,    // A and B both rank 0 (Network.h:963)
+    kCtaTiled = 1u << 7,     // interpreter: the whole CTA runs this step as a tiled product
 };
+
+// CTA-wide tiled steps: C (M x N, flat c = m + M n, M = 4^fA, N = 4^fB) =
+// sum_k A~(m, k) B~(k, n).  Tiles of at most kCtaTileDim x kCtaTileDim outputs, the
+// summed range in chunks of kCtaTileChunk (mixed) or kCtaTileChunk / 2 (FP64) staged
+// in shared memory, 16 x 16 threads with up to 4 x 4 outputs each.
+constexpr int kCtaTileDim = 64;
+constexpr int kCtaTileChunk = 16;
+constexpr uint32_t kCtaTileBytes = 2u * kCtaTileChunk * kCtaTileDim * 8u + 2u * kCtaTileDim * 4u;
 
 struct StepDesc {
     int64_t a_off;           // byte offset into the leaf buffer or the workspace
@@ -65,11 +74,17 @@ struct PlanDesc {
     // tab[tab_off + c] = (A offset, B offset) of output c (n_out entries), then
     // tab[tab_off + n_out + k] = (A offset, B offset) of summed index k (K entries).
     const ushort2 *tables;
+    const int32_t *level_cta;    // first CTA-tiled step of each level (tiled steps close their level)
+    const uint2 *rotations;      // rotation leaves: (byte offset in the leaf image, RotationKind)
     int32_t n_steps;
     int32_t n_levels;
     int32_t n_rank0;
-    int32_t pad;
+    int32_t n_rot;
 };
+
+// Parametrised leaves the interpreter can rebuild from an angle on the device
+// (complex64 leaves of mixed plans only).
+enum RotationKind : uint32_t { kRotRx = 0, kRotRy = 1, kRotRz = 2, kRotCPhase = 3 };
 
 // One instance of a batch: a plan with its own leaves.  Intermediates live in
 // the workspace of the CTA that runs the instance.
@@ -81,6 +96,7 @@ struct InstanceDesc {
     uint32_t leaf_bytes;         // bytes of the leaf image (multiple of 16)
     uint32_t ws_bytes;           // workspace this instance needs
     uint32_t pad;
+    const double *angles;        // rotation angles to build on the device (null: leaves as uploaded)
 };
 
 // Parameters of one interpreter launch.  Shared memory of a CTA: the scale
@@ -94,13 +110,8 @@ struct PlanLaunch {
     char *ws_base;               // global workspace: ws_base + blockIdx.x * ws_stride
     uint64_t ws_stride;
     uint32_t stage_bytes;        // shared memory for a staged plan block + leaf image (0: none)
-    uint32_t pad;
-};
-
-// What one CTA works with while it interprets an instance.
-struct CtaScratch {
-    char *workspace;             // intermediate tensors
-    int32_t *exps;               // per-step power-of-two exponent (mixed precision)
+    uint32_t tile_bytes;         // shared memory for CTA-tiled steps (0: no instance has one)
+    uint32_t *next;              // dynamic schedule: instance counter, zero at launch (null: round robin)
 };
 
 __host__ __device__ inline uint64_t scatter_digits(uint64_t x, const uint8_t *pos, int n) {

@@ -9,12 +9,14 @@
 //    instance (a whole network) level by level: all steps of a dependency
 //    level run concurrently across the CTA's threads, tiny outputs split their
 //    k loop over lane groups that finish with warp shuffles (mixed mode), and
-//    intermediates stay in an L2-resident per-instance workspace.  Mixed mode
-//    keeps every intermediate normalised by a power of two (per-tensor
-//    exponent) and runs rank-0/1 outputs (the expectation-value reductions)
-//    in FP64.
+//    intermediates stay in a shared-memory (small plans) or global per-CTA
+//    workspace.  Mixed mode keeps every intermediate normalised by a power of
+//    two (per-tensor exponent) and accumulates the expectation-value
+//    reductions with compensated FP32 dot products (no FP64 arithmetic).
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <type_traits>
+
 #include "engine.cuh"
 #include "kernels.h"
 
@@ -38,11 +40,42 @@ __device__ __forceinline__ void cmac_f32(float &cre, float &cim, float2 a, float
     cim = fmaf(a.y, b.x, cim);
 }
 
-__device__ __forceinline__ void cmac_f64(double &cre, double &cim, double2 a, double2 b) {
-    cre = fma(a.x, b.x, cre);
-    cre = fma(-a.y, b.y, cre);
-    cim = fma(a.x, b.y, cim);
-    cim = fma(a.y, b.x, cim);
+// Compensated FP32 dot product (Ogita, Rump and Oishi, "Accurate sum and dot
+// product", SIAM J. Sci. Comput. 26(6), 2005, algorithm Dot2): the running sum
+// is p + s, every product is split exactly into h + r with one FMA (TwoProduct)
+// and every addition into p + q (Knuth's TwoSum); the errors q + r are summed
+// in s.  The result is as accurate as an FP32 loop run in twice the working
+// precision, and it runs on the FP32 pipe, which on GB300 is many times wider
+// than the FP64 one.  The _rn intrinsics keep the compiler from fusing the
+// error-free transformations into FMAs.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ void dot2_acc(float &p, float &s, float x, float y) {
+    const float h = __fmul_rn(x, y);
+    const float r = __fmaf_rn(x, y, -h);
+    float q, np;
+    two_sum(p, h, np, q);
+    p = np;
+    s = __fadd_rn(s, __fadd_rn(q, r));
+}
+
+__device__ __forceinline__ void cmac_dot2(float &pre, float &sre, float &pim, float &sim, float2 a, float2 b) {
+    dot2_acc(pre, sre, a.x, b.x);
+    dot2_acc(pre, sre, -a.y, b.y);
+    dot2_acc(pim, sim, a.x, b.y);
+    dot2_acc(pim, sim, a.y, b.x);
+}
+
+// (p1 + s1) += (p2 + s2)
+__device__ __forceinline__ void dot2_merge(float &p, float &s, float p2, float s2) {
+    float np, q;
+    two_sum(p, p2, np, q);
+    p = np;
+    s = __fadd_rn(s, __fadd_rn(s2, q));
 }
 
 // ---------------------------------------------------------------------------
@@ -161,10 +194,10 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
             si = lo;
         }
         const StepDesc &d = steps[si];
-        const uint32_t g = d.group;
+        const uint32_t g = d.group;   // a power of two
         const uint32_t local = item - d.item_start;
-        const uint32_t c = local / g;
-        const uint32_t lane_k = local % g;
+        const uint32_t c = local >> (__ffs(g) - 1);
+        const uint32_t lane_k = local & (g - 1);
         const int nFree = d.nFree, nSum = d.nSum;
         const uint32_t n_out = 1u << (2 * nFree);
         const bool valid = item < total && c < n_out;
@@ -217,10 +250,11 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
                 reinterpret_cast<double2 *>(ws + d.c_off)[c] = make_double2(cre, cim);
             }
         } else {
+            // f64: a reduction where cancellation lives; accumulated with Dot2
+            // (fre + ere, fim + eim) and stored as complex128
             const bool f64 = (flags & kCF64) != 0;
             const bool a64 = (flags & kAF64) != 0, b64 = (flags & kBF64) != 0;
-            double dre = 0.0, dim = 0.0;
-            float fre = 0.f, fim = 0.f;
+            float fre = 0.f, fim = 0.f, ere = 0.f, eim = 0.f;
             if (valid) {
                 if (!f64 && !a64 && !b64 && tab != kNoTable) {
                     // the common case: complex64 operands, tabled offsets
@@ -259,39 +293,46 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
                             ka = (uint32_t) scatter_digits(k, d.posAs, nSum);
                             kb = (uint32_t) scatter_digits(k, d.posBs, nSum);
                         }
-                        double2 a, b;
-                        if (a64) a = reinterpret_cast<const double2 *>(abase)[oa0 + ka];
-                        else { const float2 t = reinterpret_cast<const float2 *>(abase)[oa0 + ka]; a = make_double2(t.x, t.y); }
-                        if (b64) b = reinterpret_cast<const double2 *>(bbase)[ob0 + kb];
-                        else { const float2 t = reinterpret_cast<const float2 *>(bbase)[ob0 + kb]; b = make_double2(t.x, t.y); }
-                        if (f64) {
-                            cmac_f64(dre, dim, a, b);
-                        } else {
-                            cmac_f32(fre, fim, make_float2((float) a.x, (float) a.y), make_float2((float) b.x, (float) b.y));
-                        }
+                        float2 a, b;
+                        if (a64) { const double2 t = reinterpret_cast<const double2 *>(abase)[oa0 + ka]; a = make_float2((float) t.x, (float) t.y); }
+                        else a = reinterpret_cast<const float2 *>(abase)[oa0 + ka];
+                        if (b64) { const double2 t = reinterpret_cast<const double2 *>(bbase)[ob0 + kb]; b = make_float2((float) t.x, (float) t.y); }
+                        else b = reinterpret_cast<const float2 *>(bbase)[ob0 + kb];
+                        if (f64) cmac_dot2(fre, ere, fim, eim, a, b);
+                        else cmac_f32(fre, fim, a, b);
                     }
                 }
             }
             // lane groups are aligned inside a warp; every lane takes part in the shuffles,
             // which run only as far as the widest group of the warp needs
             const uint32_t gmax = __reduce_max_sync(0xffffffffu, valid ? g : 1u);
-            const bool dbl = __any_sync(0xffffffffu, valid && f64 && g > 1);
+            const bool comp = __any_sync(0xffffffffu, valid && f64 && g > 1);
             for (uint32_t off = gmax >> 1; off >= 1; off >>= 1) {
                 const float ore = __shfl_xor_sync(0xffffffffu, fre, (int) off);
                 const float oim = __shfl_xor_sync(0xffffffffu, fim, (int) off);
-                if (off < g) { fre += ore; fim += oim; }
-                if (dbl) {
-                    const double dro = __shfl_xor_sync(0xffffffffu, dre, (int) off);
-                    const double dio = __shfl_xor_sync(0xffffffffu, dim, (int) off);
-                    if (off < g) { dre += dro; dim += dio; }
+                float oere = 0.f, oeim = 0.f;
+                if (comp) {
+                    oere = __shfl_xor_sync(0xffffffffu, ere, (int) off);
+                    oeim = __shfl_xor_sync(0xffffffffu, eim, (int) off);
+                }
+                if (off < g) {
+                    if (f64) {
+                        dot2_merge(fre, ere, ore, oere);
+                        dot2_merge(fim, eim, oim, oeim);
+                    } else {
+                        fre += ore;
+                        fim += oim;
+                    }
                 }
             }
-            if (valid && lane_k == 0) {
+            const bool writer = valid && lane_k == 0;
+            uint32_t magbits = 0;
+            if (writer) {
                 const int ma = step_scale(h, d.a_step), mb = step_scale(h, d.b_step);
                 float mag;
                 if (f64) {
-                    dre = scale2d(dre, -(ma + mb));
-                    dim = scale2d(dim, -(ma + mb));
+                    const double dre = scale2d((double) fre + (double) ere, -(ma + mb));
+                    const double dim = scale2d((double) fim + (double) eim, -(ma + mb));
                     reinterpret_cast<double2 *>(ws + d.c_off)[c] = make_double2(dre, dim);
                     mag = (float) fmax(fabs(dre), fabs(dim));
                 } else {
@@ -300,14 +341,184 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
                     reinterpret_cast<float2 *>(ws + d.c_off)[c] = make_float2(fre, fim);
                     mag = fmaxf(fabsf(fre), fabsf(fim));
                 }
-                atomicMax(&h.maxbits[si], __float_as_uint(mag));
+                magbits = __float_as_uint(mag);
                 if (c == 0) {
                     const int ea = d.a_step >= 0 ? h.expo[d.a_step] : 0;
                     const int eb = d.b_step >= 0 ? h.expo[d.b_step] : 0;
                     h.expo[si] = ea + eb + ma + mb;
                 }
             }
+            // one shared-memory atomic per (warp, step): the writers of a step
+            // agree on the maximum first (non-negative floats order as their bits)
+            const uint32_t key = writer ? (uint32_t) si : 0xffffffffu;
+            const uint32_t peers = __match_any_sync(0xffffffffu, key);
+            const uint32_t wmax = __reduce_max_sync(peers, magbits);
+            if (writer && (threadIdx.x & 31) == (uint32_t) (__ffs(peers) - 1)) atomicMax(&h.maxbits[si], wmax);
         }
+    }
+}
+
+// CTA-wide tiled step: the contraction as a product of the gathered matrices
+// A~(m, k) = A[oa(m) + ka(k)] and B~(k, n) = B[ob(n) + kb(k)], C[m + M n].
+// A tile of TM x TN outputs is split over 16 x 16 threads (MI x NJ outputs
+// each, rows tx + 16 i, columns ty + 16 j); the summed range runs in chunks
+// whose A~ and B~ slices are gathered into shared memory once and reused by
+// every thread of the tile.  Each output still accumulates over k in
+// increasing order, so the FP64 form keeps the reference's rounding.
+template <bool kMixed, int MI, int NJ>
+__device__ void tiled_step(const StepDesc &d, int si, const char *leaves, char *ws, PlanSmemHeader &h,
+                           unsigned char *tile) {
+    using V = typename std::conditional<kMixed, float2, double2>::type;
+    using T = typename std::conditional<kMixed, float, double>::type;
+    constexpr uint32_t KC = kMixed ? kCtaTileChunk : kCtaTileChunk / 2;
+    constexpr uint32_t TM = 16 * MI, TN = 16 * NJ;
+    V *As = reinterpret_cast<V *>(tile);            // [KC][kCtaTileDim]
+    V *Bs = As + KC * kCtaTileDim;                      // [KC][kCtaTileDim]
+    uint32_t *s_oa = reinterpret_cast<uint32_t *>(tile + 2u * kCtaTileChunk * kCtaTileDim * 8u);
+    uint32_t *s_ob = s_oa + kCtaTileDim;
+    const uint32_t tid = threadIdx.x, tx = tid & 15u, ty = tid >> 4;
+    const uint32_t fA = d.fA, fB = d.fB, nSum = d.nSum;
+    const uint32_t M = 1u << (2 * fA), N = 1u << (2 * fB), K = 1u << (2 * nSum);
+    const uint32_t kc = K < KC ? K : KC;
+    const uint32_t tiles_m = M / TM, n_tiles = tiles_m * (N / TN);
+    const V *A = reinterpret_cast<const V *>(((d.flags & kALeaf) ? leaves : ws) + d.a_off);
+    const V *B = reinterpret_cast<const V *>(((d.flags & kBLeaf) ? leaves : ws) + d.b_off);
+    V *C = reinterpret_cast<V *>(ws + d.c_off);
+    int ma = 0, mb = 0;
+    if constexpr (kMixed) {
+        ma = step_scale(h, d.a_step);
+        mb = step_scale(h, d.b_step);
+    }
+    float tmax = 0.f;
+    for (uint32_t t = 0; t < n_tiles; t++) {
+        const uint32_t m0 = (t % tiles_m) * TM, n0 = (t / tiles_m) * TN;
+        __syncthreads();   // readers of the previous tile's offsets and slices are done
+        if (tid < TM) {
+            const uint32_t x = m0 + tid;
+            uint32_t o = 0;
+            for (uint32_t i = 0; i < fA; i++) o += ((x >> (2 * i)) & 3u) << (2 * d.cA[i]);
+            s_oa[tid] = o;
+        } else if (tid >= 128 && tid - 128 < TN) {
+            const uint32_t x = n0 + tid - 128;
+            uint32_t o = 0;
+            for (uint32_t i = 0; i < fB; i++) o += ((x >> (2 * i)) & 3u) << (2 * d.cB[fA + i]);
+            s_ob[tid - 128] = o;
+        }
+        T cre[MI][NJ], cim[MI][NJ];
+#pragma unroll
+        for (int i = 0; i < MI; i++)
+#pragma unroll
+            for (int j = 0; j < NJ; j++) cre[i][j] = cim[i][j] = T(0);
+        for (uint32_t k0 = 0; k0 < K; k0 += kc) {
+            __syncthreads();   // offsets visible; the previous chunk's slices are consumed
+            for (uint32_t e = tid; e < TM * kc; e += blockDim.x) {
+                const uint32_t m = e % TM, kk = e / TM;
+                As[kk * kCtaTileDim + m] = A[s_oa[m] + (uint32_t) scatter_digits(k0 + kk, d.posAs, (int) nSum)];
+            }
+            for (uint32_t e = tid; e < TN * kc; e += blockDim.x) {
+                const uint32_t n = e % TN, kk = e / TN;
+                Bs[kk * kCtaTileDim + n] = B[s_ob[n] + (uint32_t) scatter_digits(k0 + kk, d.posBs, (int) nSum)];
+            }
+            __syncthreads();
+            for (uint32_t kk = 0; kk < kc; kk++) {
+                V a[MI];
+#pragma unroll
+                for (int i = 0; i < MI; i++) a[i] = As[kk * kCtaTileDim + tx + 16 * i];
+#pragma unroll
+                for (int j = 0; j < NJ; j++) {
+                    const V b = Bs[kk * kCtaTileDim + ty + 16 * j];
+#pragma unroll
+                    for (int i = 0; i < MI; i++) {
+                        if constexpr (kMixed) cmac_f32(cre[i][j], cim[i][j], a[i], b);
+                        else cmac_exact(cre[i][j], cim[i][j], a[i], b);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < MI; i++)
+#pragma unroll
+            for (int j = 0; j < NJ; j++) {
+                const uint32_t c = (m0 + tx + 16 * i) + M * (n0 + ty + 16 * j);
+                V v;
+                if constexpr (kMixed) {
+                    v.x = scale2f(cre[i][j], -(ma + mb));
+                    v.y = scale2f(cim[i][j], -(ma + mb));
+                    tmax = fmaxf(tmax, fmaxf(fabsf(v.x), fabsf(v.y)));
+                } else {
+                    v.x = cre[i][j];
+                    v.y = cim[i][j];
+                }
+                C[c] = v;
+            }
+    }
+    if constexpr (kMixed) {
+        const uint32_t wmax = __reduce_max_sync(0xffffffffu, __float_as_uint(tmax));
+        if ((tid & 31u) == 0) atomicMax(&h.maxbits[si], wmax);
+        if (tid == 0) {
+            const int ea = d.a_step >= 0 ? h.expo[d.a_step] : 0;
+            const int eb = d.b_step >= 0 ? h.expo[d.b_step] : 0;
+            h.expo[si] = ea + eb + ma + mb;
+        }
+    }
+}
+
+template <bool kMixed>
+__device__ __forceinline__ void run_tiled(const StepDesc &d, int si, const char *leaves, char *ws, PlanSmemHeader &h,
+                                          unsigned char *tile) {
+    const bool wide_m = d.fA >= 3, wide_n = d.fB >= 3;
+    if (wide_m && wide_n) tiled_step<kMixed, 4, 4>(d, si, leaves, ws, h, tile);
+    else if (wide_m) tiled_step<kMixed, 4, 1>(d, si, leaves, ws, h, tile);
+    else if (wide_n) tiled_step<kMixed, 1, 4>(d, si, leaves, ws, h, tile);
+    else tiled_step<kMixed, 1, 1>(d, si, leaves, ws, h, tile);
+}
+
+// Rotation leaves rebuilt from an angle (mixed plans): the superoperators the
+// host gate factory writes, T[in + 4 out] for one-qubit gates and the
+// controlled phase's diagonal T[i1 + 4 i2 + 16 i1 + 64 i2] (src/Node.h
+// RxNode .. CPhaseNode).  Rx/Ry/Rz angles are narrowed to float first, as the
+// reference's parser does with std::stof (src/Network.h:342, 383, 402, 422);
+// the trigonometry runs in FP64 and every entry is rounded to complex64 once,
+// like the host-built leaves.
+__device__ void build_rotation(char *leaves, uint2 rot, double angle) {
+    float2 *t = reinterpret_cast<float2 *>(leaves + rot.x);
+    auto put = [&](int in, int out, double re, double im) { t[in + 4 * out] = make_float2((float) re, (float) im); };
+    if (rot.y == kRotCPhase) {
+        double s, c;
+        sincos(angle, &s, &c);
+        for (int i1 = 0; i1 < 4; i1++)
+            for (int i2 = 0; i2 < 4; i2++) {
+                const bool rowph = (i1 >> 1) && (i2 >> 1), colph = (i1 & 1) && (i2 & 1);
+                float2 v = make_float2(1.f, 0.f);
+                if (rowph && !colph) v = make_float2((float) c, (float) s);
+                else if (!rowph && colph) v = make_float2((float) c, (float) -s);
+                t[i1 + 4 * i2 + 16 * i1 + 64 * i2] = v;
+            }
+        return;
+    }
+    const double th = (double) (float) angle;
+    for (int e = 0; e < 16; e++) t[e] = make_float2(0.f, 0.f);
+    if (rot.y == kRotRz) {
+        double s, c;
+        sincos(th, &s, &c);
+        put(0, 0, 1.0, 0.0);
+        put(3, 3, 1.0, 0.0);
+        put(1, 1, c, -s);
+        put(2, 2, c, s);
+        return;
+    }
+    double sh2, ch2;
+    sincos(th / 2.0, &sh2, &ch2);
+    const double cc = ch2 * ch2, ss = sh2 * sh2, sh = sin(th) / 2.0;
+    for (int i = 0; i < 4; i++) put(i, i, cc, 0.0);
+    if (rot.y == kRotRx) {
+        put(0, 3, ss, 0.0); put(1, 2, ss, 0.0); put(2, 1, ss, 0.0); put(3, 0, ss, 0.0);
+        put(0, 1, 0.0, sh); put(1, 0, 0.0, sh); put(2, 3, 0.0, sh); put(3, 2, 0.0, sh);
+        put(0, 2, 0.0, -sh); put(1, 3, 0.0, -sh); put(2, 0, 0.0, -sh); put(3, 1, 0.0, -sh);
+    } else {
+        put(0, 3, ss, 0.0); put(3, 0, ss, 0.0); put(1, 2, -ss, 0.0); put(2, 1, -ss, 0.0);
+        put(0, 1, sh, 0.0); put(0, 2, sh, 0.0); put(1, 3, sh, 0.0); put(2, 3, sh, 0.0);
+        put(1, 0, -sh, 0.0); put(2, 0, -sh, 0.0); put(3, 1, -sh, 0.0); put(3, 2, -sh, 0.0);
     }
 }
 
@@ -368,6 +579,8 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
     char *const ws_smem = reinterpret_cast<char *>(region);
     char *const ws_global = lp.ws_base ? lp.ws_base + (uint64_t) blockIdx.x * lp.ws_stride : nullptr;
     unsigned char *stage = region + lp.ws_smem_bytes;
+    unsigned char *tile = stage + lp.stage_bytes;
+    __shared__ int s_next;
     const uint32_t mbar = smem_addr(mbar_slot);
     if (lp.stage_bytes && threadIdx.x == 0) {
         mbar_init(mbar);
@@ -375,12 +588,22 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
     }
     __syncthreads();
     uint32_t parity = 0;
-    for (int inst = blockIdx.x; inst < lp.n_instances; inst += gridDim.x) {
+    for (int inst = blockIdx.x;;) {
+        // dynamic schedule: instances come in the order the host sorted them
+        // (longest first), each CTA takes the next one when it is free
+        if (lp.next) {
+            if (threadIdx.x == 0) s_next = (int) atomicAdd(lp.next, 1u);
+            __syncthreads();
+            inst = s_next;
+        }
+        if (inst >= lp.n_instances) break;
         const InstanceDesc I = lp.instances[inst];
         char *const ws = I.ws_bytes <= lp.ws_smem_bytes ? ws_smem : ws_global;
         const bool staged = lp.stage_bytes && I.plan_bytes && I.plan_bytes + I.leaf_bytes <= lp.stage_bytes;
         const StepDesc *steps;
-        const int32_t *level_start, *rank0_steps;
+        const int32_t *level_start, *rank0_steps, *level_cta;
+        const uint2 *rotations;
+        char *leaves_rw;
         const uint32_t *level_items;
         const ushort2 *tables;
         const char *leaves;
@@ -397,9 +620,17 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
             parity ^= 1u;
             if (__syncthreads_or(!ok)) {
                 // the copies never completed: this CTA's instances report NaN instead of hanging
-                if (threadIdx.x == 0)
-                    for (int j = inst; j < lp.n_instances; j += gridDim.x)
-                        lp.instances[j].value[0] = lp.instances[j].value[1] = __longlong_as_double(0x7ff8000000000000ll);
+                if (threadIdx.x == 0) {
+                    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+                    I.value[0] = I.value[1] = nan;
+                    if (lp.next) {
+                        for (int j = (int) atomicAdd(lp.next, 1u); j < lp.n_instances; j = (int) atomicAdd(lp.next, 1u))
+                            lp.instances[j].value[0] = lp.instances[j].value[1] = nan;
+                    } else {
+                        for (int j = inst + (int) gridDim.x; j < lp.n_instances; j += gridDim.x)
+                            lp.instances[j].value[0] = lp.instances[j].value[1] = nan;
+                    }
+                }
                 return;
             }
             P = *reinterpret_cast<const PlanDesc *>(stage);
@@ -410,7 +641,9 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
             rank0_steps = reinterpret_cast<const int32_t *>(sbase + (reinterpret_cast<const char *>(P.rank0_steps) - gbase));
             level_items = reinterpret_cast<const uint32_t *>(sbase + (reinterpret_cast<const char *>(P.level_items) - gbase));
             tables = reinterpret_cast<const ushort2 *>(sbase + (reinterpret_cast<const char *>(P.tables) - gbase));
-            leaves = sbase + I.plan_bytes;
+            level_cta = reinterpret_cast<const int32_t *>(sbase + (reinterpret_cast<const char *>(P.level_cta) - gbase));
+            rotations = reinterpret_cast<const uint2 *>(sbase + (reinterpret_cast<const char *>(P.rotations) - gbase));
+            leaves_rw = reinterpret_cast<char *>(stage) + I.plan_bytes;
         } else {
             P = *I.plan;
             steps = P.steps;
@@ -418,7 +651,17 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
             rank0_steps = P.rank0_steps;
             level_items = P.level_items;
             tables = P.tables;
-            leaves = I.leaves;
+            level_cta = P.level_cta;
+            rotations = P.rotations;
+            leaves_rw = const_cast<char *>(I.leaves);   // the instance's own leaf image
+        }
+        leaves = leaves_rw;
+        if constexpr (kMixed) {
+            // the step's angles arrive as numbers; the gate tensors are built here
+            if (I.angles && P.n_rot) {
+                for (int r = threadIdx.x; r < P.n_rot; r += blockDim.x) build_rotation(leaves_rw, rotations[r], I.angles[r]);
+                __syncthreads();
+            }
         }
         if (kMixed) {
             for (int s = threadIdx.x; s < P.n_steps; s += blockDim.x) {
@@ -428,7 +671,9 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
             __syncthreads();
         }
         for (int L = 0; L < P.n_levels; L++) {
-            plan_level<kMixed>(steps, level_start[L], level_start[L + 1], level_items[L], leaves, ws, h, tables);
+            const int sc = level_cta[L], s1 = level_start[L + 1];
+            plan_level<kMixed>(steps, level_start[L], sc, level_items[L], leaves, ws, h, tables);
+            for (int s = sc; s < s1; s++) run_tiled<kMixed>(steps[s], s, leaves, ws, h, tile);
             __syncthreads();
         }
         // final-value rule of src/Network.h:961-965, applied in contraction order
@@ -457,7 +702,8 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
             I.value[0] = fre;
             I.value[1] = fim;
         }
-        __syncthreads();
+        __syncthreads();   // the next instance reuses the header, the workspace and s_next
+        if (!lp.next) inst += gridDim.x;
     }
 }
 
@@ -502,7 +748,7 @@ int plan_max_grid(size_t smem_bytes) {
 }
 
 size_t plan_smem_bytes(const PlanLaunch &lp) {
-    return kPlanHeaderBytes + 128 + lp.ws_smem_bytes + lp.stage_bytes;
+    return kPlanHeaderBytes + 128 + lp.ws_smem_bytes + lp.stage_bytes + lp.tile_bytes;
 }
 
 cudaError_t launch_plan(const PlanLaunch &lp, bool mixed, int grid, cudaStream_t stream) {

@@ -63,6 +63,22 @@ private:
     uint64_t top_ = 0;
 };
 
+// A step runs CTA-wide as a tiled product when C's digits are A's free wires
+// followed by B's (the ContractNodes order), both sides give at least 16 rows
+// and the output has at least 4 elements per thread.
+static bool cta_tiled(const qtorch::StepRecord &r) {
+    int fa = 0, fb = 0;
+    for (size_t i = 0; i < r.freeIdx.size(); i++) {
+        if (r.freeIdx[i].first) {
+            if (fb) return false;   // an A wire after a B wire
+            fa++;
+        } else {
+            fb++;
+        }
+    }
+    return fa >= 2 && fb >= 2 && fa + fb >= 5 && !r.sumIdx.empty();
+}
+
 qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
     const auto &leaves = net.Leaves();
     const auto &rec = net.Steps();
@@ -82,8 +98,15 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
         n_levels = std::max(n_levels, level[s]);
     }
     std::vector<int> order(S);
-    for (int s = 0; s < S; s++) order[s] = s;
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return level[x] < level[y]; });
+    std::vector<bool> tiled(S);
+    for (int s = 0; s < S; s++) {
+        order[s] = s;
+        tiled[s] = cta_tiled(rec[s]);
+    }
+    // by level; inside a level the CTA-tiled steps come last
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return level[x] != level[y] ? level[x] < level[y] : (!tiled[x] && tiled[y]);
+    });
     std::vector<int> sorted_of(S);
     for (int i = 0; i < S; i++) sorted_of[order[i]] = i;
     // consumer level of every intermediate tensor
@@ -93,9 +116,16 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
         consumer_level[rec[s].b] = level[s];
     }
     p->level_start.assign(n_levels + 1, 0);
+    p->level_cta.assign(n_levels, 0);
+    p->n_tiled = 0;
     for (int i = 0, L0 = 1; L0 <= n_levels; L0++) {
         p->level_start[L0 - 1] = i;
-        while (i < S && level[order[i]] == L0) i++;
+        while (i < S && level[order[i]] == L0 && !tiled[order[i]]) i++;
+        p->level_cta[L0 - 1] = i;
+        while (i < S && level[order[i]] == L0) {
+            i++;
+            p->n_tiled++;
+        }
         p->level_start[L0] = i;
     }
     p->rank0_steps.clear();
@@ -125,6 +155,12 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
         }
         p->leaf_bytes[prec] = loff;
         p->leaf_off[prec] = leaf_off;
+        p->rot_table[prec].clear();
+        for (size_t r = 0; r < p->rot_kind.size(); r++) {
+            const std::string &k = p->rot_kind[r];
+            const uint32_t kind = k == "Rx" ? kRotRx : k == "Ry" ? kRotRy : k == "CPHASE" ? kRotCPhase : kRotRz;
+            p->rot_table[prec].push_back(make_uint2((uint32_t) leaf_off[p->rot_leaf[r]], kind));
+        }
         // workspace layout, level by level
         OffsetAllocator alloc;
         std::map<int64_t, std::pair<uint64_t, uint64_t>> live;   // tensor id -> (offset, bytes)
@@ -145,8 +181,9 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
             for (int i = p->level_start[L0 - 1]; i < p->level_start[L0]; i++) {
                 const int s = order[i];
                 const int nf = (int) rec[s].freeIdx.size();
-                // mixed plans keep the expectation-value reductions (outputs of rank <= 1) in FP64
-                const bool f64 = !mixed || nf <= kMixedTailRank;
+                // mixed plans keep the expectation-value reductions in twice-FP32 accuracy
+                const int ns = (int) rec[s].sumIdx.size();
+                const bool f64 = !mixed || nf == 0 || (nf <= kMixedTailRank && ns >= kMixedTailMinSum);
                 const uint64_t bytes = (uint64_t) (f64 ? 16 : 8) << (2 * nf);
                 c_off[s] = alloc.alloc(bytes);
                 c_bytes[s] = bytes;
@@ -205,13 +242,18 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
             if (c_f64[s]) d.flags |= kCF64;
             if (r.freeIdx.empty()) d.flags |= kOutRank0;
             if (r.rankA == 0 && r.rankB == 0) d.flags |= kBothRank0;
+            if (tiled[s]) d.flags |= kCtaTiled;
         }
         // interpreter schedule: work items of each level, lane groups for tiny outputs
         // (mixed form only; FP64 keeps one accumulator per output element)
         p->level_items[prec].assign(n_levels, 0);
         for (int L0 = 0; L0 < n_levels; L0++) {
             uint32_t acc = 0;
-            for (int i = p->level_start[L0]; i < p->level_start[L0 + 1]; i++) {
+            for (int i = p->level_cta[L0]; i < p->level_start[L0 + 1]; i++) {
+                steps[i].group = 1;
+                steps[i].item_start = 0xffffffffu;   // never found by the item search
+            }
+            for (int i = p->level_start[L0]; i < p->level_cta[L0]; i++) {
                 StepDesc &d = steps[i];
                 const uint64_t n_out = 1ull << (2 * d.nFree), K = 1ull << (2 * d.nSum);
                 uint32_t g = 1;
@@ -274,12 +316,16 @@ qt_status upload_plan(qt_plan *p, int prec) {
     const size_t lvl_bytes = sizeof(int32_t) * p->level_start.size();
     const size_t r0_bytes = sizeof(int32_t) * (p->rank0_steps.size() + 1);
     const size_t items_bytes = sizeof(uint32_t) * (p->level_items[prec].size() + 1);
+    const size_t cta_bytes = sizeof(int32_t) * (p->level_cta.size() + 1);
     const size_t off_steps = align_up(sizeof(PlanDesc), 256);
     const size_t off_lvl = align_up(off_steps + steps_bytes, 256);
     const size_t off_r0 = align_up(off_lvl + lvl_bytes, 256);
     const size_t off_items = align_up(off_r0 + r0_bytes, 256);
     const size_t tab_bytes = sizeof(ushort2) * p->tables.size();
-    const size_t off_tab = align_up(off_items + items_bytes, 256);
+    const size_t off_cta = align_up(off_items + items_bytes, 16);
+    const size_t rot_bytes = sizeof(uint2) * p->rot_table[prec].size();
+    const size_t off_rot = align_up(off_cta + cta_bytes, 16);
+    const size_t off_tab = align_up(off_rot + rot_bytes, 256);
     const size_t total = off_tab + tab_bytes + 16;
     void *d = nullptr;
     qt_status s = dev_alloc(ctx, total, &d);
@@ -292,11 +338,16 @@ qt_status upload_plan(qt_plan *p, int prec) {
     pd.rank0_steps = reinterpret_cast<const int32_t *>((char *) d + off_r0);
     pd.level_items = reinterpret_cast<const uint32_t *>((char *) d + off_items);
     pd.tables = reinterpret_cast<const ushort2 *>((char *) d + off_tab);
+    pd.level_cta = reinterpret_cast<const int32_t *>((char *) d + off_cta);
+    pd.rotations = reinterpret_cast<const uint2 *>((char *) d + off_rot);
+    if (rot_bytes) std::memcpy(host.data() + off_rot, p->rot_table[prec].data(), rot_bytes);
+    if (!p->level_cta.empty())
+        std::memcpy(host.data() + off_cta, p->level_cta.data(), cta_bytes - sizeof(int32_t));
     if (tab_bytes) std::memcpy(host.data() + off_tab, p->tables.data(), tab_bytes);
     pd.n_steps = p->n_steps;
     pd.n_levels = p->n_levels;
     pd.n_rank0 = (int32_t) p->rank0_steps.size();
-    pd.pad = 0;
+    pd.n_rot = (int32_t) p->rot_table[prec].size();
     std::memcpy(host.data(), &pd, sizeof(pd));
     if (steps_bytes) std::memcpy(host.data() + off_steps, p->steps[prec].data(), steps_bytes);
     if (lvl_bytes) std::memcpy(host.data() + off_lvl, p->level_start.data(), lvl_bytes);

@@ -9,8 +9,12 @@
 
 namespace qtg {
 
-// mixed plans compute outputs of rank <= this in FP64 (the expectation-value reductions)
+// Mixed plans accumulate the reductions where cancellation lives with
+// compensated (twice-FP32) dot products and store them as complex128: every
+// rank-0 output, and outputs of rank <= kMixedTailRank summed over at least
+// 4^kMixedTailMinSum terms.  Everything else is complex64 with FP32 FMA.
 constexpr int kMixedTailRank = 1;
+constexpr int kMixedTailMinSum = 3;
 // limits of the grouped interpreter (one CTA per instance)
 constexpr int kGroupedMaxRank = 11;
 constexpr int kGroupedMaxSum = 8;
@@ -21,6 +25,8 @@ constexpr uint64_t kGroupedMaxWorkspace = 96ull << 20;
 // (the register budget allows two), larger instances run from global memory.
 constexpr uint64_t kSmemWorkspaceMax = 32ull << 10;
 constexpr uint64_t kSmemStageMax = 64ull << 10;
+// staging cap when the CTA also holds the tile buffers of CTA-tiled steps
+constexpr uint64_t kSmemStageMaxTiled = 52ull << 10;
 inline uint64_t round16(uint64_t x) { return (x + 15) / 16 * 16; }
 // offset tables are built when they take at most this many bytes
 constexpr uint64_t kMaxTableBytes = 64ull << 10;
@@ -37,9 +43,13 @@ struct qt_plan {
     std::vector<std::string> rot_kind;
     std::vector<double> rot_angle;
     std::vector<uint64_t> rot_elem;
+    std::vector<int> rot_leaf;                        // leaf index of each rotation
+    std::vector<uint2> rot_table[2];                  // per precision: (leaf byte offset, RotationKind)
     std::vector<qtg::StepDesc> steps[2];              // per precision, sorted by level
     std::vector<int> a_leaf, b_leaf;                  // leaf index of each operand or -1
     std::vector<int32_t> level_start;
+    std::vector<int32_t> level_cta;                   // first CTA-tiled step of each level
+    int n_tiled = 0;                                  // CTA-tiled steps
     std::vector<int32_t> rank0_steps;
     std::vector<uint32_t> level_items[2];             // interpreter work items per level, per precision
     std::vector<ushort2> tables;                      // interpreter offset tables (empty: none)
@@ -67,8 +77,9 @@ struct qt_batch {
     void *d_inst = nullptr;
     void *d_values = nullptr;
     void *d_ws = nullptr;
-    void *d_exps = nullptr;
-    uint64_t ws_stride = 0, exps_stride = 0;
+    void *d_next = nullptr;                           // dynamic-schedule counter (null: round robin)
+    uint32_t tile_bytes = 0;
+    uint64_t ws_stride = 0;
     bool ws_in_smem = false;                          // every instance's workspace fits shared memory
     uint32_t ws_smem_bytes = 0;                       // shared-memory workspace region per CTA
     uint32_t stage_bytes = 0;                         // shared memory for staged plan block + leaves
@@ -80,6 +91,15 @@ struct qt_batch {
     cudaGraphExec_t graph = nullptr;
     bool all_grouped = true;
     std::vector<int> stepwise;                        // instances run step by step
+    // rotation angles applied on the device (mixed precision): pinned + device copies
+    bool dev_rot = false;
+    int64_t n_angles = 0;
+    double *h_angles = nullptr;
+    void *d_angles = nullptr;
+    std::vector<int64_t> inst_angle_off;              // first angle of each instance
+    std::vector<qtg::InstanceDesc> inst_desc;         // host copy of the descriptors
+    std::vector<int> inst_index;                      // batch index of each descriptor
+    cudaEvent_t angles_done = nullptr;                // the last angle upload has left h_angles
 };
 
 namespace qtg {

@@ -64,7 +64,8 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
                          "plan exceeds the grouped interpreter's limits; qt_plan_execute_static takes grouped plans only");
     std::lock_guard<std::recursive_mutex> g(ctx->lock);
     // layout inside the static array: plan descriptor, steps, level starts,
-    // rank-0 list, level work items, instance descriptor, workspace
+    // rank-0 list, level work items, first tiled step per level, offset tables,
+    // instance descriptor, workspace
     const uint64_t steps_bytes = sizeof(StepDesc) * p->steps[prec].size();
     const uint64_t lvl_bytes = sizeof(int32_t) * p->level_start.size();
     const uint64_t r0_bytes = sizeof(int32_t) * p->rank0_steps.size();
@@ -73,8 +74,10 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     const uint64_t off_lvl = align256(off_steps + steps_bytes);
     const uint64_t off_r0 = align256(off_lvl + lvl_bytes);
     const uint64_t off_items = align256(off_r0 + r0_bytes);
+    const uint64_t cta_bytes = sizeof(int32_t) * p->level_cta.size();
+    const uint64_t off_cta = align256(off_items + items_bytes);
     const uint64_t tab_bytes = sizeof(ushort2) * p->tables.size();
-    const uint64_t off_tab = align256(off_items + items_bytes);
+    const uint64_t off_tab = align256(off_cta + cta_bytes);
     const uint64_t off_inst = align256(off_tab + tab_bytes);
     const uint64_t off_ws = align256(off_inst + sizeof(InstanceDesc));
     const uint64_t total = off_ws + align256(p->ws_bytes[prec]);
@@ -93,10 +96,11 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     pd.rank0_steps = reinterpret_cast<const int32_t *>(b + off_r0);
     pd.level_items = reinterpret_cast<const uint32_t *>(b + off_items);
     pd.tables = reinterpret_cast<const ushort2 *>(b + off_tab);
+    pd.level_cta = reinterpret_cast<const int32_t *>(b + off_cta);
     pd.n_steps = p->n_steps;
     pd.n_levels = p->n_levels;
     pd.n_rank0 = (int32_t) p->rank0_steps.size();
-    InstanceDesc inst;
+    InstanceDesc inst{};
     inst.plan = reinterpret_cast<const PlanDesc *>(b);
     inst.leaves = static_cast<const char *>(d_leaves);
     inst.value = d_value;
@@ -104,6 +108,7 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     inst.leaf_bytes = 0;
     inst.ws_bytes = (uint32_t) align256(p->ws_bytes[prec]);
     inst.pad = 0;
+    inst.angles = nullptr;   // the caller's leaves are used as they are
     // the descriptors of the previous call are overwritten; the workspace needs
     // no clearing (every intermediate is written before it is read)
     cudaError_t e = cudaMemcpyAsync(b, &pd, sizeof pd, cudaMemcpyHostToDevice, ctx->stream);
@@ -115,6 +120,8 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
         e = cudaMemcpyAsync(b + off_r0, p->rank0_steps.data(), r0_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && items_bytes)
         e = cudaMemcpyAsync(b + off_items, p->level_items[prec].data(), items_bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && cta_bytes)
+        e = cudaMemcpyAsync(b + off_cta, p->level_cta.data(), cta_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && tab_bytes)
         e = cudaMemcpyAsync(b + off_tab, p->tables.data(), tab_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess)
@@ -122,14 +129,15 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     // the stack copies above must not go out of scope before the transfers are done
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_error(ctx, e, "static scratch upload");
-    PlanLaunch lp;
+    PlanLaunch lp{};
     lp.instances = reinterpret_cast<const InstanceDesc *>(b + off_inst);
     lp.n_instances = 1;
     lp.ws_smem_bytes = 0;   // the workspace is the static array's tail
     lp.ws_base = b + off_ws;
     lp.ws_stride = align256(p->ws_bytes[prec]);
     lp.stage_bytes = 0;
-    lp.pad = 0;
+    lp.tile_bytes = p->n_tiled ? kCtaTileBytes : 0;
+    lp.next = nullptr;
     e = launch_plan(lp, prec == QT_PREC_MIXED, 1, ctx->stream);
     ctx->launches++;
     return cuda_error(ctx, e, "plan kernel launch");

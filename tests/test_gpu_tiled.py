@@ -1,0 +1,64 @@
+"""CTA-tiled steps and the dynamic instance schedule of the grouped interpreter.
+
+p=2 QAOA light cones on 3-regular graphs have rank 5-9 intermediates whose
+steps run CTA-wide as tiled products.  The FP64 form keeps the reference's
+per-element summation order there too, so it stays bit-exact against the
+oracle; the mixed form stays within the stated 1e-6."""
+import numpy as np
+import pytest
+
+import qtorch_gb300 as qg
+from oracle import port
+
+pytestmark = pytest.mark.gpu
+
+MIXED_TOL = 1e-6
+TILED = 1 << 7
+
+
+def tiled_terms(dgf, p, point, want, max_peak=8):
+    out = []
+    for e in range(qg.qaoa_num_edges(dgf)):
+        q, m = qg.qaoa_term_text(dgf, p, point, e)
+        pl = qg.Plan(q, m, ordering="linegraph", symbolic=True)
+        if pl.peak_rank <= max_peak and (pl.step_info(qg.FP64)[:, 6] & TILED).any():
+            out.append((q, m))
+        if len(out) == want:
+            break
+    return out
+
+
+def test_tiled_steps_fp64_bit_exact_and_mixed_within_tolerance(ctx):
+    dgf = qg.random_regular_graph(26, 3, seed=105)
+    terms = tiled_terms(dgf, 2, [0.3, 0.9, 0.7, 0.2], 3)
+    assert terms, "no term with a CTA-tiled step"
+    for q, m in terms:
+        plan = qg.Plan(q, m, ordering="linegraph", ctx=ctx)
+        v_or, _ = port.replay_value(q, m, plan.sequence())
+        assert plan.execute(qg.FP64) == v_or
+        assert abs(plan.execute(qg.MIXED) - v_or) <= MIXED_TOL
+
+
+def test_dynamic_schedule_keeps_instance_order(ctx):
+    """More instances than CTAs: instances run longest first under the dynamic
+    schedule, and every value still lands in its own slot."""
+    dgf1 = qg.random_regular_graph(26, 3, seed=105)
+    dgf2 = qg.random_regular_graph(20, 3, seed=7)
+    plans = [qg.Plan(q, m, ordering="linegraph", ctx=ctx) for q, m in tiled_terms(dgf1, 2, [0.3, 0.9, 0.7, 0.2], 2)]
+    for e in range(qg.qaoa_num_edges(dgf2)):
+        q, m = qg.qaoa_term_text(dgf2, 1, [0.5, 1.3], e)
+        plans.append(qg.Plan(q, m, ordering="linegraph", ctx=ctx))
+    single = {id(p): p.execute(qg.FP64) for p in plans}
+    rng = np.random.default_rng(3)
+    order = [plans[i] for i in rng.integers(0, len(plans), 1500)]
+    b = qg.Batch(ctx)
+    for p in order:
+        b.add(p)
+    for prec in (qg.FP64, qg.MIXED):
+        got = b.execute(prec)
+        want = np.array([single[id(p)] for p in order])
+        if prec == qg.FP64:
+            assert np.array_equal(got, want)
+        else:
+            assert np.abs(got - want).max() <= MIXED_TOL
+

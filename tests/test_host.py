@@ -206,3 +206,30 @@ def test_reduce_circuit_matches_reference(case):
     assert n.is_done
     v, _ = port.replay_value(case["qasm"], case["measure"], case["sequence"])
     assert v == complex(*case["value"])
+
+
+def test_interpreter_schedule_invariants():
+    """Steps run level by level; inside a level the CTA-tiled products come
+    last, and only steps that are products of two wide gathered matrices
+    (>= 16 rows each side, >= 1024 outputs) are tiled."""
+    dgf = qg.random_regular_graph(26, 3, seed=105)
+    seen_tiled = 0
+    for e in range(0, qg.qaoa_num_edges(dgf), 5):
+        q, m = qg.qaoa_term_text(dgf, 2, [0.3, 0.9, 0.7, 0.2], e)
+        plan = qg.Plan(q, m, ordering="linegraph", symbolic=True)
+        for prec in (qg.FP64, qg.MIXED):
+            si = plan.step_info(prec)
+            assert len(si) == plan.num_steps
+            assert np.all(np.diff(si[:, 0]) >= 0)
+            for level in np.unique(si[:, 0]):
+                tiled = (si[si[:, 0] == level, 6] & 128) != 0
+                # a suffix of the level
+                assert not np.any(tiled[:-1] & ~tiled[1:])
+            for ra, rb, rc, ns, g, flags in si[:, 1:7]:
+                if flags & 128:
+                    fa, fb = ra - ns, rb - ns
+                    assert fa >= 2 and fb >= 2 and fa + fb >= 5 and ns >= 1 and g == 1
+                    seen_tiled += 1
+                elif prec == qg.FP64:
+                    assert g == 1   # the FP64 form keeps one accumulator per output
+    assert seen_tiled > 0
