@@ -15,6 +15,7 @@
 //    reductions with compensated FP32 dot products (no FP64 arithmetic).
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <mutex>
 #include <type_traits>
 
 #include "engine.cuh"
@@ -738,9 +739,40 @@ cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C
     return cudaGetLastError();
 }
 
+// The dynamic shared-memory limit of a kernel is process-wide state.  It is
+// raised once per device to the opt-in maximum and never lowered, so launches
+// made from several threads at once (the server's lanes) never see another
+// thread's smaller setting.
+static std::mutex g_attr_mutex;
+static bool g_attr_done[64];
+
+template <bool kMixed>
+static cudaError_t raise_smem_limit(int dev) {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, plan_kernel<kMixed>);
+    int optin = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(plan_kernel<kMixed>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 optin - (int) fa.sharedSizeBytes);
+    return e;
+}
+
+static cudaError_t plan_attributes() {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> g(g_attr_mutex);
+    if (dev >= 0 && dev < 64 && g_attr_done[dev]) return cudaSuccess;
+    e = raise_smem_limit<true>(dev);
+    if (e == cudaSuccess) e = raise_smem_limit<false>(dev);
+    if (e == cudaSuccess && dev >= 0 && dev < 64) g_attr_done[dev] = true;
+    return e;
+}
+
 int plan_max_grid(size_t smem_bytes) {
     int per_sm = 0;
-    cudaFuncSetAttribute(plan_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_bytes);
+    plan_attributes();
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, plan_kernel<true>, kPlanThreads, smem_bytes);
     cudaGetLastError();
     if (per_sm < 1) per_sm = 1;
@@ -754,8 +786,7 @@ size_t plan_smem_bytes(const PlanLaunch &lp) {
 cudaError_t launch_plan(const PlanLaunch &lp, bool mixed, int grid, cudaStream_t stream) {
     if (lp.n_instances <= 0) return cudaSuccess;
     const size_t smem = plan_smem_bytes(lp);
-    cudaError_t e = mixed ? cudaFuncSetAttribute(plan_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)
-                          : cudaFuncSetAttribute(plan_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    cudaError_t e = plan_attributes();
     if (e != cudaSuccess) return e;
     if (grid <= 0 || grid > lp.n_instances) grid = lp.n_instances;
     if (mixed) plan_kernel<true><<<grid, kPlanThreads, smem, stream>>>(lp);
