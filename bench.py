@@ -274,6 +274,18 @@ def run_batched(ctx, args, stream, flush):
             "launches_per_step": res[qg.MIXED][3]}
 
 
+def run_only_batched(args):
+    import torch
+
+    import qtorch_gb300 as qg
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = qg.Context(0, stream=stream.cuda_stream)
+    flush_buf = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    print(json.dumps(run_batched(ctx, args, stream, lambda: flush_buf.fill_(1))), flush=True)
+    ctx.close()
+
+
 def run_engine(args):
     import torch
 
@@ -469,6 +481,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-point x 16-graph batched workload")
     ap.add_argument("--batched-points", type=int, default=64)
     ap.add_argument("--batched-steps", type=int, default=5)
+    ap.add_argument("--only-batched", action="store_true",
+                    help="run only the batched workload and print its numbers (a small case for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -478,6 +492,8 @@ def main():
     port.build()
     if args.impl == "reference":
         run_reference(args)
+    elif args.only_batched:
+        run_only_batched(args)
     else:
         run_engine(args)
 

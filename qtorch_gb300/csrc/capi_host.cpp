@@ -12,6 +12,13 @@
 using namespace qtg;
 
 struct qt_network {
+    explicit qt_network(qt_ctx *c) : ctx(c) { ctx_retain(ctx); }
+    ~qt_network() {
+        net.reset();   // the nodes give their device tensors back first
+        ctx_release(ctx);
+    }
+    qt_network(const qt_network &) = delete;
+    qt_network &operator=(const qt_network &) = delete;
     qt_ctx *ctx = nullptr;
     std::string qasm, measure, gate_dir;
     std::shared_ptr<qtorch::Network> net;
@@ -64,8 +71,7 @@ qt_status qt_network_create(qt_ctx *ctx, const char *qasm_text, const char *meas
     if (!qasm_text || !out) return QT_ERR_INVALID_ARGUMENT;
     *out = nullptr;
     return guard(ctx, [&]() {
-        auto *n = new qt_network();
-        n->ctx = ctx;
+        auto *n = new qt_network(ctx);
         n->qasm = qasm_text;
         n->measure = measure_text ? measure_text : "";
         n->gate_dir = gate_dir ? gate_dir : "";
@@ -238,8 +244,7 @@ qt_status qt_plan_build(qt_ctx *ctx, const char *qasm_text, const char *measure_
     if (!qasm_text || !out) return QT_ERR_INVALID_ARGUMENT;
     *out = nullptr;
     return guard(ctx, [&]() {
-        auto *p = new qt_plan();
-        p->ctx = ctx;
+        auto *p = new qt_plan(ctx);
         p->qasm = qasm_text;
         p->measure = measure_text ? measure_text : "";
         p->gate_dir = gate_dir ? gate_dir : "";
@@ -411,18 +416,19 @@ static void batch_release(qt_batch *b) {
 
 qt_status qt_batch_create(qt_ctx *ctx, qt_batch **out) {
     if (!ctx || !out) return QT_ERR_INVALID_ARGUMENT;
-    *out = new (std::nothrow) qt_batch();
+    *out = new (std::nothrow) qt_batch(ctx);
     if (!*out) return QT_ERR_OUT_OF_MEMORY;
-    (*out)->ctx = ctx;
     return QT_OK;
 }
 
 qt_status qt_batch_free(qt_batch *b) {
     if (!b) return QT_ERR_INVALID_ARGUMENT;
-    std::lock_guard<std::recursive_mutex> g(b->ctx->lock);
-    cudaStreamSynchronize(b->ctx->stream);
-    batch_release(b);
-    delete b;
+    {
+        std::lock_guard<std::recursive_mutex> g(b->ctx->lock);
+        cudaStreamSynchronize(b->ctx->stream);
+        batch_release(b);
+    }
+    delete b;   // may drop the context's last reference
     return QT_OK;
 }
 

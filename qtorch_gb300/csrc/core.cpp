@@ -33,6 +33,22 @@ static size_t size_class(size_t bytes) {
     return c;
 }
 
+void ctx_retain(qt_ctx *ctx) {
+    if (ctx) ctx->refs.fetch_add(1);
+}
+
+void ctx_release(qt_ctx *ctx) {
+    if (!ctx || ctx->refs.fetch_sub(1) != 1) return;
+    cudaSetDevice(ctx->device);
+    // a caller's stream may be gone by now; cudaFree waits for the device anyway
+    if (ctx->own_stream) cudaStreamSynchronize(ctx->stream);
+    for (auto &kv : ctx->free_blocks)
+        for (void *p : kv.second) cudaFree(p);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
 qt_status dev_alloc(qt_ctx *ctx, size_t bytes, void **out) {
     std::lock_guard<std::recursive_mutex> g(ctx->lock);
     const size_t cls = size_class(bytes ? bytes : 1);
@@ -229,13 +245,12 @@ qt_status qt_ctx_create(int device, void *stream, qt_ctx **out) {
 
 qt_status qt_ctx_destroy(qt_ctx *ctx) {
     if (!ctx) return QT_ERR_INVALID_ARGUMENT;
-    cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
-    for (auto &kv : ctx->free_blocks)
-        for (void *p : kv.second) cudaFree(p);
-    if (ctx->pinned) cudaFreeHost(ctx->pinned);
-    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
-    delete ctx;
+    {
+        std::lock_guard<std::recursive_mutex> g(ctx->lock);
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    ctx_release(ctx);
     return QT_OK;
 }
 

@@ -14,6 +14,10 @@
 #include "engine.cuh"
 
 struct qt_ctx {
+    // references: the owner's (dropped by qt_ctx_destroy) plus one per plan,
+    // batch, network and server made on it; the context is torn down when the
+    // last one goes, so objects freed after qt_ctx_destroy stay valid
+    std::atomic<int> refs{1};
     int device = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -43,6 +47,8 @@ struct qt_tensor {
 
 namespace qtg {
 
+void ctx_retain(qt_ctx *ctx);
+void ctx_release(qt_ctx *ctx);
 qt_status set_error(qt_ctx *ctx, qt_status s, const std::string &msg);
 qt_status cuda_error(qt_ctx *ctx, cudaError_t e, const char *what);
 // allocate from the context cache (bytes rounded up to a size class)

@@ -34,6 +34,10 @@ constexpr uint64_t kMaxTableBytes = 64ull << 10;
 }  // namespace qtg
 
 struct qt_plan {
+    explicit qt_plan(qt_ctx *c) : ctx(c) { qtg::ctx_retain(ctx); }
+    ~qt_plan() { qtg::ctx_release(ctx); }
+    qt_plan(const qt_plan &) = delete;
+    qt_plan &operator=(const qt_plan &) = delete;
     qt_ctx *ctx = nullptr;
     std::string qasm, measure, gate_dir;
     std::vector<int> leaf_rank;
@@ -65,6 +69,10 @@ struct qt_plan {
 };
 
 struct qt_batch {
+    explicit qt_batch(qt_ctx *c) : ctx(c) { qtg::ctx_retain(ctx); }
+    ~qt_batch() { qtg::ctx_release(ctx); }
+    qt_batch(const qt_batch &) = delete;
+    qt_batch &operator=(const qt_batch &) = delete;
     qt_ctx *ctx = nullptr;
     std::vector<qt_plan *> plans;                     // per instance
     std::vector<std::vector<std::complex<double>>> leaves;   // per instance, complex128

@@ -157,6 +157,7 @@ qt_status qt_server_create(qt_ctx *ctx, int max_inflight, qt_precision prec, qt_
     if (!ctx || !out || max_inflight < 1 || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return QT_ERR_INVALID_ARGUMENT;
     auto *s = new qt_server();
     s->ctx = ctx;
+    ctx_retain(ctx);
     s->max_inflight = max_inflight;
     s->prec = prec;
     const int n_lanes = 2;
@@ -165,6 +166,7 @@ qt_status qt_server_create(qt_ctx *ctx, int max_inflight, qt_precision prec, qt_
         qt_status st = qt_ctx_create(ctx->device, nullptr, &s->lanes[i].ctx);
         if (st != QT_OK) {
             for (int j = 0; j < i; j++) qt_ctx_destroy(s->lanes[j].ctx);
+            ctx_release(ctx);
             delete s;
             return st;
         }
@@ -186,6 +188,7 @@ qt_status qt_server_free(qt_server *s) {
     s->dispatcher.join();
     for (auto &l : s->lanes) l.th.join();
     for (auto &l : s->lanes) qt_ctx_destroy(l.ctx);
+    ctx_release(s->ctx);
     delete s;
     return QT_OK;
 }
