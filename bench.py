@@ -9,11 +9,17 @@ at one (gamma, beta) point.
   value      mixed-precision terms/s with the inputs resident in HBM (one grouped
              launch per step, per-step CUDA events on the launching stream, L2
              flushed between steps)
-  e2e        the same through the public API with host buffers: every step sets
-             the rotation angles of a new (gamma, beta) point on the host, uploads
-             the leaf tensors from pinned memory, runs, and reads the 60 values back
+  e2e        the same through the public API with host buffers: every step hands
+             the rotation angles of a new (gamma, beta) point to the batch (one
+             pinned H2D copy of the angles; the gate tensors are built on the
+             device), runs, and reads the 60 values back
   fp64       the plain complex128 path (bit-exact with the reference) for the
              mixed/FP64 ratio; error = |mixed - fp64| per term
+  batched    64 (gamma, beta) points x every edge term of 16 random 3-regular
+             graphs (20-40 vertices, p = 1 and 2) in one grouped launch per step,
+             mixed vs FP64
+  serving    Poisson arrivals of QAOA / random-circuit / QFT requests through the
+             continuous-batching server under a 150 GB budget: p50/p99 latency
   cpu_baseline / --impl reference: the CPU oracle port (a C restatement of the
              reference's ContractIndices loop, QASM parse included per term, as
              the reference pays it) on the host cores
@@ -274,6 +280,124 @@ def run_batched(ctx, args, stream, flush):
             "launches_per_step": res[qg.MIXED][3]}
 
 
+def qft_text(n, seed):
+    """QFT on n qubits from a random computational-basis input (X on a seeded
+    subset), laid out like the reference's Samples/qft*.qasm: H and a ladder of
+    CRk per qubit, then the qubit-reversal swaps (three CNOTs each)."""
+    rng = np.random.default_rng(seed)
+    lines = [str(n)]
+    for q in range(n):
+        if rng.integers(2):
+            lines.append(f"X {q}")
+    for i in range(n):
+        lines.append(f"H {i}")
+        for j in range(i + 1, n):
+            lines.append(f"CRk {j} {i}")
+    for i in range(n // 2):
+        a, b = i, n - 1 - i
+        lines += [f"CNOT {a} {b}", f"CNOT {b} {a}", f"CNOT {a} {b}"]
+    return "\n".join(lines) + "\n"
+
+
+def random_circuit_text(n, depth, seed):
+    """Layers of seeded Rx/Ry/Rz on every qubit, then CZ on n/4 disjoint random pairs."""
+    rng = np.random.default_rng(seed)
+    lines = [str(n)]
+    for _ in range(depth):
+        for q in range(n):
+            lines.append(f"{rng.choice(['Rx', 'Ry', 'Rz'])} {rng.uniform(0, 2 * math.pi):.4f} {q}")
+        perm = rng.permutation(n)
+        for j in range(0, n // 4 * 2, 2):
+            lines.append(f"CZ {perm[j]} {perm[j + 1]}")
+    return "\n".join(lines) + "\n"
+
+
+SERVE_BUDGET = 150 << 30
+
+
+def run_serving(args):
+    """Config 5: Poisson arrivals of contraction requests against a 150 GB
+    device-memory budget; the mix is QAOA edge terms (p=1 and p=2), random
+    Rx/Ry/Rz + CZ circuits and QFT circuits on a random basis input, with
+    heavy-tailed sizes (smaller circuits more likely, 2^-i)."""
+    import qtorch_gb300 as qg
+    ctx = qg.Context(0)
+    ctx.set_memory_budget(SERVE_BUDGET)
+    pool = []   # (class, plan)
+    dgf = qg.random_regular_graph(NODES, DEGREE, seed=args.graph_seed)
+    for e in range(qg.qaoa_num_edges(dgf)):
+        q, m = qg.qaoa_term_text(dgf, 1, [0.4, 1.1], e)
+        pool.append(("qaoa", qg.Plan(q, m, ordering="linegraph", ctx=ctx)))
+    dgf2 = qg.random_regular_graph(30, 3, seed=5)
+    for e in range(0, qg.qaoa_num_edges(dgf2), 3):
+        q, m = qg.qaoa_term_text(dgf2, 2, [0.3, 0.8, 0.6, 0.2], e)
+        pool.append(("qaoa", qg.Plan(q, m, ordering="linegraph", ctx=ctx)))
+    rand_sizes = [(10, 8), (12, 10), (14, 10), (16, 12)]
+    qft_sizes = [8, 10, 12, 14]
+    rand_plans = [qg.Plan(random_circuit_text(n, d, 7 + i), "Z", ordering="linegraph", ctx=ctx)
+                  for i, (n, d) in enumerate(rand_sizes)]
+    qft_plans = [qg.Plan(qft_text(n, 3 + i), "Z", ordering="linegraph", ctx=ctx) for i, n in enumerate(qft_sizes)]
+    qaoa = [p for _, p in pool]
+    # FP64 value of every distinct request: the error bound of the served values
+    ref = {id(p): p.execute(qg.FP64) for p in qaoa + rand_plans + qft_plans}
+    rng = np.random.default_rng(2024)
+    tail = np.array([2.0 ** -i for i in range(4)])
+    tail /= tail.sum()
+    reqs = []
+    for _ in range(args.serve_requests):
+        u = rng.uniform()
+        if u < 0.80:
+            reqs.append(("qaoa", qaoa[int(rng.integers(len(qaoa)))]))
+        elif u < 0.92:
+            reqs.append(("random", rand_plans[int(rng.choice(4, p=tail))]))
+        else:
+            reqs.append(("qft", qft_plans[int(rng.choice(4, p=tail))]))
+    gaps = rng.exponential(1.0 / args.serve_rate, len(reqs))
+    srv = qg.Server(max_inflight=256, precision=qg.MIXED, ctx=ctx)
+    tickets = []
+    t0 = time.perf_counter()
+    t_next = t0
+    for (cls, plan), gap in zip(reqs, gaps):
+        t_next += gap
+        while True:
+            now = time.perf_counter()
+            if now >= t_next:
+                break
+            time.sleep(min(t_next - now, 0.0005))
+        tickets.append(srv.submit(plan))
+    srv.drain()
+    wall = time.perf_counter() - t0
+    lat = {"qaoa": [], "random": [], "qft": []}
+    err = 0.0
+    for (cls, plan), t in zip(reqs, tickets):
+        v, l = srv.poll(t)
+        lat[cls].append(l)
+        err = max(err, abs(v - ref[id(plan)]))
+    stats = srv.stats()
+    srv.close()
+    all_lat = sorted(x for v in lat.values() for x in v)
+
+    def pct(xs, f):
+        xs = sorted(xs)
+        return 1e3 * xs[min(len(xs) - 1, max(0, int(math.ceil(f * len(xs))) - 1))] if xs else None
+
+    out = {
+        "workload": f"{len(reqs)} requests, Poisson arrivals at {args.serve_rate:g}/s: 80% QAOA edge terms "
+                    f"(30-vertex 4-regular p=1, 30-vertex 3-regular p=2), 12% random Rx/Ry/Rz+CZ circuits "
+                    f"{rand_sizes} (qubits, depth), 8% QFT {qft_sizes} qubits on a random basis input; "
+                    "sizes drawn 2^-i (heavy tail: 5e3 to 6e10 complex MACs per request); <Z_0> measured, "
+                    "line-graph ordering; plans built before the stream (requests carry a plan)",
+        "precision": "mixed", "memory_budget_bytes": SERVE_BUDGET,
+        "p50_ms": pct(all_lat, 0.50), "p99_ms": pct(all_lat, 0.99),
+        "p50_ms_by_class": {k: pct(v, 0.50) for k, v in lat.items()},
+        "p99_ms_by_class": {k: pct(v, 0.99) for k, v in lat.items()},
+        "requests_per_s": len(reqs) / wall, "completed": stats["completed"],
+        "error_vs_fp64_max_abs": err, "error_bound": 1e-6,
+    }
+    ctx.close()
+    return out
+
+
 def run_only_batched(args):
     import torch
 
@@ -412,6 +536,8 @@ def run_engine(args):
     if not args.no_batched:
         bm._release()
         line["batched"] = run_batched(ctx, args, stream, flush)
+    if not args.no_serving:
+        line["serving"] = run_serving(args)
     if rank == 0 and world == 1 and not args.no_cpu:
         seqs = sequences_for(terms)
         jobs = [(q, m, s) for (q, m), s in zip(terms, seqs)]
@@ -481,6 +607,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-point x 16-graph batched workload")
     ap.add_argument("--batched-points", type=int, default=64)
     ap.add_argument("--batched-steps", type=int, default=5)
+    ap.add_argument("--no-serving", action="store_true", help="skip the request-serving workload")
+    ap.add_argument("--serve-requests", type=int, default=3000)
+    ap.add_argument("--serve-rate", type=float, default=2000.0, help="Poisson arrival rate, requests/s")
     ap.add_argument("--only-batched", action="store_true",
                     help="run only the batched workload and print its numbers (a small case for profiling)")
     args = ap.parse_args()

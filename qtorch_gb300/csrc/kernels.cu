@@ -410,56 +410,17 @@ __device__ void tiled_step(const StepDesc &d, int si, const char *leaves, char *
         for (int i = 0; i < MI; i++)
 #pragma unroll
             for (int j = 0; j < NJ; j++) cre[i][j] = cim[i][j] = T(0);
-        // mixed form: the next chunk's gathers are issued into registers before
-        // the current chunk is multiplied, so their latency hides behind it
-        constexpr int PA = kMixed ? (int) ((TM * KC + kPlanThreads - 1) / kPlanThreads) : 1;
-        constexpr int PB = kMixed ? (int) ((TN * KC + kPlanThreads - 1) / kPlanThreads) : 1;
-        V pa[PA], pb[PB];
-        auto fetch = [&](uint32_t k0) {
-#pragma unroll
-            for (int r = 0; r < PA; r++) {
-                const uint32_t e = tid + (uint32_t) r * kPlanThreads;
-                if (e < TM * kc)
-                    pa[r] = A[s_oa[e % TM] + (uint32_t) scatter_digits(k0 + e / TM, d.posAs, (int) nSum)];
-            }
-#pragma unroll
-            for (int r = 0; r < PB; r++) {
-                const uint32_t e = tid + (uint32_t) r * kPlanThreads;
-                if (e < TN * kc)
-                    pb[r] = B[s_ob[e % TN] + (uint32_t) scatter_digits(k0 + e / TN, d.posBs, (int) nSum)];
-            }
-        };
-        if constexpr (kMixed) {
-            __syncthreads();   // offsets visible
-            fetch(0);
-        }
         for (uint32_t k0 = 0; k0 < K; k0 += kc) {
             __syncthreads();   // offsets visible; the previous chunk's slices are consumed
-            if constexpr (kMixed) {
-#pragma unroll
-                for (int r = 0; r < PA; r++) {
-                    const uint32_t e = tid + (uint32_t) r * kPlanThreads;
-                    if (e < TM * kc) As[(e / TM) * kCtaTileDim + e % TM] = pa[r];
-                }
-#pragma unroll
-                for (int r = 0; r < PB; r++) {
-                    const uint32_t e = tid + (uint32_t) r * kPlanThreads;
-                    if (e < TN * kc) Bs[(e / TN) * kCtaTileDim + e % TN] = pb[r];
-                }
-            } else {
-                for (uint32_t e = tid; e < TM * kc; e += blockDim.x) {
-                    const uint32_t m = e % TM, kk = e / TM;
-                    As[kk * kCtaTileDim + m] = A[s_oa[m] + (uint32_t) scatter_digits(k0 + kk, d.posAs, (int) nSum)];
-                }
-                for (uint32_t e = tid; e < TN * kc; e += blockDim.x) {
-                    const uint32_t n = e % TN, kk = e / TN;
-                    Bs[kk * kCtaTileDim + n] = B[s_ob[n] + (uint32_t) scatter_digits(k0 + kk, d.posBs, (int) nSum)];
-                }
+            for (uint32_t e = tid; e < TM * kc; e += blockDim.x) {
+                const uint32_t m = e % TM, kk = e / TM;
+                As[kk * kCtaTileDim + m] = A[s_oa[m] + (uint32_t) scatter_digits(k0 + kk, d.posAs, (int) nSum)];
+            }
+            for (uint32_t e = tid; e < TN * kc; e += blockDim.x) {
+                const uint32_t n = e % TN, kk = e / TN;
+                Bs[kk * kCtaTileDim + n] = B[s_ob[n] + (uint32_t) scatter_digits(k0 + kk, d.posBs, (int) nSum)];
             }
             __syncthreads();
-            if constexpr (kMixed) {
-                if (k0 + kc < K) fetch(k0 + kc);
-            }
             for (uint32_t kk = 0; kk < kc; kk++) {
                 V a[MI];
 #pragma unroll

@@ -253,14 +253,21 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
                 steps[i].group = 1;
                 steps[i].item_start = 0xffffffffu;   // never found by the item search
             }
+            // Mixed form: outputs share their k loop among a lane group (a power of
+            // two, at most a warp).  The level's group size is the largest that
+            // keeps all of its outputs within one round of the CTA's threads, so a
+            // level of many small steps is not spread over extra rounds; a step
+            // with a long sum gets enough lanes for <= 64 terms per lane anyway.
+            // The FP64 form keeps one accumulator per output (the reference's order).
+            uint64_t base = 0;
+            for (int i = p->level_start[L0]; i < p->level_cta[L0]; i++) base += 1ull << (2 * steps[i].nFree);
+            uint64_t gl = 1;
+            while (gl < 32 && base * gl * 2 <= (uint64_t) kPlanThreads) gl *= 2;
             for (int i = p->level_start[L0]; i < p->level_cta[L0]; i++) {
                 StepDesc &d = steps[i];
                 const uint64_t n_out = 1ull << (2 * d.nFree), K = 1ull << (2 * d.nSum);
                 uint32_t g = 1;
-                // mixed form: small outputs share their k loop among up to a warp of lanes
-                // (FP64-accumulated reductions too; the FP64 form keeps the reference's order)
-                if (mixed)
-                    while (g < 32 && g * 2 <= K && n_out * g * 2 <= (uint64_t) kPlanThreads) g *= 2;
+                if (mixed) g = (uint32_t) std::min<uint64_t>({K, 32, std::max<uint64_t>(gl, K / 64)});
                 acc = (acc + g - 1) / g * g;   // a lane group starts on a multiple of its size
                 d.group = (uint8_t) g;
                 d.item_start = acc;

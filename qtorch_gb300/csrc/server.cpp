@@ -2,11 +2,13 @@
 //
 // Requests (a plan plus its leaf values) are admitted in arrival order while
 // their device footprint (plan workspace + leaves, per precision) fits the
-// memory budget and an in-flight slot is free.  Admitted requests are grouped
-// into waves; every wave runs as one batch (one grouped launch, or step by step
-// for plans too large for a CTA) on one of several lanes, each lane with its
-// own CUDA stream, so a wave formed from requests that arrived while another
-// wave is on the GPU runs concurrently with it.  Each request's result is
+// memory budget and an in-flight slot is free.  Light requests (plans the
+// grouped interpreter takes) are grouped into waves that run as one grouped
+// launch; a heavy request (a plan run step by step with the whole-GPU
+// kernels) is a wave of its own.  Waves run on lanes, each lane with its own
+// CUDA stream, so a wave formed from requests that arrived while another wave
+// is on the GPU runs concurrently with it.  Lane 0 takes light waves only, so
+// light requests never queue behind a heavy one.  Each request's result is
 // independent of what it was batched with: an instance only ever touches its
 // own leaves and its CTA's workspace.
 #include <algorithm>
@@ -27,6 +29,7 @@ struct Request {
     std::vector<double> leaves;
     std::chrono::steady_clock::time_point t_submit;
     uint64_t footprint;
+    bool heavy;
 };
 
 struct Result {
@@ -115,30 +118,40 @@ static void dispatcher_main(qt_server *s) {
     std::unique_lock<std::mutex> g(s->m);
     for (;;) {
         s->cv.wait(g, [&] {
-            if (s->stop) return true;
+                if (s->stop) return true;
             if (s->pending.empty()) return false;
-            for (auto &l : s->lanes)
-                if (!l.busy) return true;
+            bool any_light = false;
+            for (auto &r : s->pending) any_light = any_light || !r.heavy;
+            for (size_t i = 0; i < s->lanes.size(); i++)
+                if (!s->lanes[i].busy && (i > 0 || any_light)) return true;
             return false;
         });
         if (s->stop) return;
+        bool any_light = false;
+        for (auto &r : s->pending) any_light = any_light || !r.heavy;
         int li = -1;
         for (int i = 0; i < (int) s->lanes.size(); i++)
-            if (!s->lanes[i].busy) {
+            if (!s->lanes[i].busy && (i > 0 || any_light)) {
                 li = i;
                 break;
             }
         if (li < 0) continue;
-        // admission: arrival order, bounded by slots and the memory budget
+        // admission: arrival order within a class, bounded by slots and the
+        // memory budget; a heavy request at the head of the queue goes alone
         std::vector<Request> wave;
         const uint64_t budget = s->ctx->memory_budget;
-        while (!s->pending.empty() && s->inflight < s->max_inflight) {
-            Request &r = s->pending.front();
-            if (budget && s->inflight_bytes + r.footprint > budget && s->inflight > 0) break;
+        const bool take_heavy = li > 0 && s->pending.front().heavy;
+        for (auto it = s->pending.begin(); it != s->pending.end() && s->inflight < s->max_inflight;) {
+            if (it->heavy != take_heavy) {
+                ++it;
+                continue;
+            }
+            if (budget && s->inflight_bytes + it->footprint > budget && s->inflight > 0) break;
             s->inflight++;
-            s->inflight_bytes += r.footprint;
-            wave.push_back(std::move(r));
-            s->pending.pop_front();
+            s->inflight_bytes += it->footprint;
+            wave.push_back(std::move(*it));
+            it = s->pending.erase(it);
+            if (take_heavy) break;
         }
         if (wave.empty()) {
             // nothing admissible until a running wave returns its memory
@@ -160,7 +173,7 @@ qt_status qt_server_create(qt_ctx *ctx, int max_inflight, qt_precision prec, qt_
     ctx_retain(ctx);
     s->max_inflight = max_inflight;
     s->prec = prec;
-    const int n_lanes = 2;
+    const int n_lanes = 3;   // lane 0: light waves only
     s->lanes.resize(n_lanes);
     for (int i = 0; i < n_lanes; i++) {
         qt_status st = qt_ctx_create(ctx->device, nullptr, &s->lanes[i].ctx);
@@ -200,6 +213,7 @@ qt_status qt_server_submit(qt_server *s, qt_plan *plan, const double *leaves, in
     if (leaves) r.leaves.assign(leaves, leaves + 2 * plan->leaf_values.size());
     r.t_submit = std::chrono::steady_clock::now();
     r.footprint = footprint(plan, s->prec);
+    r.heavy = !plan->grouped;
     {
         std::lock_guard<std::mutex> g(s->m);
         const uint64_t budget = s->ctx->memory_budget;
