@@ -398,6 +398,64 @@ def run_serving(args):
     return out
 
 
+def run_config3(args):
+    """Config 3: MaxCut QAOA p=2 on a seeded 3-regular 50-vertex graph, every
+    light-cone edge term, mixed vs FP64 with the error per term, under the
+    line-graph and the seeded stochastic ordering; plus the GEMM-shaped
+    contractions that do reach the tcgen05 path (a 16-qubit depth-12 random
+    circuit, a 14-qubit QFT), mixed (3xTF32 tensor cores) vs FP64."""
+    import torch
+
+    import qtorch_gb300 as qg
+    ctx = qg.Context(0)
+    dgf = qg.random_regular_graph(50, 3, seed=3)
+    out = {"workload": "MaxCut QAOA p=2, seeded random 3-regular graph, 50 vertices, all 75 light-cone edge terms"}
+    for ordering in ("linegraph", "stochastic"):
+        plans = []
+        for e in range(qg.qaoa_num_edges(dgf)):
+            q, m = qg.qaoa_term_text(dgf, 2, [0.3, 0.8, 0.6, 0.2], e)
+            plans.append(qg.Plan(q, m, ordering=ordering, seed=e + 1, ctx=ctx))
+        res = {}
+        for prec in (qg.MIXED, qg.FP64):
+            b = qg.Batch(ctx)
+            for pl in plans:
+                b.add(pl)
+            vals = b.execute(prec)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(3):
+                b.run()
+            b.fetch()
+            res[prec] = (vals, (time.perf_counter() - t0) / 3)
+            b._release()
+        err = np.abs(res[qg.MIXED][0] - res[qg.FP64][0])
+        out[ordering] = {"peak_rank_max": max(p.peak_rank for p in plans),
+                         "complex_macs": int(sum(p.flops for p in plans)),
+                         "mixed_terms_per_s": len(plans) / res[qg.MIXED][1],
+                         "fp64_terms_per_s": len(plans) / res[qg.FP64][1],
+                         "error_vs_fp64": {"max_abs": float(err.max()), "mean_abs": float(err.mean())}}
+    gemm = []
+    for name, text in (("random 16 qubits depth 12", random_circuit_text(16, 12, 1)), ("QFT 14 qubits", qft_text(14, 5))):
+        pl = qg.Plan(text, "Z", ordering="linegraph", ctx=ctx)
+        t0 = time.perf_counter()
+        v64 = pl.execute(qg.FP64)
+        t64 = time.perf_counter() - t0
+        pl.execute(qg.MIXED)
+        t0 = time.perf_counter()
+        vmx = pl.execute(qg.MIXED)
+        tmx = time.perf_counter() - t0
+        gemm.append({"circuit": name, "peak_rank": pl.peak_rank, "complex_macs": int(pl.flops),
+                     "mixed_s": tmx, "fp64_s": t64, "mixed_over_fp64": t64 / tmx, "error_abs": abs(vmx - v64),
+                     "value_fp64": [v64.real, v64.imag]})
+    out["gemm_shaped"] = gemm
+    ctx.close()
+    return out
+
+
+def run_only_config3(args):
+    print(json.dumps(run_config3(args)), flush=True)
+
+
 def run_only_batched(args):
     import torch
 
@@ -538,6 +596,8 @@ def run_engine(args):
         line["batched"] = run_batched(ctx, args, stream, flush)
     if not args.no_serving:
         line["serving"] = run_serving(args)
+    if not args.no_config3:
+        line["config3"] = run_config3(args)
     if rank == 0 and world == 1 and not args.no_cpu:
         seqs = sequences_for(terms)
         jobs = [(q, m, s) for (q, m), s in zip(terms, seqs)]
@@ -610,6 +670,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the request-serving workload")
     ap.add_argument("--serve-requests", type=int, default=3000)
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="Poisson arrival rate, requests/s")
+    ap.add_argument("--no-config3", action="store_true", help="skip the p=2 50-vertex and GEMM-shaped cases")
+    ap.add_argument("--only-config3", action="store_true", help="run only the config-3 cases (for profiling)")
     ap.add_argument("--only-batched", action="store_true",
                     help="run only the batched workload and print its numbers (a small case for profiling)")
     args = ap.parse_args()
@@ -623,6 +685,8 @@ def main():
         run_reference(args)
     elif args.only_batched:
         run_only_batched(args)
+    elif args.only_config3:
+        run_only_config3(args)
     else:
         run_engine(args)
 
