@@ -26,7 +26,7 @@ constexpr int kPlanHeaderBytes = 8 * kPlanMaxSteps;   // per-step scale bookkeep
 enum StepFlags : uint32_t {
     kALeaf = 1u << 0,        // A is read from the leaf buffer (else workspace)
     kBLeaf = 1u << 1,
-    kAF64 = 1u << 2,         // A stored as complex128 (mixed plans only; FP64 plans are all complex128)
+    kAF64 = 1u << 2,         // A stored as complex128 (FP64 plans; mixed plans read complex64 copies)
     kBF64 = 1u << 3,
     kCF64 = 1u << 4,         // C stored as complex128; mixed plans accumulate it with compensated FP32 (Dot2)
     kOutRank0 = 1u << 5,     // C has rank 0: it takes part in the final-value rule

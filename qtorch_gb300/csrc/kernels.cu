@@ -253,11 +253,11 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
         } else {
             // f64: a reduction where cancellation lives; accumulated with Dot2
             // (fre + ere, fim + eim) and stored as complex128
+            // operands are complex64 (a complex128 producer leaves a complex64 copy)
             const bool f64 = (flags & kCF64) != 0;
-            const bool a64 = (flags & kAF64) != 0, b64 = (flags & kBF64) != 0;
             float fre = 0.f, fim = 0.f, ere = 0.f, eim = 0.f;
             if (valid) {
-                if (!f64 && !a64 && !b64 && tab != kNoTable) {
+                if (!f64 && tab != kNoTable) {
                     // the common case: complex64 operands, tabled offsets
                     const float2 *A = reinterpret_cast<const float2 *>(abase) + oa0;
                     const float2 *B = reinterpret_cast<const float2 *>(bbase) + ob0;
@@ -294,11 +294,8 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
                             ka = (uint32_t) scatter_digits(k, d.posAs, nSum);
                             kb = (uint32_t) scatter_digits(k, d.posBs, nSum);
                         }
-                        float2 a, b;
-                        if (a64) { const double2 t = reinterpret_cast<const double2 *>(abase)[oa0 + ka]; a = make_float2((float) t.x, (float) t.y); }
-                        else a = reinterpret_cast<const float2 *>(abase)[oa0 + ka];
-                        if (b64) { const double2 t = reinterpret_cast<const double2 *>(bbase)[ob0 + kb]; b = make_float2((float) t.x, (float) t.y); }
-                        else b = reinterpret_cast<const float2 *>(bbase)[ob0 + kb];
+                        const float2 a = reinterpret_cast<const float2 *>(abase)[oa0 + ka];
+                        const float2 b = reinterpret_cast<const float2 *>(bbase)[ob0 + kb];
                         if (f64) cmac_dot2(fre, ere, fim, eim, a, b);
                         else cmac_f32(fre, fim, a, b);
                     }
@@ -335,6 +332,8 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
                     const double dre = scale2d((double) fre + (double) ere, -(ma + mb));
                     const double dim = scale2d((double) fim + (double) eim, -(ma + mb));
                     reinterpret_cast<double2 *>(ws + d.c_off)[c] = make_double2(dre, dim);
+                    // the complex64 copy its consumers read
+                    reinterpret_cast<float2 *>(ws + d.c_off + 16ull * n_out)[c] = make_float2((float) dre, (float) dim);
                     mag = (float) fmax(fabs(dre), fabs(dim));
                 } else {
                     fre = scale2f(fre, -(ma + mb));

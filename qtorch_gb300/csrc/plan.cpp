@@ -166,11 +166,14 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
         std::map<int64_t, std::pair<uint64_t, uint64_t>> live;   // tensor id -> (offset, bytes)
         std::vector<uint64_t> c_off(S), c_bytes(S);
         std::vector<bool> c_f64(S);
+        std::vector<uint64_t> shadow(S, 0);   // mixed: offset of the complex64 copy of a complex128 output
+        std::map<int64_t, bool> rank0_out;
+        for (int s = 0; s < S; s++) rank0_out[rec[s].c] = rec[s].freeIdx.empty();
         for (int L0 = 1; L0 <= n_levels; L0++) {
             for (auto it = live.begin(); it != live.end();) {
                 auto cl = consumer_level.find(it->first);
                 // rank-0 outputs stay: the final-value rule reads all of them at the end
-                const bool keep = it->second.second <= 16;
+                const bool keep = rank0_out[it->first];
                 if (!keep && cl != consumer_level.end() && cl->second < L0) {
                     alloc.release(it->second.first, it->second.second);
                     it = live.erase(it);
@@ -184,8 +187,11 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
                 // mixed plans keep the expectation-value reductions in twice-FP32 accuracy
                 const int ns = (int) rec[s].sumIdx.size();
                 const bool f64 = !mixed || nf == 0 || (nf <= kMixedTailRank && ns >= kMixedTailMinSum);
-                const uint64_t bytes = (uint64_t) (f64 ? 16 : 8) << (2 * nf);
+                // a mixed complex128 output carries a complex64 copy for its consumers,
+                // which then never convert on the (narrow) FP64 pipe
+                const uint64_t bytes = (uint64_t) (f64 ? (mixed ? 24 : 16) : 8) << (2 * nf);
                 c_off[s] = alloc.alloc(bytes);
+                if (mixed && f64) shadow[s] = c_off[s] + (16ull << (2 * nf));
                 c_bytes[s] = bytes;
                 c_f64[s] = f64;
                 live[rec[s].c] = {c_off[s], bytes};
@@ -225,7 +231,10 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
             } else {
                 d.a_off = (int64_t) c_off[ia->second];
                 d.a_step = sorted_of[ia->second];
-                if (c_f64[ia->second]) d.flags |= kAF64;
+                if (c_f64[ia->second]) {
+                    if (mixed) d.a_off = (int64_t) shadow[ia->second];
+                    else d.flags |= kAF64;
+                }
             }
             if (ib == producer.end()) {
                 d.flags |= kBLeaf;
@@ -236,7 +245,10 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
             } else {
                 d.b_off = (int64_t) c_off[ib->second];
                 d.b_step = sorted_of[ib->second];
-                if (c_f64[ib->second]) d.flags |= kBF64;
+                if (c_f64[ib->second]) {
+                    if (mixed) d.b_off = (int64_t) shadow[ib->second];
+                    else d.flags |= kBF64;
+                }
             }
             d.c_off = (int64_t) c_off[s];
             if (c_f64[s]) d.flags |= kCF64;
