@@ -403,13 +403,13 @@ static void batch_release(qt_batch *b) {
     dev_free(ctx, b->d_angles);
     b->d_leaves = b->d_inst = b->d_values = b->d_ws = b->d_next = b->d_angles = nullptr;
     b->tile_bytes = 0;
-    if (b->h_angles) cudaFreeHost(b->h_angles);
+    host_free(ctx, b->h_angles);
     b->h_angles = nullptr;
     if (b->angles_done) cudaEventDestroy(b->angles_done);
     b->angles_done = nullptr;
     b->dev_rot = false;
-    if (b->h_leaves) cudaFreeHost(b->h_leaves);
-    if (b->h_values) cudaFreeHost(b->h_values);
+    host_free(ctx, b->h_leaves);
+    host_free(ctx, b->h_values);
     b->h_leaves = b->h_values = nullptr;
     b->prepared_prec = -1;
 }
@@ -492,8 +492,11 @@ qt_status qt_batch_set_rotations_device(qt_batch *b, const double *angles, int64
     if (!n_angles) return QT_OK;
     qt_status s = QT_OK;
     if (!b->d_angles) {
-        cudaError_t e = cudaMallocHost((void **) &b->h_angles, sizeof(double) * n_angles);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->angles_done, cudaEventDisableTiming);
+        void *ha = nullptr;
+        s = host_alloc(ctx, sizeof(double) * n_angles, &ha);
+        if (s != QT_OK) return s;
+        b->h_angles = static_cast<double *>(ha);
+        cudaError_t e = cudaEventCreateWithFlags(&b->angles_done, cudaEventDisableTiming);
         if (e != cudaSuccess) return cuda_error(ctx, e, "angle staging");
         s = dev_alloc(ctx, sizeof(double) * n_angles, &b->d_angles);
         if (s != QT_OK) return s;
@@ -611,11 +614,11 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
         if (s == QT_OK && e != cudaSuccess) s = cuda_error(ctx, e, w);
     };
     if (off) {
-        chk(cudaMallocHost(&b->h_leaves, off), "cudaMallocHost");
+        s = host_alloc(ctx, off, &b->h_leaves);
         if (s == QT_OK) s = dev_alloc(ctx, off, &b->d_leaves);
     }
     if (s == QT_OK && n) {
-        chk(cudaMallocHost(&b->h_values, sizeof(double) * 2 * n), "cudaMallocHost");
+        s = host_alloc(ctx, sizeof(double) * 2 * n, &b->h_values);
         if (s == QT_OK) s = dev_alloc(ctx, sizeof(double) * 2 * n, &b->d_values);
     }
     if (s == QT_OK && b->grid > 0 && !b->ws_in_smem) s = dev_alloc(ctx, b->ws_stride * b->grid, &b->d_ws);

@@ -45,8 +45,35 @@ void ctx_release(qt_ctx *ctx) {
     for (auto &kv : ctx->free_blocks)
         for (void *p : kv.second) cudaFree(p);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    for (auto &kv : ctx->free_pinned)
+        for (void *p : kv.second) cudaFreeHost(p);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
+}
+
+qt_status host_alloc(qt_ctx *ctx, size_t bytes, void **out) {
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    const size_t cls = size_class(bytes ? bytes : 1);
+    auto it = ctx->free_pinned.find(cls);
+    if (it != ctx->free_pinned.end() && !it->second.empty()) {
+        *out = it->second.back();
+        it->second.pop_back();
+        return QT_OK;
+    }
+    void *p = nullptr;
+    cudaError_t e = cudaMallocHost(&p, cls);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "cudaMallocHost");
+    ctx->pinned_size[p] = cls;
+    *out = p;
+    return QT_OK;
+}
+
+void host_free(qt_ctx *ctx, void *p) {
+    if (!p) return;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    auto it = ctx->pinned_size.find(p);
+    if (it == ctx->pinned_size.end()) return;
+    ctx->free_pinned[it->second].push_back(p);
 }
 
 qt_status dev_alloc(qt_ctx *ctx, size_t bytes, void **out) {
@@ -122,6 +149,21 @@ bool tensor_cores_enabled() {
 }
 
 qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const void *B, void *C, bool f64) {
+    if (reduce_shaped(d)) {
+        // a long sum into a few outputs: the whole GPU on one sum
+        if (f64) {
+            cudaError_t e = launch_reduce_exact(d, (const double2 *) A, (const double2 *) B, (double2 *) C, ctx->stream);
+            ctx->launches++;
+            return cuda_error(ctx, e, "reduction launch");
+        }
+        void *scratch = nullptr;
+        qt_status s = dev_alloc(ctx, reduce_scratch_bytes(d), &scratch);
+        if (s != QT_OK) return s;
+        cudaError_t e = launch_reduce_f32(d, (const float2 *) A, (const float2 *) B, (float2 *) C, scratch, ctx->stream);
+        ctx->launches += 2;
+        dev_free(ctx, scratch);   // stream-ordered: the next user of the block runs after these kernels
+        return cuda_error(ctx, e, "reduction launch");
+    }
     if (!f64 && tensor_cores_enabled() && gemm_eligible(d)) {
         void *scratch = nullptr, *flag = nullptr;
         qt_status s = dev_alloc(ctx, sizeof(float) * gemm_scratch_floats(d), &scratch);

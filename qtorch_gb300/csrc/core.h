@@ -36,6 +36,10 @@ struct qt_ctx {
     // pinned staging buffer for small host<->device transfers
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
+    // caching allocator of pinned host memory (batch staging buffers): a
+    // server forms a batch per wave, and cudaMallocHost costs far more than a wave
+    std::map<size_t, std::vector<void *>> free_pinned;
+    std::map<void *, size_t> pinned_size;
 };
 
 struct qt_tensor {
@@ -55,6 +59,9 @@ qt_status cuda_error(qt_ctx *ctx, cudaError_t e, const char *what);
 qt_status dev_alloc(qt_ctx *ctx, size_t bytes, void **out);
 void dev_free(qt_ctx *ctx, void *p);
 qt_status ensure_pinned(qt_ctx *ctx, size_t bytes);
+// pinned host memory from the context cache (bytes rounded up to a size class)
+qt_status host_alloc(qt_ctx *ctx, size_t bytes, void **out);
+void host_free(qt_ctx *ctx, void *p);
 bool deadline_passed(qt_ctx *ctx);
 inline size_t elem_bytes(qt_dtype d) { return d == QT_C128 ? 16 : 8; }
 

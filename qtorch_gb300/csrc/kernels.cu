@@ -138,6 +138,133 @@ pair_kernel(const typename Vec2<T>::type *__restrict__ A, const typename Vec2<T>
 }
 
 // ---------------------------------------------------------------------------
+// Long reductions into a few outputs (steps run one at a time).
+
+constexpr int kReduceThreads = 256;
+
+// Dot2 partial sums of output c over a grid-strided share of the k range; one
+// (p_re, s_re, p_im, s_im) per CTA and output.
+__global__ void __launch_bounds__(kReduceThreads)
+reduce_partial_f32(const float2 *__restrict__ A, const float2 *__restrict__ B, const StepDesc d, uint32_t n_out,
+                   uint64_t K, float4 *__restrict__ partials) {
+    __shared__ float4 s_part[kReduceThreads / 32];
+    for (uint32_t c = 0; c < n_out; c++) {
+        uint64_t oa0, ob0;
+        scatter_c(c, d, oa0, ob0);
+        float pre = 0.f, sre = 0.f, pim = 0.f, sim = 0.f;
+        const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+        for (uint64_t k = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; k < K; k += stride)
+            cmac_dot2(pre, sre, pim, sim, A[oa0 + scatter_digits(k, d.posAs, d.nSum)],
+                      B[ob0 + scatter_digits(k, d.posBs, d.nSum)]);
+        for (int off = 16; off >= 1; off >>= 1) {
+            const float a = __shfl_xor_sync(0xffffffffu, pre, off), b = __shfl_xor_sync(0xffffffffu, sre, off);
+            const float e = __shfl_xor_sync(0xffffffffu, pim, off), f = __shfl_xor_sync(0xffffffffu, sim, off);
+            dot2_merge(pre, sre, a, b);
+            dot2_merge(pim, sim, e, f);
+        }
+        if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = make_float4(pre, sre, pim, sim);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float4 t = s_part[0];
+            for (int w = 1; w < kReduceThreads / 32; w++) {
+                dot2_merge(t.x, t.y, s_part[w].x, s_part[w].y);
+                dot2_merge(t.z, t.w, s_part[w].z, s_part[w].w);
+            }
+            partials[(uint64_t) c * gridDim.x + blockIdx.x] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// one warp per output: merge the CTAs' partial sums, round once to complex64
+__global__ void reduce_final_f32(const float4 *__restrict__ partials, uint32_t n_parts, uint32_t n_out,
+                                 float2 *__restrict__ C) {
+    const uint32_t c = blockIdx.x;
+    if (c >= n_out) return;
+    float pre = 0.f, sre = 0.f, pim = 0.f, sim = 0.f;
+    for (uint32_t j = threadIdx.x; j < n_parts; j += 32) {
+        const float4 t = partials[(uint64_t) c * n_parts + j];
+        dot2_merge(pre, sre, t.x, t.y);
+        dot2_merge(pim, sim, t.z, t.w);
+    }
+    for (int off = 16; off >= 1; off >>= 1) {
+        const float a = __shfl_xor_sync(0xffffffffu, pre, off), b = __shfl_xor_sync(0xffffffffu, sre, off);
+        const float e = __shfl_xor_sync(0xffffffffu, pim, off), f = __shfl_xor_sync(0xffffffffu, sim, off);
+        dot2_merge(pre, sre, a, b);
+        dot2_merge(pim, sim, e, f);
+    }
+    if (threadIdx.x == 0) C[c] = make_float2((float) ((double) pre + (double) sre), (float) ((double) pim + (double) sim));
+}
+
+// Exact complex128 reduction: one CTA per output.  The products of a chunk of
+// kReduceThreads consecutive k are formed in parallel (each rounded as the
+// reference rounds it) into a double-buffered shared array; thread 0 adds them
+// in increasing k, so the sum is the reference's sequential sum bit for bit.
+__global__ void __launch_bounds__(kReduceThreads)
+reduce_exact(const double2 *__restrict__ A, const double2 *__restrict__ B, const StepDesc d, uint64_t K,
+             double2 *__restrict__ C) {
+    __shared__ double2 prod[2][kReduceThreads];
+    const uint32_t c = blockIdx.x;
+    uint64_t oa0, ob0;
+    scatter_c(c, d, oa0, ob0);
+    double cre = 0.0, cim = 0.0;
+    int buf = 0;
+    for (uint64_t k0 = 0; k0 < K; k0 += kReduceThreads, buf ^= 1) {
+        const uint64_t k = k0 + threadIdx.x;
+        if (k < K) {
+            const double2 a = A[oa0 + scatter_digits(k, d.posAs, d.nSum)];
+            const double2 b = B[ob0 + scatter_digits(k, d.posBs, d.nSum)];
+            prod[buf][threadIdx.x] = make_double2(__dsub_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)),
+                                                  __dadd_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x)));
+        }
+        // one barrier per chunk: thread 0 reaches the next one only after summing
+        // this buffer, and the buffer is written again two chunks later
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const uint64_t n = K - k0 < (uint64_t) kReduceThreads ? K - k0 : (uint64_t) kReduceThreads;
+            for (uint64_t j = 0; j < n; j++) {
+                cre = __dadd_rn(cre, prod[buf][j].x);
+                cim = __dadd_rn(cim, prod[buf][j].y);
+            }
+        }
+    }
+    if (threadIdx.x == 0) C[c] = make_double2(cre, cim);
+}
+
+static int num_sms();
+
+static uint32_t reduce_grid(const StepDesc &d) {
+    const uint64_t K = 1ull << (2 * d.nSum);
+    uint64_t g = K / (kReduceThreads * 64ull);   // >= 64 terms per thread
+    const uint64_t cap = (uint64_t) num_sms() * 4;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (uint32_t) g;
+}
+
+size_t reduce_scratch_bytes(const StepDesc &d) {
+    return sizeof(float4) * (size_t) reduce_grid(d) * (size_t) (1ull << (2 * d.nFree));
+}
+
+cudaError_t launch_reduce_f32(const StepDesc &d, const float2 *A, const float2 *B, float2 *C, void *scratch,
+                              cudaStream_t stream) {
+    const uint32_t n_out = (uint32_t) (1ull << (2 * d.nFree));
+    const uint64_t K = 1ull << (2 * d.nSum);
+    const uint32_t g = reduce_grid(d);
+    float4 *parts = static_cast<float4 *>(scratch);
+    reduce_partial_f32<<<g, kReduceThreads, 0, stream>>>(A, B, d, n_out, K, parts);
+    reduce_final_f32<<<n_out, 32, 0, stream>>>(parts, g, n_out, C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_exact(const StepDesc &d, const double2 *A, const double2 *B, double2 *C,
+                                cudaStream_t stream) {
+    const uint32_t n_out = (uint32_t) (1ull << (2 * d.nFree));
+    reduce_exact<<<n_out, kReduceThreads, 0, stream>>>(A, B, d, 1ull << (2 * d.nSum), C);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Grouped plan interpreter.
 
 // The schedule of a level is precomputed on the host: every step carries the

@@ -9,6 +9,23 @@ namespace qtg {
 // rounding; otherwise complex64 with FP32 FMA.
 cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C, bool f64, cudaStream_t stream);
 
+// Steps with at most kReduceMaxOut outputs and a sum of at least kReduceMinK
+// terms (the final expectation values of large networks).
+constexpr uint64_t kReduceMaxOut = 16;
+constexpr uint64_t kReduceMinK = 1ull << 16;
+inline bool reduce_shaped(const StepDesc &d) {
+    return (1ull << (2 * d.nFree)) <= kReduceMaxOut && (1ull << (2 * d.nSum)) >= kReduceMinK;
+}
+// complex64: the sum split over the whole GPU, compensated (Dot2) partial sums
+// merged in a second kernel; scratch holds reduce_scratch_bytes(d) bytes
+size_t reduce_scratch_bytes(const StepDesc &d);
+cudaError_t launch_reduce_f32(const StepDesc &d, const float2 *A, const float2 *B, float2 *C, void *scratch,
+                              cudaStream_t stream);
+// complex128 with the reference's rounding: every thread of a CTA forms the
+// products of a chunk of k, one thread adds them in the reference's order
+cudaError_t launch_reduce_exact(const StepDesc &d, const double2 *A, const double2 *B, double2 *C,
+                                cudaStream_t stream);
+
 // Grouped interpreter over plan instances.  The workspace of a CTA is either
 // its shared memory (ws_in_smem; ws_stride bytes after the header) or
 // ws_base + blockIdx.x * ws_stride in global memory; with stage_bytes > 0 each

@@ -62,3 +62,26 @@ def test_dynamic_schedule_keeps_instance_order(ctx):
         else:
             assert np.abs(got - want).max() <= MIXED_TOL
 
+
+
+@pytest.mark.parametrize("ra,rb,ns", [(9, 9, 9), (9, 10, 9), (9, 9, 8)])
+def test_long_reduction_steps(ctx, ra, rb, ns):
+    """A sum of >= 4^8 terms into <= 16 outputs runs over the whole GPU: the
+    FP64 form forms products in parallel and adds them in the reference's order
+    (bit-exact), the complex64 form merges compensated partial sums."""
+    rng = np.random.default_rng(ra + rb + ns)
+    sa = list(rng.permutation(ra)[:ns])
+    sb = list(rng.permutation(rb)[:ns])
+    fa = [i for i in range(ra) if i not in sa]
+    fb = [i for i in range(rb) if i not in sb]
+    ffa, fi = [1] * len(fa) + [0] * len(fb), fa + fb
+    a = rng.standard_normal(4 ** ra) + 1j * rng.standard_normal(4 ** ra)
+    b = rng.standard_normal(4 ** rb) + 1j * rng.standard_normal(4 ** rb)
+    want = port.contract_indices(a, b, ffa, fi, sa, sb)
+    got = qg.contract_pair(a, b, ffa, fi, sa, sb, ctx=ctx)
+    assert np.array_equal(got, want)
+    a32, b32 = a.astype(np.complex64), b.astype(np.complex64)
+    want32 = port.contract_indices(a32.astype(np.complex128), b32.astype(np.complex128), ffa, fi, sa, sb)
+    got32 = qg.contract_pair_c64(a32, b32, ffa, fi, sa, sb, ctx=ctx)
+    # compensated sums: the result is the exact sum of the complex64 products rounded once
+    assert np.max(np.abs(got32 - want32)) <= 1e-6 * np.max(np.abs(want32)) + 1e-6
