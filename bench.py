@@ -560,9 +560,7 @@ def run_engine(args):
         a = angles_for(points[1 + (j % (len(points) - 1))])
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        bm.set_rotations_device(a)
-        bm.run()
-        vals = bm.fetch()
+        vals = bm.evaluate(a)
         t1 = time.perf_counter()
         if j >= args.warmup:
             e2e_times.append(t1 - t0)
@@ -601,7 +599,8 @@ def run_engine(args):
         "error_vs_fp64": {"max_abs": float(err.max()), "mean_abs": float(err.mean()), "bound": 1e-6},
         "e2e": {"value": e2e_value, "unit": "terms/s", "h2d_bytes_per_step": bm.h2d_bytes,
                 "d2h_bytes_per_step": bm.d2h_bytes, "ms_per_step": 1e3 * sum_e2e / args.steps,
-                "path": "Batch.set_rotations_device (angles H2D, gate tensors built on the device) -> run -> fetch",
+                "path": "Batch.evaluate(angles) = qt_batch_evaluate: angles H2D from pinned memory, gate tensors "
+                        "built on the device, one graph launch, values D2H",
                 "error_vs_fp64_max_abs": float(e2e_err.max())},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind, "kernel": "plan_kernel<mixed>",

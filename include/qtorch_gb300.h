@@ -264,6 +264,10 @@ qt_status qt_batch_set_rotations(qt_batch *b, const double *angles, int64_t n_an
  * only; instances run step by step get their leaves on the host.  A later
  * qt_batch_set_rotations or qt_batch_set_leaves switches back to host leaves. */
 qt_status qt_batch_set_rotations_device(qt_batch *b, const double *angles, int64_t n_angles);
+/* One evaluation of a prepared batch at new angles in a single call (the inner
+ * loop of a QAOA optimiser): qt_batch_set_rotations_device (angles may be NULL
+ * to keep the current leaves), qt_batch_run, qt_batch_fetch. */
+qt_status qt_batch_evaluate(qt_batch *b, const double *angles, int64_t n_angles, double *values);
 /* Upload all leaf values again from the host copies (async; part of an end-to-end step). */
 qt_status qt_batch_upload(qt_batch *b);
 /* Capture qt_batch_run into a CUDA graph and replay it (0 disables). */

@@ -551,6 +551,18 @@ class Batch(_Owned):
         a = np.ascontiguousarray(np.asarray(angles, dtype=np.float64))
         _check(_lib().qt_batch_set_rotations(self.handle, _dp(a), a.size), self.ctx)
 
+    def evaluate(self, angles=None):
+        """Values of every instance at new rotation angles in one call (gate
+        tensors built on the device; the batch must be prepared for MIXED when
+        angles are given)."""
+        out = np.zeros(2 * len(self))
+        if angles is None:
+            _check(_lib().qt_batch_evaluate(self.handle, None, 0, _dp(out)), self.ctx)
+        else:
+            a = np.ascontiguousarray(np.asarray(angles, dtype=np.float64))
+            _check(_lib().qt_batch_evaluate(self.handle, _dp(a), a.size, _dp(out)), self.ctx)
+        return out[0::2] + 1j * out[1::2]
+
     def set_rotations_device(self, angles):
         """New rotation angles whose gate tensors are built on the device at the
         next run (batches prepared for MIXED); only the angles are copied."""

@@ -747,6 +747,15 @@ qt_status qt_batch_run(qt_batch *b) {
     return QT_OK;
 }
 
+qt_status qt_batch_evaluate(qt_batch *b, const double *angles, int64_t n_angles, double *values) {
+    if (!b || !values || b->prepared_prec < 0) return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::recursive_mutex> g(b->ctx->lock);
+    qt_status s = angles ? qt_batch_set_rotations_device(b, angles, n_angles) : QT_OK;
+    if (s == QT_OK) s = qt_batch_run(b);
+    if (s == QT_OK) s = qt_batch_fetch(b, values);
+    return s;
+}
+
 qt_status qt_batch_fetch(qt_batch *b, double *values) {
     if (!b || !values || b->prepared_prec < 0) return QT_ERR_INVALID_ARGUMENT;
     qt_ctx *ctx = b->ctx;

@@ -62,3 +62,22 @@ def test_device_rotations_need_a_mixed_batch(ctx):
     b.prepare(qg.FP64)
     with pytest.raises(qg.QtError):
         b.set_rotations_device(np.array(term_angles(q)))
+
+
+def test_evaluate_is_set_run_fetch(ctx):
+    dgf = qg.random_regular_graph(30, 4, seed=11)
+    plans, angles = [], []
+    for e in range(qg.qaoa_num_edges(dgf)):
+        q, m = qg.qaoa_term_text(dgf, 1, [0.3, 0.7], e)
+        plans.append(qg.Plan(q, m, ordering="linegraph", ctx=ctx))
+        angles += term_angles(qg.qaoa_term_text(dgf, 1, [1.2, 0.4], e)[0])
+    b = qg.Batch(ctx)
+    for pl in plans:
+        b.add(pl)
+    b.prepare(qg.MIXED)
+    b.use_graph(True)
+    one = b.evaluate(np.array(angles))
+    b.set_rotations_device(np.array(angles))
+    b.run()
+    assert np.array_equal(one, b.fetch())
+    assert np.array_equal(b.evaluate(), one)   # no angles: the current leaves again
