@@ -18,6 +18,8 @@
 #include <algorithm>
 #include <cmath>
 #include <fstream>
+#include <functional>
+#include <map>
 #include <set>
 #include <sstream>
 
@@ -246,16 +248,52 @@ const std::vector<int> &LineGraph::MinFillOrdering() {
     std::vector<long long> fill(n);
     for (int v = 0; v < n; v++) fill[v] = fill_of(v);
     std::vector<int> mark(n, -1);
-    // greedy min-fill: fewest added edges, then smallest degree, then smallest id
+    // The walk LGContract makes from this order merges the two nodes on each
+    // eliminated wire; the contraction tree's height is the number of
+    // dependent steps a GPU must run one after another.  Node heights are
+    // tracked (union-find over the nodes) so that ties of the min-fill score go
+    // to the wire whose contraction stays lowest: equal fill, shallower tree.
+    std::map<const Node *, int> node_index;
+    std::vector<std::array<int, 2>> ends(n);
+    for (int v = 0; v < n; v++) {
+        for (int s = 0; s < 2; s++) {
+            auto nd = s == 0 ? mGraphWires[v]->GetNodeA().lock() : mGraphWires[v]->GetNodeB().lock();
+            const Node *key = nd.get();
+            auto it = node_index.find(key);
+            if (it == node_index.end()) it = node_index.emplace(key, (int) node_index.size()).first;
+            ends[v][s] = it->second;
+        }
+    }
+    std::vector<int> parent(node_index.size()), height(node_index.size(), 0);
+    for (size_t i = 0; i < parent.size(); i++) parent[i] = (int) i;
+    std::function<int(int)> find = [&](int x) { return parent[x] == x ? x : parent[x] = find(parent[x]); };
+    auto merged_height = [&](int v) {
+        const int a = find(ends[v][0]), b = find(ends[v][1]);
+        return a == b ? 0 : std::max(height[a], height[b]) + 1;
+    };
+    // greedy min-fill: fewest added edges, then the lowest merged node, then
+    // smallest degree, then smallest id
     for (int step = 0; step < n; step++) {
-        int best = -1;
+        int best = -1, best_h = 0;
         for (int v = 0; v < n; v++) {
             if (gone[v]) continue;
-            if (best < 0 || fill[v] < fill[best] || (fill[v] == fill[best] && adj[v].size() < adj[best].size()))
+            if (best >= 0 && fill[v] > fill[best]) continue;
+            const int h = merged_height(v);
+            if (best < 0 || fill[v] < fill[best] || h < best_h ||
+                (h == best_h && adj[v].size() < adj[best].size())) {
                 best = v;
+                best_h = h;
+            }
         }
         gone[best] = 1;
         mOrder.push_back(best + 1);
+        {
+            const int a = find(ends[best][0]), b = find(ends[best][1]);
+            if (a != b) {
+                parent[a] = b;
+                height[b] = std::max(height[a], height[b]) + 1;
+            }
+        }
         std::vector<int> nb(adj[best].begin(), adj[best].end());
         for (size_t i = 0; i < nb.size(); i++)
             for (size_t j = i + 1; j < nb.size(); j++) {
