@@ -233,3 +233,15 @@ def test_interpreter_schedule_invariants():
                 elif prec == qg.FP64:
                     assert g == 1   # the FP64 form keeps one accumulator per output
     assert seen_tiled > 0
+
+
+def test_linegraph_ordering_keeps_the_tree_shallow():
+    """Min-fill ties go to the wire whose contraction stays lowest in the tree:
+    every light-cone term of a 30-vertex 4-regular p=1 QAOA has at most 16
+    dependent levels (31 without the tie-break) and peak rank 4."""
+    dgf = qg.random_regular_graph(30, 4, seed=1)
+    for e in range(qg.qaoa_num_edges(dgf)):
+        q, m = qg.qaoa_term_text(dgf, 1, [0.3, 0.7], e)
+        plan = qg.Plan(q, m, ordering="linegraph", symbolic=True)
+        assert plan.peak_rank <= 4
+        assert plan.step_info(qg.MIXED)[:, 0].max() + 1 <= 16
