@@ -353,10 +353,13 @@ def run_serving(args):
         else:
             reqs.append(("qft", qft_plans[int(rng.choice(4, p=tail))]))
 
+    # one server for both phases: the saturation phase also warms its lanes'
+    # device and pinned-memory caches and the plans' device blocks
+    srv = qg.Server(max_inflight=256, precision=qg.MIXED, ctx=ctx)
+
     def serve(gaps):
         """Submit every request at its arrival time (gaps None: all at once);
         latencies by class, wall time, max error against FP64."""
-        srv = qg.Server(max_inflight=256, precision=qg.MIXED, ctx=ctx)
         tickets = []
         t0 = time.perf_counter()
         t_next = t0
@@ -377,8 +380,7 @@ def run_serving(args):
             v, l = srv.poll(t)
             lat[cls].append(l)
             err = max(err, abs(v - ref[id(plan)]))
-        done = srv.stats()["completed"]
-        srv.close()
+        done = len(tickets)
         return lat, wall, err, done
 
     def pct(xs, f):
@@ -391,7 +393,13 @@ def run_serving(args):
     capacity = len(reqs) / wall_sat
     rate = args.serve_rate if args.serve_rate > 0 else args.serve_load * capacity
     gaps = rng.exponential(1.0 / rate, len(reqs))
+    st0 = srv.stats()
     lat, wall, err, done = serve(gaps)
+    st1 = srv.stats()
+    srv.close()
+    waves = st1["waves"] - st0["waves"]
+    wave_reqs = st1["wave_requests"] - st0["wave_requests"]
+    wave_s = st1["lane_seconds"] - st0["lane_seconds"]
     all_lat = [x for v in lat.values() for x in v]
     out = {
         "workload": f"{len(reqs)} requests, Poisson arrivals at {rate:.0f}/s ({rate / capacity:.2f} of the "
@@ -406,6 +414,8 @@ def run_serving(args):
         "p50_ms_by_class": {k: pct(v, 0.50) for k, v in lat.items()},
         "p99_ms_by_class": {k: pct(v, 0.99) for k, v in lat.items()},
         "requests_per_s": len(reqs) / wall, "completed": done,
+        "waves": waves, "mean_requests_per_wave": wave_reqs / max(waves, 1),
+        "mean_wave_ms": 1e3 * wave_s / max(waves, 1),
         "error_vs_fp64_max_abs": max(err, err_sat), "error_bound": 1e-6,
     }
     ctx.close()

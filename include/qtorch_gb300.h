@@ -304,6 +304,9 @@ int qt_server_poll(qt_server *s, int64_t ticket, double *re_im, double *latency_
 qt_status qt_server_drain(qt_server *s);
 /* p50/p99 latency in seconds and completed count since creation. */
 qt_status qt_server_stats(qt_server *s, double *p50, double *p99, int64_t *completed, int64_t *launches);
+/* Waves run so far, the requests they carried, and the lane time they took
+ * (building the batch, launching, reading values back), summed over lanes. */
+qt_status qt_server_wave_stats(qt_server *s, int64_t *waves, int64_t *requests, double *lane_seconds);
 
 #ifdef __cplusplus
 }

@@ -631,7 +631,11 @@ class Server(_Owned):
         done, launches = ctypes.c_int64(0), ctypes.c_int64(0)
         _check(_lib().qt_server_stats(self.handle, ctypes.byref(p50), ctypes.byref(p99), ctypes.byref(done),
                                       ctypes.byref(launches)), self.ctx)
-        return {"p50_s": p50.value, "p99_s": p99.value, "completed": done.value, "launches": launches.value}
+        waves, reqs, secs = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_double(0)
+        _check(_lib().qt_server_wave_stats(self.handle, ctypes.byref(waves), ctypes.byref(reqs), ctypes.byref(secs)),
+               self.ctx)
+        return {"p50_s": p50.value, "p99_s": p99.value, "completed": done.value, "launches": launches.value,
+                "waves": waves.value, "wave_requests": reqs.value, "lane_seconds": secs.value}
 
 
 def qaoa_num_edges(dgf_text):

@@ -672,10 +672,7 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
             chk(cudaStreamSynchronize(ctx->stream), "sync");
         }
     }
-    if (s == QT_OK) {
-        batch_pack(b);
-        s = qt_batch_upload(b);
-    }
+    if (s == QT_OK) s = qt_batch_upload(b);   // packs the leaf images and copies them
     if (s == QT_OK) chk(cudaStreamSynchronize(ctx->stream), "sync");
     if (s != QT_OK) batch_release(b);
     b->dirty = false;

@@ -56,6 +56,8 @@ struct qt_server {
     std::vector<double> latencies;
     int64_t completed = 0;
     int64_t launches = 0;
+    int64_t waves = 0, wave_requests = 0;
+    double wave_seconds = 0;                 // lane time spent on waves (batch build, launch, read-back)
     struct Lane {
         qt_ctx *ctx = nullptr;
         std::thread th;
@@ -81,6 +83,7 @@ static void lane_main(qt_server *s, int li) {
             wave.swap(lane.wave);
         }
         std::vector<double> vals(2 * wave.size(), 0.0);
+        const auto t_wave = std::chrono::steady_clock::now();
         qt_batch *b = nullptr;
         qt_status st = qt_batch_create(lane.ctx, &b);
         for (auto &r : wave)
@@ -107,6 +110,9 @@ static void lane_main(qt_server *s, int li) {
                 s->inflight_bytes -= wave[i].footprint;
             }
             s->launches += nl;
+            s->waves++;
+            s->wave_requests += (int64_t) wave.size();
+            s->wave_seconds += std::chrono::duration<double>(now - t_wave).count();
             lane.busy = false;
         }
         s->cv.notify_all();
@@ -246,6 +252,15 @@ qt_status qt_server_drain(qt_server *s) {
     if (!s) return QT_ERR_INVALID_ARGUMENT;
     std::unique_lock<std::mutex> g(s->m);
     s->done_cv.wait(g, [&] { return s->pending.empty() && s->inflight == 0; });
+    return QT_OK;
+}
+
+qt_status qt_server_wave_stats(qt_server *s, int64_t *waves, int64_t *requests, double *lane_seconds) {
+    if (!s) return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->m);
+    if (waves) *waves = s->waves;
+    if (requests) *requests = s->wave_requests;
+    if (lane_seconds) *lane_seconds = s->wave_seconds;
     return QT_OK;
 }
 
