@@ -225,15 +225,18 @@ void LineGraph::Build() {
     }
 }
 
-const std::vector<int> &LineGraph::MinFillOrdering() {
-    if (!mOrder.empty() || mGraphWires.empty()) return mOrder;
-    const int n = (int) mGraphWires.size();
-    std::vector<std::set<int>> adj(n);
-    for (auto &e : mEdges) {
-        if (e[0] == e[1]) continue;
-        adj[e[0]].insert(e[1]);
-        adj[e[1]].insert(e[0]);
-    }
+namespace {
+
+// Greedy min-fill elimination of the line graph (adjacency adj0, n wires).
+// ends[v] = the two nodes wire v joins.  The walk LGContract makes from the
+// order merges the two nodes on each eliminated wire, so the order fixes the
+// contraction tree.  Ties of the fill score go to the smaller degree (classic
+// min-fill), or, with shallow_ties, first to the wire whose merge reaches the
+// lowest height in the tree (node heights tracked with a union-find).
+std::vector<int> min_fill_order(const std::vector<std::set<int>> &adj0, const std::vector<std::array<int, 2>> &ends,
+                                int n_nodes, bool shallow_ties) {
+    const int n = (int) adj0.size();
+    std::vector<std::set<int>> adj = adj0;
     std::vector<char> gone(n, 0);
     auto fill_of = [&](int v) {
         long long fill = 0;
@@ -248,37 +251,21 @@ const std::vector<int> &LineGraph::MinFillOrdering() {
     std::vector<long long> fill(n);
     for (int v = 0; v < n; v++) fill[v] = fill_of(v);
     std::vector<int> mark(n, -1);
-    // The walk LGContract makes from this order merges the two nodes on each
-    // eliminated wire; the contraction tree's height is the number of
-    // dependent steps a GPU must run one after another.  Node heights are
-    // tracked (union-find over the nodes) so that ties of the min-fill score go
-    // to the wire whose contraction stays lowest: equal fill, shallower tree.
-    std::map<const Node *, int> node_index;
-    std::vector<std::array<int, 2>> ends(n);
-    for (int v = 0; v < n; v++) {
-        for (int s = 0; s < 2; s++) {
-            auto nd = s == 0 ? mGraphWires[v]->GetNodeA().lock() : mGraphWires[v]->GetNodeB().lock();
-            const Node *key = nd.get();
-            auto it = node_index.find(key);
-            if (it == node_index.end()) it = node_index.emplace(key, (int) node_index.size()).first;
-            ends[v][s] = it->second;
-        }
-    }
-    std::vector<int> parent(node_index.size()), height(node_index.size(), 0);
-    for (size_t i = 0; i < parent.size(); i++) parent[i] = (int) i;
+    std::vector<int> parent(n_nodes), height(n_nodes, 0);
+    for (int i = 0; i < n_nodes; i++) parent[i] = i;
     std::function<int(int)> find = [&](int x) { return parent[x] == x ? x : parent[x] = find(parent[x]); };
     auto merged_height = [&](int v) {
         const int a = find(ends[v][0]), b = find(ends[v][1]);
         return a == b ? 0 : std::max(height[a], height[b]) + 1;
     };
-    // greedy min-fill: fewest added edges, then the lowest merged node, then
-    // smallest degree, then smallest id
+    std::vector<int> order;
+    order.reserve(n);
     for (int step = 0; step < n; step++) {
         int best = -1, best_h = 0;
         for (int v = 0; v < n; v++) {
             if (gone[v]) continue;
             if (best >= 0 && fill[v] > fill[best]) continue;
-            const int h = merged_height(v);
+            const int h = shallow_ties ? merged_height(v) : 0;
             if (best < 0 || fill[v] < fill[best] || h < best_h ||
                 (h == best_h && adj[v].size() < adj[best].size())) {
                 best = v;
@@ -286,7 +273,7 @@ const std::vector<int> &LineGraph::MinFillOrdering() {
             }
         }
         gone[best] = 1;
-        mOrder.push_back(best + 1);
+        order.push_back(best);
         {
             const int a = find(ends[best][0]), b = find(ends[best][1]);
             if (a != b) {
@@ -316,6 +303,79 @@ const std::vector<int> &LineGraph::MinFillOrdering() {
         }
         for (int u : affected) fill[u] = fill_of(u);
     }
+    return order;
+}
+
+struct WalkCost {
+    double macs = 0;   // complex MACs of the walk
+    int peak = 0;      // largest rank it creates
+    int height = 0;    // height of its contraction tree
+};
+
+// The walk LGContract makes from an order, without data: every merge sums over
+// all wires the two nodes share (ContractNodes), 4^(rank C + shared) MACs.
+WalkCost walk_cost(const std::vector<int> &order, const std::vector<std::array<int, 2>> &ends, int n_nodes) {
+    std::vector<int> parent(n_nodes), height(n_nodes, 0);
+    std::vector<std::set<int>> wires(n_nodes);
+    for (int i = 0; i < n_nodes; i++) parent[i] = i;
+    for (size_t v = 0; v < ends.size(); v++) {
+        wires[ends[v][0]].insert((int) v);
+        wires[ends[v][1]].insert((int) v);
+    }
+    std::function<int(int)> find = [&](int x) { return parent[x] == x ? x : parent[x] = find(parent[x]); };
+    WalkCost c;
+    for (int v : order) {
+        const int a = find(ends[v][0]), b = find(ends[v][1]);
+        if (a == b) continue;
+        std::set<int> merged;
+        int shared = 0;
+        for (int w : wires[a]) {
+            if (wires[b].count(w)) shared++;
+            else merged.insert(w);
+        }
+        for (int w : wires[b])
+            if (!wires[a].count(w)) merged.insert(w);
+        c.macs += std::pow(4.0, (double) (merged.size() + shared));
+        c.peak = std::max(c.peak, (int) merged.size());
+        parent[a] = b;
+        height[b] = std::max(height[a], height[b]) + 1;
+        c.height = std::max(c.height, height[b]);
+        wires[b].swap(merged);
+        wires[a].clear();
+    }
+    return c;
+}
+
+}  // namespace
+
+const std::vector<int> &LineGraph::MinFillOrdering() {
+    if (!mOrder.empty() || mGraphWires.empty()) return mOrder;
+    const int n = (int) mGraphWires.size();
+    std::vector<std::set<int>> adj(n);
+    for (auto &e : mEdges) {
+        if (e[0] == e[1]) continue;
+        adj[e[0]].insert(e[1]);
+        adj[e[1]].insert(e[0]);
+    }
+    std::map<const Node *, int> node_index;
+    std::vector<std::array<int, 2>> ends(n);
+    for (int v = 0; v < n; v++) {
+        for (int s = 0; s < 2; s++) {
+            auto nd = s == 0 ? mGraphWires[v]->GetNodeA().lock() : mGraphWires[v]->GetNodeB().lock();
+            auto it = node_index.find(nd.get());
+            if (it == node_index.end()) it = node_index.emplace(nd.get(), (int) node_index.size()).first;
+            ends[v][s] = it->second;
+        }
+    }
+    const int n_nodes = (int) node_index.size();
+    // On the GPU a small network's latency is the height of its contraction
+    // tree, a large one's is its MACs: the shallow-tie order is taken when it
+    // costs no larger intermediate and at most 1.5x the MACs of classic min-fill.
+    std::vector<int> classic = min_fill_order(adj, ends, n_nodes, false);
+    std::vector<int> shallow = min_fill_order(adj, ends, n_nodes, true);
+    const WalkCost cc = walk_cost(classic, ends, n_nodes), cs = walk_cost(shallow, ends, n_nodes);
+    const std::vector<int> &pick = (cs.peak <= cc.peak && cs.macs <= 1.5 * cc.macs) ? shallow : classic;
+    for (int v : pick) mOrder.push_back(v + 1);
     return mOrder;
 }
 
