@@ -373,7 +373,7 @@ qt_status qt_plan_leaf_values(const qt_plan *p, double *out, uint64_t cap) {
 
 qt_status qt_plan_execute(qt_ctx *ctx, qt_plan *p, qt_precision prec, double *v) {
     if (!ctx || !p || !p->ctx || !v || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return QT_ERR_INVALID_ARGUMENT;
-    if (!p->grouped) return execute_stepwise(p, prec, p->leaf_values.data(), v);
+    if (!p->grouped || p->flops > kLoneInstanceMaxMacs) return execute_stepwise(p, prec, p->leaf_values.data(), v);
     qt_batch *b = nullptr;
     qt_status s = qt_batch_create(ctx, &b);
     if (s != QT_OK) return s;
@@ -394,6 +394,10 @@ static void batch_release(qt_batch *b) {
     if (b->graph) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
+    }
+    if (b->eval_graph) {
+        cudaGraphExecDestroy(b->eval_graph);
+        b->eval_graph = nullptr;
     }
     dev_free(ctx, b->d_leaves);
     dev_free(ctx, b->d_inst);
@@ -555,7 +559,7 @@ qt_status qt_batch_set_rotations(qt_batch *b, const double *angles, int64_t n_an
 static qt_status batch_pack(qt_batch *b) {
     const int prec = b->prepared_prec;
     for (size_t i = 0; i < b->plans.size(); i++) {
-        if (!b->plans[i]->grouped) continue;
+        if (!b->in_group[i]) continue;
         pack_leaves(b->plans[i], prec, b->leaves[i].data(), (char *) b->h_leaves + b->inst_leaf_off[i]);
     }
     return QT_OK;
@@ -571,15 +575,17 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
     const int n = (int) b->plans.size();
     b->stepwise.clear();
     b->inst_leaf_off.assign(n, 0);
+    b->in_group.assign(n, 0);
     uint64_t off = 0, ws = 0, ws_small = 0;
     int n_grouped = 0;
     bool any_tiled = false;
     for (int i = 0; i < n; i++) {
         qt_plan *p = b->plans[i];
-        if (!p->grouped) {
+        if (!p->grouped || p->flops > b->stepwise_macs) {
             b->stepwise.push_back(i);
             continue;
         }
+        b->in_group[i] = 1;
         qt_status s = upload_plan(p, prec);
         if (s != QT_OK) return s;
         b->inst_leaf_off[i] = off;
@@ -598,7 +604,7 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
     uint64_t stage_small = 0;
     for (int i = 0; i < n; i++) {
         const qt_plan *p = b->plans[i];
-        if (!p->grouped) continue;
+        if (!b->in_group[i]) continue;
         const uint64_t st = round16(p->dev_bytes[prec]) + round16(p->leaf_bytes[prec]);
         if (st <= stage_cap) stage_small = std::max<uint64_t>(stage_small, st);
     }
@@ -633,7 +639,7 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
     // the dynamic schedule)
     std::vector<int> inst_order;
     for (int i = 0; i < n; i++)
-        if (b->plans[i]->grouped) inst_order.push_back(i);
+        if (b->in_group[i]) inst_order.push_back(i);
     if (b->d_next) {
         auto cost = [&](int i) {
             const qt_plan *p = b->plans[i];
@@ -746,11 +752,51 @@ qt_status qt_batch_run(qt_batch *b) {
 
 qt_status qt_batch_evaluate(qt_batch *b, const double *angles, int64_t n_angles, double *values) {
     if (!b || !values || b->prepared_prec < 0) return QT_ERR_INVALID_ARGUMENT;
-    std::lock_guard<std::recursive_mutex> g(b->ctx->lock);
-    qt_status s = angles ? qt_batch_set_rotations_device(b, angles, n_angles) : QT_OK;
-    if (s == QT_OK) s = qt_batch_run(b);
-    if (s == QT_OK) s = qt_batch_fetch(b, values);
-    return s;
+    qt_ctx *ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    const bool one_graph = angles && n_angles > 0 && b->use_graph && b->stepwise.empty() &&
+                           b->prepared_prec == QT_PREC_MIXED && !b->plans.empty();
+    if (!one_graph) {
+        qt_status s = angles ? qt_batch_set_rotations_device(b, angles, n_angles) : QT_OK;
+        if (s == QT_OK) s = qt_batch_run(b);
+        if (s == QT_OK) s = qt_batch_fetch(b, values);
+        return s;
+    }
+    if (deadline_passed(ctx)) return set_error(ctx, QT_ERR_DEADLINE, "deadline expired");
+    if (!b->eval_graph) {
+        // first call: the regular path sets up the angle buffers and the descriptors,
+        // then the whole step -- angles H2D, the grouped launch, values D2H -- is
+        // captured as one graph
+        qt_status s = qt_batch_set_rotations_device(b, angles, n_angles);
+        if (s == QT_OK) s = qt_batch_run(b);
+        if (s == QT_OK) s = qt_batch_fetch(b, values);
+        if (s != QT_OK) return s;
+        cudaGraph_t graph;
+        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "begin capture");
+        cudaMemcpyAsync(b->d_angles, b->h_angles, sizeof(double) * n_angles, cudaMemcpyHostToDevice, ctx->stream);
+        s = batch_launch(b);
+        cudaMemcpyAsync(b->h_values, b->d_values, sizeof(double) * 2 * b->plans.size(), cudaMemcpyDeviceToHost,
+                        ctx->stream);
+        e = cudaStreamEndCapture(ctx->stream, &graph);
+        if (s != QT_OK) return s;
+        if (e != cudaSuccess) return cuda_error(ctx, e, "end capture");
+        e = cudaGraphInstantiate(&b->eval_graph, graph, 0);
+        cudaGraphDestroy(graph);
+        return cuda_error(ctx, e, "graph instantiate");
+    }
+    if (n_angles != b->n_angles) return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "angle count does not match the batch");
+    qt_status s = batch_device_rotations(b, true);
+    if (s != QT_OK) return s;
+    // the previous evaluation finished (stream synchronised), so the pinned
+    // copies are free
+    std::memcpy(b->h_angles, angles, sizeof(double) * n_angles);
+    cudaError_t e = cudaGraphLaunch(b->eval_graph, ctx->stream);
+    ctx->launches++;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "evaluation graph");
+    std::memcpy(values, b->h_values, sizeof(double) * 2 * b->plans.size());
+    return QT_OK;
 }
 
 qt_status qt_batch_fetch(qt_batch *b, double *values) {
@@ -783,6 +829,10 @@ qt_status qt_batch_use_graph(qt_batch *b, int enable) {
     if (!b->use_graph && b->graph) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
+    }
+    if (!b->use_graph && b->eval_graph) {
+        cudaGraphExecDestroy(b->eval_graph);
+        b->eval_graph = nullptr;
     }
     return QT_OK;
 }

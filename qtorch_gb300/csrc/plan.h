@@ -30,6 +30,10 @@ constexpr uint64_t kSmemStageMaxTiled = 52ull << 10;
 inline uint64_t round16(uint64_t x) { return (x + 15) / 16 * 16; }
 // offset tables are built when they take at most this many bytes
 constexpr uint64_t kMaxTableBytes = 64ull << 10;
+// One CTA runs a grouped instance at a few percent of the GPU: a plan above
+// this many complex MACs that runs alone (qt_plan_execute) or in a server wave
+// goes step by step through the whole-GPU kernels instead.
+constexpr int64_t kLoneInstanceMaxMacs = 1ll << 24;
 
 }  // namespace qtg
 
@@ -97,8 +101,11 @@ struct qt_batch {
     void *h_values = nullptr;                         // pinned values
     bool use_graph = false;
     cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t eval_graph = nullptr;             // qt_batch_evaluate: angles H2D + launch + values D2H
     bool all_grouped = true;
     std::vector<int> stepwise;                        // instances run step by step
+    std::vector<char> in_group;                       // instance runs in the grouped launch
+    int64_t stepwise_macs = INT64_MAX;                // grouped plans above this run step by step
     // rotation angles applied on the device (mixed precision): pinned + device copies
     bool dev_rot = false;
     int64_t n_angles = 0;

@@ -86,6 +86,7 @@ static void lane_main(qt_server *s, int li) {
         const auto t_wave = std::chrono::steady_clock::now();
         qt_batch *b = nullptr;
         qt_status st = qt_batch_create(lane.ctx, &b);
+        if (st == QT_OK) b->stepwise_macs = kLoneInstanceMaxMacs;   // waves are small: big plans take the whole GPU
         for (auto &r : wave)
             if (st == QT_OK) st = qt_batch_add(b, r.plan, r.leaves.empty() ? nullptr : r.leaves.data(), nullptr);
         if (st == QT_OK) st = qt_batch_execute(b, s->prec, vals.data());
@@ -219,7 +220,7 @@ qt_status qt_server_submit(qt_server *s, qt_plan *plan, const double *leaves, in
     if (leaves) r.leaves.assign(leaves, leaves + 2 * plan->leaf_values.size());
     r.t_submit = std::chrono::steady_clock::now();
     r.footprint = footprint(plan, s->prec);
-    r.heavy = !plan->grouped;
+    r.heavy = !plan->grouped || plan->flops > kLoneInstanceMaxMacs;
     {
         std::lock_guard<std::mutex> g(s->m);
         const uint64_t budget = s->ctx->memory_budget;

@@ -81,3 +81,11 @@ def test_evaluate_is_set_run_fetch(ctx):
     b.run()
     assert np.array_equal(one, b.fetch())
     assert np.array_equal(b.evaluate(), one)   # no angles: the current leaves again
+    # later calls replay one captured graph (angles in, launch, values out)
+    other = np.array(angles) * 0.5
+    two = b.evaluate(other)
+    b.set_rotations_device(other)
+    b.run()
+    assert np.array_equal(two, b.fetch())
+    assert not np.array_equal(two, one)
+    assert np.array_equal(b.evaluate(np.array(angles)), one)
