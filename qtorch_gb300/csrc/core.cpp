@@ -184,6 +184,11 @@ qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const v
         dev_free(ctx, flag);
         return s;
     }
+    if (tiled_shaped(d)) {
+        cudaError_t e = launch_tiled_pair(d, A, B, C, f64, ctx->stream);
+        ctx->launches++;
+        return cuda_error(ctx, e, "tiled kernel launch");
+    }
     cudaError_t e = launch_pair(d, A, B, C, f64, ctx->stream);
     ctx->launches++;
     return cuda_error(ctx, e, "pair kernel launch");

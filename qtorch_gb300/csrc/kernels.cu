@@ -493,8 +493,10 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
 // every thread of the tile.  Each output still accumulates over k in
 // increasing order, so the FP64 form keeps the reference's rounding.
 template <bool kMixed, int MI, int NJ>
-__device__ void tiled_step(const StepDesc &d, int si, const char *leaves, char *ws, PlanSmemHeader &h,
-                           unsigned char *tile) {
+__device__ float tiled_tiles(const StepDesc &d, const typename std::conditional<kMixed, float2, double2>::type *A,
+                             const typename std::conditional<kMixed, float2, double2>::type *B,
+                             typename std::conditional<kMixed, float2, double2>::type *C, int shift,
+                             unsigned char *tile, uint32_t t_first, uint32_t t_stride) {
     using V = typename std::conditional<kMixed, float2, double2>::type;
     using T = typename std::conditional<kMixed, float, double>::type;
     constexpr uint32_t KC = kMixed ? kCtaTileChunk : kCtaTileChunk / 2;
@@ -508,16 +510,8 @@ __device__ void tiled_step(const StepDesc &d, int si, const char *leaves, char *
     const uint32_t M = 1u << (2 * fA), N = 1u << (2 * fB), K = 1u << (2 * nSum);
     const uint32_t kc = K < KC ? K : KC;
     const uint32_t tiles_m = M / TM, n_tiles = tiles_m * (N / TN);
-    const V *A = reinterpret_cast<const V *>(((d.flags & kALeaf) ? leaves : ws) + d.a_off);
-    const V *B = reinterpret_cast<const V *>(((d.flags & kBLeaf) ? leaves : ws) + d.b_off);
-    V *C = reinterpret_cast<V *>(ws + d.c_off);
-    int ma = 0, mb = 0;
-    if constexpr (kMixed) {
-        ma = step_scale(h, d.a_step);
-        mb = step_scale(h, d.b_step);
-    }
     float tmax = 0.f;
-    for (uint32_t t = 0; t < n_tiles; t++) {
+    for (uint32_t t = t_first; t < n_tiles; t += t_stride) {
         const uint32_t m0 = (t % tiles_m) * TM, n0 = (t / tiles_m) * TN;
         __syncthreads();   // readers of the previous tile's offsets and slices are done
         if (tid < TM) {
@@ -569,8 +563,8 @@ __device__ void tiled_step(const StepDesc &d, int si, const char *leaves, char *
                 const uint32_t c = (m0 + tx + 16 * i) + M * (n0 + ty + 16 * j);
                 V v;
                 if constexpr (kMixed) {
-                    v.x = scale2f(cre[i][j], -(ma + mb));
-                    v.y = scale2f(cim[i][j], -(ma + mb));
+                    v.x = scale2f(cre[i][j], shift);
+                    v.y = scale2f(cim[i][j], shift);
                     tmax = fmaxf(tmax, fmaxf(fabsf(v.x), fabsf(v.y)));
                 } else {
                     v.x = cre[i][j];
@@ -579,7 +573,24 @@ __device__ void tiled_step(const StepDesc &d, int si, const char *leaves, char *
                 C[c] = v;
             }
     }
+    return tmax;
+}
+
+template <bool kMixed, int MI, int NJ>
+__device__ void tiled_step(const StepDesc &d, int si, const char *leaves, char *ws, PlanSmemHeader &h,
+                           unsigned char *tile) {
+    using V = typename std::conditional<kMixed, float2, double2>::type;
+    const V *A = reinterpret_cast<const V *>(((d.flags & kALeaf) ? leaves : ws) + d.a_off);
+    const V *B = reinterpret_cast<const V *>(((d.flags & kBLeaf) ? leaves : ws) + d.b_off);
+    V *C = reinterpret_cast<V *>(ws + d.c_off);
+    int ma = 0, mb = 0;
     if constexpr (kMixed) {
+        ma = step_scale(h, d.a_step);
+        mb = step_scale(h, d.b_step);
+    }
+    const float tmax = tiled_tiles<kMixed, MI, NJ>(d, A, B, C, -(ma + mb), tile, 0, 1);
+    if constexpr (kMixed) {
+        const uint32_t tid = threadIdx.x;
         const uint32_t wmax = __reduce_max_sync(0xffffffffu, __float_as_uint(tmax));
         if ((tid & 31u) == 0) atomicMax(&h.maxbits[si], wmax);
         if (tid == 0) {
@@ -598,6 +609,17 @@ __device__ __forceinline__ void run_tiled(const StepDesc &d, int si, const char 
     else if (wide_m) tiled_step<kMixed, 4, 1>(d, si, leaves, ws, h, tile);
     else if (wide_n) tiled_step<kMixed, 1, 4>(d, si, leaves, ws, h, tile);
     else tiled_step<kMixed, 1, 1>(d, si, leaves, ws, h, tile);
+}
+
+// The same tiled product as a whole-GPU kernel for steps run one at a time
+// (no power-of-two scaling there): the CTAs stride over the output tiles.
+template <bool kMixed, int MI, int NJ>
+__global__ void __launch_bounds__(kPlanThreads)
+tiled_pair_kernel(const typename std::conditional<kMixed, float2, double2>::type *A,
+                  const typename std::conditional<kMixed, float2, double2>::type *B,
+                  typename std::conditional<kMixed, float2, double2>::type *C, const StepDesc d) {
+    extern __shared__ __align__(16) unsigned char tile_smem[];
+    tiled_tiles<kMixed, MI, NJ>(d, A, B, C, 0, tile_smem, blockIdx.x, gridDim.x);
 }
 
 // Rotation leaves rebuilt from an angle (mixed plans): the superoperators the
@@ -894,6 +916,35 @@ static cudaError_t plan_attributes() {
     if (e == cudaSuccess) e = raise_smem_limit<false>(dev);
     if (e == cudaSuccess && dev >= 0 && dev < 64) g_attr_done[dev] = true;
     return e;
+}
+
+bool tiled_shaped(const StepDesc &d) {
+    for (int i = 0; i < d.nFree; i++)
+        if ((d.cA[i] != kNoWire) != (i < d.fA)) return false;   // A's free wires first
+    return d.fA >= 2 && d.fB >= 2 && d.fA + d.fB >= 5 && d.nSum >= 1 && d.rA <= 15 && d.rB <= 15 && d.nFree <= 15;
+}
+
+template <bool kMixed>
+static cudaError_t launch_tiled_t(const StepDesc &d, const void *A, const void *B, void *C, cudaStream_t stream) {
+    using V = typename std::conditional<kMixed, float2, double2>::type;
+    const bool wide_m = d.fA >= 3, wide_n = d.fB >= 3;
+    const uint64_t tiles = (1ull << (2 * d.fA)) / (wide_m ? 64 : 16) * ((1ull << (2 * d.fB)) / (wide_n ? 64 : 16));
+    uint64_t grid = tiles;
+    const uint64_t cap = (uint64_t) num_sms() * 4;
+    if (grid > cap) grid = cap;
+    const V *a = static_cast<const V *>(A);
+    const V *b = static_cast<const V *>(B);
+    V *c = static_cast<V *>(C);
+    const size_t smem = kCtaTileBytes;
+    if (wide_m && wide_n) tiled_pair_kernel<kMixed, 4, 4><<<(unsigned) grid, kPlanThreads, smem, stream>>>(a, b, c, d);
+    else if (wide_m) tiled_pair_kernel<kMixed, 4, 1><<<(unsigned) grid, kPlanThreads, smem, stream>>>(a, b, c, d);
+    else tiled_pair_kernel<kMixed, 1, 4><<<(unsigned) grid, kPlanThreads, smem, stream>>>(a, b, c, d);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tiled_pair(const StepDesc &d, const void *A, const void *B, void *C, bool f64,
+                              cudaStream_t stream) {
+    return f64 ? launch_tiled_t<false>(d, A, B, C, stream) : launch_tiled_t<true>(d, A, B, C, stream);
 }
 
 int plan_max_grid(size_t smem_bytes) {

@@ -9,6 +9,13 @@ namespace qtg {
 // rounding; otherwise complex64 with FP32 FMA.
 cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C, bool f64, cudaStream_t stream);
 
+// Wide steps (C = A~ B~ with both gathered sides >= 16 and >= 1024 outputs,
+// A's free wires first, ranks <= 15) as tiled products over the whole GPU;
+// each output sums over k in increasing order (FP64: the reference's rounding).
+bool tiled_shaped(const StepDesc &d);
+cudaError_t launch_tiled_pair(const StepDesc &d, const void *A, const void *B, void *C, bool f64,
+                              cudaStream_t stream);
+
 // Steps with at most kReduceMaxOut outputs and a sum of at least kReduceMinK
 // terms (the final expectation values of large networks).
 constexpr uint64_t kReduceMaxOut = 16;

@@ -85,3 +85,22 @@ def test_long_reduction_steps(ctx, ra, rb, ns):
     got32 = qg.contract_pair_c64(a32, b32, ffa, fi, sa, sb, ctx=ctx)
     # compensated sums: the result is the exact sum of the complex64 products rounded once
     assert np.max(np.abs(got32 - want32)) <= 1e-6 * np.max(np.abs(want32)) + 1e-6
+
+
+@pytest.mark.parametrize("ra,rb,ns", [(7, 7, 2), (8, 6, 3), (6, 8, 2), (7, 5, 1)])
+def test_wide_pair_steps_run_tiled_over_the_gpu(ctx, ra, rb, ns):
+    """Wide single contractions (the steps of plans run one at a time) use the
+    whole-GPU tiled kernel: FP64 bit-exact, complex64 within rounding."""
+    rng = np.random.default_rng(7 * ra + rb + ns)
+    sa = list(rng.permutation(ra)[:ns])
+    sb = list(rng.permutation(rb)[:ns])
+    fa = [i for i in range(ra) if i not in sa]
+    fb = [i for i in range(rb) if i not in sb]
+    ffa, fi = [1] * len(fa) + [0] * len(fb), fa + fb
+    a = rng.standard_normal(4 ** ra) + 1j * rng.standard_normal(4 ** ra)
+    b = rng.standard_normal(4 ** rb) + 1j * rng.standard_normal(4 ** rb)
+    assert np.array_equal(qg.contract_pair(a, b, ffa, fi, sa, sb, ctx=ctx), port.contract_indices(a, b, ffa, fi, sa, sb))
+    a32, b32 = a.astype(np.complex64), b.astype(np.complex64)
+    want = port.contract_indices(a32.astype(np.complex128), b32.astype(np.complex128), ffa, fi, sa, sb)
+    got = qg.contract_pair_c64(a32, b32, ffa, fi, sa, sb, ctx=ctx)
+    assert np.max(np.abs(got - want)) <= 2e-6 * np.sqrt(4 ** ns) * 4
