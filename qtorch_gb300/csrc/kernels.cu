@@ -221,10 +221,13 @@ reduce_exact(const double2 *__restrict__ A, const double2 *__restrict__ B, const
         // this buffer, and the buffer is written again two chunks later
         __syncthreads();
         if (threadIdx.x == 0) {
-            const uint64_t n = K - k0 < (uint64_t) kReduceThreads ? K - k0 : (uint64_t) kReduceThreads;
-            for (uint64_t j = 0; j < n; j++) {
-                cre = __dadd_rn(cre, prod[buf][j].x);
-                cim = __dadd_rn(cim, prod[buf][j].y);
+            const uint32_t n = K - k0 < (uint64_t) kReduceThreads ? (uint32_t) (K - k0) : (uint32_t) kReduceThreads;
+            // loads run ahead of the two dependent add chains
+#pragma unroll 8
+            for (uint32_t j = 0; j < n; j++) {
+                const double2 p = prod[buf][j];
+                cre = __dadd_rn(cre, p.x);
+                cim = __dadd_rn(cim, p.y);
             }
         }
     }
