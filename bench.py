@@ -375,11 +375,11 @@ def run_serving(args):
         srv.drain()
         wall = time.perf_counter() - t0
         lat = {"qaoa": [], "random": [], "qft": []}
-        err = 0.0
+        err = {"qaoa": 0.0, "random": 0.0, "qft": 0.0}
         for (cls, plan), t in zip(reqs, tickets):
             v, l = srv.poll(t)
             lat[cls].append(l)
-            err = max(err, abs(v - ref[id(plan)]))
+            err[cls] = max(err[cls], abs(v - ref[id(plan)]))
         done = len(tickets)
         return lat, wall, err, done
 
@@ -416,7 +416,8 @@ def run_serving(args):
         "requests_per_s": len(reqs) / wall, "completed": done,
         "waves": waves, "mean_requests_per_wave": wave_reqs / max(waves, 1),
         "mean_wave_ms": 1e3 * wave_s / max(waves, 1),
-        "error_vs_fp64_max_abs": max(err, err_sat), "error_bound": 1e-6,
+        "error_vs_fp64_max_abs": max(max(err.values()), max(err_sat.values())),
+        "error_vs_fp64_max_abs_by_class": {k: max(err[k], err_sat[k]) for k in err}, "error_bound": 1e-6,
     }
     ctx.close()
     return out

@@ -149,8 +149,11 @@ bool tensor_cores_enabled() {
 }
 
 qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const void *B, void *C, bool f64) {
-    if (reduce_shaped(d)) {
-        // a long sum into a few outputs: the whole GPU on one sum
+    // a long sum into a few outputs: the whole GPU on one sum.  In complex64
+    // every such reduction (rank <= 2, >= 64 terms) takes the compensated kernel:
+    // these are the expectation values where cancellation lives.
+    const bool small_out = (1ull << (2 * d.nFree)) <= kReduceMaxOut;
+    if (reduce_shaped(d) || (!f64 && small_out && d.nSum >= 3)) {
         if (f64) {
             cudaError_t e = launch_reduce_exact(d, (const double2 *) A, (const double2 *) B, (double2 *) C, ctx->stream);
             ctx->launches++;
