@@ -76,6 +76,9 @@ struct PlanDesc {
     const ushort2 *tables;
     const int32_t *level_cta;    // first CTA-tiled step of each level (tiled steps close their level)
     const uint2 *rotations;      // rotation leaves: (byte offset in the leaf image, RotationKind)
+    // step of every work item (relative to its level's first step), levels
+    // concatenated; null when the plan has too many items (binary search then)
+    const uint8_t *item_step;
     int32_t n_steps;
     int32_t n_levels;
     int32_t n_rank0;

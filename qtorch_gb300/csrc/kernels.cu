@@ -311,12 +311,18 @@ __device__ __forceinline__ double scale2d(double x, int e) {
 
 template <bool kMixed>
 __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, uint32_t total, const char *leaves,
-                           char *ws, PlanSmemHeader &h, const ushort2 *__restrict__ tables) {
+                           char *ws, PlanSmemHeader &h, const ushort2 *__restrict__ tables,
+                           const uint8_t *__restrict__ imap) {
     const int tid = threadIdx.x;
     for (uint32_t base = 0; base < total; base += blockDim.x) {
+        // warps with no item this round skip it (the body has warp-level
+        // collectives only, no CTA barrier)
+        if (base + (tid & ~31) >= total) continue;
         const uint32_t item = base + tid;
         int si = s0;
-        if (item < total) {
+        if (item < total && imap) {
+            si = s0 + imap[item];
+        } else if (item < total) {
             int lo = s0, hi = s1 - 1;   // last step whose first item is <= item
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
@@ -755,6 +761,7 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
         const StepDesc *steps;
         const int32_t *level_start, *rank0_steps, *level_cta;
         const uint2 *rotations;
+        const uint8_t *item_step;
         char *leaves_rw;
         const uint32_t *level_items;
         const ushort2 *tables;
@@ -795,6 +802,8 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
             tables = reinterpret_cast<const ushort2 *>(sbase + (reinterpret_cast<const char *>(P.tables) - gbase));
             level_cta = reinterpret_cast<const int32_t *>(sbase + (reinterpret_cast<const char *>(P.level_cta) - gbase));
             rotations = reinterpret_cast<const uint2 *>(sbase + (reinterpret_cast<const char *>(P.rotations) - gbase));
+            item_step = P.item_step ? reinterpret_cast<const uint8_t *>(sbase + (reinterpret_cast<const char *>(P.item_step) - gbase))
+                                    : nullptr;
             leaves_rw = reinterpret_cast<char *>(stage) + I.plan_bytes;
         } else {
             P = *I.plan;
@@ -805,6 +814,7 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
             tables = P.tables;
             level_cta = P.level_cta;
             rotations = P.rotations;
+            item_step = P.item_step;
             leaves_rw = const_cast<char *>(I.leaves);   // the instance's own leaf image
         }
         leaves = leaves_rw;
@@ -822,9 +832,12 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
             }
             __syncthreads();
         }
+        uint32_t items_before = 0;
         for (int L = 0; L < P.n_levels; L++) {
             const int sc = level_cta[L], s1 = level_start[L + 1];
-            plan_level<kMixed>(steps, level_start[L], sc, level_items[L], leaves, ws, h, tables);
+            plan_level<kMixed>(steps, level_start[L], sc, level_items[L], leaves, ws, h, tables,
+                               item_step ? item_step + items_before : nullptr);
+            items_before += level_items[L];
             for (int s = sc; s < s1; s++) run_tiled<kMixed>(steps[s], s, leaves, ws, h, tile);
             __syncthreads();
         }

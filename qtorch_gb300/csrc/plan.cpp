@@ -288,6 +288,23 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
             }
             p->level_items[prec][L0] = acc;
         }
+        // item -> step map for small plans (replaces the per-item binary search)
+        p->item_step[prec].clear();
+        uint64_t total_items = 0;
+        bool fits = true;
+        for (int L0 = 0; L0 < n_levels; L0++) {
+            total_items += p->level_items[prec][L0];
+            fits = fits && p->level_cta[L0] - p->level_start[L0] <= 256;
+        }
+        if (fits && total_items <= kMaxItemMap) {
+            for (int L0 = 0; L0 < n_levels; L0++) {
+                int si = p->level_start[L0];
+                for (uint32_t item = 0; item < p->level_items[prec][L0]; item++) {
+                    while (si + 1 < p->level_cta[L0] && steps[si + 1].item_start <= item) si++;
+                    p->item_step[prec].push_back((uint8_t) (si - p->level_start[L0]));
+                }
+            }
+        }
     }
     // offset tables for the interpreter when every operand fits 16-bit offsets
     // (same maps for both precisions; offsets in elements)
@@ -344,7 +361,9 @@ qt_status upload_plan(qt_plan *p, int prec) {
     const size_t off_cta = align_up(off_items + items_bytes, 16);
     const size_t rot_bytes = sizeof(uint2) * p->rot_table[prec].size();
     const size_t off_rot = align_up(off_cta + cta_bytes, 16);
-    const size_t off_tab = align_up(off_rot + rot_bytes, 256);
+    const size_t map_bytes = p->item_step[prec].size();
+    const size_t off_map = align_up(off_rot + rot_bytes, 16);
+    const size_t off_tab = align_up(off_map + map_bytes, 256);
     const size_t total = off_tab + tab_bytes + 16;
     void *d = nullptr;
     qt_status s = dev_alloc(ctx, total, &d);
@@ -359,6 +378,8 @@ qt_status upload_plan(qt_plan *p, int prec) {
     pd.tables = reinterpret_cast<const ushort2 *>((char *) d + off_tab);
     pd.level_cta = reinterpret_cast<const int32_t *>((char *) d + off_cta);
     pd.rotations = reinterpret_cast<const uint2 *>((char *) d + off_rot);
+    pd.item_step = map_bytes ? reinterpret_cast<const uint8_t *>((char *) d + off_map) : nullptr;
+    if (map_bytes) std::memcpy(host.data() + off_map, p->item_step[prec].data(), map_bytes);
     if (rot_bytes) std::memcpy(host.data() + off_rot, p->rot_table[prec].data(), rot_bytes);
     if (!p->level_cta.empty())
         std::memcpy(host.data() + off_cta, p->level_cta.data(), cta_bytes - sizeof(int32_t));

@@ -34,6 +34,8 @@ constexpr uint64_t kMaxTableBytes = 64ull << 10;
 // this many complex MACs that runs alone (qt_plan_execute) or in a server wave
 // goes step by step through the whole-GPU kernels instead.
 constexpr int64_t kLoneInstanceMaxMacs = 1ll << 24;
+// plans with at most this many work items carry an item -> step map
+constexpr uint64_t kMaxItemMap = 8192;
 
 }  // namespace qtg
 
@@ -60,6 +62,7 @@ struct qt_plan {
     int n_tiled = 0;                                  // CTA-tiled steps
     std::vector<int32_t> rank0_steps;
     std::vector<uint32_t> level_items[2];             // interpreter work items per level, per precision
+    std::vector<uint8_t> item_step[2];                // step of each work item (empty: none)
     std::vector<ushort2> tables;                      // interpreter offset tables (empty: none)
     std::vector<uint64_t> leaf_off[2];
     uint64_t leaf_bytes[2] = {0, 0};

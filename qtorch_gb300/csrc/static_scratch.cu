@@ -76,8 +76,10 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     const uint64_t off_items = align256(off_r0 + r0_bytes);
     const uint64_t cta_bytes = sizeof(int32_t) * p->level_cta.size();
     const uint64_t off_cta = align256(off_items + items_bytes);
+    const uint64_t map_bytes = p->item_step[prec].size();
+    const uint64_t off_map = align256(off_cta + cta_bytes);
     const uint64_t tab_bytes = sizeof(ushort2) * p->tables.size();
-    const uint64_t off_tab = align256(off_cta + cta_bytes);
+    const uint64_t off_tab = align256(off_map + map_bytes);
     const uint64_t off_inst = align256(off_tab + tab_bytes);
     const uint64_t off_ws = align256(off_inst + sizeof(InstanceDesc));
     const uint64_t total = off_ws + align256(p->ws_bytes[prec]);
@@ -97,6 +99,7 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     pd.level_items = reinterpret_cast<const uint32_t *>(b + off_items);
     pd.tables = reinterpret_cast<const ushort2 *>(b + off_tab);
     pd.level_cta = reinterpret_cast<const int32_t *>(b + off_cta);
+    pd.item_step = map_bytes ? reinterpret_cast<const uint8_t *>(b + off_map) : nullptr;
     pd.n_steps = p->n_steps;
     pd.n_levels = p->n_levels;
     pd.n_rank0 = (int32_t) p->rank0_steps.size();
@@ -122,6 +125,8 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
         e = cudaMemcpyAsync(b + off_items, p->level_items[prec].data(), items_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && cta_bytes)
         e = cudaMemcpyAsync(b + off_cta, p->level_cta.data(), cta_bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && map_bytes)
+        e = cudaMemcpyAsync(b + off_map, p->item_step[prec].data(), map_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && tab_bytes)
         e = cudaMemcpyAsync(b + off_tab, p->tables.data(), tab_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess)
