@@ -6,7 +6,9 @@
 //   Y (2N x 2K) row 2n   = [Br_n | -Bi_n]          -> D[m][2n]   = Re C
 //               row 2n+1 = [Bi_n |  Br_n]          -> D[m][2n+1] = Im C
 // computed with three TF32 products per term (x_hi y_hi + x_hi y_lo + x_lo y_hi,
-// FP32 accumulation in tensor memory), which carries ~21 bits per product.
+// FP32 accumulation in tensor memory); with both parts rounded to nearest the
+// dropped x_lo y_lo and the rounding of the lo parts leave ~2^-21 per product,
+// unbiased.
 //
 // pack_operand writes X and Y (hi and lo planes) already in the UMMA canonical
 // K-major layout without swizzle, tile by tile (128 rows x 32 columns, 16 KB),
@@ -44,10 +46,18 @@ __host__ __device__ inline uint64_t tiled_offset(uint64_t r, uint64_t k, uint64_
     return tile * (kTileBytes / 4) + ((rr / 8) * 8 + kk / 4) * 32 + (rr % 8) * 4 + (kk % 4);
 }
 
+// x -> hi + lo, both exact TF32 values (10 explicit mantissa bits), each rounded
+// to nearest (ties away from zero: add half an ulp of TF32, then clear the 13
+// low bits).  Rounding both parts keeps the errors unbiased: truncation left
+// x_lo with the sign of x, so the dropped x_lo * y_lo term had the sign of every
+// product and accumulated along the summed range (~1e-6 on 1e8-MAC circuits).
+__device__ __forceinline__ float round_tf32(float x) {
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xffffe000u);
+}
+
 __device__ __forceinline__ void split_tf32(float x, float &hi, float &lo) {
-    // hi keeps the top 10 mantissa bits (what a TF32 operand holds), lo the next ones
-    hi = __uint_as_float(__float_as_uint(x) & 0xffffe000u);
-    lo = x - hi;
+    hi = round_tf32(x);
+    lo = round_tf32(x - hi);   // x - hi is exact in FP32
 }
 
 // X: rows m < M, columns j < 2K; Y: rows i < 2N, columns j < 2K (see the file comment).
