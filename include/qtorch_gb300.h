@@ -266,7 +266,10 @@ qt_status qt_batch_set_rotations(qt_batch *b, const double *angles, int64_t n_an
 qt_status qt_batch_set_rotations_device(qt_batch *b, const double *angles, int64_t n_angles);
 /* One evaluation of a prepared batch at new angles in a single call (the inner
  * loop of a QAOA optimiser): qt_batch_set_rotations_device (angles may be NULL
- * to keep the current leaves), qt_batch_run, qt_batch_fetch. */
+ * to keep the current leaves), qt_batch_run, qt_batch_fetch.  From the second
+ * call on a mixed batch with graphs enabled, the interpreter reads the angles
+ * from and writes the values to pinned host memory directly, and one captured
+ * graph launch plus a stream synchronisation make the whole evaluation. */
 qt_status qt_batch_evaluate(qt_batch *b, const double *angles, int64_t n_angles, double *values);
 /* Upload all leaf values again from the host copies (async; part of an end-to-end step). */
 qt_status qt_batch_upload(qt_batch *b);

@@ -405,6 +405,8 @@ static void batch_release(qt_batch *b) {
     dev_free(ctx, b->d_ws);
     dev_free(ctx, b->d_next);
     dev_free(ctx, b->d_angles);
+    dev_free(ctx, b->d_inst_eval);
+    b->d_inst_eval = nullptr;
     b->d_leaves = b->d_inst = b->d_values = b->d_ws = b->d_next = b->d_angles = nullptr;
     b->tile_bytes = 0;
     host_free(ctx, b->h_angles);
@@ -695,12 +697,12 @@ qt_status qt_batch_upload(qt_batch *b) {
                       "leaf upload");
 }
 
-static qt_status batch_launch(qt_batch *b) {
+static qt_status batch_launch(qt_batch *b, const void *instances = nullptr) {
     qt_ctx *ctx = b->ctx;
     const int n_grouped = (int) b->plans.size() - (int) b->stepwise.size();
     if (n_grouped <= 0) return QT_OK;
     PlanLaunch lp{};
-    lp.instances = (const InstanceDesc *) b->d_inst;
+    lp.instances = (const InstanceDesc *) (instances ? instances : b->d_inst);
     lp.n_instances = n_grouped;
     lp.ws_smem_bytes = b->ws_smem_bytes;
     lp.ws_base = (char *) b->d_ws;
@@ -764,20 +766,36 @@ qt_status qt_batch_evaluate(qt_batch *b, const double *angles, int64_t n_angles,
     }
     if (deadline_passed(ctx)) return set_error(ctx, QT_ERR_DEADLINE, "deadline expired");
     if (!b->eval_graph) {
-        // first call: the regular path sets up the angle buffers and the descriptors,
-        // then the whole step -- angles H2D, the grouped launch, values D2H -- is
-        // captured as one graph
+        // first call: the regular path sets up the angle buffers and the
+        // descriptors, then the step is captured as one graph
         qt_status s = qt_batch_set_rotations_device(b, angles, n_angles);
         if (s == QT_OK) s = qt_batch_run(b);
         if (s == QT_OK) s = qt_batch_fetch(b, values);
         if (s != QT_OK) return s;
+        // Zero-copy descriptors: the kernel reads the angles from, and writes the
+        // values to, the pinned host buffers directly (GB300's coherent C2C link),
+        // so the graph is the grouped launch alone -- no copy nodes.
+        std::vector<InstanceDesc> zc = b->inst_desc;
+        void *ha = nullptr, *hv = nullptr;
+        cudaError_t e = cudaHostGetDevicePointer(&ha, b->h_angles, 0);
+        if (e == cudaSuccess) e = cudaHostGetDevicePointer(&hv, b->h_values, 0);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "mapped host buffers");
+        for (size_t j = 0; j < zc.size(); j++) {
+            const int i = b->inst_index[j];
+            zc[j].angles = b->plans[i]->rot_kind.empty() ? nullptr
+                                                         : static_cast<const double *>(ha) + b->inst_angle_off[i];
+            zc[j].value = static_cast<double *>(hv) + 2 * i;
+        }
+        s = dev_alloc(ctx, sizeof(InstanceDesc) * zc.size(), &b->d_inst_eval);
+        if (s != QT_OK) return s;
+        e = cudaMemcpyAsync(b->d_inst_eval, zc.data(), sizeof(InstanceDesc) * zc.size(), cudaMemcpyHostToDevice,
+                            ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "instance descriptor upload");
         cudaGraph_t graph;
-        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return cuda_error(ctx, e, "begin capture");
-        cudaMemcpyAsync(b->d_angles, b->h_angles, sizeof(double) * n_angles, cudaMemcpyHostToDevice, ctx->stream);
-        s = batch_launch(b);
-        cudaMemcpyAsync(b->h_values, b->d_values, sizeof(double) * 2 * b->plans.size(), cudaMemcpyDeviceToHost,
-                        ctx->stream);
+        s = batch_launch(b, b->d_inst_eval);
         e = cudaStreamEndCapture(ctx->stream, &graph);
         if (s != QT_OK) return s;
         if (e != cudaSuccess) return cuda_error(ctx, e, "end capture");

@@ -104,7 +104,8 @@ struct qt_batch {
     void *h_values = nullptr;                         // pinned values
     bool use_graph = false;
     cudaGraphExec_t graph = nullptr;
-    cudaGraphExec_t eval_graph = nullptr;             // qt_batch_evaluate: angles H2D + launch + values D2H
+    cudaGraphExec_t eval_graph = nullptr;             // qt_batch_evaluate: the grouped launch on zero-copy descriptors
+    void *d_inst_eval = nullptr;                      // descriptors with host-mapped angles and values
     bool all_grouped = true;
     std::vector<int> stepwise;                        // instances run step by step
     std::vector<char> in_group;                       // instance runs in the grouped launch
