@@ -233,8 +233,10 @@ namespace {
 // contraction tree.  Ties of the fill score go to the smaller degree (classic
 // min-fill), or, with shallow_ties, first to the wire whose merge reaches the
 // lowest height in the tree (node heights tracked with a union-find).
+// salt != 0 breaks the remaining ties (equal fill, height and degree) with a
+// seeded hash instead of the smallest id, for restarts.
 std::vector<int> min_fill_order(const std::vector<std::set<int>> &adj0, const std::vector<std::array<int, 2>> &ends,
-                                int n_nodes, bool shallow_ties) {
+                                int n_nodes, bool shallow_ties, uint64_t salt = 0, long long slack = 0) {
     const int n = (int) adj0.size();
     std::vector<std::set<int>> adj = adj0;
     std::vector<char> gone(n, 0);
@@ -261,15 +263,42 @@ std::vector<int> min_fill_order(const std::vector<std::set<int>> &adj0, const st
     std::vector<int> order;
     order.reserve(n);
     for (int step = 0; step < n; step++) {
+        // with slack, any wire within `slack` of the smallest fill competes on height
+        long long min_fill = -1;
+        if (slack > 0)
+            for (int v = 0; v < n; v++)
+                if (!gone[v] && (min_fill < 0 || fill[v] < min_fill)) min_fill = fill[v];
         int best = -1, best_h = 0;
+        uint64_t best_key = 0;
+        auto key_of = [&](int v) {
+            uint64_t x = (uint64_t) v * 0x9e3779b97f4a7c15ull ^ salt;   // splitmix64 finaliser
+            x ^= x >> 30;
+            x *= 0xbf58476d1ce4e5b9ull;
+            x ^= x >> 27;
+            x *= 0x94d049bb133111ebull;
+            return x ^ (x >> 31);
+        };
         for (int v = 0; v < n; v++) {
             if (gone[v]) continue;
+            if (slack > 0) {
+                if (fill[v] > min_fill + slack) continue;
+                const int h = merged_height(v);
+                if (best < 0 || h < best_h || (h == best_h && fill[v] < fill[best]) ||
+                    (h == best_h && fill[v] == fill[best] && adj[v].size() < adj[best].size())) {
+                    best = v;
+                    best_h = h;
+                }
+                continue;
+            }
             if (best >= 0 && fill[v] > fill[best]) continue;
             const int h = shallow_ties ? merged_height(v) : 0;
+            const uint64_t key = salt ? key_of(v) : 0;
             if (best < 0 || fill[v] < fill[best] || h < best_h ||
-                (h == best_h && adj[v].size() < adj[best].size())) {
+                (h == best_h && adj[v].size() < adj[best].size()) ||
+                (salt && h == best_h && adj[v].size() == adj[best].size() && key < best_key)) {
                 best = v;
                 best_h = h;
+                best_key = key;
             }
         }
         gone[best] = 1;
@@ -371,10 +400,31 @@ const std::vector<int> &LineGraph::MinFillOrdering() {
     // On the GPU a small network's latency is the height of its contraction
     // tree, a large one's is its MACs: the shallow-tie order is taken when it
     // costs no larger intermediate and at most 1.5x the MACs of classic min-fill.
+    // Candidates: classic min-fill, the shallow-tie order, and for small line
+    // graphs seeded restarts of it (remaining ties at random) and orders that let
+    // wires within 1-3 of the smallest fill compete on height.  The walk with
+    // the lowest estimated GPU time wins among those that create no larger
+    // intermediate than classic min-fill: ~1.5 us per dependent level of the
+    // interpreter plus the MACs at one CTA's ~2e9 complex MAC/s -- height decides
+    // for tiny networks, MACs for large ones.
+    auto est = [](const WalkCost &c) { return 1.5e-6 * c.height + c.macs / 2e9; };
     std::vector<int> classic = min_fill_order(adj, ends, n_nodes, false);
-    std::vector<int> shallow = min_fill_order(adj, ends, n_nodes, true);
-    const WalkCost cc = walk_cost(classic, ends, n_nodes), cs = walk_cost(shallow, ends, n_nodes);
-    const std::vector<int> &pick = (cs.peak <= cc.peak && cs.macs <= 1.5 * cc.macs) ? shallow : classic;
+    const WalkCost cc = walk_cost(classic, ends, n_nodes);
+    std::vector<int> pick = classic;
+    WalkCost pc = cc;
+    const int restarts = n <= 400 ? 8 : 0;
+    for (int r = 0; r <= restarts + (n <= 400 ? 3 : 0); r++) {
+        // r <= restarts: seeded ties; beyond: fill slack 1..3 traded for height
+        const long long slack = r > restarts ? r - restarts : 0;
+        std::vector<int> o = min_fill_order(adj, ends, n_nodes, true,
+                                            (r == 0 || slack) ? 0 : 0x5eed0000ull + (uint64_t) r, slack);
+        const WalkCost c = walk_cost(o, ends, n_nodes);
+        if (c.peak > cc.peak) continue;
+        if (est(c) < est(pc)) {
+            pick = std::move(o);
+            pc = c;
+        }
+    }
     for (int v : pick) mOrder.push_back(v + 1);
     return mOrder;
 }
