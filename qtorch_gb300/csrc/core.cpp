@@ -293,6 +293,8 @@ qt_status qt_ctx_create(int device, void *stream, qt_ctx **out) {
     return QT_OK;
 }
 
+
+
 qt_status qt_ctx_destroy(qt_ctx *ctx) {
     if (!ctx) return QT_ERR_INVALID_ARGUMENT;
     {
@@ -473,3 +475,24 @@ qt_status qt_contract_pair_host(qt_ctx *ctx, const double *a, int rank_a, const 
 }
 
 }  // extern "C"
+
+namespace qtg {
+
+// A context whose own stream has the device's highest (or lowest) priority:
+// CTAs of kernels on a high-priority stream are dispatched before waiting CTAs
+// of lower-priority kernels, so short launches do not queue behind long ones.
+qt_status ctx_create_prioritised(int device, bool high_priority, qt_ctx **out) {
+    qt_status s = qt_ctx_create(device, nullptr, out);
+    if (s != QT_OK) return s;
+    int least = 0, greatest = 0;
+    cudaStream_t st = nullptr;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess &&
+        cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, high_priority ? greatest : least) == cudaSuccess) {
+        cudaStreamDestroy((*out)->stream);
+        (*out)->stream = st;
+    }
+    cudaGetLastError();
+    return QT_OK;
+}
+
+}  // namespace qtg

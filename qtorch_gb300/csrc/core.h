@@ -52,6 +52,8 @@ struct qt_tensor {
 namespace qtg {
 
 void ctx_retain(qt_ctx *ctx);
+// a context with its own stream at the device's highest or lowest priority
+qt_status ctx_create_prioritised(int device, bool high_priority, qt_ctx **out);
 void ctx_release(qt_ctx *ctx);
 qt_status set_error(qt_ctx *ctx, qt_status s, const std::string &msg);
 qt_status cuda_error(qt_ctx *ctx, cudaError_t e, const char *what);

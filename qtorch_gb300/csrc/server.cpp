@@ -183,7 +183,8 @@ qt_status qt_server_create(qt_ctx *ctx, int max_inflight, qt_precision prec, qt_
     const int n_lanes = 3;   // lane 0: light waves only
     s->lanes.resize(n_lanes);
     for (int i = 0; i < n_lanes; i++) {
-        qt_status st = qt_ctx_create(ctx->device, nullptr, &s->lanes[i].ctx);
+        // lane 0 (light waves) launches at the highest stream priority
+        qt_status st = ctx_create_prioritised(ctx->device, i == 0, &s->lanes[i].ctx);
         if (st != QT_OK) {
             for (int j = 0; j < i; j++) qt_ctx_destroy(s->lanes[j].ctx);
             ctx_release(ctx);
