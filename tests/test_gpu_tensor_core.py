@@ -43,11 +43,12 @@ def random_circuit(n, depth, seed):
 
 
 def test_large_circuit_mixed_with_tensor_cores_matches_fp64(ctx):
-    """A 16-qubit depth-12 random circuit: its three heaviest steps (4.3e9 complex
+    """A 16-qubit depth-12 random circuit: its heaviest steps (>= 2^26 complex
     MACs each) are GEMMs; the mixed result stays within 1e-6 of the FP64 one."""
     q = random_circuit(16, 12, 1)
     plan = qg.Plan(q, "Z", ordering="linegraph", ctx=ctx)
-    assert plan.peak_rank >= 12
+    info = plan.step_info(qg.MIXED)
+    assert any(4 ** (int(r[3]) + int(r[4])) >= 1 << 26 for r in info)
     v64 = plan.execute(qg.FP64)
     vmx = plan.execute(qg.MIXED)
     assert abs(vmx - v64) <= 1e-6
