@@ -659,7 +659,7 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
         d.plan_bytes = b->stage_bytes ? (uint32_t) round16(p->dev_bytes[prec]) : 0;
         d.leaf_bytes = (uint32_t) round16(p->leaf_bytes[prec]);
         d.ws_bytes = (uint32_t) ((p->ws_bytes[prec] + 255) / 256 * 256);
-        d.pad = 0;
+        d.n_steps = (uint32_t) p->n_steps;
         d.angles = nullptr;
         inst.push_back(d);
     }

@@ -64,6 +64,18 @@ struct StepDesc {
 constexpr uint32_t kNoTable = 0xffffffffu;
 static_assert(sizeof(StepDesc) % 8 == 0, "StepDesc alignment");
 
+// The fields a work item reads, packed into 32 bytes (two 16-byte loads):
+// the interpreter's per-item path reads these instead of the 152-byte StepDesc.
+struct HotStep {
+    uint32_t a_off, b_off, c_off;   // byte offsets (leaf buffer or workspace)
+    uint32_t tab_off;               // offset tables (kNoTable: none)
+    uint32_t item_start;            // first work item inside the level
+    int16_t a_step, b_step;         // producers (-1: a leaf)
+    uint8_t group_log2, nFree, nSum, flags;   // flags: the low 8 bits of StepFlags
+    uint32_t pad;
+};
+static_assert(sizeof(HotStep) == 32, "HotStep layout");
+
 // One executable plan in device memory.
 struct PlanDesc {
     const StepDesc *steps;       // sorted by level
@@ -79,6 +91,7 @@ struct PlanDesc {
     // step of every work item (relative to its level's first step), levels
     // concatenated; null when the plan has too many items (binary search then)
     const uint8_t *item_step;
+    const HotStep *hot;          // per-step packed fields, same order as steps
     int32_t n_steps;
     int32_t n_levels;
     int32_t n_rank0;
@@ -98,7 +111,7 @@ struct InstanceDesc {
     uint32_t plan_bytes;         // bytes of the plan block (multiple of 16) when it may be staged, else 0
     uint32_t leaf_bytes;         // bytes of the leaf image (multiple of 16)
     uint32_t ws_bytes;           // workspace this instance needs
-    uint32_t pad;
+    uint32_t n_steps;            // steps of the plan (the scale header is cleared before the plan arrives)
     const double *angles;        // rotation angles to build on the device (null: leaves as uploaded)
 };
 

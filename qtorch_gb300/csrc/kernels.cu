@@ -310,9 +310,9 @@ __device__ __forceinline__ double scale2d(double x, int e) {
 }
 
 template <bool kMixed>
-__device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, uint32_t total, const char *leaves,
-                           char *ws, PlanSmemHeader &h, const ushort2 *__restrict__ tables,
-                           const uint8_t *__restrict__ imap) {
+__device__ void plan_level(const StepDesc *__restrict__ steps, const HotStep *__restrict__ hot, int s0, int s1,
+                           uint32_t total, const char *leaves, char *ws, PlanSmemHeader &h,
+                           const ushort2 *__restrict__ tables, const uint8_t *__restrict__ imap) {
     const int tid = threadIdx.x;
     for (uint32_t base = 0; base < total; base += blockDim.x) {
         // warps with no item this round skip it (the body has warp-level
@@ -326,23 +326,39 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
             int lo = s0, hi = s1 - 1;   // last step whose first item is <= item
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
-                if (steps[mid].item_start <= item) lo = mid; else hi = mid - 1;
+                if (hot[mid].item_start <= item) lo = mid; else hi = mid - 1;
             }
             si = lo;
         }
-        const StepDesc &d = steps[si];
-        const uint32_t g = d.group;   // a power of two
-        const uint32_t local = item - d.item_start;
-        const uint32_t c = local >> (__ffs(g) - 1);
+        // the packed fields: two 16-byte shared-memory loads
+        const uint4 w0 = reinterpret_cast<const uint4 *>(hot + si)[0];
+        const uint4 w1 = reinterpret_cast<const uint4 *>(hot + si)[1];
+        HotStep hs;
+        hs.a_off = w0.x;
+        hs.b_off = w0.y;
+        hs.c_off = w0.z;
+        hs.tab_off = w0.w;
+        hs.item_start = w1.x;
+        hs.a_step = (int16_t) (w1.y & 0xffffu);
+        hs.b_step = (int16_t) (w1.y >> 16);
+        hs.group_log2 = (uint8_t) (w1.z & 0xffu);
+        hs.nFree = (uint8_t) ((w1.z >> 8) & 0xffu);
+        hs.nSum = (uint8_t) ((w1.z >> 16) & 0xffu);
+        hs.flags = (uint8_t) (w1.z >> 24);
+        const uint32_t lg = hs.group_log2;
+        const uint32_t g = 1u << lg;
+        const uint32_t local = item - hs.item_start;
+        const uint32_t c = local >> lg;
         const uint32_t lane_k = local & (g - 1);
-        const int nFree = d.nFree, nSum = d.nSum;
+        const int nFree = hs.nFree, nSum = hs.nSum;
         const uint32_t n_out = 1u << (2 * nFree);
         const bool valid = item < total && c < n_out;
         const uint32_t K = 1u << (2 * nSum);
-        const uint32_t flags = d.flags;
-        const char *abase = ((flags & kALeaf) ? leaves : ws) + d.a_off;
-        const char *bbase = ((flags & kBLeaf) ? leaves : ws) + d.b_off;
-        const uint32_t tab = d.tab_off;
+        const uint32_t flags = hs.flags;
+        const char *abase = ((flags & kALeaf) ? leaves : ws) + hs.a_off;
+        const char *bbase = ((flags & kBLeaf) ? leaves : ws) + hs.b_off;
+        const uint32_t tab = hs.tab_off;
+        const StepDesc &d = steps[si];   // full maps, read only where there are no offset tables
         const ushort2 *ktab = tables + tab + n_out;   // used only when tab != kNoTable
         uint32_t oa0 = 0, ob0 = 0;
         if (valid) {
@@ -384,7 +400,7 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
                     for (uint32_t k = 0; k < K; k++)
                         cmac_exact(cre, cim, A[scatter_digits(k, d.posAs, nSum)], B[scatter_digits(k, d.posBs, nSum)]);
                 }
-                reinterpret_cast<double2 *>(ws + d.c_off)[c] = make_double2(cre, cim);
+                reinterpret_cast<double2 *>(ws + hs.c_off)[c] = make_double2(cre, cim);
             }
         } else {
             // f64: a reduction where cancellation lives; accumulated with Dot2
@@ -462,25 +478,25 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, int s0, int s1, u
             const bool writer = valid && lane_k == 0;
             uint32_t magbits = 0;
             if (writer) {
-                const int ma = step_scale(h, d.a_step), mb = step_scale(h, d.b_step);
+                const int ma = step_scale(h, hs.a_step), mb = step_scale(h, hs.b_step);
                 float mag;
                 if (f64) {
                     const double dre = scale2d((double) fre + (double) ere, -(ma + mb));
                     const double dim = scale2d((double) fim + (double) eim, -(ma + mb));
-                    reinterpret_cast<double2 *>(ws + d.c_off)[c] = make_double2(dre, dim);
+                    reinterpret_cast<double2 *>(ws + hs.c_off)[c] = make_double2(dre, dim);
                     // the complex64 copy its consumers read
-                    reinterpret_cast<float2 *>(ws + d.c_off + 16ull * n_out)[c] = make_float2((float) dre, (float) dim);
+                    reinterpret_cast<float2 *>(ws + hs.c_off + 16ull * n_out)[c] = make_float2((float) dre, (float) dim);
                     mag = (float) fmax(fabs(dre), fabs(dim));
                 } else {
                     fre = scale2f(fre, -(ma + mb));
                     fim = scale2f(fim, -(ma + mb));
-                    reinterpret_cast<float2 *>(ws + d.c_off)[c] = make_float2(fre, fim);
+                    reinterpret_cast<float2 *>(ws + hs.c_off)[c] = make_float2(fre, fim);
                     mag = fmaxf(fabsf(fre), fabsf(fim));
                 }
                 magbits = __float_as_uint(mag);
                 if (c == 0) {
-                    const int ea = d.a_step >= 0 ? h.expo[d.a_step] : 0;
-                    const int eb = d.b_step >= 0 ? h.expo[d.b_step] : 0;
+                    const int ea = hs.a_step >= 0 ? h.expo[hs.a_step] : 0;
+                    const int eb = hs.b_step >= 0 ? h.expo[hs.b_step] : 0;
                     h.expo[si] = ea + eb + ma + mb;
                 }
             }
@@ -756,12 +772,20 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
         }
         if (inst >= lp.n_instances) break;
         const InstanceDesc I = lp.instances[inst];
+        if constexpr (kMixed) {
+            // the scale header is cleared while the plan block is in flight
+            for (uint32_t s = threadIdx.x; s < I.n_steps; s += blockDim.x) {
+                h.maxbits[s] = 0;
+                h.expo[s] = 0;
+            }
+        }
         char *const ws = I.ws_bytes <= lp.ws_smem_bytes ? ws_smem : ws_global;
         const bool staged = lp.stage_bytes && I.plan_bytes && I.plan_bytes + I.leaf_bytes <= lp.stage_bytes;
         const StepDesc *steps;
         const int32_t *level_start, *rank0_steps, *level_cta;
         const uint2 *rotations;
         const uint8_t *item_step;
+        const HotStep *hot;
         char *leaves_rw;
         const uint32_t *level_items;
         const ushort2 *tables;
@@ -804,6 +828,7 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
             rotations = reinterpret_cast<const uint2 *>(sbase + (reinterpret_cast<const char *>(P.rotations) - gbase));
             item_step = P.item_step ? reinterpret_cast<const uint8_t *>(sbase + (reinterpret_cast<const char *>(P.item_step) - gbase))
                                     : nullptr;
+            hot = reinterpret_cast<const HotStep *>(sbase + (reinterpret_cast<const char *>(P.hot) - gbase));
             leaves_rw = reinterpret_cast<char *>(stage) + I.plan_bytes;
         } else {
             P = *I.plan;
@@ -815,6 +840,7 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
             level_cta = P.level_cta;
             rotations = P.rotations;
             item_step = P.item_step;
+            hot = P.hot;
             leaves_rw = const_cast<char *>(I.leaves);   // the instance's own leaf image
         }
         leaves = leaves_rw;
@@ -825,17 +851,11 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
                 __syncthreads();
             }
         }
-        if (kMixed) {
-            for (int s = threadIdx.x; s < P.n_steps; s += blockDim.x) {
-                h.maxbits[s] = 0;
-                h.expo[s] = 0;
-            }
-            __syncthreads();
-        }
+        if (kMixed && !staged) __syncthreads();   // the cleared header (staging waited with a barrier)
         uint32_t items_before = 0;
         for (int L = 0; L < P.n_levels; L++) {
             const int sc = level_cta[L], s1 = level_start[L + 1];
-            plan_level<kMixed>(steps, level_start[L], sc, level_items[L], leaves, ws, h, tables,
+            plan_level<kMixed>(steps, hot, level_start[L], sc, level_items[L], leaves, ws, h, tables,
                                item_step ? item_step + items_before : nullptr);
             items_before += level_items[L];
             for (int s = sc; s < s1; s++) run_tiled<kMixed>(steps[s], s, leaves, ws, h, tile);

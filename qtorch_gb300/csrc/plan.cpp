@@ -336,6 +336,27 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
                 for (auto &d : p->steps[prec]) d.tab_off = kNoTable;
         }
     }
+    // packed per-step fields for the work-item path (after the offset tables)
+    for (int prec = 0; prec < 2; prec++) {
+        const std::vector<StepDesc> &steps = p->steps[prec];
+        p->hot[prec].assign(S, HotStep());
+        for (int i = 0; i < S; i++) {
+            const StepDesc &d = steps[i];
+            HotStep &hs = p->hot[prec][i];
+            hs.a_off = (uint32_t) d.a_off;
+            hs.b_off = (uint32_t) d.b_off;
+            hs.c_off = (uint32_t) d.c_off;
+            hs.tab_off = d.tab_off;
+            hs.item_start = d.item_start;
+            hs.a_step = (int16_t) d.a_step;
+            hs.b_step = (int16_t) d.b_step;
+            hs.group_log2 = (uint8_t) __builtin_ctz(d.group ? d.group : 1);
+            hs.nFree = d.nFree;
+            hs.nSum = d.nSum;
+            hs.flags = (uint8_t) d.flags;
+            hs.pad = 0;
+        }
+    }
     p->n_steps = S;
     p->n_levels = n_levels;
     p->grouped = p->max_step_out <= kGroupedMaxRank && p->max_step_k <= kGroupedMaxSum &&
@@ -363,7 +384,9 @@ qt_status upload_plan(qt_plan *p, int prec) {
     const size_t off_rot = align_up(off_cta + cta_bytes, 16);
     const size_t map_bytes = p->item_step[prec].size();
     const size_t off_map = align_up(off_rot + rot_bytes, 16);
-    const size_t off_tab = align_up(off_map + map_bytes, 256);
+    const size_t hot_bytes = sizeof(HotStep) * p->hot[prec].size();
+    const size_t off_hot = align_up(off_map + map_bytes, 16);
+    const size_t off_tab = align_up(off_hot + hot_bytes, 256);
     const size_t total = off_tab + tab_bytes + 16;
     void *d = nullptr;
     qt_status s = dev_alloc(ctx, total, &d);
@@ -379,6 +402,8 @@ qt_status upload_plan(qt_plan *p, int prec) {
     pd.level_cta = reinterpret_cast<const int32_t *>((char *) d + off_cta);
     pd.rotations = reinterpret_cast<const uint2 *>((char *) d + off_rot);
     pd.item_step = map_bytes ? reinterpret_cast<const uint8_t *>((char *) d + off_map) : nullptr;
+    pd.hot = reinterpret_cast<const HotStep *>((char *) d + off_hot);
+    if (hot_bytes) std::memcpy(host.data() + off_hot, p->hot[prec].data(), hot_bytes);
     if (map_bytes) std::memcpy(host.data() + off_map, p->item_step[prec].data(), map_bytes);
     if (rot_bytes) std::memcpy(host.data() + off_rot, p->rot_table[prec].data(), rot_bytes);
     if (!p->level_cta.empty())

@@ -78,8 +78,10 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     const uint64_t off_cta = align256(off_items + items_bytes);
     const uint64_t map_bytes = p->item_step[prec].size();
     const uint64_t off_map = align256(off_cta + cta_bytes);
+    const uint64_t hot_bytes = sizeof(HotStep) * p->hot[prec].size();
+    const uint64_t off_hot = align256(off_map + map_bytes);
     const uint64_t tab_bytes = sizeof(ushort2) * p->tables.size();
-    const uint64_t off_tab = align256(off_map + map_bytes);
+    const uint64_t off_tab = align256(off_hot + hot_bytes);
     const uint64_t off_inst = align256(off_tab + tab_bytes);
     const uint64_t off_ws = align256(off_inst + sizeof(InstanceDesc));
     const uint64_t total = off_ws + align256(p->ws_bytes[prec]);
@@ -100,6 +102,7 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     pd.tables = reinterpret_cast<const ushort2 *>(b + off_tab);
     pd.level_cta = reinterpret_cast<const int32_t *>(b + off_cta);
     pd.item_step = map_bytes ? reinterpret_cast<const uint8_t *>(b + off_map) : nullptr;
+    pd.hot = reinterpret_cast<const HotStep *>(b + off_hot);
     pd.n_steps = p->n_steps;
     pd.n_levels = p->n_levels;
     pd.n_rank0 = (int32_t) p->rank0_steps.size();
@@ -110,7 +113,7 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     inst.plan_bytes = 0;   // read in place from the static array, never staged
     inst.leaf_bytes = 0;
     inst.ws_bytes = (uint32_t) align256(p->ws_bytes[prec]);
-    inst.pad = 0;
+    inst.n_steps = (uint32_t) p->n_steps;
     inst.angles = nullptr;   // the caller's leaves are used as they are
     // the descriptors of the previous call are overwritten; the workspace needs
     // no clearing (every intermediate is written before it is read)
@@ -125,6 +128,8 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
         e = cudaMemcpyAsync(b + off_items, p->level_items[prec].data(), items_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && cta_bytes)
         e = cudaMemcpyAsync(b + off_cta, p->level_cta.data(), cta_bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && hot_bytes)
+        e = cudaMemcpyAsync(b + off_hot, p->hot[prec].data(), hot_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && map_bytes)
         e = cudaMemcpyAsync(b + off_map, p->item_step[prec].data(), map_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && tab_bytes)
