@@ -309,10 +309,23 @@ __device__ __forceinline__ double scale2d(double x, int e) {
     return (e >= -1022 && e <= 1023) ? x * __longlong_as_double((long long) (1023 + e) << 52) : ldexp(x, e);
 }
 
-template <bool kMixed>
+// Mixed plans run first without the power-of-two scaling: every stored value
+// is checked against [2^-60, 2^60] (zeros and FP64-class values pass), and a
+// value outside it -- or inf/NaN -- makes the CTA run the instance again with
+// the scaling.  With |values| <= 2^60 and sums of at most 4^8 terms no product
+// or sum can overflow FP32 and no nonzero product underflows, so a clean
+// unscaled pass is exact FP32 arithmetic on normal numbers.
+constexpr float kUnscaledMax = 1.152921504606847e18f;   // 2^60
+constexpr float kUnscaledMin = 8.673617379884035e-19f;  // 2^-60
+
+__device__ __forceinline__ bool out_of_range(float mag, float mag_min_nonzero) {
+    return !(mag <= kUnscaledMax) || (mag_min_nonzero > 0.f && mag_min_nonzero < kUnscaledMin);
+}
+
+template <bool kMixed, bool kScaled>
 __device__ void plan_level(const StepDesc *__restrict__ steps, const HotStep *__restrict__ hot, int s0, int s1,
                            uint32_t total, const char *leaves, char *ws, PlanSmemHeader &h,
-                           const ushort2 *__restrict__ tables, const uint8_t *__restrict__ imap) {
+                           const ushort2 *__restrict__ tables, const uint8_t *__restrict__ imap, int *bad) {
     const int tid = threadIdx.x;
     for (uint32_t base = 0; base < total; base += blockDim.x) {
         // warps with no item this round skip it (the body has warp-level
@@ -476,6 +489,24 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, const HotStep *__
                 }
             }
             const bool writer = valid && lane_k == 0;
+            if constexpr (!kScaled) {
+                if (writer) {
+                    float mag, lo;
+                    if (f64) {
+                        const double dre = (double) fre + (double) ere, dim = (double) fim + (double) eim;
+                        reinterpret_cast<double2 *>(ws + hs.c_off)[c] = make_double2(dre, dim);
+                        const float2 f = make_float2((float) dre, (float) dim);
+                        reinterpret_cast<float2 *>(ws + hs.c_off + 16ull * n_out)[c] = f;
+                        mag = fmaxf(fabsf(f.x), fabsf(f.y));
+                    } else {
+                        reinterpret_cast<float2 *>(ws + hs.c_off)[c] = make_float2(fre, fim);
+                        mag = fmaxf(fabsf(fre), fabsf(fim));
+                    }
+                    lo = mag;   // a complex value with one tiny part is fine; a tiny magnitude is not
+                    if (out_of_range(mag, lo)) *bad = 1;
+                }
+                continue;
+            }
             uint32_t magbits = 0;
             if (writer) {
                 const int ma = step_scale(h, hs.a_step), mb = step_scale(h, hs.b_step);
@@ -521,7 +552,7 @@ template <bool kMixed, int MI, int NJ>
 __device__ float tiled_tiles(const StepDesc &d, const typename std::conditional<kMixed, float2, double2>::type *A,
                              const typename std::conditional<kMixed, float2, double2>::type *B,
                              typename std::conditional<kMixed, float2, double2>::type *C, int shift,
-                             unsigned char *tile, uint32_t t_first, uint32_t t_stride) {
+                             unsigned char *tile, uint32_t t_first, uint32_t t_stride, float *tmin_out = nullptr) {
     using V = typename std::conditional<kMixed, float2, double2>::type;
     using T = typename std::conditional<kMixed, float, double>::type;
     constexpr uint32_t KC = kMixed ? kCtaTileChunk : kCtaTileChunk / 2;
@@ -535,7 +566,7 @@ __device__ float tiled_tiles(const StepDesc &d, const typename std::conditional<
     const uint32_t M = 1u << (2 * fA), N = 1u << (2 * fB), K = 1u << (2 * nSum);
     const uint32_t kc = K < KC ? K : KC;
     const uint32_t tiles_m = M / TM, n_tiles = tiles_m * (N / TN);
-    float tmax = 0.f;
+    float tmax = 0.f, tmin = 0.f;   // tmin: smallest nonzero magnitude (0: none yet)
     for (uint32_t t = t_first; t < n_tiles; t += t_stride) {
         const uint32_t m0 = (t % tiles_m) * TM, n0 = (t / tiles_m) * TN;
         __syncthreads();   // readers of the previous tile's offsets and slices are done
@@ -590,7 +621,9 @@ __device__ float tiled_tiles(const StepDesc &d, const typename std::conditional<
                 if constexpr (kMixed) {
                     v.x = scale2f(cre[i][j], shift);
                     v.y = scale2f(cim[i][j], shift);
-                    tmax = fmaxf(tmax, fmaxf(fabsf(v.x), fabsf(v.y)));
+                    const float mag = fmaxf(fabsf(v.x), fabsf(v.y));
+                    tmax = fmaxf(tmax, mag);
+                    if (mag > 0.f) tmin = tmin > 0.f ? fminf(tmin, mag) : mag;
                 } else {
                     v.x = cre[i][j];
                     v.y = cim[i][j];
@@ -598,23 +631,28 @@ __device__ float tiled_tiles(const StepDesc &d, const typename std::conditional<
                 C[c] = v;
             }
     }
+    if (tmin_out) *tmin_out = tmin;
     return tmax;
 }
 
-template <bool kMixed, int MI, int NJ>
+template <bool kMixed, bool kScaled, int MI, int NJ>
 __device__ void tiled_step(const StepDesc &d, int si, const char *leaves, char *ws, PlanSmemHeader &h,
-                           unsigned char *tile) {
+                           unsigned char *tile, int *bad) {
     using V = typename std::conditional<kMixed, float2, double2>::type;
     const V *A = reinterpret_cast<const V *>(((d.flags & kALeaf) ? leaves : ws) + d.a_off);
     const V *B = reinterpret_cast<const V *>(((d.flags & kBLeaf) ? leaves : ws) + d.b_off);
     V *C = reinterpret_cast<V *>(ws + d.c_off);
     int ma = 0, mb = 0;
-    if constexpr (kMixed) {
+    if constexpr (kMixed && kScaled) {
         ma = step_scale(h, d.a_step);
         mb = step_scale(h, d.b_step);
     }
-    const float tmax = tiled_tiles<kMixed, MI, NJ>(d, A, B, C, -(ma + mb), tile, 0, 1);
-    if constexpr (kMixed) {
+    float tmin = 0.f;
+    const float tmax = tiled_tiles<kMixed, MI, NJ>(d, A, B, C, -(ma + mb), tile, 0, 1, &tmin);
+    if constexpr (kMixed && !kScaled) {
+        if (out_of_range(tmax, tmin)) *bad = 1;
+    }
+    if constexpr (kMixed && kScaled) {
         const uint32_t tid = threadIdx.x;
         const uint32_t wmax = __reduce_max_sync(0xffffffffu, __float_as_uint(tmax));
         if ((tid & 31u) == 0) atomicMax(&h.maxbits[si], wmax);
@@ -626,14 +664,14 @@ __device__ void tiled_step(const StepDesc &d, int si, const char *leaves, char *
     }
 }
 
-template <bool kMixed>
+template <bool kMixed, bool kScaled>
 __device__ __forceinline__ void run_tiled(const StepDesc &d, int si, const char *leaves, char *ws, PlanSmemHeader &h,
-                                          unsigned char *tile) {
+                                          unsigned char *tile, int *bad) {
     const bool wide_m = d.fA >= 3, wide_n = d.fB >= 3;
-    if (wide_m && wide_n) tiled_step<kMixed, 4, 4>(d, si, leaves, ws, h, tile);
-    else if (wide_m) tiled_step<kMixed, 4, 1>(d, si, leaves, ws, h, tile);
-    else if (wide_n) tiled_step<kMixed, 1, 4>(d, si, leaves, ws, h, tile);
-    else tiled_step<kMixed, 1, 1>(d, si, leaves, ws, h, tile);
+    if (wide_m && wide_n) tiled_step<kMixed, kScaled, 4, 4>(d, si, leaves, ws, h, tile, bad);
+    else if (wide_m) tiled_step<kMixed, kScaled, 4, 1>(d, si, leaves, ws, h, tile, bad);
+    else if (wide_n) tiled_step<kMixed, kScaled, 1, 4>(d, si, leaves, ws, h, tile, bad);
+    else tiled_step<kMixed, kScaled, 1, 1>(d, si, leaves, ws, h, tile, bad);
 }
 
 // The same tiled product as a whole-GPU kernel for steps run one at a time
@@ -755,6 +793,7 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
     unsigned char *stage = region + lp.ws_smem_bytes;
     unsigned char *tile = stage + lp.stage_bytes;
     __shared__ int s_next;
+    __shared__ int s_bad;   // the unscaled pass of the current instance left the safe range
     const uint32_t mbar = smem_addr(mbar_slot);
     if (lp.stage_bytes && threadIdx.x == 0) {
         mbar_init(mbar);
@@ -778,6 +817,7 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
                 h.maxbits[s] = 0;
                 h.expo[s] = 0;
             }
+            if (threadIdx.x == 0) s_bad = 0;
         }
         char *const ws = I.ws_bytes <= lp.ws_smem_bytes ? ws_smem : ws_global;
         const bool staged = lp.stage_bytes && I.plan_bytes && I.plan_bytes + I.leaf_bytes <= lp.stage_bytes;
@@ -852,14 +892,31 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
             }
         }
         if (kMixed && !staged) __syncthreads();   // the cleared header (staging waited with a barrier)
-        uint32_t items_before = 0;
-        for (int L = 0; L < P.n_levels; L++) {
-            const int sc = level_cta[L], s1 = level_start[L + 1];
-            plan_level<kMixed>(steps, hot, level_start[L], sc, level_items[L], leaves, ws, h, tables,
-                               item_step ? item_step + items_before : nullptr);
-            items_before += level_items[L];
-            for (int s = sc; s < s1; s++) run_tiled<kMixed>(steps[s], s, leaves, ws, h, tile);
-            __syncthreads();
+        auto levels = [&](auto scaled) {
+            constexpr bool kScaled = decltype(scaled)::value;
+            uint32_t items_before = 0;
+            for (int L = 0; L < P.n_levels; L++) {
+                const int sc = level_cta[L], s1 = level_start[L + 1];
+                plan_level<kMixed, kScaled>(steps, hot, level_start[L], sc, level_items[L], leaves, ws, h, tables,
+                                            item_step ? item_step + items_before : nullptr, &s_bad);
+                items_before += level_items[L];
+                for (int s = sc; s < s1; s++) run_tiled<kMixed, kScaled>(steps[s], s, leaves, ws, h, tile, &s_bad);
+                __syncthreads();
+            }
+        };
+        if constexpr (kMixed) {
+            levels(std::false_type());
+            if (s_bad) {
+                // a value left the safe range: again, with power-of-two scaling
+                for (uint32_t s = threadIdx.x; s < I.n_steps; s += blockDim.x) {
+                    h.maxbits[s] = 0;
+                    h.expo[s] = 0;
+                }
+                __syncthreads();
+                levels(std::true_type());
+            }
+        } else {
+            levels(std::true_type());
         }
         // final-value rule of src/Network.h:961-965, applied in contraction order
         if (threadIdx.x == 0) {

@@ -121,3 +121,22 @@ def test_mid_size_plans_alone_run_step_by_step(ctx, which):
         v_or, _ = port.replay_value(text, "Z", plan.sequence())
         assert v64 == v_or
     assert abs(plan.execute(qg.MIXED) - v64) <= MIXED_TOL
+
+
+@pytest.mark.parametrize("scale", [1e12, 1e-12])
+def test_values_outside_the_unscaled_range_rerun_with_scaling(ctx, tmp_path, scale):
+    """Mixed plans run first without power-of-two scaling and check every stored
+    value against [2^-60, 2^60]; an unnormalised gate (entries 1e12 or 1e-12,
+    superoperator entries 1e24 / 1e-24) pushes values out -- the value itself is
+    5e71 / 5e-73, beyond FP32 -- the instance runs again with the scaling, and
+    the result still matches FP64 to FP32 relative accuracy."""
+    (tmp_path / "big.gate").write_text(f"{scale} 0 0 ({scale},0)")
+    qasm = "3\ndef1 BIG big.gate\nH 0\nH 1\nCNOT 0 1\nBIG 0\nBIG 1\nRx 0.3 2\nCNOT 1 2\nBIG 2\nH 2\n"
+    plan = qg.Plan(qasm, "0 T T", ordering="linegraph", gate_dir=str(tmp_path), ctx=ctx)
+    v64 = plan.execute(qg.FP64)
+    assert abs(v64) > 0
+    b = qg.Batch(ctx)
+    b.add(plan)
+    vmx = b.execute(qg.MIXED)[0]
+    assert np.isfinite(vmx)
+    assert abs(vmx - v64) <= 1e-5 * abs(v64)
