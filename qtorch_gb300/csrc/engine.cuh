@@ -92,6 +92,9 @@ struct PlanDesc {
     // concatenated; null when the plan has too many items (binary search then)
     const uint8_t *item_step;
     const HotStep *hot;          // per-step packed fields, same order as steps
+    // per level: bits 0-7 the largest lane-group log2 of its work items, bit 8
+    // set when a compensated (FP64-class) step of it uses lane groups
+    const uint32_t *level_meta;
     int32_t n_steps;
     int32_t n_levels;
     int32_t n_rank0;

@@ -325,7 +325,8 @@ __device__ __forceinline__ bool out_of_range(float mag, float mag_min_nonzero) {
 template <bool kMixed, bool kScaled>
 __device__ void plan_level(const StepDesc *__restrict__ steps, const HotStep *__restrict__ hot, int s0, int s1,
                            uint32_t total, const char *leaves, char *ws, PlanSmemHeader &h,
-                           const ushort2 *__restrict__ tables, const uint8_t *__restrict__ imap, int *bad) {
+                           const ushort2 *__restrict__ tables, const uint8_t *__restrict__ imap, int *bad,
+                           uint32_t meta) {
     const int tid = threadIdx.x;
     for (uint32_t base = 0; base < total; base += blockDim.x) {
         // warps with no item this round skip it (the body has warp-level
@@ -466,10 +467,11 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, const HotStep *__
                     }
                 }
             }
-            // lane groups are aligned inside a warp; every lane takes part in the shuffles,
-            // which run only as far as the widest group of the warp needs
-            const uint32_t gmax = __reduce_max_sync(0xffffffffu, valid ? g : 1u);
-            const bool comp = __any_sync(0xffffffffu, valid && f64 && g > 1);
+            // lane groups are aligned inside a warp; every lane takes part in the
+            // shuffles, which run as far as the level's widest group needs (levels
+            // of single-lane items skip them)
+            const uint32_t gmax = 1u << (meta & 0xffu);
+            const bool comp = (meta & 0x100u) != 0;
             for (uint32_t off = gmax >> 1; off >= 1; off >>= 1) {
                 const float ore = __shfl_xor_sync(0xffffffffu, fre, (int) off);
                 const float oim = __shfl_xor_sync(0xffffffffu, fim, (int) off);
@@ -690,14 +692,16 @@ tiled_pair_kernel(const typename std::conditional<kMixed, float2, double2>::type
 // controlled phase's diagonal T[i1 + 4 i2 + 16 i1 + 64 i2] (src/Node.h
 // RxNode .. CPhaseNode).  Rx/Ry/Rz angles are narrowed to float first, as the
 // reference's parser does with std::stof (src/Network.h:342, 383, 402, 422);
-// the trigonometry runs in FP64 and every entry is rounded to complex64 once,
-// like the host-built leaves.
+// the trigonometry runs in FP32 (GB300's FP64 pipe is narrow and this is on
+// every instance's critical path): one sincosf per gate, sin(th)/2 as
+// sin(th/2) cos(th/2).  Entries agree with the host-built complex64 leaves to
+// a few ulp.
 __device__ void build_rotation(char *leaves, uint2 rot, double angle) {
     float2 *t = reinterpret_cast<float2 *>(leaves + rot.x);
-    auto put = [&](int in, int out, double re, double im) { t[in + 4 * out] = make_float2((float) re, (float) im); };
+    auto put = [&](int in, int out, float re, float im) { t[in + 4 * out] = make_float2(re, im); };
     if (rot.y == kRotCPhase) {
-        double s, c;
-        sincos(angle, &s, &c);
+        float s, c;
+        sincosf((float) angle, &s, &c);
         for (int i1 = 0; i1 < 4; i1++)
             for (int i2 = 0; i2 < 4; i2++) {
                 const bool rowph = (i1 >> 1) && (i2 >> 1), colph = (i1 & 1) && (i2 & 1);
@@ -708,29 +712,29 @@ __device__ void build_rotation(char *leaves, uint2 rot, double angle) {
             }
         return;
     }
-    const double th = (double) (float) angle;
+    const float th = (float) angle;
     for (int e = 0; e < 16; e++) t[e] = make_float2(0.f, 0.f);
     if (rot.y == kRotRz) {
-        double s, c;
-        sincos(th, &s, &c);
-        put(0, 0, 1.0, 0.0);
-        put(3, 3, 1.0, 0.0);
+        float s, c;
+        sincosf(th, &s, &c);
+        put(0, 0, 1.f, 0.f);
+        put(3, 3, 1.f, 0.f);
         put(1, 1, c, -s);
         put(2, 2, c, s);
         return;
     }
-    double sh2, ch2;
-    sincos(th / 2.0, &sh2, &ch2);
-    const double cc = ch2 * ch2, ss = sh2 * sh2, sh = sin(th) / 2.0;
-    for (int i = 0; i < 4; i++) put(i, i, cc, 0.0);
+    float sh2, ch2;
+    sincosf(0.5f * th, &sh2, &ch2);
+    const float cc = ch2 * ch2, ss = sh2 * sh2, sh = sh2 * ch2;
+    for (int i = 0; i < 4; i++) put(i, i, cc, 0.f);
     if (rot.y == kRotRx) {
-        put(0, 3, ss, 0.0); put(1, 2, ss, 0.0); put(2, 1, ss, 0.0); put(3, 0, ss, 0.0);
-        put(0, 1, 0.0, sh); put(1, 0, 0.0, sh); put(2, 3, 0.0, sh); put(3, 2, 0.0, sh);
-        put(0, 2, 0.0, -sh); put(1, 3, 0.0, -sh); put(2, 0, 0.0, -sh); put(3, 1, 0.0, -sh);
+        put(0, 3, ss, 0.f); put(1, 2, ss, 0.f); put(2, 1, ss, 0.f); put(3, 0, ss, 0.f);
+        put(0, 1, 0.f, sh); put(1, 0, 0.f, sh); put(2, 3, 0.f, sh); put(3, 2, 0.f, sh);
+        put(0, 2, 0.f, -sh); put(1, 3, 0.f, -sh); put(2, 0, 0.f, -sh); put(3, 1, 0.f, -sh);
     } else {
-        put(0, 3, ss, 0.0); put(3, 0, ss, 0.0); put(1, 2, -ss, 0.0); put(2, 1, -ss, 0.0);
-        put(0, 1, sh, 0.0); put(0, 2, sh, 0.0); put(1, 3, sh, 0.0); put(2, 3, sh, 0.0);
-        put(1, 0, -sh, 0.0); put(2, 0, -sh, 0.0); put(3, 1, -sh, 0.0); put(3, 2, -sh, 0.0);
+        put(0, 3, ss, 0.f); put(3, 0, ss, 0.f); put(1, 2, -ss, 0.f); put(2, 1, -ss, 0.f);
+        put(0, 1, sh, 0.f); put(0, 2, sh, 0.f); put(1, 3, sh, 0.f); put(2, 3, sh, 0.f);
+        put(1, 0, -sh, 0.f); put(2, 0, -sh, 0.f); put(3, 1, -sh, 0.f); put(3, 2, -sh, 0.f);
     }
 }
 
@@ -826,6 +830,7 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
         const uint2 *rotations;
         const uint8_t *item_step;
         const HotStep *hot;
+        const uint32_t *level_meta;
         char *leaves_rw;
         const uint32_t *level_items;
         const ushort2 *tables;
@@ -869,6 +874,7 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
             item_step = P.item_step ? reinterpret_cast<const uint8_t *>(sbase + (reinterpret_cast<const char *>(P.item_step) - gbase))
                                     : nullptr;
             hot = reinterpret_cast<const HotStep *>(sbase + (reinterpret_cast<const char *>(P.hot) - gbase));
+            level_meta = reinterpret_cast<const uint32_t *>(sbase + (reinterpret_cast<const char *>(P.level_meta) - gbase));
             leaves_rw = reinterpret_cast<char *>(stage) + I.plan_bytes;
         } else {
             P = *I.plan;
@@ -881,6 +887,7 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
             rotations = P.rotations;
             item_step = P.item_step;
             hot = P.hot;
+            level_meta = P.level_meta;
             leaves_rw = const_cast<char *>(I.leaves);   // the instance's own leaf image
         }
         leaves = leaves_rw;
@@ -898,7 +905,7 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
             for (int L = 0; L < P.n_levels; L++) {
                 const int sc = level_cta[L], s1 = level_start[L + 1];
                 plan_level<kMixed, kScaled>(steps, hot, level_start[L], sc, level_items[L], leaves, ws, h, tables,
-                                            item_step ? item_step + items_before : nullptr, &s_bad);
+                                            item_step ? item_step + items_before : nullptr, &s_bad, level_meta[L]);
                 items_before += level_items[L];
                 for (int s = sc; s < s1; s++) run_tiled<kMixed, kScaled>(steps[s], s, leaves, ws, h, tile, &s_bad);
                 __syncthreads();
@@ -933,8 +940,8 @@ __global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch 
                     vre = v.x; vim = v.y;
                 }
                 if (kMixed) {
-                    vre = ldexp(vre, h.expo[s]);
-                    vim = ldexp(vim, h.expo[s]);
+                    vre = scale2d(vre, h.expo[s]);
+                    vim = scale2d(vim, h.expo[s]);
                 }
                 if ((fabs(fre) <= 1.0e-30 && fabs(fim) <= 1.0e-30) || (d.flags & kBothRank0)) {
                     fre = vre;

@@ -339,6 +339,17 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
     // packed per-step fields for the work-item path (after the offset tables)
     for (int prec = 0; prec < 2; prec++) {
         const std::vector<StepDesc> &steps = p->steps[prec];
+        p->level_meta[prec].assign(n_levels, 0);
+        for (int L0 = 0; L0 < n_levels; L0++) {
+            uint32_t lg = 0, comp = 0;
+            for (int i = p->level_start[L0]; i < p->level_cta[L0]; i++) {
+                const uint32_t g = steps[i].group ? steps[i].group : 1;
+                const uint32_t l = (uint32_t) __builtin_ctz(g);
+                lg = std::max(lg, l);
+                if (l > 0 && (steps[i].flags & kCF64)) comp = 1;
+            }
+            p->level_meta[prec][L0] = lg | (comp << 8);
+        }
         p->hot[prec].assign(S, HotStep());
         for (int i = 0; i < S; i++) {
             const StepDesc &d = steps[i];
@@ -386,7 +397,9 @@ qt_status upload_plan(qt_plan *p, int prec) {
     const size_t off_map = align_up(off_rot + rot_bytes, 16);
     const size_t hot_bytes = sizeof(HotStep) * p->hot[prec].size();
     const size_t off_hot = align_up(off_map + map_bytes, 16);
-    const size_t off_tab = align_up(off_hot + hot_bytes, 256);
+    const size_t meta_bytes = sizeof(uint32_t) * p->level_meta[prec].size();
+    const size_t off_meta = align_up(off_hot + hot_bytes, 16);
+    const size_t off_tab = align_up(off_meta + meta_bytes, 256);
     const size_t total = off_tab + tab_bytes + 16;
     void *d = nullptr;
     qt_status s = dev_alloc(ctx, total, &d);
@@ -403,6 +416,8 @@ qt_status upload_plan(qt_plan *p, int prec) {
     pd.rotations = reinterpret_cast<const uint2 *>((char *) d + off_rot);
     pd.item_step = map_bytes ? reinterpret_cast<const uint8_t *>((char *) d + off_map) : nullptr;
     pd.hot = reinterpret_cast<const HotStep *>((char *) d + off_hot);
+    pd.level_meta = reinterpret_cast<const uint32_t *>((char *) d + off_meta);
+    if (meta_bytes) std::memcpy(host.data() + off_meta, p->level_meta[prec].data(), meta_bytes);
     if (hot_bytes) std::memcpy(host.data() + off_hot, p->hot[prec].data(), hot_bytes);
     if (map_bytes) std::memcpy(host.data() + off_map, p->item_step[prec].data(), map_bytes);
     if (rot_bytes) std::memcpy(host.data() + off_rot, p->rot_table[prec].data(), rot_bytes);

@@ -64,6 +64,7 @@ struct qt_plan {
     std::vector<uint32_t> level_items[2];             // interpreter work items per level, per precision
     std::vector<uint8_t> item_step[2];                // step of each work item (empty: none)
     std::vector<qtg::HotStep> hot[2];                 // packed per-step fields of the interpreter
+    std::vector<uint32_t> level_meta[2];              // per level: max lane-group log2, compensated groups
     std::vector<ushort2> tables;                      // interpreter offset tables (empty: none)
     std::vector<uint64_t> leaf_off[2];
     uint64_t leaf_bytes[2] = {0, 0};

@@ -80,8 +80,10 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     const uint64_t off_map = align256(off_cta + cta_bytes);
     const uint64_t hot_bytes = sizeof(HotStep) * p->hot[prec].size();
     const uint64_t off_hot = align256(off_map + map_bytes);
+    const uint64_t meta_bytes = sizeof(uint32_t) * p->level_meta[prec].size();
+    const uint64_t off_meta = align256(off_hot + hot_bytes);
     const uint64_t tab_bytes = sizeof(ushort2) * p->tables.size();
-    const uint64_t off_tab = align256(off_hot + hot_bytes);
+    const uint64_t off_tab = align256(off_meta + meta_bytes);
     const uint64_t off_inst = align256(off_tab + tab_bytes);
     const uint64_t off_ws = align256(off_inst + sizeof(InstanceDesc));
     const uint64_t total = off_ws + align256(p->ws_bytes[prec]);
@@ -103,6 +105,7 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     pd.level_cta = reinterpret_cast<const int32_t *>(b + off_cta);
     pd.item_step = map_bytes ? reinterpret_cast<const uint8_t *>(b + off_map) : nullptr;
     pd.hot = reinterpret_cast<const HotStep *>(b + off_hot);
+    pd.level_meta = reinterpret_cast<const uint32_t *>(b + off_meta);
     pd.n_steps = p->n_steps;
     pd.n_levels = p->n_levels;
     pd.n_rank0 = (int32_t) p->rank0_steps.size();
@@ -128,6 +131,8 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
         e = cudaMemcpyAsync(b + off_items, p->level_items[prec].data(), items_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && cta_bytes)
         e = cudaMemcpyAsync(b + off_cta, p->level_cta.data(), cta_bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && meta_bytes)
+        e = cudaMemcpyAsync(b + off_meta, p->level_meta[prec].data(), meta_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && hot_bytes)
         e = cudaMemcpyAsync(b + off_hot, p->hot[prec].data(), hot_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && map_bytes)
