@@ -1,10 +1,11 @@
 """Rotation leaves built on the device from angles (qt_batch_set_rotations_device).
 
 Moving a batch of QAOA terms to a new (gamma, beta) point sends only the
-angles; the interpreter rebuilds the Rx/Rz gate tensors before contracting.
-The result must agree with the host-built leaves (same narrowing of the angle
-to float, entries rounded to complex64 once) and with the FP64 form at the new
-point within the mixed tolerance."""
+angles; the interpreter rebuilds the Rx/Rz gate tensors before contracting
+(same narrowing of the angle to float; FP32 trigonometry, so entries differ
+from the host-built complex64 leaves by a few ulp).  The result must agree with
+the host-built leaves to a few 1e-7 and with the FP64 form at the new point
+within the mixed tolerance."""
 import numpy as np
 import pytest
 
@@ -48,7 +49,7 @@ def test_device_rotations_match_host_rotations(ctx, p, nodes, degree):
     b.upload()
     b.run()
     host = b.fetch()
-    assert np.abs(dev - host).max() <= 1e-7
+    assert np.abs(dev - host).max() <= 5e-7
     want = np.array([qg.Plan(q, m, ordering="linegraph", ctx=ctx).execute(qg.FP64) for q, m in new_terms])
     assert np.abs(dev - want).max() <= MIXED_TOL
 
