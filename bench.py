@@ -263,9 +263,10 @@ def run_batched(ctx, args, stream, flush):
         b.set_rotations(np.array(angles))
         b.prepare(prec)
         b.use_graph(True)
+        policy = b.autotune()[0] if args.autotune else b.launch_policy
         vals = b.execute(prec)
         t = time_steps(b.run, args.batched_steps, 3, stream, flush)
-        res[prec] = (vals, sum(t) / len(t), len(b), b.launches_per_run)
+        res[prec] = (vals, sum(t) / len(t), len(b), b.launches_per_run, policy, b.launch_info())
         b._release()
     n_inst = res[qg.MIXED][2]
     err = np.abs(res[qg.MIXED][0] - res[qg.FP64][0])
@@ -277,7 +278,11 @@ def run_batched(ctx, args, stream, flush):
             "fp64_terms_per_s": fp64_rate, "mixed_over_fp64": mixed_rate / fp64_rate,
             "mixed_ms_per_step": 1e3 * res[qg.MIXED][1], "fp64_ms_per_step": 1e3 * res[qg.FP64][1],
             "error_vs_fp64": {"max_abs": float(err.max()), "mean_abs": float(err.mean())},
-            "launches_per_step": res[qg.MIXED][3]}
+            "launches_per_step": res[qg.MIXED][3],
+            "launch_policy": {"autotuned": bool(args.autotune), "mixed": res[qg.MIXED][4],
+                              "fp64": res[qg.FP64][4],
+                              "mixed_grid": res[qg.MIXED][5]["grid"],
+                              "mixed_smem_bytes": res[qg.MIXED][5]["smem_bytes"]}}
 
 
 from qtorch_gb300.circuits import qft_text, random_circuit_text   # noqa: E402
@@ -497,6 +502,10 @@ def run_engine(args):
         b.prepare(prec)
         b.use_graph(True)
         batches[prec] = b
+    # launch policies (shared-memory regions, CTAs per SM, schedule) chosen by
+    # timing candidates on this batch; part of the setup, not the timed region
+    policies = {prec: (batches[prec].autotune()[0] if args.autotune else batches[prec].launch_policy)
+                for prec in batches}
 
     flush_buf = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
@@ -574,7 +583,9 @@ def run_engine(args):
         "config": {"workload": WORKLOAD, "graph_seed": args.graph_seed, "terms_per_step": n_terms,
                    "angles": "beta,gamma ~ U[0,pi) seeded per rank", "precision": "mixed",
                    "l2": "flushed between steps (256 MiB write), per-step CUDA events",
-                   "parallelism": f"weak: each rank evaluates its own {n_terms} terms per step"},
+                   "parallelism": f"weak: each rank evaluates its own {n_terms} terms per step",
+                   "launch_policy": {"autotuned": bool(args.autotune), "mixed": policies[qg.MIXED],
+                                     "fp64": policies[qg.FP64]}},
         "fp64": {"value": fp64_value, "unit": "terms/s", "ms_per_step": 1e3 * sum_fp64 / args.steps,
                  "parity": "bit-exact with the reference CPU loop under the same ordering"},
         "mixed_over_fp64": value / fp64_value,
@@ -676,7 +687,10 @@ def main():
     ap.add_argument("--only-serving", action="store_true", help="run only the serving workload")
     ap.add_argument("--only-batched", action="store_true",
                     help="run only the batched workload and print its numbers (a small case for profiling)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default launch policies instead of timing candidates (qt_batch_autotune)")
     args = ap.parse_args()
+    args.autotune = not args.no_autotune
     if args.warmup < 3:
         args.warmup = 3
     from qtorch_gb300 import build as qbuild

@@ -260,7 +260,7 @@ qt_status qt_batch_set_rotations(qt_batch *b, const double *angles, int64_t n_an
  * from pinned memory on the context stream), and every following qt_batch_run
  * rebuilds the rotation leaves inside the interpreter before contracting --
  * Rx/Ry/Rz narrowed to float like the reference's parser, the trigonometry in
- * FP64, each entry rounded to complex64.  Batches prepared for QT_PREC_MIXED
+ * FP32 (entries within a few ulp of the host-built complex64 leaves).  Batches prepared for QT_PREC_MIXED
  * only; instances run step by step get their leaves on the host.  A later
  * qt_batch_set_rotations or qt_batch_set_leaves switches back to host leaves. */
 qt_status qt_batch_set_rotations_device(qt_batch *b, const double *angles, int64_t n_angles);
@@ -279,6 +279,63 @@ uint64_t qt_batch_h2d_bytes(const qt_batch *b);
 uint64_t qt_batch_d2h_bytes(const qt_batch *b);
 /* kernels launched by one qt_batch_run */
 int qt_batch_launches_per_run(const qt_batch *b);
+
+/* Launch policy of a batch's grouped launch (no reference counterpart).  Each
+ * interpreter CTA holds, in shared memory, the workspace of instances whose
+ * workspace is at most ws_smem_cap bytes (larger ones use a global slab) and a
+ * staged copy of the plan block + leaf image of instances whose copy is at most
+ * stage_cap bytes (larger ones are read in place).  Larger regions mean fewer
+ * CTAs per SM.  Negative caps take the defaults (32 KiB; 64 KiB, 52 KiB when an
+ * instance has CTA-tiled steps), 0 turns a region off.  ctas_per_sm = 0 runs as
+ * many CTAs as fit; static_schedule = 1 replaces the longest-first dynamic
+ * schedule (used when there are more instances than CTAs) by a round robin in
+ * batch order.  kernel_ctas picks the interpreter's register budget: the
+ * variant compiled for 2 (128 registers a thread), 3 (80) or 4 (64) resident
+ * CTAs per SM -- fewer registers, more warps to hide latency, a few spills;
+ * 0 takes 3 when there are more instances than two CTAs per SM can hold at
+ * once, else 2.  The policy changes where data sits, which CTA runs an
+ * instance and how registers are allocated, never the arithmetic: values are
+ * bit-identical under every policy. */
+typedef struct qt_launch_policy {
+    int32_t ws_smem_cap;
+    int32_t stage_cap;
+    int32_t ctas_per_sm;
+    int32_t static_schedule;
+    int32_t kernel_ctas;
+} qt_launch_policy;
+/* Set the policy; a prepared batch is reconfigured in place (leaves and plan
+ * blocks stay on the device). */
+qt_status qt_batch_set_launch_policy(qt_batch *b, const qt_launch_policy *policy);
+qt_status qt_batch_get_launch_policy(const qt_batch *b, qt_launch_policy *policy);
+/* What the policy resolved to for the prepared batch. */
+typedef struct qt_launch_info {
+    int32_t grid;              /* CTAs of the grouped launch (0: none) */
+    int32_t n_grouped;         /* instances in the grouped launch */
+    int32_t n_stepwise;        /* instances run step by step on the whole GPU */
+    int32_t dynamic_schedule;  /* 1: longest-first dynamic schedule */
+    int32_t n_ws_smem;         /* instances whose workspace is in shared memory */
+    int32_t n_staged;          /* instances staged in shared memory */
+    uint32_t smem_bytes;       /* dynamic shared memory of a CTA */
+    uint32_t ws_smem_bytes;    /*   of which workspace region */
+    uint32_t stage_bytes;      /*   of which staging region */
+    uint32_t tile_bytes;       /*   of which CTA-tile buffers */
+    uint64_t ws_slab_bytes;    /* global workspace slab, all CTAs */
+    int32_t kernel_ctas;       /* register-budget variant of the interpreter */
+    int32_t pad;
+} qt_launch_info;
+qt_status qt_batch_launch_info(const qt_batch *b, qt_launch_info *info);
+/* Autotuner: times the prepared batch's grouped launch (CUDA events on the
+ * context stream, one untimed launch then the median of `reps`, more for
+ * launches shorter than a few hundred microseconds) under candidate
+ * policies -- register budget x workspace cap x staging cap as a grid (they
+ * trade against each other for CTAs per SM), then CTAs per SM and the
+ * schedule one at a time -- and keeps the fastest.  Candidates that resolve to
+ * a configuration already timed, or whose shared memory leaves fewer CTAs per
+ * SM than their register budget when instances outnumber CTAs, are skipped;
+ * the search takes no new candidate after about three seconds.  The chosen policy and its time per launch (microseconds) are returned when the
+ * pointers are non-null.  Runs the batch several times; the values it leaves
+ * are those of the current leaves. */
+qt_status qt_batch_autotune(qt_batch *b, int reps, qt_launch_policy *chosen, double *best_us);
 
 /* ---- QAOA MaxCut term generator (src/maxcut.h:31-233, maxcut.cpp:166-190) --- */
 

@@ -587,6 +587,31 @@ class Batch(_Owned):
     def launches_per_run(self):
         return int(_lib().qt_batch_launches_per_run(self.handle))
 
+    @property
+    def launch_policy(self):
+        """dict of qt_launch_policy (negative caps: defaults)"""
+        pol = _capi.LaunchPolicy()
+        _check(_lib().qt_batch_get_launch_policy(self.handle, ctypes.byref(pol)), self.ctx)
+        return {k: getattr(pol, k) for k, _ in pol._fields_}
+
+    def set_launch_policy(self, ws_smem_cap=-1, stage_cap=-1, ctas_per_sm=0, static_schedule=0, kernel_ctas=0):
+        pol = _capi.LaunchPolicy(ws_smem_cap, stage_cap, ctas_per_sm, static_schedule, kernel_ctas)
+        _check(_lib().qt_batch_set_launch_policy(self.handle, ctypes.byref(pol)), self.ctx)
+
+    def launch_info(self):
+        """dict of qt_launch_info for the prepared batch"""
+        info = _capi.LaunchInfo()
+        _check(_lib().qt_batch_launch_info(self.handle, ctypes.byref(info)), self.ctx)
+        return {k: getattr(info, k) for k, _ in info._fields_}
+
+    def autotune(self, reps=3):
+        """Time candidate launch policies on the prepared batch and keep the
+        fastest; returns (policy dict, microseconds per grouped launch)."""
+        pol = _capi.LaunchPolicy()
+        us = ctypes.c_double()
+        _check(_lib().qt_batch_autotune(self.handle, reps, ctypes.byref(pol), ctypes.byref(us)), self.ctx)
+        return {k: getattr(pol, k) for k, _ in pol._fields_}, us.value
+
 
 class Server(_Owned):
     """Continuous-batching request loop (qt_server_*)."""

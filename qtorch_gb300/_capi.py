@@ -11,6 +11,21 @@ c_int, c_int32, c_int64, c_uint64, c_double, c_char_p, c_void_p, c_size_t, c_uin
 P = ctypes.POINTER
 PP = lambda: P(c_void_p)  # noqa: E731
 
+
+class LaunchPolicy(ctypes.Structure):
+    """qt_launch_policy"""
+    _fields_ = [("ws_smem_cap", c_int32), ("stage_cap", c_int32), ("ctas_per_sm", c_int32),
+                ("static_schedule", c_int32), ("kernel_ctas", c_int32)]
+
+
+class LaunchInfo(ctypes.Structure):
+    """qt_launch_info"""
+    _fields_ = [("grid", c_int32), ("n_grouped", c_int32), ("n_stepwise", c_int32), ("dynamic_schedule", c_int32),
+                ("n_ws_smem", c_int32), ("n_staged", c_int32), ("smem_bytes", ctypes.c_uint32),
+                ("ws_smem_bytes", ctypes.c_uint32), ("stage_bytes", ctypes.c_uint32), ("tile_bytes", ctypes.c_uint32),
+                ("ws_slab_bytes", c_uint64), ("kernel_ctas", c_int32), ("pad", c_int32)]
+
+
 # (name, restype, argtypes)
 SIGNATURES = [
     ("qt_status_string", c_char_p, [c_int]),
@@ -90,6 +105,10 @@ SIGNATURES = [
     ("qt_batch_h2d_bytes", c_uint64, [c_void_p]),
     ("qt_batch_d2h_bytes", c_uint64, [c_void_p]),
     ("qt_batch_launches_per_run", c_int, [c_void_p]),
+    ("qt_batch_set_launch_policy", c_int, [c_void_p, P(LaunchPolicy)]),
+    ("qt_batch_get_launch_policy", c_int, [c_void_p, P(LaunchPolicy)]),
+    ("qt_batch_launch_info", c_int, [c_void_p, P(LaunchInfo)]),
+    ("qt_batch_autotune", c_int, [c_void_p, c_int, P(LaunchPolicy), P(c_double)]),
     ("qt_qaoa_term_text", c_int64, [c_char_p, c_int, P(c_double), c_int, c_char_p, c_int64, c_char_p, c_int64]),
     ("qt_qaoa_num_edges", c_int, [c_char_p]),
     ("qt_random_regular_graph", c_int64, [c_int, c_int, c_uint64, c_char_p, c_int64]),

@@ -1,9 +1,12 @@
 // C ABI over the host library: networks (Network / ContractionTools /
 // LineGraph), plans and batches.
 #include <algorithm>
+#include <chrono>
+#include <cmath>
 #include <cstring>
 #include <fstream>
 #include <new>
+#include <set>
 #include <sstream>
 
 #include "kernels.h"
@@ -567,82 +570,78 @@ static qt_status batch_pack(qt_batch *b) {
     return QT_OK;
 }
 
-qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
-    if (!b || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return QT_ERR_INVALID_ARGUMENT;
+// Launch parameters of the grouped launch under the batch's policy: the shared-
+// memory regions of a CTA, the grid, the schedule, the global workspace slab
+// and the instance descriptors.  Leaf images, values and plan blocks stay where
+// they are, so a policy change (and each autotuner candidate) only re-runs this.
+static qt_status batch_configure(qt_batch *b) {
     qt_ctx *ctx = b->ctx;
-    std::lock_guard<std::recursive_mutex> g(ctx->lock);
-    cudaStreamSynchronize(ctx->stream);
-    batch_release(b);
-    b->prepared_prec = prec;
+    const int prec = b->prepared_prec;
     const int n = (int) b->plans.size();
-    b->stepwise.clear();
-    b->inst_leaf_off.assign(n, 0);
-    b->in_group.assign(n, 0);
-    uint64_t off = 0, ws = 0, ws_small = 0;
+    cudaError_t se = cudaStreamSynchronize(ctx->stream);
+    if (se != cudaSuccess) return cuda_error(ctx, se, "sync");
+    for (cudaGraphExec_t *g : {&b->graph, &b->eval_graph})
+        if (*g) {
+            cudaGraphExecDestroy(*g);
+            *g = nullptr;
+        }
+    dev_free(ctx, b->d_ws);
+    dev_free(ctx, b->d_next);
+    dev_free(ctx, b->d_inst);
+    dev_free(ctx, b->d_inst_eval);
+    b->d_ws = b->d_next = b->d_inst = b->d_inst_eval = nullptr;
+    b->inst_desc.clear();
+    b->inst_index.clear();
+    uint64_t ws = 0;
     int n_grouped = 0;
     bool any_tiled = false;
     for (int i = 0; i < n; i++) {
-        qt_plan *p = b->plans[i];
-        if (!p->grouped || p->flops > b->stepwise_macs) {
-            b->stepwise.push_back(i);
-            continue;
-        }
-        b->in_group[i] = 1;
-        qt_status s = upload_plan(p, prec);
-        if (s != QT_OK) return s;
-        b->inst_leaf_off[i] = off;
-        off += (p->leaf_bytes[prec] + 255) / 256 * 256;
-        const uint64_t w = (p->ws_bytes[prec] + 255) / 256 * 256;
-        ws = std::max<uint64_t>(ws, w);
-        if (w <= kSmemWorkspaceMax) ws_small = std::max<uint64_t>(ws_small, w);
+        if (!b->in_group[i]) continue;
+        const qt_plan *p = b->plans[i];
+        ws = std::max<uint64_t>(ws, (p->ws_bytes[prec] + 255) / 256 * 256);
         any_tiled = any_tiled || p->n_tiled > 0;
         n_grouped++;
     }
-    // shared memory of a CTA: a workspace region as large as the largest workspace
-    // that fits it, a staging region as large as the largest plan block + leaf
-    // image that fits, and the tile buffers when an instance has CTA-tiled steps;
-    // instances beyond either region use the global slab / read in place
-    const uint64_t stage_cap = any_tiled ? kSmemStageMaxTiled : kSmemStageMax;
-    uint64_t stage_small = 0;
+    // a workspace region as large as the largest workspace under the cap, a
+    // staging region as large as the largest plan block + leaf image under the
+    // cap, and the tile buffers when an instance has CTA-tiled steps; instances
+    // beyond either region use the global slab / read in place
+    const qt_launch_policy &pol = b->policy;
+    const uint64_t ws_cap = pol.ws_smem_cap < 0 ? kSmemWorkspaceMax : (uint64_t) pol.ws_smem_cap;
+    const uint64_t stage_cap =
+        pol.stage_cap < 0 ? (any_tiled ? kSmemStageMaxTiled : kSmemStageMax) : (uint64_t) pol.stage_cap;
+    uint64_t ws_small = 0, stage_small = 0;
+    b->header_steps = 1;
     for (int i = 0; i < n; i++) {
-        const qt_plan *p = b->plans[i];
         if (!b->in_group[i]) continue;
+        const qt_plan *p = b->plans[i];
+        const uint64_t w = (p->ws_bytes[prec] + 255) / 256 * 256;
+        if (w <= ws_cap) ws_small = std::max(ws_small, w);
         const uint64_t st = round16(p->dev_bytes[prec]) + round16(p->leaf_bytes[prec]);
-        if (st <= stage_cap) stage_small = std::max<uint64_t>(stage_small, st);
+        if (st <= stage_cap) stage_small = std::max(stage_small, st);
+        b->header_steps = std::max<uint32_t>(b->header_steps, (uint32_t) p->n_steps);
     }
-    b->leaf_bytes = off;
     b->ws_stride = ws;
     b->ws_smem_bytes = (uint32_t) ws_small;
-    b->stage_bytes = b->allow_stage ? (uint32_t) stage_small : 0;
+    b->stage_bytes = (uint32_t) stage_small;
     b->tile_bytes = any_tiled ? kCtaTileBytes : 0;
     b->ws_in_smem = ws <= b->ws_smem_bytes;   // no global slab needed
-    b->grid = std::min(n_grouped, plan_max_grid(kPlanHeaderBytes + 128 + b->ws_smem_bytes + b->stage_bytes + b->tile_bytes));
+    const size_t smem = plan_header_bytes(b->header_steps) + 128 + b->ws_smem_bytes + b->stage_bytes + b->tile_bytes;
+    if (n_grouped && smem > plan_smem_limit())
+        return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "launch policy needs more shared memory than a CTA may have");
+    b->variant = pol.kernel_ctas ? pol.kernel_ctas : (n_grouped > 2 * plan_num_sms() ? 3 : 2);
+    b->grid = n_grouped ? std::min(n_grouped, plan_max_grid(smem, pol.ctas_per_sm, b->variant)) : 0;
     qt_status s = QT_OK;
-    auto chk = [&](cudaError_t e, const char *w) {
-        if (s == QT_OK && e != cudaSuccess) s = cuda_error(ctx, e, w);
-    };
-    if (off) {
-        s = host_alloc(ctx, off, &b->h_leaves);
-        if (s == QT_OK) s = dev_alloc(ctx, off, &b->d_leaves);
-    }
-    if (s == QT_OK && n) {
-        s = host_alloc(ctx, sizeof(double) * 2 * n, &b->h_values);
-        if (s == QT_OK) s = dev_alloc(ctx, sizeof(double) * 2 * n, &b->d_values);
-    }
-    if (s == QT_OK && b->grid > 0 && !b->ws_in_smem) s = dev_alloc(ctx, b->ws_stride * b->grid, &b->d_ws);
+    if (b->grid > 0 && !b->ws_in_smem) s = dev_alloc(ctx, b->ws_stride * b->grid, &b->d_ws);
     // more instances than CTAs: a dynamic schedule over the instances sorted by
-    // estimated cost, longest first
-    if (s == QT_OK && n_grouped > b->grid) s = dev_alloc(ctx, 256, &b->d_next);
-    if (s != QT_OK) {
-        batch_release(b);
-        return s;
-    }
-    // instance descriptors (grouped instances only, packed; longest first under
-    // the dynamic schedule)
+    // estimated cost, longest first (unless the policy asks for a round robin)
+    const bool dynamic = n_grouped > b->grid && !pol.static_schedule;
+    if (s == QT_OK && dynamic) s = dev_alloc(ctx, 256, &b->d_next);
+    if (s != QT_OK) return s;
     std::vector<int> inst_order;
     for (int i = 0; i < n; i++)
         if (b->in_group[i]) inst_order.push_back(i);
-    if (b->d_next) {
+    if (dynamic) {
         auto cost = [&](int i) {
             const qt_plan *p = b->plans[i];
             return (double) p->flops + 2048.0 * p->n_levels;   // MACs plus a per-level latency term
@@ -660,28 +659,65 @@ qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
         d.leaf_bytes = (uint32_t) round16(p->leaf_bytes[prec]);
         d.ws_bytes = (uint32_t) ((p->ws_bytes[prec] + 255) / 256 * 256);
         d.n_steps = (uint32_t) p->n_steps;
-        d.angles = nullptr;
+        d.angles = b->dev_rot && b->d_angles && !p->rot_kind.empty()
+                       ? static_cast<const double *>(b->d_angles) + b->inst_angle_off[i]
+                       : nullptr;
         inst.push_back(d);
     }
     b->inst_desc = inst;
     b->inst_index = inst_order;
+    if (inst.empty()) return QT_OK;
+    s = dev_alloc(ctx, sizeof(InstanceDesc) * inst.size(), &b->d_inst);
+    if (s != QT_OK) return s;
+    cudaError_t e = cudaMemcpyAsync(b->d_inst, inst.data(), sizeof(InstanceDesc) * inst.size(),
+                                    cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);   // the host copy may change again
+    return cuda_error(ctx, e, "instance upload");
+}
+
+qt_status qt_batch_prepare(qt_batch *b, qt_precision prec) {
+    if (!b || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return QT_ERR_INVALID_ARGUMENT;
+    qt_ctx *ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    cudaStreamSynchronize(ctx->stream);
+    batch_release(b);
+    b->prepared_prec = prec;
+    const int n = (int) b->plans.size();
+    b->stepwise.clear();
+    b->inst_leaf_off.assign(n, 0);
+    b->in_group.assign(n, 0);
+    uint64_t off = 0;
+    for (int i = 0; i < n; i++) {
+        qt_plan *p = b->plans[i];
+        if (!p->grouped || p->flops > b->stepwise_macs) {
+            b->stepwise.push_back(i);
+            continue;
+        }
+        b->in_group[i] = 1;
+        qt_status s = upload_plan(p, prec);
+        if (s != QT_OK) return s;
+        b->inst_leaf_off[i] = off;
+        off += (p->leaf_bytes[prec] + 255) / 256 * 256;
+    }
+    b->leaf_bytes = off;
     b->inst_angle_off.assign(n, 0);
     b->n_angles = 0;
     for (int i = 0; i < n; i++) {
         b->inst_angle_off[i] = b->n_angles;
         b->n_angles += (int64_t) b->plans[i]->rot_kind.size();
     }
-    if (!inst.empty()) {
-        s = dev_alloc(ctx, sizeof(InstanceDesc) * inst.size(), &b->d_inst);
-        if (s == QT_OK) {
-            chk(cudaMemcpyAsync(b->d_inst, inst.data(), sizeof(InstanceDesc) * inst.size(), cudaMemcpyHostToDevice,
-                                ctx->stream),
-                "instance upload");
-            chk(cudaStreamSynchronize(ctx->stream), "sync");
-        }
+    qt_status s = QT_OK;
+    if (off) {
+        s = host_alloc(ctx, off, &b->h_leaves);
+        if (s == QT_OK) s = dev_alloc(ctx, off, &b->d_leaves);
     }
+    if (s == QT_OK && n) {
+        s = host_alloc(ctx, sizeof(double) * 2 * n, &b->h_values);
+        if (s == QT_OK) s = dev_alloc(ctx, sizeof(double) * 2 * n, &b->d_values);
+    }
+    if (s == QT_OK) s = batch_configure(b);
     if (s == QT_OK) s = qt_batch_upload(b);   // packs the leaf images and copies them
-    if (s == QT_OK) chk(cudaStreamSynchronize(ctx->stream), "sync");
+    if (s == QT_OK) s = cuda_error(ctx, cudaStreamSynchronize(ctx->stream), "sync");
     if (s != QT_OK) batch_release(b);
     b->dirty = false;
     return s;
@@ -710,9 +746,10 @@ static qt_status batch_launch(qt_batch *b, const void *instances = nullptr) {
     lp.stage_bytes = b->stage_bytes;
     lp.tile_bytes = b->tile_bytes;
     lp.next = (uint32_t *) b->d_next;
+    lp.header_steps = b->header_steps;
     cudaError_t e = cudaSuccess;
     if (lp.next) e = cudaMemsetAsync(lp.next, 0, sizeof(uint32_t), ctx->stream);
-    if (e == cudaSuccess) e = launch_plan(lp, b->prepared_prec == QT_PREC_MIXED, b->grid, ctx->stream);
+    if (e == cudaSuccess) e = launch_plan(lp, b->prepared_prec == QT_PREC_MIXED, b->grid, ctx->stream, b->variant);
     ctx->launches++;
     return cuda_error(ctx, e, "plan kernel launch");
 }
@@ -866,6 +903,168 @@ int qt_batch_launches_per_run(const qt_batch *b) {
     int n = ((int) b->plans.size() - (int) b->stepwise.size()) > 0 ? 1 : 0;
     for (int i : b->stepwise) n += b->plans[i]->n_steps;
     return n;
+}
+
+qt_status qt_batch_set_launch_policy(qt_batch *b, const qt_launch_policy *policy) {
+    if (!b || !policy || policy->ctas_per_sm < 0 || (policy->static_schedule != 0 && policy->static_schedule != 1) ||
+        (policy->kernel_ctas != 0 && std::find(std::begin(kPlanVariants), std::end(kPlanVariants),
+                                               policy->kernel_ctas) == std::end(kPlanVariants)))
+        return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::recursive_mutex> g(b->ctx->lock);
+    const qt_launch_policy old = b->policy;
+    b->policy = *policy;
+    if (b->prepared_prec < 0) return QT_OK;
+    qt_status s = batch_configure(b);
+    if (s != QT_OK) {
+        const std::string why = b->ctx->last_error;
+        b->policy = old;
+        if (batch_configure(b) != QT_OK) batch_release(b);
+        set_error(b->ctx, s, why);
+    }
+    return s;
+}
+
+qt_status qt_batch_get_launch_policy(const qt_batch *b, qt_launch_policy *policy) {
+    if (!b || !policy) return QT_ERR_INVALID_ARGUMENT;
+    *policy = b->policy;
+    return QT_OK;
+}
+
+qt_status qt_batch_launch_info(const qt_batch *b, qt_launch_info *info) {
+    if (!b || !info || b->prepared_prec < 0) return QT_ERR_INVALID_ARGUMENT;
+    qt_launch_info r{};
+    r.grid = b->inst_desc.empty() ? 0 : b->grid;
+    r.n_grouped = (int32_t) b->inst_desc.size();
+    r.n_stepwise = (int32_t) b->stepwise.size();
+    r.dynamic_schedule = b->d_next != nullptr;
+    for (const InstanceDesc &d : b->inst_desc) {
+        r.n_ws_smem += d.ws_bytes <= b->ws_smem_bytes;
+        r.n_staged += b->stage_bytes && d.plan_bytes && d.plan_bytes + d.leaf_bytes <= b->stage_bytes;
+    }
+    r.ws_smem_bytes = b->ws_smem_bytes;
+    r.stage_bytes = b->stage_bytes;
+    r.tile_bytes = b->tile_bytes;
+    r.smem_bytes = plan_header_bytes(b->header_steps) + 128 + b->ws_smem_bytes + b->stage_bytes + b->tile_bytes;
+    r.ws_slab_bytes = b->d_ws ? b->ws_stride * (uint64_t) b->grid : 0;
+    r.kernel_ctas = b->variant;
+    *info = r;
+    return QT_OK;
+}
+
+// Times one grouped launch of the configured batch: one untimed launch, then
+// the median of `reps` launches bracketed by events on the context stream.
+static qt_status time_grouped_launch(qt_batch *b, int reps, cudaEvent_t e0, cudaEvent_t e1, double *us) {
+    qt_ctx *ctx = b->ctx;
+    qt_status s = batch_launch(b);
+    std::vector<float> t;
+    for (int r = 0; r < reps && s == QT_OK; r++) {
+        cudaError_t e = cudaEventRecord(e0, ctx->stream);
+        if (e == cudaSuccess) s = batch_launch(b);
+        if (s != QT_OK) break;
+        e = cudaEventRecord(e1, ctx->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "autotune timing");
+        t.push_back(ms);
+    }
+    if (s != QT_OK) return s;
+    std::sort(t.begin(), t.end());
+    *us = 1e3 * t[t.size() / 2];
+    return QT_OK;
+}
+
+qt_status qt_batch_autotune(qt_batch *b, int reps, qt_launch_policy *chosen, double *best_us) {
+    if (!b || reps < 0 || b->prepared_prec < 0) return QT_ERR_INVALID_ARGUMENT;
+    qt_ctx *ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    if (reps == 0) reps = 3;
+    double best_t = 0;
+    if (b->inst_desc.empty()) {   // nothing in the grouped launch
+        if (chosen) *chosen = b->policy;
+        if (best_us) *best_us = 0;
+        return QT_OK;
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t ce = cudaEventCreate(&e0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return cuda_error(ctx, ce, "autotune events");
+    }
+    // candidates differ in what they resolve to: skip policies that give a
+    // configuration already timed
+    auto key = [&]() {
+        return std::to_string(b->ws_smem_bytes) + "/" + std::to_string(b->stage_bytes) + "/" +
+               std::to_string(b->grid) + "/" + std::to_string(b->d_next != nullptr) + "/" + std::to_string(b->variant);
+    };
+    std::set<std::string> tried;
+    qt_launch_policy best = b->policy;
+    qt_status s = batch_configure(b);
+    if (s == QT_OK) s = time_grouped_launch(b, reps, e0, e1, &best_t);
+    // short launches are noisy: enough repetitions for about 2 ms per
+    // candidate; launches of several milliseconds need one
+    if (s == QT_OK && best_t * reps < 2000.0) {
+        reps = std::min(200, (int) std::ceil(2000.0 / std::max(best_t, 1.0)));
+        s = time_grouped_launch(b, reps, e0, e1, &best_t);
+    } else if (best_t > 5000.0) {
+        reps = 1;
+    }
+    tried.insert(key());
+    // the search stops taking new candidates after about three seconds
+    const auto t_start = std::chrono::steady_clock::now();
+    const int n_grouped = (int) b->inst_desc.size();
+    auto try_policy = [&](const qt_launch_policy &cand) -> qt_status {
+        if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() > 3.0) return QT_OK;
+        b->policy = cand;
+        qt_status cs = batch_configure(b);
+        if (cs == QT_ERR_INVALID_ARGUMENT) return QT_OK;   // does not fit a CTA: not a candidate
+        if (cs != QT_OK) return cs;
+        // with more instances than CTAs, shared memory that leaves fewer CTAs
+        // per SM than the register budget allows only loses warps
+        if (cand.ctas_per_sm == 0 && n_grouped > b->grid && b->grid < plan_num_sms() * b->variant) return QT_OK;
+        if (!tried.insert(key()).second) return QT_OK;
+        double t = 0;
+        cs = time_grouped_launch(b, reps, e0, e1, &t);
+        if (cs == QT_OK && t < 0.99 * best_t) {
+            best_t = t;
+            best = cand;
+        }
+        return cs;
+    };
+    // register budget and shared-memory regions together (they trade against
+    // each other for CTAs per SM), then CTAs per SM and the schedule
+    const int32_t ws_caps[] = {0, 8 << 10, 16 << 10, 32 << 10, 48 << 10, 64 << 10, 96 << 10};
+    const int32_t stage_caps[] = {0, 24 << 10, 52 << 10, 64 << 10, 96 << 10};
+    const qt_launch_policy start = best;
+    for (int32_t v : kPlanVariants)
+        for (int32_t w : ws_caps)
+            for (int32_t st : stage_caps) {
+                qt_launch_policy cand = start;
+                cand.kernel_ctas = v;
+                cand.ws_smem_cap = w;
+                cand.stage_cap = st;
+                if (s == QT_OK) s = try_policy(cand);
+            }
+    for (int32_t c : {1, 2, 3}) {
+        qt_launch_policy cand = best;
+        cand.ctas_per_sm = c;
+        if (s == QT_OK) s = try_policy(cand);
+    }
+    for (int32_t c : {0, 1}) {
+        qt_launch_policy cand = best;
+        cand.static_schedule = c;
+        if (s == QT_OK) s = try_policy(cand);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->policy = best;
+    if (s == QT_OK) s = batch_configure(b);
+    if (s == QT_OK) s = batch_launch(b);   // leave the values of the current leaves
+    if (s == QT_OK) s = cuda_error(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    if (s == QT_OK && chosen) *chosen = best;
+    if (s == QT_OK && best_us) *best_us = best_t;
+    return s;
 }
 
 }  // extern "C"

@@ -21,7 +21,9 @@ constexpr int kMaxWires = 24;      // rank limit of one operand (4^24 elements i
 constexpr uint8_t kNoWire = 0xff;
 constexpr int kPlanThreads = 256;              // threads of one interpreter CTA
 constexpr int kPlanMaxSteps = 1024;            // steps of a plan the interpreter takes
-constexpr int kPlanHeaderBytes = 8 * kPlanMaxSteps;   // per-step scale bookkeeping in shared memory
+// per-step scale bookkeeping in shared memory: 8 bytes a step, for as many
+// steps as the largest plan of a launch has (rounded up to 128 bytes)
+inline __host__ __device__ uint32_t plan_header_bytes(uint32_t steps) { return (8u * steps + 127u) / 128u * 128u; }
 
 enum StepFlags : uint32_t {
     kALeaf = 1u << 0,        // A is read from the leaf buffer (else workspace)
@@ -131,6 +133,8 @@ struct PlanLaunch {
     uint32_t stage_bytes;        // shared memory for a staged plan block + leaf image (0: none)
     uint32_t tile_bytes;         // shared memory for CTA-tiled steps (0: no instance has one)
     uint32_t *next;              // dynamic schedule: instance counter, zero at launch (null: round robin)
+    uint32_t header_steps;       // steps of the largest plan of the launch (scale header size)
+    uint32_t pad2;
 };
 
 __host__ __device__ inline uint64_t scatter_digits(uint64_t x, const uint8_t *pos, int n) {

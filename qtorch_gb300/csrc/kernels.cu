@@ -14,6 +14,7 @@
 //    two (per-tensor exponent) and accumulates the expectation-value
 //    reductions with compensated FP32 dot products (no FP64 arithmetic).
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdint>
 #include <mutex>
 #include <type_traits>
@@ -283,8 +284,8 @@ cudaError_t launch_reduce_exact(const StepDesc &d, const double2 *A, const doubl
 // of 1 (no overflow, no underflow drift) without a separate normalisation pass.
 
 struct PlanSmemHeader {
-    uint32_t maxbits[kPlanMaxSteps];   // float bits of max |S| of each step's output
-    int32_t expo[kPlanMaxSteps];       // E of each step's output
+    uint32_t *maxbits;   // float bits of max |S| of each step's output
+    int32_t *expo;       // E of each step's output
 };
 
 // exponent m of the producer's largest |S| (max = f 2^m, f in [0.5, 1)), from the float bits
@@ -786,12 +787,16 @@ __device__ __forceinline__ void bulk_copy_chunks(unsigned char *dst, const char 
     }
 }
 
-template <bool kMixed>
-__global__ void __launch_bounds__(kPlanThreads, 2) plan_kernel(const PlanLaunch lp) {
+// kMinCtas: the register budget -- the variant is compiled for that many
+// resident CTAs per SM (2: up to 128 registers a thread; 3: 80 and 4: 64, with
+// a few spills), trading single-instance latency for warps per SM
+template <bool kMixed, int kMinCtas>
+__global__ void __launch_bounds__(kPlanThreads, kMinCtas) plan_kernel(const PlanLaunch lp) {
     extern __shared__ __align__(256) unsigned char smem_raw[];
-    PlanSmemHeader &h = *reinterpret_cast<PlanSmemHeader *>(smem_raw);
-    uint64_t *mbar_slot = reinterpret_cast<uint64_t *>(smem_raw + kPlanHeaderBytes);
-    unsigned char *region = smem_raw + kPlanHeaderBytes + 128;
+    const uint32_t header_bytes = plan_header_bytes(lp.header_steps);
+    PlanSmemHeader h{reinterpret_cast<uint32_t *>(smem_raw), reinterpret_cast<int32_t *>(smem_raw + 4u * lp.header_steps)};
+    uint64_t *mbar_slot = reinterpret_cast<uint64_t *>(smem_raw + header_bytes);
+    unsigned char *region = smem_raw + header_bytes + 128;
     char *const ws_smem = reinterpret_cast<char *>(region);
     char *const ws_global = lp.ws_base ? lp.ws_base + (uint64_t) blockIdx.x * lp.ws_stride : nullptr;
     unsigned char *stage = region + lp.ws_smem_bytes;
@@ -994,15 +999,23 @@ cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C
 static std::mutex g_attr_mutex;
 static bool g_attr_done[64];
 
-template <bool kMixed>
-static cudaError_t raise_smem_limit(int dev) {
+using PlanKernelFn = void (*)(const PlanLaunch);
+
+static PlanKernelFn plan_kernel_fn(bool mixed, int ctas) {
+    switch (ctas) {
+    case 3: return mixed ? plan_kernel<true, 3> : plan_kernel<false, 3>;
+    case 4: return mixed ? plan_kernel<true, 4> : plan_kernel<false, 4>;
+    default: return mixed ? plan_kernel<true, 2> : plan_kernel<false, 2>;
+    }
+}
+
+static cudaError_t raise_smem_limit(PlanKernelFn fn, int dev) {
     cudaFuncAttributes fa;
-    cudaError_t e = cudaFuncGetAttributes(&fa, plan_kernel<kMixed>);
+    cudaError_t e = cudaFuncGetAttributes(&fa, fn);
     int optin = 0;
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(plan_kernel<kMixed>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 optin - (int) fa.sharedSizeBytes);
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int) fa.sharedSizeBytes);
     return e;
 }
 
@@ -1012,8 +1025,9 @@ static cudaError_t plan_attributes() {
     if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> g(g_attr_mutex);
     if (dev >= 0 && dev < 64 && g_attr_done[dev]) return cudaSuccess;
-    e = raise_smem_limit<true>(dev);
-    if (e == cudaSuccess) e = raise_smem_limit<false>(dev);
+    for (int ctas : kPlanVariants)
+        for (bool mixed : {true, false})
+            if (e == cudaSuccess) e = raise_smem_limit(plan_kernel_fn(mixed, ctas), dev);
     if (e == cudaSuccess && dev >= 0 && dev < 64) g_attr_done[dev] = true;
     return e;
 }
@@ -1047,27 +1061,49 @@ cudaError_t launch_tiled_pair(const StepDesc &d, const void *A, const void *B, v
     return f64 ? launch_tiled_t<false>(d, A, B, C, stream) : launch_tiled_t<true>(d, A, B, C, stream);
 }
 
-int plan_max_grid(size_t smem_bytes) {
+int plan_num_sms() { return num_sms(); }
+
+int plan_max_grid(size_t smem_bytes, int per_sm_cap, int variant) {
     int per_sm = 0;
     plan_attributes();
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, plan_kernel<true>, kPlanThreads, smem_bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, plan_kernel_fn(true, variant), kPlanThreads, smem_bytes);
     cudaGetLastError();
+    if (per_sm_cap > 0) per_sm = std::min(per_sm, per_sm_cap);
     if (per_sm < 1) per_sm = 1;
     return num_sms() * per_sm;
 }
 
-size_t plan_smem_bytes(const PlanLaunch &lp) {
-    return kPlanHeaderBytes + 128 + lp.ws_smem_bytes + lp.stage_bytes + lp.tile_bytes;
+size_t plan_smem_limit() {
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    size_t static_max = 0;
+    for (int ctas : kPlanVariants)
+        for (bool mixed : {true, false}) {
+            cudaFuncAttributes fa;
+            if (cudaFuncGetAttributes(&fa, plan_kernel_fn(mixed, ctas)) != cudaSuccess) {
+                cudaGetLastError();
+                return 0;
+            }
+            static_max = std::max(static_max, fa.sharedSizeBytes);
+        }
+    return (size_t) optin - static_max;
 }
 
-cudaError_t launch_plan(const PlanLaunch &lp, bool mixed, int grid, cudaStream_t stream) {
+size_t plan_smem_bytes(const PlanLaunch &lp) {
+    return plan_header_bytes(lp.header_steps) + 128 + lp.ws_smem_bytes + lp.stage_bytes + lp.tile_bytes;
+}
+
+cudaError_t launch_plan(const PlanLaunch &lp, bool mixed, int grid, cudaStream_t stream, int variant) {
     if (lp.n_instances <= 0) return cudaSuccess;
     const size_t smem = plan_smem_bytes(lp);
     cudaError_t e = plan_attributes();
     if (e != cudaSuccess) return e;
     if (grid <= 0 || grid > lp.n_instances) grid = lp.n_instances;
-    if (mixed) plan_kernel<true><<<grid, kPlanThreads, smem, stream>>>(lp);
-    else plan_kernel<false><<<grid, kPlanThreads, smem, stream>>>(lp);
+    plan_kernel_fn(mixed, variant)<<<grid, kPlanThreads, smem, stream>>>(lp);
     return cudaGetLastError();
 }
 

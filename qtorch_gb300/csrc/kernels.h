@@ -37,10 +37,18 @@ cudaError_t launch_reduce_exact(const StepDesc &d, const double2 *A, const doubl
 // its shared memory (ws_in_smem; ws_stride bytes after the header) or
 // ws_base + blockIdx.x * ws_stride in global memory; with stage_bytes > 0 each
 // instance's plan block and leaf image are copied into shared memory first.
-cudaError_t launch_plan(const PlanLaunch &lp, bool mixed, int grid, cudaStream_t stream);
+// variant: the register budget, one of kPlanVariants (CTAs per SM it is built for)
+constexpr int kPlanVariants[] = {2, 3, 4};
+constexpr int kPlanDefaultVariant = 2;
+cudaError_t launch_plan(const PlanLaunch &lp, bool mixed, int grid, cudaStream_t stream,
+                        int variant = kPlanDefaultVariant);
 // dynamic shared memory of one interpreter CTA for these parameters
 size_t plan_smem_bytes(const PlanLaunch &lp);
-// resident CTAs of the interpreter for a given dynamic shared memory size
-int plan_max_grid(size_t smem_bytes);
+// CTAs of a grouped launch with this much dynamic shared memory: all SMs times
+// the CTAs of the variant that fit one SM, at most per_sm_cap when positive
+int plan_max_grid(size_t smem_bytes, int per_sm_cap = 0, int variant = kPlanDefaultVariant);
+int plan_num_sms();
+// largest dynamic shared memory an interpreter CTA may have on this device
+size_t plan_smem_limit();
 
 }  // namespace qtg

@@ -96,11 +96,13 @@ struct qt_batch {
     void *d_ws = nullptr;
     void *d_next = nullptr;                           // dynamic-schedule counter (null: round robin)
     uint32_t tile_bytes = 0;
+    uint32_t header_steps = 1;                        // scale header entries per CTA (largest plan)
     uint64_t ws_stride = 0;
     bool ws_in_smem = false;                          // every instance's workspace fits shared memory
     uint32_t ws_smem_bytes = 0;                       // shared-memory workspace region per CTA
     uint32_t stage_bytes = 0;                         // shared memory for staged plan block + leaves
-    bool allow_stage = true;
+    qt_launch_policy policy{-1, -1, 0, 0, 0};          // defaults (qt_batch_set_launch_policy)
+    int variant = 2;                                  // register budget of the interpreter (CTAs per SM)
     int grid = 0;
     void *h_leaves = nullptr;                         // pinned staging of the leaf image
     void *h_values = nullptr;                         // pinned values

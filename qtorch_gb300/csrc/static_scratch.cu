@@ -153,6 +153,7 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
     lp.stage_bytes = 0;
     lp.tile_bytes = p->n_tiled ? kCtaTileBytes : 0;
     lp.next = nullptr;
+    lp.header_steps = (uint32_t) p->n_steps;
     e = launch_plan(lp, prec == QT_PREC_MIXED, 1, ctx->stream);
     ctx->launches++;
     return cuda_error(ctx, e, "plan kernel launch");
