@@ -405,8 +405,6 @@ def run_config3(args):
     line-graph and the seeded stochastic ordering; plus the GEMM-shaped
     contractions that do reach the tcgen05 path (a 16-qubit depth-12 random
     circuit, a 14-qubit QFT), mixed (3xTF32 tensor cores) vs FP64."""
-    import torch
-
     import qtorch_gb300 as qg
     ctx = qg.Context(0)
     dgf = qg.random_regular_graph(50, 3, seed=3)
@@ -421,20 +419,28 @@ def run_config3(args):
             b = qg.Batch(ctx)
             for pl in plans:
                 b.add(pl)
+            b.prepare(prec)
+            b.use_graph(True)
+            policy = b.autotune()[0] if args.autotune else b.launch_policy
             vals = b.execute(prec)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
+            reps = 20
             for _ in range(3):
                 b.run()
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                b.run()
             b.fetch()
-            res[prec] = (vals, (time.perf_counter() - t0) / 3)
+            res[prec] = (vals, (time.perf_counter() - t0) / reps, policy)
             b._release()
         err = np.abs(res[qg.MIXED][0] - res[qg.FP64][0])
         out[ordering] = {"peak_rank_max": max(p.peak_rank for p in plans),
                          "complex_macs": int(sum(p.flops for p in plans)),
                          "mixed_terms_per_s": len(plans) / res[qg.MIXED][1],
                          "fp64_terms_per_s": len(plans) / res[qg.FP64][1],
-                         "error_vs_fp64": {"max_abs": float(err.max()), "mean_abs": float(err.mean())}}
+                         "error_vs_fp64": {"max_abs": float(err.max()), "mean_abs": float(err.mean())},
+                         "timing": "host clock over 20 graph launches after 3 warm-up launches",
+                         "launch_policy": {"mixed": res[qg.MIXED][2], "fp64": res[qg.FP64][2]}}
     gemm = []
     for name, text in (("random 16 qubits depth 12", random_circuit_text(16, 12, 1)), ("QFT 14 qubits", qft_text(14, 5))):
         pl = qg.Plan(text, "Z", ordering="linegraph", ctx=ctx)

@@ -286,16 +286,17 @@ int qt_batch_launches_per_run(const qt_batch *b);
  * staged copy of the plan block + leaf image of instances whose copy is at most
  * stage_cap bytes (larger ones are read in place).  Larger regions mean fewer
  * CTAs per SM.  Negative caps take the defaults (32 KiB; 64 KiB, 52 KiB when an
- * instance has CTA-tiled steps), 0 turns a region off.  ctas_per_sm = 0 runs as
+ * instance has CTA-tiled steps; 16 KiB and no staging when the instances
+ * outnumber two CTAs per SM), 0 turns a region off.  ctas_per_sm = 0 runs as
  * many CTAs as fit; static_schedule = 1 replaces the longest-first dynamic
  * schedule (used when there are more instances than CTAs) by a round robin in
  * batch order.  kernel_ctas picks the interpreter's register budget: the
- * variant compiled for 2 (128 registers a thread), 3 (80) or 4 (64) resident
- * CTAs per SM -- fewer registers, more warps to hide latency, a few spills;
- * 0 takes 3 when there are more instances than two CTAs per SM can hold at
- * once, else 2.  The policy changes where data sits, which CTA runs an
- * instance and how registers are allocated, never the arithmetic: values are
- * bit-identical under every policy. */
+ * variant compiled for 2 (128 registers a thread), 3 (80), 4 (64) or 5 (48)
+ * resident CTAs per SM -- fewer registers, more warps to hide latency, some
+ * spills; 0 takes 4 when the instances outnumber two CTAs per SM, else 2.
+ * The policy changes where data sits, which CTA runs an instance and how
+ * registers are allocated, never the arithmetic: values are bit-identical
+ * under every policy. */
 typedef struct qt_launch_policy {
     int32_t ws_smem_cap;
     int32_t stage_cap;

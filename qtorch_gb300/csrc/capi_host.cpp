@@ -606,10 +606,19 @@ static qt_status batch_configure(qt_batch *b) {
     // staging region as large as the largest plan block + leaf image under the
     // cap, and the tile buffers when an instance has CTA-tiled steps; instances
     // beyond either region use the global slab / read in place
+    // Defaults: a few instances (at most two CTAs per SM) get the 128-register
+    // interpreter and room to keep small workspaces and staged copies in shared
+    // memory; many instances are latency-bound and get the 64-register variant
+    // with four CTAs per SM, which leaves room for small workspaces only.
     const qt_launch_policy &pol = b->policy;
-    const uint64_t ws_cap = pol.ws_smem_cap < 0 ? kSmemWorkspaceMax : (uint64_t) pol.ws_smem_cap;
-    const uint64_t stage_cap =
-        pol.stage_cap < 0 ? (any_tiled ? kSmemStageMaxTiled : kSmemStageMax) : (uint64_t) pol.stage_cap;
+    const bool many = n_grouped > 2 * plan_num_sms();
+    const uint64_t ws_cap = pol.ws_smem_cap >= 0 ? (uint64_t) pol.ws_smem_cap
+                            : many                ? kSmemWorkspaceMaxMany
+                                                  : kSmemWorkspaceMax;
+    const uint64_t stage_cap = pol.stage_cap >= 0 ? (uint64_t) pol.stage_cap
+                               : many             ? 0
+                               : any_tiled        ? kSmemStageMaxTiled
+                                                  : kSmemStageMax;
     uint64_t ws_small = 0, stage_small = 0;
     b->header_steps = 1;
     for (int i = 0; i < n; i++) {
@@ -629,7 +638,7 @@ static qt_status batch_configure(qt_batch *b) {
     const size_t smem = plan_header_bytes(b->header_steps) + 128 + b->ws_smem_bytes + b->stage_bytes + b->tile_bytes;
     if (n_grouped && smem > plan_smem_limit())
         return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "launch policy needs more shared memory than a CTA may have");
-    b->variant = pol.kernel_ctas ? pol.kernel_ctas : (n_grouped > 2 * plan_num_sms() ? 3 : 2);
+    b->variant = pol.kernel_ctas ? pol.kernel_ctas : (many ? 4 : 2);
     b->grid = n_grouped ? std::min(n_grouped, plan_max_grid(smem, pol.ctas_per_sm, b->variant)) : 0;
     qt_status s = QT_OK;
     if (b->grid > 0 && !b->ws_in_smem) s = dev_alloc(ctx, b->ws_stride * b->grid, &b->d_ws);

@@ -310,24 +310,59 @@ __device__ __forceinline__ double scale2d(double x, int e) {
     return (e >= -1022 && e <= 1023) ? x * __longlong_as_double((long long) (1023 + e) << 52) : ldexp(x, e);
 }
 
-// Mixed plans run first without the power-of-two scaling: every stored value
-// is checked against [2^-60, 2^60] (zeros and FP64-class values pass), and a
-// value outside it -- or inf/NaN -- makes the CTA run the instance again with
-// the scaling.  With |values| <= 2^60 and sums of at most 4^8 terms no product
-// or sum can overflow FP32 and no nonzero product underflows, so a clean
-// unscaled pass is exact FP32 arithmetic on normal numbers.
+// Mixed plans run first without the power-of-two scaling.  A stored value
+// above 2^60 -- or inf/NaN -- makes the CTA run the instance again with the
+// scaling; with every magnitude <= 2^60 and sums of at most 4^8 terms no
+// product or sum can overflow FP32.  On the small side what matters is a
+// tensor's largest magnitude, not its smallest: a tensor whose largest
+// magnitude is at least 2^-60 keeps the relative precision of FP32 (products
+// of its entries underflow only where they are 2^-66 or more below the
+// tensor's scale, far under FP32 rounding), whereas a tensor of small entries
+// only could lose its products to underflow.  So a nonzero magnitude below
+// 2^-60 only flags its step; at the end of the level the CTA looks at each
+// flagged step's largest magnitude and reruns with scaling when it is below
+// 2^-60.  (Cancellation residues next to O(1) entries are common in larger
+// light cones and cost nothing this way.)
 constexpr float kUnscaledMax = 1.152921504606847e18f;   // 2^60
 constexpr float kUnscaledMin = 8.673617379884035e-19f;  // 2^-60
 
-__device__ __forceinline__ bool out_of_range(float mag, float mag_min_nonzero) {
-    return !(mag <= kUnscaledMax) || (mag_min_nonzero > 0.f && mag_min_nonzero < kUnscaledMin);
+// range check of one stored magnitude (mag) / of a set with smallest nonzero
+// magnitude tmin, in the unscaled pass
+__device__ __forceinline__ void unscaled_check(float mag, float tmin, int si, PlanSmemHeader &h, int *bad,
+                                               uint32_t &tiny) {
+    if (!(mag <= kUnscaledMax)) {
+        *bad = 1;
+    } else if (tmin > 0.f && tmin < kUnscaledMin) {
+        if (!(h.maxbits[si] & 1u)) atomicOr(&h.maxbits[si], 1u);
+        tiny = 1;
+    }
+}
+
+// End of a level of the unscaled pass: for every step of the level flagged
+// by unscaled_check, whether its output has a magnitude of at least 2^-60
+// (float values; the complex64 copy of a complex128 output).  Uniform across
+// the CTA: the flags were written before the barrier that precedes this.
+__device__ void unscaled_level_check(const StepDesc *__restrict__ steps, int s0, int s1, const char *ws,
+                                     const PlanSmemHeader &h, int *bad) {
+    for (int s = s0; s < s1; s++) {
+        if (!(h.maxbits[s] & 1u)) continue;
+        const StepDesc &d = steps[s];
+        const uint32_t n_out = 1u << (2 * d.nFree);
+        const float2 *v = reinterpret_cast<const float2 *>(ws + d.c_off + ((d.flags & kCF64) ? 16ull * n_out : 0ull));
+        int normal = 0;
+        for (uint32_t e = threadIdx.x; e < n_out; e += blockDim.x) {
+            const float2 x = v[e];
+            normal |= fmaxf(fabsf(x.x), fabsf(x.y)) >= kUnscaledMin;
+        }
+        if (!__syncthreads_or(normal) && threadIdx.x == 0) *bad = 1;
+    }
 }
 
 template <bool kMixed, bool kScaled>
 __device__ void plan_level(const StepDesc *__restrict__ steps, const HotStep *__restrict__ hot, int s0, int s1,
                            uint32_t total, const char *leaves, char *ws, PlanSmemHeader &h,
                            const ushort2 *__restrict__ tables, const uint8_t *__restrict__ imap, int *bad,
-                           uint32_t meta) {
+                           uint32_t meta, uint32_t &tiny) {
     const int tid = threadIdx.x;
     for (uint32_t base = 0; base < total; base += blockDim.x) {
         // warps with no item this round skip it (the body has warp-level
@@ -494,7 +529,7 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, const HotStep *__
             const bool writer = valid && lane_k == 0;
             if constexpr (!kScaled) {
                 if (writer) {
-                    float mag, lo;
+                    float mag;
                     if (f64) {
                         const double dre = (double) fre + (double) ere, dim = (double) fim + (double) eim;
                         reinterpret_cast<double2 *>(ws + hs.c_off)[c] = make_double2(dre, dim);
@@ -505,8 +540,8 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, const HotStep *__
                         reinterpret_cast<float2 *>(ws + hs.c_off)[c] = make_float2(fre, fim);
                         mag = fmaxf(fabsf(fre), fabsf(fim));
                     }
-                    lo = mag;   // a complex value with one tiny part is fine; a tiny magnitude is not
-                    if (out_of_range(mag, lo)) *bad = 1;
+                    // a complex value with one tiny part is fine; a tiny magnitude is flagged
+                    unscaled_check(mag, mag, si, h, bad, tiny);
                 }
                 continue;
             }
@@ -640,7 +675,7 @@ __device__ float tiled_tiles(const StepDesc &d, const typename std::conditional<
 
 template <bool kMixed, bool kScaled, int MI, int NJ>
 __device__ void tiled_step(const StepDesc &d, int si, const char *leaves, char *ws, PlanSmemHeader &h,
-                           unsigned char *tile, int *bad) {
+                           unsigned char *tile, int *bad, uint32_t &tiny) {
     using V = typename std::conditional<kMixed, float2, double2>::type;
     const V *A = reinterpret_cast<const V *>(((d.flags & kALeaf) ? leaves : ws) + d.a_off);
     const V *B = reinterpret_cast<const V *>(((d.flags & kBLeaf) ? leaves : ws) + d.b_off);
@@ -652,9 +687,7 @@ __device__ void tiled_step(const StepDesc &d, int si, const char *leaves, char *
     }
     float tmin = 0.f;
     const float tmax = tiled_tiles<kMixed, MI, NJ>(d, A, B, C, -(ma + mb), tile, 0, 1, &tmin);
-    if constexpr (kMixed && !kScaled) {
-        if (out_of_range(tmax, tmin)) *bad = 1;
-    }
+    if constexpr (kMixed && !kScaled) unscaled_check(tmax, tmin, si, h, bad, tiny);
     if constexpr (kMixed && kScaled) {
         const uint32_t tid = threadIdx.x;
         const uint32_t wmax = __reduce_max_sync(0xffffffffu, __float_as_uint(tmax));
@@ -669,12 +702,12 @@ __device__ void tiled_step(const StepDesc &d, int si, const char *leaves, char *
 
 template <bool kMixed, bool kScaled>
 __device__ __forceinline__ void run_tiled(const StepDesc &d, int si, const char *leaves, char *ws, PlanSmemHeader &h,
-                                          unsigned char *tile, int *bad) {
+                                          unsigned char *tile, int *bad, uint32_t &tiny) {
     const bool wide_m = d.fA >= 3, wide_n = d.fB >= 3;
-    if (wide_m && wide_n) tiled_step<kMixed, kScaled, 4, 4>(d, si, leaves, ws, h, tile, bad);
-    else if (wide_m) tiled_step<kMixed, kScaled, 4, 1>(d, si, leaves, ws, h, tile, bad);
-    else if (wide_n) tiled_step<kMixed, kScaled, 1, 4>(d, si, leaves, ws, h, tile, bad);
-    else tiled_step<kMixed, kScaled, 1, 1>(d, si, leaves, ws, h, tile, bad);
+    if (wide_m && wide_n) tiled_step<kMixed, kScaled, 4, 4>(d, si, leaves, ws, h, tile, bad, tiny);
+    else if (wide_m) tiled_step<kMixed, kScaled, 4, 1>(d, si, leaves, ws, h, tile, bad, tiny);
+    else if (wide_n) tiled_step<kMixed, kScaled, 1, 4>(d, si, leaves, ws, h, tile, bad, tiny);
+    else tiled_step<kMixed, kScaled, 1, 1>(d, si, leaves, ws, h, tile, bad, tiny);
 }
 
 // The same tiled product as a whole-GPU kernel for steps run one at a time
@@ -788,8 +821,8 @@ __device__ __forceinline__ void bulk_copy_chunks(unsigned char *dst, const char 
 }
 
 // kMinCtas: the register budget -- the variant is compiled for that many
-// resident CTAs per SM (2: up to 128 registers a thread; 3: 80 and 4: 64, with
-// a few spills), trading single-instance latency for warps per SM
+// resident CTAs per SM (2: up to 128 registers a thread; 3: 80, 4: 64 and
+// 5: 48, with some spills), trading single-instance latency for warps per SM
 template <bool kMixed, int kMinCtas>
 __global__ void __launch_bounds__(kPlanThreads, kMinCtas) plan_kernel(const PlanLaunch lp) {
     extern __shared__ __align__(256) unsigned char smem_raw[];
@@ -907,13 +940,22 @@ __global__ void __launch_bounds__(kPlanThreads, kMinCtas) plan_kernel(const Plan
         auto levels = [&](auto scaled) {
             constexpr bool kScaled = decltype(scaled)::value;
             uint32_t items_before = 0;
+            uint32_t tiny = 0;   // this thread flagged a step of the level (unscaled pass)
             for (int L = 0; L < P.n_levels; L++) {
                 const int sc = level_cta[L], s1 = level_start[L + 1];
                 plan_level<kMixed, kScaled>(steps, hot, level_start[L], sc, level_items[L], leaves, ws, h, tables,
-                                            item_step ? item_step + items_before : nullptr, &s_bad, level_meta[L]);
+                                            item_step ? item_step + items_before : nullptr, &s_bad, level_meta[L],
+                                            tiny);
                 items_before += level_items[L];
-                for (int s = sc; s < s1; s++) run_tiled<kMixed, kScaled>(steps[s], s, leaves, ws, h, tile, &s_bad);
-                __syncthreads();
+                for (int s = sc; s < s1; s++) run_tiled<kMixed, kScaled>(steps[s], s, leaves, ws, h, tile, &s_bad, tiny);
+                if constexpr (kMixed && !kScaled) {
+                    if (__syncthreads_or(tiny)) {
+                        unscaled_level_check(steps, level_start[L], s1, ws, h, &s_bad);
+                        tiny = 0;
+                    }
+                } else {
+                    __syncthreads();
+                }
             }
         };
         if constexpr (kMixed) {
@@ -1005,6 +1047,7 @@ static PlanKernelFn plan_kernel_fn(bool mixed, int ctas) {
     switch (ctas) {
     case 3: return mixed ? plan_kernel<true, 3> : plan_kernel<false, 3>;
     case 4: return mixed ? plan_kernel<true, 4> : plan_kernel<false, 4>;
+    case 5: return mixed ? plan_kernel<true, 5> : plan_kernel<false, 5>;
     default: return mixed ? plan_kernel<true, 2> : plan_kernel<false, 2>;
     }
 }

@@ -38,7 +38,7 @@ cudaError_t launch_reduce_exact(const StepDesc &d, const double2 *A, const doubl
 // ws_base + blockIdx.x * ws_stride in global memory; with stage_bytes > 0 each
 // instance's plan block and leaf image are copied into shared memory first.
 // variant: the register budget, one of kPlanVariants (CTAs per SM it is built for)
-constexpr int kPlanVariants[] = {2, 3, 4};
+constexpr int kPlanVariants[] = {2, 3, 4, 5};
 constexpr int kPlanDefaultVariant = 2;
 cudaError_t launch_plan(const PlanLaunch &lp, bool mixed, int grid, cudaStream_t stream,
                         int variant = kPlanDefaultVariant);

@@ -24,6 +24,8 @@ constexpr uint64_t kGroupedMaxWorkspace = 96ull << 20;
 // are at most kSmemStageMax are staged there.  The caps keep two CTAs per SM
 // (the register budget allows two), larger instances run from global memory.
 constexpr uint64_t kSmemWorkspaceMax = 32ull << 10;
+// workspace cap when instances outnumber two CTAs per SM (four CTAs per SM)
+constexpr uint64_t kSmemWorkspaceMaxMany = 16ull << 10;
 constexpr uint64_t kSmemStageMax = 64ull << 10;
 // staging cap when the CTA also holds the tile buffers of CTA-tiled steps
 constexpr uint64_t kSmemStageMaxTiled = 52ull << 10;

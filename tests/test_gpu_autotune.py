@@ -40,6 +40,7 @@ POLICIES = [
     dict(kernel_ctas=2),                               # 128 registers a thread
     dict(kernel_ctas=4, ws_smem_cap=16 << 10),         # 64 registers a thread
     dict(kernel_ctas=3, stage_cap=0),
+    dict(kernel_ctas=5, ws_smem_cap=0, stage_cap=0),   # 48 registers a thread
 ]
 
 
@@ -50,7 +51,8 @@ def test_policies_give_identical_values(ctx, prec):
     want = b.fetch()
     base = b.launch_info()
     assert base["n_grouped"] == len(b) and base["dynamic_schedule"] == 1
-    assert base["kernel_ctas"] == 3   # default with more instances than two CTAs per SM hold
+    assert base["kernel_ctas"] == 4   # default with more instances than two CTAs per SM hold
+    assert base["grid"] == 4 * 152 and base["stage_bytes"] == 0
     for pol in POLICIES:
         b.set_launch_policy(**pol)
         info = b.launch_info()
@@ -105,7 +107,7 @@ def test_policy_that_does_not_fit_is_refused(ctx):
     with pytest.raises(qg.QtError):
         b.set_launch_policy(ws_smem_cap=1 << 30, stage_cap=1 << 30)
     with pytest.raises(qg.QtError):
-        b.set_launch_policy(kernel_ctas=5)   # no such variant
+        b.set_launch_policy(kernel_ctas=7)   # no such variant
     assert b.launch_policy == before
     b.run()
     assert np.array_equal(b.fetch(), want)

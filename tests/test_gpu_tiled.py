@@ -140,3 +140,18 @@ def test_values_outside_the_unscaled_range_rerun_with_scaling(ctx, tmp_path, sca
     vmx = b.execute(qg.MIXED)[0]
     assert np.isfinite(vmx)
     assert abs(vmx - v64) <= 1e-5 * abs(v64)
+
+
+def test_tiny_entries_next_to_normal_ones(ctx, tmp_path):
+    """A gate with entries 1 and 1e-12 (superoperator entries down to 1e-24,
+    below 2^-60) next to O(1) ones: the unscaled pass flags those steps, finds
+    their largest magnitudes normal and keeps its result, which must match FP64
+    within the mixed tolerance.  An all-small tensor is the 1e-12 case above."""
+    (tmp_path / "skew.gate").write_text("1 0 0 (1e-12,0)")
+    qasm = "3\ndef1 SKEW skew.gate\nH 0\nH 1\nCNOT 0 1\nSKEW 0\nSKEW 1\nRx 0.3 2\nCNOT 1 2\nSKEW 2\nH 2\n"
+    plan = qg.Plan(qasm, "0 T T", ordering="linegraph", gate_dir=str(tmp_path), ctx=ctx)
+    v64 = plan.execute(qg.FP64)
+    b = qg.Batch(ctx)
+    b.add(plan)
+    vmx = b.execute(qg.MIXED)[0]
+    assert abs(vmx - v64) <= MIXED_TOL
