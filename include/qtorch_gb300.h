@@ -275,6 +275,24 @@ qt_status qt_batch_evaluate(qt_batch *b, const double *angles, int64_t n_angles,
 qt_status qt_batch_upload(qt_batch *b);
 /* Capture qt_batch_run into a CUDA graph and replay it (0 disables). */
 qt_status qt_batch_use_graph(qt_batch *b, int enable);
+/* Resident evaluation (no reference counterpart; GB300's coherent CPU-GPU
+ * link): with idle_seconds > 0, qt_batch_evaluate with angles keeps one CTA per
+ * instance on the GPU between calls, on a stream of the batch's own.  The plan
+ * blocks and leaf images stay staged in shared memory; a call writes the angles
+ * and a request number into pinned host memory, every CTA rebuilds its
+ * rotation leaves, contracts and writes its value and a done flag there, and
+ * the call returns when all flags are set -- no launch, copy or stream
+ * synchronisation per call.  The engine leaves after idle_seconds without a
+ * request and starts again on the next one.  Any other use of the batch
+ * (run, upload, new leaves or rotations, a policy change, prepare, free) stops
+ * it first.  While it runs the GPU is not idle, so device-wide synchronisation
+ * (cudaDeviceSynchronize, cudaFree) waits up to idle_seconds.  Needs a mixed
+ * batch whose instances all run in the grouped launch with one CTA each
+ * (QT_ERR_INVALID_ARGUMENT otherwise).  idle_seconds <= 0 turns it off.
+ * Values are bit-identical with qt_batch_evaluate's other paths. */
+qt_status qt_batch_use_resident(qt_batch *b, double idle_seconds);
+/* How many times the resident engine was launched (starts after idle exits included). */
+uint64_t qt_batch_resident_starts(const qt_batch *b);
 uint64_t qt_batch_h2d_bytes(const qt_batch *b);
 uint64_t qt_batch_d2h_bytes(const qt_batch *b);
 /* kernels launched by one qt_batch_run */

@@ -575,6 +575,16 @@ class Batch(_Owned):
     def use_graph(self, enable=True):
         _check(_lib().qt_batch_use_graph(self.handle, 1 if enable else 0), self.ctx)
 
+    def use_resident(self, idle_seconds=0.5):
+        """Keep one CTA per instance on the GPU between evaluate() calls
+        (qt_batch_use_resident); 0 stops it."""
+        _check(_lib().qt_batch_use_resident(self.handle, float(idle_seconds)), self.ctx)
+
+    @property
+    def resident_starts(self):
+        """launches of the resident engine so far"""
+        return int(_lib().qt_batch_resident_starts(self.handle))
+
     @property
     def h2d_bytes(self):
         return int(_lib().qt_batch_h2d_bytes(self.handle))

@@ -102,6 +102,8 @@ SIGNATURES = [
     ("qt_batch_set_leaves", c_int, [c_void_p, c_int, P(c_double)]),
     ("qt_batch_upload", c_int, [c_void_p]),
     ("qt_batch_use_graph", c_int, [c_void_p, c_int]),
+    ("qt_batch_use_resident", c_int, [c_void_p, c_double]),
+    ("qt_batch_resident_starts", c_uint64, [c_void_p]),
     ("qt_batch_h2d_bytes", c_uint64, [c_void_p]),
     ("qt_batch_d2h_bytes", c_uint64, [c_void_p]),
     ("qt_batch_launches_per_run", c_int, [c_void_p]),

@@ -392,8 +392,156 @@ qt_status qt_plan_execute(qt_ctx *ctx, qt_plan *p, qt_precision prec, double *v)
 
 static qt_status batch_device_rotations(qt_batch *b, bool on);
 
+// Resident evaluation engine (qt_batch_use_resident).
+// Stops the engine if it runs and waits for its CTAs to leave (each polls the
+// request word about once a microsecond).
+static qt_status resident_stop(qt_batch *b) {
+    if (!b->res_running) return QT_OK;
+    __atomic_store_n(&b->h_mail[0], kResidentStop, __ATOMIC_RELEASE);
+    const cudaError_t e = cudaStreamSynchronize(b->res_stream);
+    b->res_running = false;
+    __atomic_store_n(&b->h_mail[0], b->res_seq, __ATOMIC_RELEASE);
+    return cuda_error(b->ctx, e, "resident engine stop");
+}
+
+// Launches the engine on the batch's own stream; requests after first_seq are new.
+static qt_status resident_start(qt_batch *b, uint32_t first_seq) {
+    qt_ctx *ctx = b->ctx;
+    const size_t n = b->inst_desc.size();
+    qt_status s = QT_OK;
+    cudaError_t e = cudaSuccess;
+    if (!b->res_stream) {
+        int lo = 0, hi = 0;
+        cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        e = cudaStreamCreateWithPriority(&b->res_stream, cudaStreamNonBlocking, hi);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "resident stream");
+    }
+    if (!b->h_mail) {
+        void *hm = nullptr;
+        s = host_alloc(ctx, sizeof(uint32_t) * (32 + n), &hm);
+        if (s != QT_OK) return s;
+        b->h_mail = static_cast<uint32_t *>(hm);
+        std::memset(b->h_mail, 0, sizeof(uint32_t) * (32 + n));
+    }
+    if (!b->h_angles && b->n_angles) {
+        void *ha = nullptr;
+        s = host_alloc(ctx, sizeof(double) * b->n_angles, &ha);
+        if (s != QT_OK) return s;
+        b->h_angles = static_cast<double *>(ha);
+    }
+    void *ha = nullptr, *hv = nullptr, *hm = nullptr;
+    if (b->h_angles) e = cudaHostGetDevicePointer(&ha, b->h_angles, 0);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer(&hv, b->h_values, 0);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer(&hm, b->h_mail, 0);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "mapped host buffers");
+    if (!b->d_inst_res) {
+        // descriptor j runs on CTA j: angles from, and the value to, pinned host memory
+        std::vector<InstanceDesc> zc = b->inst_desc;
+        for (size_t j = 0; j < n; j++) {
+            const int i = b->inst_index[j];
+            zc[j].angles = b->plans[i]->rot_kind.empty() ? nullptr
+                                                         : static_cast<const double *>(ha) + b->inst_angle_off[i];
+            zc[j].value = static_cast<double *>(hv) + 2 * i;
+        }
+        s = dev_alloc(ctx, sizeof(InstanceDesc) * n, &b->d_inst_res);
+        if (s != QT_OK) return s;
+        e = cudaMemcpyAsync(b->d_inst_res, zc.data(), sizeof(InstanceDesc) * n, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "resident descriptors");
+    }
+    ResidentLaunch rl{};
+    rl.lp.instances = static_cast<const InstanceDesc *>(b->d_inst_res);
+    rl.lp.n_instances = (int) n;
+    rl.lp.ws_smem_bytes = b->ws_smem_bytes;
+    rl.lp.ws_base = (char *) b->d_ws;
+    rl.lp.ws_stride = b->ws_stride;
+    rl.lp.stage_bytes = b->stage_bytes;
+    rl.lp.tile_bytes = b->tile_bytes;
+    rl.lp.next = nullptr;
+    rl.lp.header_steps = b->header_steps;
+    rl.seq = static_cast<const uint32_t *>(hm);
+    rl.done = static_cast<uint32_t *>(hm) + 32;
+    rl.first_seq = first_seq;
+    rl.idle_polls = (uint32_t) std::min(4.0e9, std::max(1.0, b->res_idle * 1.0e6));
+    for (size_t j = 0; j < n; j++) __atomic_store_n(&b->h_mail[32 + j], 0u, __ATOMIC_RELAXED);   // no flag from a previous run
+    __atomic_store_n(&b->h_mail[0], first_seq, __ATOMIC_RELEASE);
+    e = launch_resident(rl, b->res_stream);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "resident engine launch");
+    ctx->launches++;
+    b->res_starts++;
+    b->res_running = true;
+    return QT_OK;
+}
+
+// One evaluation through the engine: angles into pinned memory, the request
+// number after them, then every CTA's done flag.
+static qt_status resident_evaluate(qt_batch *b, const double *angles, int64_t n_angles, double *values) {
+    qt_ctx *ctx = b->ctx;
+    if (n_angles != b->n_angles) return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "angle count does not match the batch");
+    qt_status s = QT_OK;
+    const size_t n = b->inst_desc.size();
+    auto any_left = [&]() {
+        for (size_t j = 0; j < n; j++)
+            if (__atomic_load_n(&b->h_mail[32 + j], __ATOMIC_ACQUIRE) == kResidentLeft) return true;
+        return false;
+    };
+    if (b->res_running && any_left()) {
+        s = resident_stop(b);   // CTAs leave on their own idle clocks: wait for the rest
+        if (s != QT_OK) return s;
+    }
+    // the previous request is complete, so the pinned angles are free
+    if (b->res_running && n_angles) std::memcpy(b->h_angles, angles, sizeof(double) * n_angles);
+    if (!b->res_running) {
+        s = resident_start(b, b->res_seq);
+        if (s != QT_OK) return s;
+        if (n_angles) std::memcpy(b->h_angles, angles, sizeof(double) * n_angles);
+    }
+    uint32_t seq = b->res_seq + 1;
+    if (seq == 0 || seq >= kResidentLeft) seq = 1;
+    b->res_seq = seq;
+    __atomic_store_n(&b->h_mail[0], seq, __ATOMIC_RELEASE);
+    // Wait for every CTA's flag.  The engine is asked about only after a
+    // millisecond without an answer (a stream query costs more than a request).
+    const auto t0 = std::chrono::steady_clock::now();
+    bool relaunched = false;
+    uint64_t spins = 0;
+    for (size_t j = 0; j < n;) {
+        const uint32_t d = __atomic_load_n(&b->h_mail[32 + j], __ATOMIC_ACQUIRE);
+        if (d == seq) {
+            j++;
+            continue;
+        }
+        bool restart = d == kResidentLeft;   // the CTA left (idle) just before this request
+        if (!restart && (++spins & 1023) == 0) {
+            const double waited = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (waited > 10.0) return set_error(ctx, QT_ERR_CUDA, "resident engine did not answer within 10 s");
+            if (waited > 1e-3) {
+                const cudaError_t q = cudaStreamQuery(b->res_stream);
+                if (q == cudaSuccess) restart = true;   // gone without a word
+                else if (q != cudaErrorNotReady) return cuda_error(ctx, q, "resident engine");
+            }
+        }
+        if (restart) {
+            if (relaunched) return set_error(ctx, QT_ERR_CUDA, "resident engine left without answering");
+            relaunched = true;
+            s = resident_stop(b);
+            if (s == QT_OK) s = resident_start(b, seq - 1);
+            if (s != QT_OK) return s;
+            __atomic_store_n(&b->h_mail[0], seq, __ATOMIC_RELEASE);
+            j = 0;
+        }
+    }
+    std::memcpy(values, b->h_values, sizeof(double) * 2 * b->plans.size());
+    return QT_OK;
+}
+
 static void batch_release(qt_batch *b) {
     qt_ctx *ctx = b->ctx;
+    resident_stop(b);
+    dev_free(ctx, b->d_inst_res);
+    b->d_inst_res = nullptr;
+    host_free(ctx, b->h_mail);
+    b->h_mail = nullptr;
     if (b->graph) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
@@ -436,6 +584,8 @@ qt_status qt_batch_free(qt_batch *b) {
         std::lock_guard<std::recursive_mutex> g(b->ctx->lock);
         cudaStreamSynchronize(b->ctx->stream);
         batch_release(b);
+        if (b->res_stream) cudaStreamDestroy(b->res_stream);
+        b->res_stream = nullptr;
     }
     delete b;   // may drop the context's last reference
     return QT_OK;
@@ -472,6 +622,10 @@ qt_status qt_batch_set_leaves(qt_batch *b, int i, const double *leaves) {
 
 // Device rotations on/off: the descriptors carry the angle pointers or null.
 static qt_status batch_device_rotations(qt_batch *b, bool on) {
+    if (b->res_running) {
+        qt_status s = resident_stop(b);
+        if (s != QT_OK) return s;
+    }
     if (b->dev_rot == on || b->inst_desc.empty()) {
         b->dev_rot = on;
         return QT_OK;
@@ -499,20 +653,25 @@ qt_status qt_batch_set_rotations_device(qt_batch *b, const double *angles, int64
         return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "device rotations need a batch prepared for QT_PREC_MIXED");
     if (n_angles != b->n_angles) return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "angle count does not match the batch");
     if (!n_angles) return QT_OK;
-    qt_status s = QT_OK;
-    if (!b->d_angles) {
+    qt_status s = resident_stop(b);
+    if (s != QT_OK) return s;
+    if (!b->h_angles) {
         void *ha = nullptr;
         s = host_alloc(ctx, sizeof(double) * n_angles, &ha);
         if (s != QT_OK) return s;
         b->h_angles = static_cast<double *>(ha);
+    }
+    if (!b->angles_done) {
         cudaError_t e = cudaEventCreateWithFlags(&b->angles_done, cudaEventDisableTiming);
         if (e != cudaSuccess) return cuda_error(ctx, e, "angle staging");
-        s = dev_alloc(ctx, sizeof(double) * n_angles, &b->d_angles);
-        if (s != QT_OK) return s;
     } else {
         // the previous upload must have read the pinned copy before it is overwritten
         cudaError_t e = cudaEventSynchronize(b->angles_done);
         if (e != cudaSuccess) return cuda_error(ctx, e, "angle staging");
+    }
+    if (!b->d_angles) {
+        s = dev_alloc(ctx, sizeof(double) * n_angles, &b->d_angles);
+        if (s != QT_OK) return s;
     }
     std::memcpy(b->h_angles, angles, sizeof(double) * n_angles);
     cudaError_t e = cudaMemcpyAsync(b->d_angles, b->h_angles, sizeof(double) * n_angles, cudaMemcpyHostToDevice,
@@ -578,6 +737,8 @@ static qt_status batch_configure(qt_batch *b) {
     qt_ctx *ctx = b->ctx;
     const int prec = b->prepared_prec;
     const int n = (int) b->plans.size();
+    qt_status rs = resident_stop(b);
+    if (rs != QT_OK) return rs;
     cudaError_t se = cudaStreamSynchronize(ctx->stream);
     if (se != cudaSuccess) return cuda_error(ctx, se, "sync");
     for (cudaGraphExec_t *g : {&b->graph, &b->eval_graph})
@@ -589,7 +750,8 @@ static qt_status batch_configure(qt_batch *b) {
     dev_free(ctx, b->d_next);
     dev_free(ctx, b->d_inst);
     dev_free(ctx, b->d_inst_eval);
-    b->d_ws = b->d_next = b->d_inst = b->d_inst_eval = nullptr;
+    dev_free(ctx, b->d_inst_res);
+    b->d_ws = b->d_next = b->d_inst = b->d_inst_eval = b->d_inst_res = nullptr;
     b->inst_desc.clear();
     b->inst_index.clear();
     uint64_t ws = 0;
@@ -736,6 +898,8 @@ qt_status qt_batch_upload(qt_batch *b) {
     if (!b || b->prepared_prec < 0) return QT_ERR_INVALID_ARGUMENT;
     qt_ctx *ctx = b->ctx;
     std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    qt_status rs = resident_stop(b);   // the engine holds a staged copy of the leaves
+    if (rs != QT_OK) return rs;
     batch_pack(b);
     if (!b->leaf_bytes) return QT_OK;
     return cuda_error(ctx, cudaMemcpyAsync(b->d_leaves, b->h_leaves, b->leaf_bytes, cudaMemcpyHostToDevice, ctx->stream),
@@ -767,6 +931,8 @@ qt_status qt_batch_run(qt_batch *b) {
     if (!b || b->prepared_prec < 0) return QT_ERR_INVALID_ARGUMENT;
     qt_ctx *ctx = b->ctx;
     std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    qt_status rs = resident_stop(b);   // the two must not rebuild the same leaves at once
+    if (rs != QT_OK) return rs;
     if (deadline_passed(ctx)) return set_error(ctx, QT_ERR_DEADLINE, "deadline expired");
     if (b->use_graph && !b->graph && b->stepwise.empty()) {
         cudaGraph_t graph;
@@ -802,6 +968,10 @@ qt_status qt_batch_evaluate(qt_batch *b, const double *angles, int64_t n_angles,
     if (!b || !values || b->prepared_prec < 0) return QT_ERR_INVALID_ARGUMENT;
     qt_ctx *ctx = b->ctx;
     std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    if (b->res_idle > 0 && angles && n_angles > 0) {
+        if (deadline_passed(ctx)) return set_error(ctx, QT_ERR_DEADLINE, "deadline expired");
+        return resident_evaluate(b, angles, n_angles, values);
+    }
     const bool one_graph = angles && n_angles > 0 && b->use_graph && b->stepwise.empty() &&
                            b->prepared_prec == QT_PREC_MIXED && !b->plans.empty();
     if (!one_graph) {
@@ -900,6 +1070,28 @@ qt_status qt_batch_use_graph(qt_batch *b, int enable) {
     }
     return QT_OK;
 }
+
+qt_status qt_batch_use_resident(qt_batch *b, double idle_seconds) {
+    if (!b) return QT_ERR_INVALID_ARGUMENT;
+    qt_ctx *ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    if (!(idle_seconds > 0)) {
+        b->res_idle = 0;
+        return resident_stop(b);
+    }
+    if (b->prepared_prec != QT_PREC_MIXED)
+        return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "resident evaluation needs a batch prepared for QT_PREC_MIXED");
+    if (!b->stepwise.empty() || b->inst_desc.empty())
+        return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "resident evaluation needs every instance in the grouped launch");
+    const size_t smem = plan_header_bytes(b->header_steps) + 128 + b->ws_smem_bytes + b->stage_bytes + b->tile_bytes;
+    if ((int) b->inst_desc.size() > b->grid || (int) b->inst_desc.size() > resident_capacity(smem))
+        return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "resident evaluation needs one resident CTA per instance");
+    qt_status s = resident_stop(b);   // a new idle limit takes effect at the next start
+    b->res_idle = std::min(idle_seconds, 3600.0);
+    return s;
+}
+
+uint64_t qt_batch_resident_starts(const qt_batch *b) { return b ? b->res_starts : 0; }
 
 uint64_t qt_batch_h2d_bytes(const qt_batch *b) {
     if (!b) return 0;

@@ -137,6 +137,22 @@ struct PlanLaunch {
     uint32_t pad2;
 };
 
+// Resident evaluation: one CTA per instance stays on the GPU between
+// evaluations and serves requests posted in pinned host memory (read and
+// written over the coherent CPU-GPU link): the host writes the angles, then
+// the request number to *seq; each CTA rebuilds its rotation leaves, contracts,
+// writes the value and then its done[] slot.  Plan blocks and leaf images stay
+// staged in shared memory across requests.
+constexpr uint32_t kResidentStop = 0xffffffffu;   // *seq value that makes the engine leave
+constexpr uint32_t kResidentLeft = 0xfffffffeu;   // done[] value of a CTA that left (idle, or staging failed)
+struct ResidentLaunch {
+    PlanLaunch lp;               // instance i on CTA i; angles and values point to mapped host memory
+    const uint32_t *seq;         // mapped host: number of the latest request
+    uint32_t *done;              // mapped host, one per instance: the last request it finished
+    uint32_t first_seq;          // requests up to this number are served already
+    uint32_t idle_polls;         // polls (about a microsecond apart) without a request before leaving
+};
+
 __host__ __device__ inline uint64_t scatter_digits(uint64_t x, const uint8_t *pos, int n) {
     uint64_t off = 0;
     for (int i = 0; i < n; i++) off += ((x >> (2 * i)) & 3ull) << (2 * pos[i]);

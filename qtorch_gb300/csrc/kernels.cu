@@ -820,6 +820,112 @@ __device__ __forceinline__ void bulk_copy_chunks(unsigned char *dst, const char 
     }
 }
 
+// The arrays of a plan block, in global memory or rebased into its staged copy
+// in shared memory (stage != null).
+struct PlanView {
+    PlanDesc P;
+    const StepDesc *steps;
+    const int32_t *level_start, *rank0_steps, *level_cta;
+    const uint32_t *level_items, *level_meta;
+    const uint2 *rotations;
+    const uint8_t *item_step;
+    const HotStep *hot;
+    const ushort2 *tables;
+};
+
+__device__ __forceinline__ PlanView plan_view(const PlanDesc *gplan, const unsigned char *stage) {
+    PlanView v;
+    v.P = stage ? *reinterpret_cast<const PlanDesc *>(stage) : *gplan;
+    const char *gbase = reinterpret_cast<const char *>(gplan);
+    const char *sbase = reinterpret_cast<const char *>(stage);
+    auto at = [&](const void *p) -> const char * {
+        return stage ? sbase + (reinterpret_cast<const char *>(p) - gbase) : reinterpret_cast<const char *>(p);
+    };
+    v.steps = reinterpret_cast<const StepDesc *>(at(v.P.steps));
+    v.level_start = reinterpret_cast<const int32_t *>(at(v.P.level_start));
+    v.rank0_steps = reinterpret_cast<const int32_t *>(at(v.P.rank0_steps));
+    v.level_items = reinterpret_cast<const uint32_t *>(at(v.P.level_items));
+    v.tables = reinterpret_cast<const ushort2 *>(at(v.P.tables));
+    v.level_cta = reinterpret_cast<const int32_t *>(at(v.P.level_cta));
+    v.rotations = reinterpret_cast<const uint2 *>(at(v.P.rotations));
+    v.item_step = v.P.item_step ? reinterpret_cast<const uint8_t *>(at(v.P.item_step)) : nullptr;
+    v.hot = reinterpret_cast<const HotStep *>(at(v.P.hot));
+    v.level_meta = reinterpret_cast<const uint32_t *>(at(v.P.level_meta));
+    return v;
+}
+
+// Every level of a plan, one CTA; a barrier after each level.
+template <bool kMixed, bool kScaled>
+__device__ __forceinline__ void plan_levels(const PlanView &v, const char *leaves, char *ws, PlanSmemHeader &h,
+                                            unsigned char *tile, int *bad) {
+    uint32_t items_before = 0;
+    uint32_t tiny = 0;   // this thread flagged a step of the level (unscaled pass)
+    for (int L = 0; L < v.P.n_levels; L++) {
+        const int sc = v.level_cta[L], s1 = v.level_start[L + 1];
+        plan_level<kMixed, kScaled>(v.steps, v.hot, v.level_start[L], sc, v.level_items[L], leaves, ws, h, v.tables,
+                                    v.item_step ? v.item_step + items_before : nullptr, bad, v.level_meta[L], tiny);
+        items_before += v.level_items[L];
+        for (int s = sc; s < s1; s++) run_tiled<kMixed, kScaled>(v.steps[s], s, leaves, ws, h, tile, bad, tiny);
+        if constexpr (kMixed && !kScaled) {
+            if (__syncthreads_or(tiny)) {
+                unscaled_level_check(v.steps, v.level_start[L], s1, ws, h, bad);
+                tiny = 0;
+            }
+        } else {
+            __syncthreads();
+        }
+    }
+}
+
+// One contraction of an instance: the header is clear, *bad is 0 and a barrier
+// has passed.  The mixed form runs unscaled first and again with power-of-two
+// scaling only when a value left the safe range.
+template <bool kMixed>
+__device__ __forceinline__ void plan_contract(const PlanView &v, const char *leaves, char *ws, PlanSmemHeader &h,
+                                              unsigned char *tile, int *bad, uint32_t n_steps) {
+    if constexpr (kMixed) {
+        plan_levels<true, false>(v, leaves, ws, h, tile, bad);
+        if (*bad) {
+            for (uint32_t s = threadIdx.x; s < n_steps; s += blockDim.x) {
+                h.maxbits[s] = 0;
+                h.expo[s] = 0;
+            }
+            __syncthreads();
+            plan_levels<true, true>(v, leaves, ws, h, tile, bad);
+        }
+    } else {
+        plan_levels<false, true>(v, leaves, ws, h, tile, bad);
+    }
+}
+
+// final-value rule of src/Network.h:961-965, applied in contraction order
+// (one thread)
+template <bool kMixed>
+__device__ __forceinline__ double2 plan_final_value(const PlanView &v, const char *ws, const PlanSmemHeader &h) {
+    double fre = 0.0, fim = 0.0;
+    for (int r = 0; r < v.P.n_rank0; r++) {
+        const int s = v.rank0_steps[r];
+        const StepDesc &d = v.steps[s];
+        double vre, vim;
+        if (!kMixed || (d.flags & kCF64)) {
+            const double2 x = *reinterpret_cast<const double2 *>(ws + d.c_off);
+            vre = x.x; vim = x.y;
+        } else {
+            const float2 x = *reinterpret_cast<const float2 *>(ws + d.c_off);
+            vre = x.x; vim = x.y;
+        }
+        if (kMixed) {
+            vre = scale2d(vre, h.expo[s]);
+            vim = scale2d(vim, h.expo[s]);
+        }
+        if ((fabs(fre) <= 1.0e-30 && fabs(fim) <= 1.0e-30) || (d.flags & kBothRank0)) {
+            fre = vre;
+            fim = vim;
+        }
+    }
+    return make_double2(fre, fim);
+}
+
 // kMinCtas: the register budget -- the variant is compiled for that many
 // resident CTAs per SM (2: up to 128 registers a thread; 3: 80, 4: 64 and
 // 5: 48, with some spills), trading single-instance latency for warps per SM
@@ -863,17 +969,6 @@ __global__ void __launch_bounds__(kPlanThreads, kMinCtas) plan_kernel(const Plan
         }
         char *const ws = I.ws_bytes <= lp.ws_smem_bytes ? ws_smem : ws_global;
         const bool staged = lp.stage_bytes && I.plan_bytes && I.plan_bytes + I.leaf_bytes <= lp.stage_bytes;
-        const StepDesc *steps;
-        const int32_t *level_start, *rank0_steps, *level_cta;
-        const uint2 *rotations;
-        const uint8_t *item_step;
-        const HotStep *hot;
-        const uint32_t *level_meta;
-        char *leaves_rw;
-        const uint32_t *level_items;
-        const ushort2 *tables;
-        const char *leaves;
-        PlanDesc P;
         if (staged) {
             if (threadIdx.x == 0) {
                 // the previous instance's generic reads of this region are ordered before the async writes
@@ -899,107 +994,118 @@ __global__ void __launch_bounds__(kPlanThreads, kMinCtas) plan_kernel(const Plan
                 }
                 return;
             }
-            P = *reinterpret_cast<const PlanDesc *>(stage);
-            const char *gbase = reinterpret_cast<const char *>(I.plan);
-            const char *sbase = reinterpret_cast<const char *>(stage);
-            steps = reinterpret_cast<const StepDesc *>(sbase + (reinterpret_cast<const char *>(P.steps) - gbase));
-            level_start = reinterpret_cast<const int32_t *>(sbase + (reinterpret_cast<const char *>(P.level_start) - gbase));
-            rank0_steps = reinterpret_cast<const int32_t *>(sbase + (reinterpret_cast<const char *>(P.rank0_steps) - gbase));
-            level_items = reinterpret_cast<const uint32_t *>(sbase + (reinterpret_cast<const char *>(P.level_items) - gbase));
-            tables = reinterpret_cast<const ushort2 *>(sbase + (reinterpret_cast<const char *>(P.tables) - gbase));
-            level_cta = reinterpret_cast<const int32_t *>(sbase + (reinterpret_cast<const char *>(P.level_cta) - gbase));
-            rotations = reinterpret_cast<const uint2 *>(sbase + (reinterpret_cast<const char *>(P.rotations) - gbase));
-            item_step = P.item_step ? reinterpret_cast<const uint8_t *>(sbase + (reinterpret_cast<const char *>(P.item_step) - gbase))
-                                    : nullptr;
-            hot = reinterpret_cast<const HotStep *>(sbase + (reinterpret_cast<const char *>(P.hot) - gbase));
-            level_meta = reinterpret_cast<const uint32_t *>(sbase + (reinterpret_cast<const char *>(P.level_meta) - gbase));
-            leaves_rw = reinterpret_cast<char *>(stage) + I.plan_bytes;
-        } else {
-            P = *I.plan;
-            steps = P.steps;
-            level_start = P.level_start;
-            rank0_steps = P.rank0_steps;
-            level_items = P.level_items;
-            tables = P.tables;
-            level_cta = P.level_cta;
-            rotations = P.rotations;
-            item_step = P.item_step;
-            hot = P.hot;
-            level_meta = P.level_meta;
-            leaves_rw = const_cast<char *>(I.leaves);   // the instance's own leaf image
         }
-        leaves = leaves_rw;
+        const PlanView v = plan_view(I.plan, staged ? stage : nullptr);
+        // the instance's own leaf image, or its staged copy
+        char *const leaves = staged ? reinterpret_cast<char *>(stage) + I.plan_bytes : const_cast<char *>(I.leaves);
         if constexpr (kMixed) {
             // the step's angles arrive as numbers; the gate tensors are built here
-            if (I.angles && P.n_rot) {
-                for (int r = threadIdx.x; r < P.n_rot; r += blockDim.x) build_rotation(leaves_rw, rotations[r], I.angles[r]);
+            if (I.angles && v.P.n_rot) {
+                for (int r = threadIdx.x; r < v.P.n_rot; r += blockDim.x)
+                    build_rotation(leaves, v.rotations[r], I.angles[r]);
                 __syncthreads();
             }
         }
         if (kMixed && !staged) __syncthreads();   // the cleared header (staging waited with a barrier)
-        auto levels = [&](auto scaled) {
-            constexpr bool kScaled = decltype(scaled)::value;
-            uint32_t items_before = 0;
-            uint32_t tiny = 0;   // this thread flagged a step of the level (unscaled pass)
-            for (int L = 0; L < P.n_levels; L++) {
-                const int sc = level_cta[L], s1 = level_start[L + 1];
-                plan_level<kMixed, kScaled>(steps, hot, level_start[L], sc, level_items[L], leaves, ws, h, tables,
-                                            item_step ? item_step + items_before : nullptr, &s_bad, level_meta[L],
-                                            tiny);
-                items_before += level_items[L];
-                for (int s = sc; s < s1; s++) run_tiled<kMixed, kScaled>(steps[s], s, leaves, ws, h, tile, &s_bad, tiny);
-                if constexpr (kMixed && !kScaled) {
-                    if (__syncthreads_or(tiny)) {
-                        unscaled_level_check(steps, level_start[L], s1, ws, h, &s_bad);
-                        tiny = 0;
-                    }
-                } else {
-                    __syncthreads();
-                }
-            }
-        };
-        if constexpr (kMixed) {
-            levels(std::false_type());
-            if (s_bad) {
-                // a value left the safe range: again, with power-of-two scaling
-                for (uint32_t s = threadIdx.x; s < I.n_steps; s += blockDim.x) {
-                    h.maxbits[s] = 0;
-                    h.expo[s] = 0;
-                }
-                __syncthreads();
-                levels(std::true_type());
-            }
-        } else {
-            levels(std::true_type());
-        }
-        // final-value rule of src/Network.h:961-965, applied in contraction order
+        plan_contract<kMixed>(v, leaves, ws, h, tile, &s_bad, I.n_steps);
         if (threadIdx.x == 0) {
-            double fre = 0.0, fim = 0.0;
-            for (int r = 0; r < P.n_rank0; r++) {
-                const int s = rank0_steps[r];
-                const StepDesc &d = steps[s];
-                double vre, vim;
-                if (!kMixed || (d.flags & kCF64)) {
-                    const double2 v = *reinterpret_cast<const double2 *>(ws + d.c_off);
-                    vre = v.x; vim = v.y;
-                } else {
-                    const float2 v = *reinterpret_cast<const float2 *>(ws + d.c_off);
-                    vre = v.x; vim = v.y;
-                }
-                if (kMixed) {
-                    vre = scale2d(vre, h.expo[s]);
-                    vim = scale2d(vim, h.expo[s]);
-                }
-                if ((fabs(fre) <= 1.0e-30 && fabs(fim) <= 1.0e-30) || (d.flags & kBothRank0)) {
-                    fre = vre;
-                    fim = vim;
-                }
-            }
-            I.value[0] = fre;
-            I.value[1] = fim;
+            const double2 val = plan_final_value<kMixed>(v, ws, h);
+            I.value[0] = val.x;
+            I.value[1] = val.y;
         }
         __syncthreads();   // the next instance reuses the header, the workspace and s_next
         if (!lp.next) inst += gridDim.x;
+    }
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_sys(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_sys(uint32_t *p, uint32_t v) {
+    asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// The resident engine (ResidentLaunch).  Every wait is bounded: the request
+// poll gives up after idle_polls (the CTA leaves; the host relaunches it on the
+// next request) and the staging wait after about a second.
+template <int kMinCtas>
+__global__ void __launch_bounds__(kPlanThreads, kMinCtas) resident_kernel(const ResidentLaunch rl) {
+    const PlanLaunch &lp = rl.lp;
+    const int inst = blockIdx.x;
+    if (inst >= lp.n_instances) return;
+    extern __shared__ __align__(256) unsigned char smem_raw[];
+    const uint32_t header_bytes = plan_header_bytes(lp.header_steps);
+    PlanSmemHeader h{reinterpret_cast<uint32_t *>(smem_raw), reinterpret_cast<int32_t *>(smem_raw + 4u * lp.header_steps)};
+    uint64_t *mbar_slot = reinterpret_cast<uint64_t *>(smem_raw + header_bytes);
+    unsigned char *region = smem_raw + header_bytes + 128;
+    char *const ws_smem = reinterpret_cast<char *>(region);
+    char *const ws_global = lp.ws_base ? lp.ws_base + (uint64_t) blockIdx.x * lp.ws_stride : nullptr;
+    unsigned char *stage = region + lp.ws_smem_bytes;
+    unsigned char *tile = stage + lp.stage_bytes;
+    __shared__ int s_bad;
+    __shared__ uint32_t s_seq;
+    const InstanceDesc I = lp.instances[inst];
+    char *const ws = I.ws_bytes <= lp.ws_smem_bytes ? ws_smem : ws_global;
+    const bool staged = lp.stage_bytes && I.plan_bytes && I.plan_bytes + I.leaf_bytes <= lp.stage_bytes;
+    if (staged) {
+        const uint32_t mbar = smem_addr(mbar_slot);
+        if (threadIdx.x == 0) {
+            mbar_init(mbar);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(mbar, I.plan_bytes + I.leaf_bytes);
+            bulk_copy_chunks(stage, reinterpret_cast<const char *>(I.plan), I.plan_bytes, mbar);
+            bulk_copy_chunks(stage + I.plan_bytes, I.leaves, I.leaf_bytes, mbar);
+        }
+        __syncthreads();   // the barrier is initialised before anyone waits on it
+        const bool ok = mbar_wait_bounded(mbar, 0);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) st_release_sys(rl.done + inst, kResidentLeft);
+            return;
+        }
+    }
+    const PlanView v = plan_view(I.plan, staged ? stage : nullptr);
+    char *const leaves = staged ? reinterpret_cast<char *>(stage) + I.plan_bytes : const_cast<char *>(I.leaves);
+    uint32_t last = rl.first_seq;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            uint32_t s = last;
+            for (uint32_t it = 0; it < rl.idle_polls; it++) {
+                s = ld_acquire_sys(rl.seq);
+                if (s != last) break;
+                __nanosleep(it < 1024 ? 100 : 1000);   // a short spin after a request, then back off
+            }
+            s_seq = s;
+        }
+        for (uint32_t k = threadIdx.x; k < I.n_steps; k += blockDim.x) {
+            h.maxbits[k] = 0;
+            h.expo[k] = 0;
+        }
+        if (threadIdx.x == 0) s_bad = 0;
+        __syncthreads();
+        const uint32_t s = s_seq;
+        if (s == kResidentStop) break;   // asked to leave
+        if (s == last) {                 // idle for too long: tell the host, then leave
+            if (threadIdx.x == 0) st_release_sys(rl.done + inst, kResidentLeft);
+            break;
+        }
+        last = s;
+        // the request's angles, read through to host memory (never a stale cached copy)
+        if (I.angles && v.P.n_rot) {
+            for (int r = threadIdx.x; r < v.P.n_rot; r += blockDim.x)
+                build_rotation(leaves, v.rotations[r], __ldcv(I.angles + r));
+            __syncthreads();
+        }
+        plan_contract<true>(v, leaves, ws, h, tile, &s_bad, I.n_steps);
+        if (threadIdx.x == 0) {
+            const double2 val = plan_final_value<true>(v, ws, h);
+            I.value[0] = val.x;
+            I.value[1] = val.y;
+            __threadfence_system();   // the value is visible to the host before the done flag
+            st_release_sys(rl.done + inst, s);
+        }
+        __syncthreads();   // s_seq, the header and the workspace are reused
     }
 }
 
@@ -1052,7 +1158,8 @@ static PlanKernelFn plan_kernel_fn(bool mixed, int ctas) {
     }
 }
 
-static cudaError_t raise_smem_limit(PlanKernelFn fn, int dev) {
+template <typename Fn>
+static cudaError_t raise_smem_limit(Fn fn, int dev) {
     cudaFuncAttributes fa;
     cudaError_t e = cudaFuncGetAttributes(&fa, fn);
     int optin = 0;
@@ -1071,6 +1178,7 @@ static cudaError_t plan_attributes() {
     for (int ctas : kPlanVariants)
         for (bool mixed : {true, false})
             if (e == cudaSuccess) e = raise_smem_limit(plan_kernel_fn(mixed, ctas), dev);
+    if (e == cudaSuccess) e = raise_smem_limit(resident_kernel<kPlanDefaultVariant>, dev);
     if (e == cudaSuccess && dev >= 0 && dev < 64) g_attr_done[dev] = true;
     return e;
 }
@@ -1133,6 +1241,12 @@ size_t plan_smem_limit() {
             }
             static_max = std::max(static_max, fa.sharedSizeBytes);
         }
+    cudaFuncAttributes fr;
+    if (cudaFuncGetAttributes(&fr, resident_kernel<kPlanDefaultVariant>) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    static_max = std::max(static_max, fr.sharedSizeBytes);
     return (size_t) optin - static_max;
 }
 
@@ -1147,6 +1261,23 @@ cudaError_t launch_plan(const PlanLaunch &lp, bool mixed, int grid, cudaStream_t
     if (e != cudaSuccess) return e;
     if (grid <= 0 || grid > lp.n_instances) grid = lp.n_instances;
     plan_kernel_fn(mixed, variant)<<<grid, kPlanThreads, smem, stream>>>(lp);
+    return cudaGetLastError();
+}
+
+int resident_capacity(size_t smem_bytes) {
+    int per_sm = 0;
+    plan_attributes();
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, resident_kernel<kPlanDefaultVariant>, kPlanThreads,
+                                                  smem_bytes);
+    cudaGetLastError();
+    return num_sms() * std::max(per_sm, 0);
+}
+
+cudaError_t launch_resident(const ResidentLaunch &rl, cudaStream_t stream) {
+    if (rl.lp.n_instances <= 0) return cudaSuccess;
+    cudaError_t e = plan_attributes();
+    if (e != cudaSuccess) return e;
+    resident_kernel<kPlanDefaultVariant><<<rl.lp.n_instances, kPlanThreads, plan_smem_bytes(rl.lp), stream>>>(rl);
     return cudaGetLastError();
 }
 

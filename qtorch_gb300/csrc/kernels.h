@@ -50,5 +50,10 @@ int plan_max_grid(size_t smem_bytes, int per_sm_cap = 0, int variant = kPlanDefa
 int plan_num_sms();
 // largest dynamic shared memory an interpreter CTA may have on this device
 size_t plan_smem_limit();
+// The resident engine (one CTA per instance, 128-register budget); returns
+// once launched.  resident_capacity: how many CTAs of that shared-memory size
+// are resident at once.
+cudaError_t launch_resident(const ResidentLaunch &rl, cudaStream_t stream);
+int resident_capacity(size_t smem_bytes);
 
 }  // namespace qtg

@@ -125,6 +125,14 @@ struct qt_batch {
     std::vector<qtg::InstanceDesc> inst_desc;         // host copy of the descriptors
     std::vector<int> inst_index;                      // batch index of each descriptor
     cudaEvent_t angles_done = nullptr;                // the last angle upload has left h_angles
+    // resident evaluation (qt_batch_use_resident)
+    double res_idle = 0;                              // idle seconds before the engine leaves; 0: off
+    cudaStream_t res_stream = nullptr;
+    uint32_t *h_mail = nullptr;                       // pinned: [0] request number, [32 + j] done of descriptor j
+    void *d_inst_res = nullptr;                       // descriptors on the mapped host angles and values
+    uint32_t res_seq = 0;                             // the last request posted
+    bool res_running = false;
+    uint64_t res_starts = 0;                          // engine launches so far
 };
 
 namespace qtg {
