@@ -364,6 +364,21 @@ qt_status qt_batch_autotune(qt_batch *b, int reps, qt_launch_policy *chosen, dou
 int64_t qt_qaoa_term_text(const char *dgf_text, int p, const double *betas_gammas, int edge,
                           char *qasm_out, int64_t qasm_cap, char *measure_out, int64_t measure_cap);
 int qt_qaoa_num_edges(const char *dgf_text);
+/* The whole MaxCut QAOA circuit of a graph (every qubit and edge), as
+ * maxcutGetFinalString writes it (src/maxcut.cpp:52-56). */
+int64_t qt_qaoa_circuit_text(const char *dgf_text, int p, const double *betas_gammas, char *qasm_out, int64_t cap);
+/* Final-cut decoding (maxcutGetFinalString, src/maxcut.cpp:29-140): qubit by
+ * qubit, the probability that it reads 0 given the bits chosen so far
+ * (measurement leaves |0><0| / |1><1| / trace on one plan of the whole
+ * circuit), the likelier bit chosen; an exact tie takes a coin from
+ * std::mt19937(seed) (the reference: rand() seeded by the clock).  bits: one
+ * 0/1 per vertex; cut_edges: edges whose ends differ; prob: the probability
+ * of the chosen string; marginals (may be NULL, cap_bits entries): the
+ * contracted value of each query, P(chosen bits before i, bit i = 0).
+ * ordering: QT_ORDER_LINEGRAPH or QT_ORDER_STOCHASTIC (seeded). */
+qt_status qt_maxcut_final_string(qt_ctx *ctx, const char *dgf_text, int p, const double *betas_gammas,
+                                 qt_precision prec, qt_ordering ordering, uint64_t seed, int32_t *bits,
+                                 int cap_bits, int *n_bits, int *cut_edges, double *prob, double *marginals);
 /* Seeded x-regular random graph in .dgf text (the XregGraphGen algorithm with
  * std::mt19937(seed), retried until every vertex reaches degree x). */
 int64_t qt_random_regular_graph(int num_nodes, int degree, uint64_t seed, char *dgf_out, int64_t cap);

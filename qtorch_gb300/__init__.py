@@ -689,6 +689,17 @@ def qaoa_term_text(dgf_text, p, betas_gammas, edge):
     return q.value.decode(), m.value.decode()
 
 
+def qaoa_circuit_text(dgf_text, p, betas_gammas):
+    """The whole MaxCut QAOA circuit of a graph (src/maxcut.cpp:52-56)."""
+    bg = np.ascontiguousarray(np.asarray(betas_gammas, dtype=np.float64))
+    n = _lib().qt_qaoa_circuit_text(dgf_text.encode(), p, _dp(bg), None, 0)
+    if n < 0:
+        raise ValueError("bad graph or p")
+    q = ctypes.create_string_buffer(int(n))
+    _lib().qt_qaoa_circuit_text(dgf_text.encode(), p, _dp(bg), q, int(n))
+    return q.value.decode()
+
+
 def random_regular_graph(num_nodes, degree, seed):
     n = _lib().qt_random_regular_graph(num_nodes, degree, int(seed), None, 0)
     if n < 0:
@@ -705,3 +716,6 @@ def run_inp(path, ctx=None, symbolic=False):
     fl = ctypes.c_int64(0)
     _check(_lib().qt_run_inp(c.handle if c else None, path.encode(), _dp(v), ctypes.byref(fl)), c)
     return complex(v[0], v[1]), fl.value
+
+
+from .maxcut import MaxCutQAOA, maxcut_final_string  # noqa: E402,F401

@@ -113,6 +113,9 @@ SIGNATURES = [
     ("qt_batch_autotune", c_int, [c_void_p, c_int, P(LaunchPolicy), P(c_double)]),
     ("qt_qaoa_term_text", c_int64, [c_char_p, c_int, P(c_double), c_int, c_char_p, c_int64, c_char_p, c_int64]),
     ("qt_qaoa_num_edges", c_int, [c_char_p]),
+    ("qt_qaoa_circuit_text", c_int64, [c_char_p, c_int, P(c_double), c_char_p, c_int64]),
+    ("qt_maxcut_final_string", c_int, [c_void_p, c_char_p, c_int, P(c_double), c_int, c_int, c_uint64,
+                                       P(c_int32), c_int, P(c_int), P(c_int), P(c_double), P(c_double)]),
     ("qt_random_regular_graph", c_int64, [c_int, c_int, c_uint64, c_char_p, c_int64]),
     ("qt_server_create", c_int, [c_void_p, c_int, c_int, P(c_void_p)]),
     ("qt_server_free", c_int, [c_void_p]),

@@ -85,6 +85,34 @@ std::string fmt_g(double x) {
     return buf;
 }
 
+// outputInitialPlusStateToFile + applyU_CsThenU_Bs (src/maxcut.h:194-233):
+// H on every qubit, then per layer i the U_C of every pair (CNOT, Rz(-gamma_i),
+// CNOT) and the U_B of every qubit (Rx(2 beta_i)); betas first, then gammas
+std::string circuit_text(const std::vector<std::pair<int, int>> &pairs, int nq, int p, const double *bg) {
+    std::string q = std::to_string(nq) + "\n";
+    for (int i = 0; i < nq; i++) q += "H " + std::to_string(i) + "\n";
+    for (int i = 0; i < p; i++) {
+        const double gamma = bg[i + p], beta = bg[i];
+        for (auto &e : pairs) {
+            const std::string a = std::to_string(e.first), b = std::to_string(e.second);
+            q += "CNOT " + a + " " + b + "\n";
+            q += "Rz " + fmt_g(-gamma) + " " + b + "\n";
+            q += "CNOT " + a + " " + b + "\n";
+        }
+        for (int j = 0; j < nq; j++) q += "Rx " + fmt_g(beta * 2.0) + " " + std::to_string(j) + "\n";
+    }
+    return q;
+}
+
+int64_t copy_out(const std::string &s, char *out, int64_t cap) {
+    if (out && cap > 0) {
+        const int64_t n = std::min<int64_t>((int64_t) s.size(), cap - 1);
+        std::memcpy(out, s.data(), (size_t) n);
+        out[n] = 0;
+    }
+    return (int64_t) s.size() + 1;
+}
+
 }  // namespace
 
 extern "C" {
@@ -108,31 +136,83 @@ int64_t qt_qaoa_term_text(const char *dgf_text, int p, const double *bg, int edg
     int nq;
     light_cone(g, adj, edge, p, real, nq);
     // F_p (src/maxcut.cpp:171-188) through outputInitialPlusStateToFile / applyU_CsThenU_Bs
-    std::string q = std::to_string(nq) + "\n";
-    for (int i = 0; i < nq; i++) q += "H " + std::to_string(i) + "\n";
-    for (int i = 0; i < p; i++) {
-        const double gamma = bg[i + p], beta = bg[i];
-        for (auto &e : real) {
-            const std::string a = std::to_string(e.first), b = std::to_string(e.second);
-            q += "CNOT " + a + " " + b + "\n";
-            q += "Rz " + fmt_g(-gamma) + " " + b + "\n";
-            q += "CNOT " + a + " " + b + "\n";
-        }
-        for (int j = 0; j < nq; j++) q += "Rx " + fmt_g(beta * 2.0) + " " + std::to_string(j) + "\n";
-    }
+    const std::string q = circuit_text(real, nq, p, bg);
     std::string m;
     for (int i = 0; i < nq; i++) m += (i == 0 || i == 1) ? "Z " : "T ";
-    if (qasm_out && qasm_cap > 0) {
-        const int64_t n = std::min<int64_t>((int64_t) q.size(), qasm_cap - 1);
-        std::memcpy(qasm_out, q.data(), (size_t) n);
-        qasm_out[n] = 0;
+    copy_out(m, measure_out, measure_cap);
+    return copy_out(q, qasm_out, qasm_cap);
+}
+
+int64_t qt_qaoa_circuit_text(const char *dgf_text, int p, const double *bg, char *qasm_out, int64_t qasm_cap) {
+    if (!dgf_text || !bg || p < 1) return -1;
+    const Graph g = read_dgf(dgf_text);
+    if (g.pairs.empty()) return -1;
+    return copy_out(circuit_text(g.pairs, g.num_qubits, p, bg), qasm_out, qasm_cap);
+}
+
+qt_status qt_maxcut_final_string(qt_ctx *ctx, const char *dgf_text, int p, const double *bg, qt_precision prec,
+                                 qt_ordering ordering, uint64_t seed, int32_t *bits, int cap_bits, int *n_bits,
+                                 int *cut_edges, double *prob, double *marginals) {
+    if (!ctx || !dgf_text || !bg || p < 1 || !bits || !n_bits || !cut_edges || !prob) return QT_ERR_INVALID_ARGUMENT;
+    if (ordering == QT_ORDER_SEQUENCE) return QT_ERR_INVALID_CONTRACTION_METHOD;
+    const Graph g = read_dgf(dgf_text);
+    const int n = g.num_qubits;
+    if (g.pairs.empty() || cap_bits < n) return QT_ERR_INVALID_ARGUMENT;
+    const std::string q = circuit_text(g.pairs, n, p, bg);
+    std::string trace;
+    for (int i = 0; i < n; i++) trace += "T ";
+    // one plan for every query: only the measurement leaves change (|0><0|,
+    // |1><1| or the trace on each qubit, all rank 1 and last in leaf order)
+    qt_plan *plan = nullptr;
+    qt_status s = qt_plan_build(ctx, q.c_str(), trace.c_str(), nullptr, ordering, seed, nullptr, 0, &plan);
+    if (s != QT_OK) return s;
+    std::vector<double> leaves(2 * qt_plan_leaf_elems(plan));
+    s = qt_plan_leaf_values(plan, leaves.data(), leaves.size() / 2);
+    qt_batch *batch = nullptr;
+    if (s == QT_OK) s = qt_batch_create(ctx, &batch);
+    int idx = -1;
+    if (s == QT_OK) s = qt_batch_add(batch, plan, nullptr, &idx);
+    // maxcutGetFinalString (src/maxcut.cpp:40-122): qubit by qubit, the
+    // probability of 0 given the bits chosen so far; ties by a seeded coin
+    std::mt19937 coin((uint32_t) seed);
+    std::vector<char> answer;
+    double current = 1.0;
+    const size_t meas0 = leaves.size() - 8 * (size_t) n;   // first measurement leaf (doubles)
+    for (int i = 0; i < n && s == QT_OK; i++) {
+        for (int j = 0; j < n; j++) {
+            double *v = leaves.data() + meas0 + 8 * (size_t) j;
+            std::fill(v, v + 8, 0.0);
+            if (j < i) v[answer[j] ? 6 : 0] = 1.0;   // |1><1| or |0><0|
+            else if (j == i) v[0] = 1.0;             // |0><0|
+            else v[0] = v[6] = 1.0;                  // trace
+        }
+        s = qt_batch_set_leaves(batch, idx, leaves.data());
+        double val[2];
+        if (s == QT_OK) s = qt_batch_execute(batch, prec, val);
+        if (s != QT_OK) break;
+        if (marginals) marginals[i] = val[0];
+        const double next = val[0] / current;
+        if (next > 0.5) {
+            current *= next;
+            answer.push_back(0);
+        } else if (next < 0.5) {
+            current *= 1.0 - next;
+            answer.push_back(1);
+        } else {
+            answer.push_back((char) (coin() & 1u));
+            current *= 0.5;
+        }
     }
-    if (measure_out && measure_cap > 0) {
-        const int64_t n = std::min<int64_t>((int64_t) m.size(), measure_cap - 1);
-        std::memcpy(measure_out, m.data(), (size_t) n);
-        measure_out[n] = 0;
-    }
-    return (int64_t) q.size() + 1;
+    if (batch) qt_batch_free(batch);
+    qt_plan_free(plan);
+    if (s != QT_OK) return s;
+    int cut = 0;
+    for (auto &e : g.pairs) cut += answer[e.first] != answer[e.second];
+    for (int i = 0; i < n; i++) bits[i] = answer[i];
+    *n_bits = n;
+    *cut_edges = cut;
+    *prob = current;
+    return QT_OK;
 }
 
 int64_t qt_random_regular_graph(int num_nodes, int degree, uint64_t seed, char *out, int64_t cap) {
