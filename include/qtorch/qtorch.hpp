@@ -199,6 +199,10 @@ public:
     const std::vector<StepRecord> &Steps() const { return mSteps; }
     const std::vector<std::shared_ptr<Node>> &Leaves() const { return mLeaves; }
     static qt_ctx *DefaultContext();
+    // Index slicing (no reference counterpart): a network whose sliced wires
+    // were cut from their leaves replays its recorded sequence, and a pair that
+    // shared only cut wires is then an outer product instead of a refusal.
+    void AllowOuterProducts(bool allow) noexcept { mAllowOuter = allow; }
 
 private:
     void ParseNetwork(const std::string &qasmText);
@@ -229,6 +233,7 @@ private:
     std::vector<StepRecord> mSteps;
     std::vector<std::shared_ptr<Node>> mLeaves;
     int64_t mNextTensorId{0};
+    bool mAllowOuter{false};
 };
 
 // ---- ContractionTools (src/ContractionTools.h:52-123) ----------------------

@@ -230,6 +230,29 @@ qt_status qt_plan_rotation_angles(const qt_plan *plan, double *angles, int cap);
 #define QT_STEP_INFO_FIELDS 8
 int qt_plan_step_info(const qt_plan *plan, qt_precision prec, int32_t *out, int cap_steps);
 
+/* ---- index slicing (no reference counterpart) ---------------------------
+ *
+ * A plan whose intermediates do not fit a workspace budget is split over the
+ * values of up to max_cuts wires: each cut wire is removed from its two leaves
+ * (the leaves keep the slice at one index), the plan's recorded sequence is
+ * replayed on the cut network (a pair that shared only cut wires becomes an
+ * outer product), and the value is the sum over all 4^cuts assignments -- the
+ * network value is linear in every leaf.  Wires are cut greedily, the one
+ * carried by the largest intermediates first, keeping every leaf and every
+ * intermediate but the final one at rank >= 1, until the sliced plan's
+ * workspace in `prec` is at most max_workspace_bytes (QT_ERR_OUT_OF_MEMORY
+ * when max_cuts do not get there).  ctx may be NULL to inspect the slicing
+ * only.  qt_sliced_execute sums the slices' values in assignment order
+ * (complex128); instances above 2^24 complex MACs run step by step one at a
+ * time, so the device holds one sliced workspace. */
+typedef struct qt_sliced qt_sliced;
+qt_status qt_plan_slice(qt_ctx *ctx, const qt_plan *plan, qt_precision prec, uint64_t max_workspace_bytes,
+                        int max_cuts, qt_sliced **out);
+int qt_sliced_num_cuts(const qt_sliced *s);
+qt_plan *qt_sliced_plan(const qt_sliced *s);   /* the plan of one slice (owned by s) */
+qt_status qt_sliced_execute(qt_sliced *s, qt_precision prec, double *re_im);
+qt_status qt_sliced_free(qt_sliced *s);
+
 /* ---- batches: many plan instances in one persistent grouped launch ------ */
 
 /* A batch holds instances (plan, leaf values).  Leaves are complex128 on the

@@ -476,6 +476,10 @@ class Plan(_Owned):
         _check(_lib().qt_plan_execute(self.ctx.handle, self.handle, precision, _dp(v)), self.ctx)
         return complex(v[0], v[1])
 
+    def slice(self, max_workspace_bytes, precision=FP64, max_cuts=8):
+        """Index slicing under a workspace budget (qt_plan_slice)."""
+        return SlicedPlan(self, max_workspace_bytes, precision, max_cuts)
+
     @property
     def num_rotations(self):
         return _lib().qt_plan_num_rotations(self.handle)
@@ -498,6 +502,43 @@ class Plan(_Owned):
         if got < 0:
             raise InvalidFunctionInput("qt_plan_step_info")
         return out[:n].copy()
+
+
+class SlicedPlan(_Owned):
+    """A plan split over the values of a few cut wires (qt_plan_slice)."""
+
+    _free_name = "qt_sliced_free"
+    _release_rank = 1
+
+    def __init__(self, plan, max_workspace_bytes, precision=FP64, max_cuts=8):
+        self.ctx = plan.ctx
+        self.plan = plan
+        h = ctypes.c_void_p()
+        _check(_lib().qt_plan_slice(self.ctx.handle if self.ctx else None, plan.handle, precision,
+                                    int(max_workspace_bytes), int(max_cuts), ctypes.byref(h)), self.ctx)
+        self.handle = h.value
+        self._register(self.ctx)
+
+    @property
+    def num_cuts(self):
+        return _lib().qt_sliced_num_cuts(self.handle)
+
+    @property
+    def num_slices(self):
+        return 4 ** self.num_cuts
+
+    def workspace_bytes(self, precision=FP64):
+        """workspace of one slice"""
+        return int(_lib().qt_plan_workspace_bytes(_lib().qt_sliced_plan(self.handle), precision))
+
+    @property
+    def slice_flops(self):
+        return int(_lib().qt_plan_flops(_lib().qt_sliced_plan(self.handle)))
+
+    def execute(self, precision=FP64):
+        v = np.zeros(2)
+        _check(_lib().qt_sliced_execute(self.handle, precision, _dp(v)), self.ctx)
+        return complex(v[0], v[1])
 
 
 class Batch(_Owned):

@@ -103,6 +103,11 @@ SIGNATURES = [
     ("qt_batch_upload", c_int, [c_void_p]),
     ("qt_batch_use_graph", c_int, [c_void_p, c_int]),
     ("qt_batch_use_resident", c_int, [c_void_p, c_double]),
+    ("qt_plan_slice", c_int, [c_void_p, c_void_p, c_int, c_uint64, c_int, P(c_void_p)]),
+    ("qt_sliced_num_cuts", c_int, [c_void_p]),
+    ("qt_sliced_plan", c_void_p, [c_void_p]),
+    ("qt_sliced_execute", c_int, [c_void_p, c_int, P(c_double)]),
+    ("qt_sliced_free", c_int, [c_void_p]),
     ("qt_batch_resident_starts", c_uint64, [c_void_p]),
     ("qt_batch_h2d_bytes", c_uint64, [c_void_p]),
     ("qt_batch_d2h_bytes", c_uint64, [c_void_p]),

@@ -25,7 +25,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-s
              "-I" + os.path.join(CUDA, "include")]
 
 CU_SOURCES = ["kernels.cu", "static_scratch.cu", "gemm_tc.cu"]
-CXX_SOURCES = ["core.cpp", "network.cpp", "orderings.cpp", "plan.cpp", "capi_host.cpp", "qaoa.cpp", "server.cpp",
+CXX_SOURCES = ["core.cpp", "network.cpp", "orderings.cpp", "plan.cpp", "capi_host.cpp", "qaoa.cpp", "server.cpp", "slicing.cpp",
                "inp.cpp"]
 HEADERS = ["engine.cuh", "kernels.h", "core.h", "plan.h", "gemm_tc.h"]
 

@@ -241,6 +241,47 @@ int64_t qt_network_node_values(qt_network *n, int id, double *out, int64_t cap) 
 // ---------------------------------------------------------------------------
 // plans
 
+}  // extern "C"
+
+namespace qtg {
+// The leaves (ranks, complex128 values, rotation leaves) of a network, and once
+// it is contracted, its recorded sequence and the lowered schedule.
+void plan_collect_leaves(qt_plan *p, const qtorch::Network &net) {
+    for (const auto &leaf : net.Leaves()) {
+        p->leaf_rank.push_back(leaf->mRank);
+        const auto &v = leaf->GetTensorVals();
+        const char *kind = nullptr;
+        switch (leaf->GetTypeOfNode()) {
+            case qtorch::GateType::RX: kind = "Rx"; break;
+            case qtorch::GateType::RY: kind = "Ry"; break;
+            case qtorch::GateType::RZ: kind = "Rz"; break;
+            case qtorch::GateType::PHASE: kind = "PHASE"; break;
+            case qtorch::GateType::CPHASE: kind = "CPHASE"; break;
+            default: break;
+        }
+        // a rotation leaf whose wires were sliced away is no longer the gate's table
+        if (kind && (int) v.size() == (1 << (2 * leaf->mRank)) && (leaf->mRank == 2 || leaf->mRank == 4)) {
+            p->rot_kind.push_back(kind);
+            p->rot_angle.push_back(qtorch::GateAngle(*leaf));
+            p->rot_elem.push_back(p->leaf_values.size());
+            p->rot_leaf.push_back((int) p->leaf_rank.size() - 1);
+        }
+        p->leaf_values.insert(p->leaf_values.end(), v.begin(), v.end());
+    }
+}
+
+qt_status plan_finish(qt_plan *p, const qtorch::Network &net) {
+    for (const auto &node : net.GetAllNodes()) {
+        if (node->mCreatedFrom.first == 0 && node->mCreatedFrom.second == 0) continue;
+        p->sequence.push_back(node->mCreatedFrom.first);
+        p->sequence.push_back(node->mCreatedFrom.second);
+    }
+    return lower_plan(p, net);
+}
+}  // namespace qtg
+
+extern "C" {
+
 qt_status qt_plan_build(qt_ctx *ctx, const char *qasm_text, const char *measure_text, const char *gate_dir,
                         qt_ordering ordering, uint64_t seed, const int32_t *pairs, int n_pairs, qt_plan **out) {
     // ctx may be NULL: the plan can then be inspected (sequence, sizes) but not executed
@@ -253,26 +294,7 @@ qt_status qt_plan_build(qt_ctx *ctx, const char *qasm_text, const char *measure_
         p->gate_dir = gate_dir ? gate_dir : "";
         std::unique_ptr<qt_plan> owner(p);
         auto net = qtorch::Network::FromText(p->qasm, p->measure, p->gate_dir, nullptr);
-        for (const auto &leaf : net->Leaves()) {
-            p->leaf_rank.push_back(leaf->mRank);
-            const auto &v = leaf->GetTensorVals();
-            const char *kind = nullptr;
-            switch (leaf->GetTypeOfNode()) {
-                case qtorch::GateType::RX: kind = "Rx"; break;
-                case qtorch::GateType::RY: kind = "Ry"; break;
-                case qtorch::GateType::RZ: kind = "Rz"; break;
-                case qtorch::GateType::PHASE: kind = "PHASE"; break;
-                case qtorch::GateType::CPHASE: kind = "CPHASE"; break;
-                default: break;
-            }
-            if (kind) {
-                p->rot_kind.push_back(kind);
-                p->rot_angle.push_back(qtorch::GateAngle(*leaf));
-                p->rot_elem.push_back(p->leaf_values.size());
-                p->rot_leaf.push_back((int) p->leaf_rank.size() - 1);
-            }
-            p->leaf_values.insert(p->leaf_values.end(), v.begin(), v.end());
-        }
+        plan_collect_leaves(p, *net);
         if (ordering == QT_ORDER_STOCHASTIC) {
             qtorch::ContractionTools t(net);
             t.Seed(seed);
@@ -290,12 +312,7 @@ qt_status qt_plan_build(qt_ctx *ctx, const char *qasm_text, const char *measure_
             return set_error(ctx, QT_ERR_INVALID_CONTRACTION_METHOD, "unknown ordering");
         }
         if (!net->IsDone()) return set_error(ctx, QT_ERR_CONTRACTION_FAILURE, "ordering did not finish the network");
-        for (const auto &node : net->GetAllNodes()) {
-            if (node->mCreatedFrom.first == 0 && node->mCreatedFrom.second == 0) continue;
-            p->sequence.push_back(node->mCreatedFrom.first);
-            p->sequence.push_back(node->mCreatedFrom.second);
-        }
-        qt_status s = lower_plan(p, *net);
+        qt_status s = plan_finish(p, *net);
         if (s != QT_OK) return s;
         *out = owner.release();
         return QT_OK;

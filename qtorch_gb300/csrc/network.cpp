@@ -587,7 +587,7 @@ std::shared_ptr<Node> Network::ContractNodes(std::shared_ptr<Node> nodeA, std::s
         }
     }
     // refusal rule of Network.h:772-777
-    if ((indicesA.empty() && !indicesC.empty()) ||
+    if ((indicesA.empty() && !indicesC.empty() && !mAllowOuter) ||
         (int) remaining.size() > std::max(nodeA->mRank, nodeB->mRank) + threshold)
         return nullptr;
     if (indicesA.size() != indicesB.size()) return nullptr;   // a wire listed twice: not a tensor network edge

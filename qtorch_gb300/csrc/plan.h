@@ -137,6 +137,8 @@ struct qt_batch {
 
 namespace qtg {
 qt_status lower_plan(qt_plan *p, const qtorch::Network &net);
+void plan_collect_leaves(qt_plan *p, const qtorch::Network &net);
+qt_status plan_finish(qt_plan *p, const qtorch::Network &net);
 qt_status upload_plan(qt_plan *p, int prec);
 void pack_leaves(const qt_plan *p, int prec, const std::complex<double> *src, char *dst);
 qt_status execute_stepwise(qt_plan *p, int prec, const std::complex<double> *leaves, double *value);
