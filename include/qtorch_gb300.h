@@ -251,6 +251,10 @@ qt_status qt_plan_slice(qt_ctx *ctx, const qt_plan *plan, qt_precision prec, uin
 int qt_sliced_num_cuts(const qt_sliced *s);
 qt_plan *qt_sliced_plan(const qt_sliced *s);   /* the plan of one slice (owned by s) */
 qt_status qt_sliced_execute(qt_sliced *s, qt_precision prec, double *re_im);
+/* The same for other values of the uncut plan's leaves (complex128, its leaf
+ * order; NULL: its own), on ctx, every slice step by step one at a time. */
+qt_status qt_sliced_execute_leaves(qt_ctx *ctx, const qt_sliced *s, qt_precision prec, const double *leaves,
+                                   double *re_im);
 qt_status qt_sliced_free(qt_sliced *s);
 
 /* ---- batches: many plan instances in one persistent grouped launch ------ */
@@ -410,7 +414,11 @@ int64_t qt_random_regular_graph(int num_nodes, int degree, uint64_t seed, char *
 
 /* A server admits requests while their plan's workspace fits the context's
  * memory budget and a slot is free, and runs every admitted request in grouped
- * launches; requests that arrive while others run join the next launch. */
+ * launches; requests that arrive while others run join the next launch.  A
+ * request whose workspace exceeds the whole budget is sliced at submission
+ * (qt_plan_slice, up to 8 cut wires, cached in the plan) so that one slice
+ * fits, and runs alone, slice by slice; QT_ERR_OUT_OF_MEMORY when no such
+ * slicing exists. */
 qt_status qt_server_create(qt_ctx *ctx, int max_inflight, qt_precision prec, qt_server **out);
 qt_status qt_server_free(qt_server *s);
 /* Submit (non-blocking).  *ticket identifies the request. */

@@ -535,9 +535,16 @@ class SlicedPlan(_Owned):
     def slice_flops(self):
         return int(_lib().qt_plan_flops(_lib().qt_sliced_plan(self.handle)))
 
-    def execute(self, precision=FP64):
+    def execute(self, precision=FP64, leaves=None):
+        """Sum over the slices; `leaves`: other values of the uncut plan's leaves
+        (complex128, its leaf order), every slice then step by step."""
         v = np.zeros(2)
-        _check(_lib().qt_sliced_execute(self.handle, precision, _dp(v)), self.ctx)
+        if leaves is None:
+            _check(_lib().qt_sliced_execute(self.handle, precision, _dp(v)), self.ctx)
+        else:
+            lv = np.ascontiguousarray(leaves, dtype=np.complex128)
+            _check(_lib().qt_sliced_execute_leaves(self.ctx.handle, self.handle, precision, _dp(lv.view(np.float64)),
+                                                   _dp(v)), self.ctx)
         return complex(v[0], v[1])
 
 

@@ -107,6 +107,7 @@ SIGNATURES = [
     ("qt_sliced_num_cuts", c_int, [c_void_p]),
     ("qt_sliced_plan", c_void_p, [c_void_p]),
     ("qt_sliced_execute", c_int, [c_void_p, c_int, P(c_double)]),
+    ("qt_sliced_execute_leaves", c_int, [c_void_p, c_void_p, c_int, P(c_double), P(c_double)]),
     ("qt_sliced_free", c_int, [c_void_p]),
     ("qt_batch_resident_starts", c_uint64, [c_void_p]),
     ("qt_batch_h2d_bytes", c_uint64, [c_void_p]),

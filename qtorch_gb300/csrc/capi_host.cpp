@@ -321,6 +321,8 @@ qt_status qt_plan_build(qt_ctx *ctx, const char *qasm_text, const char *measure_
 
 qt_status qt_plan_free(qt_plan *p) {
     if (!p) return QT_ERR_INVALID_ARGUMENT;
+    for (auto &v : p->slicings)
+        for (auto &e : v) qt_sliced_free(e.second);
     for (int i = 0; i < 2; i++)
         if (p->dev[i] && p->ctx) dev_free(p->ctx, p->dev[i]);
     delete p;

@@ -77,6 +77,8 @@ struct qt_plan {
     bool grouped = false;
     void *dev[2] = {nullptr, nullptr};
     size_t dev_bytes[2] = {0, 0};
+    // slicings made for a workspace budget (per precision: budget, slicing), freed with the plan
+    std::vector<std::pair<uint64_t, qt_sliced *>> slicings[2];
 };
 
 struct qt_batch {

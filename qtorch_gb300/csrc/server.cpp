@@ -5,7 +5,9 @@
 // memory budget and an in-flight slot is free.  Light requests (plans the
 // grouped interpreter takes) are grouped into waves that run as one grouped
 // launch; a heavy request (a plan run step by step with the whole-GPU
-// kernels) is a wave of its own.  Waves run on lanes, each lane with its own
+// kernels) is a wave of its own, and so is a request larger than the whole
+// budget, which is sliced at submission (qt_plan_slice) and runs slice by
+// slice.  Waves run on lanes, each lane with its own
 // CUDA stream, so a wave formed from requests that arrived while another wave
 // is on the GPU runs concurrently with it.  Lane 0 takes light waves only, so
 // light requests never queue behind a heavy one.  Each request's result is
@@ -26,6 +28,7 @@ namespace {
 struct Request {
     int64_t ticket;
     qt_plan *plan;
+    const qt_sliced *sliced = nullptr;   // the plan sliced to fit the budget (runs alone, slice by slice)
     std::vector<double> leaves;
     std::chrono::steady_clock::time_point t_submit;
     uint64_t footprint;
@@ -68,6 +71,9 @@ struct qt_server {
     std::thread dispatcher;
 };
 
+// slicings are cached in the plans, which several servers may share
+static std::mutex g_slicing_lock;
+
 static uint64_t footprint(const qt_plan *p, qt_precision prec) {
     return p->ws_bytes[prec] + p->leaf_bytes[prec] + 4096;
 }
@@ -85,13 +91,21 @@ static void lane_main(qt_server *s, int li) {
         std::vector<double> vals(2 * wave.size(), 0.0);
         const auto t_wave = std::chrono::steady_clock::now();
         qt_batch *b = nullptr;
-        qt_status st = qt_batch_create(lane.ctx, &b);
-        if (st == QT_OK) b->stepwise_macs = kLoneInstanceMaxMacs;   // waves are small: big plans take the whole GPU
-        for (auto &r : wave)
-            if (st == QT_OK) st = qt_batch_add(b, r.plan, r.leaves.empty() ? nullptr : r.leaves.data(), nullptr);
-        if (st == QT_OK) st = qt_batch_execute(b, s->prec, vals.data());
-        int nl = b ? qt_batch_launches_per_run(b) : 0;
-        if (b) qt_batch_free(b);
+        qt_status st = QT_OK;
+        int nl = 0;
+        if (wave.size() == 1 && wave[0].sliced) {
+            const Request &r = wave[0];
+            st = qt_sliced_execute_leaves(lane.ctx, r.sliced, s->prec, r.leaves.empty() ? nullptr : r.leaves.data(),
+                                          vals.data());
+        } else {
+            st = qt_batch_create(lane.ctx, &b);
+            if (st == QT_OK) b->stepwise_macs = kLoneInstanceMaxMacs;   // waves are small: big plans take the whole GPU
+            for (auto &r : wave)
+                if (st == QT_OK) st = qt_batch_add(b, r.plan, r.leaves.empty() ? nullptr : r.leaves.data(), nullptr);
+            if (st == QT_OK) st = qt_batch_execute(b, s->prec, vals.data());
+            nl = b ? qt_batch_launches_per_run(b) : 0;
+            if (b) qt_batch_free(b);
+        }
         const auto now = std::chrono::steady_clock::now();
         {
             std::lock_guard<std::mutex> g(s->m);
@@ -222,10 +236,27 @@ qt_status qt_server_submit(qt_server *s, qt_plan *plan, const double *leaves, in
     r.t_submit = std::chrono::steady_clock::now();
     r.footprint = footprint(plan, s->prec);
     r.heavy = !plan->grouped || plan->flops > kLoneInstanceMaxMacs;
+    const uint64_t budget = s->ctx->memory_budget;
+    if (budget && r.footprint > budget) {
+        // larger than the whole budget: sliced so that one slice fits, run alone
+        const uint64_t fixed = plan->leaf_bytes[s->prec] + 4096;
+        if (budget <= fixed) return set_error(s->ctx, QT_ERR_OUT_OF_MEMORY, "request larger than the budget");
+        const uint64_t target = budget - fixed;
+        std::lock_guard<std::mutex> g(g_slicing_lock);
+        for (auto &e : plan->slicings[s->prec])
+            if (e.first == target) r.sliced = e.second;
+        if (!r.sliced) {
+            qt_sliced *sl = nullptr;
+            qt_status st = qt_plan_slice(s->ctx, plan, s->prec, target, 8, &sl);
+            if (st != QT_OK) return set_error(s->ctx, st, "request larger than the budget, and no slicing fits it");
+            plan->slicings[s->prec].push_back({target, sl});
+            r.sliced = sl;
+        }
+        r.footprint = qt_plan_workspace_bytes(qt_sliced_plan(r.sliced), s->prec) + fixed;
+        r.heavy = true;
+    }
     {
         std::lock_guard<std::mutex> g(s->m);
-        const uint64_t budget = s->ctx->memory_budget;
-        if (budget && r.footprint > budget) return set_error(s->ctx, QT_ERR_OUT_OF_MEMORY, "request larger than the budget");
         r.ticket = s->next_ticket++;
         s->results[r.ticket] = Result();
         *ticket = r.ticket;

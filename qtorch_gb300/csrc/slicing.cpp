@@ -233,48 +233,54 @@ qt_status qt_plan_slice(qt_ctx *ctx, const qt_plan *p, qt_precision prec, uint64
 int qt_sliced_num_cuts(const qt_sliced *s) { return s ? (int) s->cuts.size() : -1; }
 qt_plan *qt_sliced_plan(const qt_sliced *s) { return s ? s->plan : nullptr; }
 
-qt_status qt_sliced_execute(qt_sliced *s, qt_precision prec, double *re_im) {
-    if (!s || !re_im || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return QT_ERR_INVALID_ARGUMENT;
-    if (!s->ctx) return QT_ERR_INVALID_ARGUMENT;   // built for inspection only
-    qt_ctx *ctx = s->ctx;
+}  // extern "C"
+
+namespace {
+
+// A batch of every slice of `s` built from the uncut leaves `orig` (the
+// plan's leaf order), on ctx.  stepwise_macs: instances above it run step by
+// step, one at a time.
+qt_status slice_batch(qt_ctx *ctx, const qt_sliced *s, const C *orig, int64_t stepwise_macs, qt_batch **out) {
     const uint64_t n = 1ull << (2 * s->cuts.size());
-    qt_status st = QT_OK;
-    if (!s->batch || s->batch_prec != (int) prec) {
-        if (s->batch) qt_batch_free(s->batch);
-        s->batch = nullptr;
-        st = qt_batch_create(ctx, &s->batch);
-        // instances that are large for one CTA run step by step, one at a time,
-        // so the budget holds one sliced workspace
-        if (st == QT_OK) s->batch->stepwise_macs = qtg::kLoneInstanceMaxMacs;
-        const size_t n_leaves = s->orig_rank.size();
-        for (uint64_t a = 0; a < n && st == QT_OK; a++) {
-            std::vector<std::vector<int>> pos, val;
-            cut_positions(s->cuts, a, n_leaves, pos, val);
-            std::vector<C> leaves;
-            leaves.reserve(s->plan->leaf_values.size());
-            for (size_t l = 0; l < n_leaves; l++) {
-                const C *t = s->orig_vals.data() + s->orig_off[l];
-                if (pos[l].empty()) {
-                    leaves.insert(leaves.end(), t, t + (1ull << (2 * s->orig_rank[l])));
-                } else {
-                    auto r = restrict_leaf(t, s->orig_rank[l], pos[l], val[l]);
-                    leaves.insert(leaves.end(), r.begin(), r.end());
-                }
-            }
-            if (leaves.size() != s->plan->leaf_values.size())
-                return qtg::set_error(ctx, QT_ERR_INVALID_ARGUMENT, "sliced leaves do not match the slice's plan");
-            int idx = 0;
-            st = qt_batch_add(s->batch, s->plan, reinterpret_cast<const double *>(leaves.data()), &idx);
-        }
-        if (st == QT_OK) st = qt_batch_prepare(s->batch, prec);
-        if (st != QT_OK) return st;
-        s->batch_prec = (int) prec;
-    }
-    std::vector<double> v(2 * n);
-    st = qt_batch_run(s->batch);
-    if (st == QT_OK) st = qt_batch_fetch(s->batch, v.data());
+    qt_batch *b = nullptr;
+    qt_status st = qt_batch_create(ctx, &b);
     if (st != QT_OK) return st;
-    double re = 0, im = 0;   // the slices' values in assignment order
+    b->stepwise_macs = stepwise_macs;
+    const size_t n_leaves = s->orig_rank.size();
+    for (uint64_t a = 0; a < n && st == QT_OK; a++) {
+        std::vector<std::vector<int>> pos, val;
+        cut_positions(s->cuts, a, n_leaves, pos, val);
+        std::vector<C> leaves;
+        leaves.reserve(s->plan->leaf_values.size());
+        for (size_t l = 0; l < n_leaves; l++) {
+            const C *t = orig + s->orig_off[l];
+            if (pos[l].empty()) {
+                leaves.insert(leaves.end(), t, t + (1ull << (2 * s->orig_rank[l])));
+            } else {
+                auto r = restrict_leaf(t, s->orig_rank[l], pos[l], val[l]);
+                leaves.insert(leaves.end(), r.begin(), r.end());
+            }
+        }
+        if (leaves.size() != s->plan->leaf_values.size())
+            st = qtg::set_error(ctx, QT_ERR_INVALID_ARGUMENT, "sliced leaves do not match the slice's plan");
+        int idx = 0;
+        if (st == QT_OK) st = qt_batch_add(b, s->plan, reinterpret_cast<const double *>(leaves.data()), &idx);
+    }
+    if (st != QT_OK) {
+        qt_batch_free(b);
+        return st;
+    }
+    *out = b;
+    return QT_OK;
+}
+
+// the slices' values summed in assignment order
+qt_status sum_slices(qt_batch *b, uint64_t n, double *re_im) {
+    std::vector<double> v(2 * n);
+    qt_status st = qt_batch_run(b);
+    if (st == QT_OK) st = qt_batch_fetch(b, v.data());
+    if (st != QT_OK) return st;
+    double re = 0, im = 0;
     for (uint64_t a = 0; a < n; a++) {
         re += v[2 * a];
         im += v[2 * a + 1];
@@ -282,6 +288,37 @@ qt_status qt_sliced_execute(qt_sliced *s, qt_precision prec, double *re_im) {
     re_im[0] = re;
     re_im[1] = im;
     return QT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+qt_status qt_sliced_execute(qt_sliced *s, qt_precision prec, double *re_im) {
+    if (!s || !re_im || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return QT_ERR_INVALID_ARGUMENT;
+    if (!s->ctx) return QT_ERR_INVALID_ARGUMENT;   // built for inspection only
+    if (!s->batch || s->batch_prec != (int) prec) {
+        if (s->batch) qt_batch_free(s->batch);
+        s->batch = nullptr;
+        // instances that are large for one CTA run step by step, one at a time
+        qt_status st = slice_batch(s->ctx, s, s->orig_vals.data(), qtg::kLoneInstanceMaxMacs, &s->batch);
+        if (st == QT_OK) st = qt_batch_prepare(s->batch, prec);
+        if (st != QT_OK) return st;
+        s->batch_prec = (int) prec;
+    }
+    return sum_slices(s->batch, 1ull << (2 * s->cuts.size()), re_im);
+}
+
+qt_status qt_sliced_execute_leaves(qt_ctx *ctx, const qt_sliced *s, qt_precision prec, const double *leaves,
+                                   double *re_im) {
+    if (!ctx || !s || !re_im || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return QT_ERR_INVALID_ARGUMENT;
+    // every slice step by step, one at a time: the device holds one slice's workspace
+    qt_batch *b = nullptr;
+    qt_status st = slice_batch(ctx, s, leaves ? reinterpret_cast<const C *>(leaves) : s->orig_vals.data(), -1, &b);
+    if (st == QT_OK) st = qt_batch_prepare(b, prec);
+    if (st == QT_OK) st = sum_slices(b, 1ull << (2 * s->cuts.size()), re_im);
+    if (b) qt_batch_free(b);
+    return st;
 }
 
 qt_status qt_sliced_free(qt_sliced *s) {

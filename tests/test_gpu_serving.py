@@ -78,3 +78,35 @@ def test_admission_respects_memory_budget():
             srv.close()
     finally:
         c.close()
+
+
+@pytest.mark.parametrize("prec", [qg.FP64, qg.MIXED])
+def test_requests_above_the_budget_are_sliced(prec):
+    """A request whose workspace exceeds the whole budget is split over cut
+    wires (qt_plan_slice) so that one slice fits, runs alone slice by slice, and
+    returns the unsliced value (FP64 to a few ulp, mixed within 1e-6); requests
+    that fit are served as before."""
+    from qtorch_gb300.circuits import random_circuit_text
+    c = qg.Context(0)
+    try:
+        big = qg.Plan(random_circuit_text(12, 12, 5), "Z", ordering="linegraph", ctx=c)
+        small = request_mix(c)[:4]
+        want = big.execute(qg.FP64)
+        budget = big.workspace_bytes(prec) // 8 + big.workspace_bytes(prec) // 64
+        c.set_memory_budget(budget)
+        srv = qg.Server(max_inflight=16, precision=prec, ctx=c)
+        try:
+            tickets = [srv.submit(big)] + [srv.submit(p) for p in small] + [srv.submit(big)]
+            srv.drain()
+            got = [srv.poll(t) for t in tickets]
+            assert all(g is not None for g in got)
+            vals = [g[0] for g in got]
+            tol = 1e-12 if prec == qg.FP64 else 1e-6
+            for v in (vals[0], vals[-1]):
+                assert abs(v - want) <= tol * max(1.0, abs(want))
+            for p, v in zip(small, vals[1:-1]):
+                assert abs(v - p.execute(prec)) <= (0 if prec == qg.FP64 else 1e-6)
+        finally:
+            srv.close()
+    finally:
+        c.close()

@@ -62,3 +62,5 @@ def test_sliced_value_equals_unsliced(ctx, name, div):
         v = s.execute(prec)
         assert abs(v - v64) <= tol * max(1.0, abs(v64)), (name, prec, s.num_cuts)
         assert s.execute(prec) == v   # the batch of slices is kept and replayed
+        # other leaf values: the same slicing, every slice step by step
+        assert abs(s.execute(prec, leaves=p.leaf_values()) - v) <= tol * max(1.0, abs(v64))
