@@ -603,13 +603,17 @@ class Batch(_Owned):
         """Values of every instance at new rotation angles in one call (gate
         tensors built on the device; the batch must be prepared for MIXED when
         angles are given)."""
-        out = np.zeros(2 * len(self))
+        out = np.empty(len(self._plans), dtype=np.complex128)
         if angles is None:
-            _check(_lib().qt_batch_evaluate(self.handle, None, 0, _dp(out)), self.ctx)
+            st = _lib().qt_batch_evaluate(self.handle, None, 0, out.ctypes.data)
         else:
-            a = np.ascontiguousarray(np.asarray(angles, dtype=np.float64))
-            _check(_lib().qt_batch_evaluate(self.handle, _dp(a), a.size, _dp(out)), self.ctx)
-        return out[0::2] + 1j * out[1::2]
+            a = angles
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+                a = np.ascontiguousarray(a, dtype=np.float64)
+            st = _lib().qt_batch_evaluate(self.handle, a.ctypes.data, a.size, out.ctypes.data)
+        if st:
+            _check(st, self.ctx)
+        return out
 
     def set_rotations_device(self, angles):
         """New rotation angles whose gate tensors are built on the device at the

@@ -90,7 +90,8 @@ SIGNATURES = [
     ("qt_plan_step_info", c_int, [c_void_p, c_int, P(c_int32), c_int]),
     ("qt_batch_set_rotations", c_int, [c_void_p, P(c_double), c_int64]),
     ("qt_batch_set_rotations_device", c_int, [c_void_p, P(c_double), c_int64]),
-    ("qt_batch_evaluate", c_int, [c_void_p, P(c_double), c_int64, P(c_double)]),
+    # the optimiser's inner loop: raw addresses, no ctypes pointer objects per call
+    ("qt_batch_evaluate", c_int, [c_void_p, c_void_p, c_int64, c_void_p]),
     ("qt_batch_create", c_int, [c_void_p, P(c_void_p)]),
     ("qt_batch_free", c_int, [c_void_p]),
     ("qt_batch_add", c_int, [c_void_p, c_void_p, P(c_double), P(c_int)]),

@@ -499,15 +499,8 @@ static qt_status resident_evaluate(qt_batch *b, const double *angles, int64_t n_
     if (n_angles != b->n_angles) return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "angle count does not match the batch");
     qt_status s = QT_OK;
     const size_t n = b->inst_desc.size();
-    auto any_left = [&]() {
-        for (size_t j = 0; j < n; j++)
-            if (__atomic_load_n(&b->h_mail[32 + j], __ATOMIC_ACQUIRE) == kResidentLeft) return true;
-        return false;
-    };
-    if (b->res_running && any_left()) {
-        s = resident_stop(b);   // CTAs leave on their own idle clocks: wait for the rest
-        if (s != QT_OK) return s;
-    }
+    // (an engine whose CTAs left while idle shows it in their flags: the wait
+    // below restarts it)
     // the previous request is complete, so the pinned angles are free
     if (b->res_running && n_angles) std::memcpy(b->h_angles, angles, sizeof(double) * n_angles);
     if (!b->res_running) {
@@ -541,6 +534,7 @@ static qt_status resident_evaluate(qt_batch *b, const double *angles, int64_t n_
             }
         }
         if (restart) {
+            // CTAs leave on their own idle clocks: stop the rest, start all again
             if (relaunched) return set_error(ctx, QT_ERR_CUDA, "resident engine left without answering");
             relaunched = true;
             s = resident_stop(b);

@@ -1102,8 +1102,7 @@ __global__ void __launch_bounds__(kPlanThreads, kMinCtas) resident_kernel(const 
             const double2 val = plan_final_value<true>(v, ws, h);
             I.value[0] = val.x;
             I.value[1] = val.y;
-            __threadfence_system();   // the value is visible to the host before the done flag
-            st_release_sys(rl.done + inst, s);
+            st_release_sys(rl.done + inst, s);   // release: the value is visible to the host before the flag
         }
         __syncthreads();   // s_seq, the header and the workspace are reused
     }
