@@ -338,7 +338,10 @@ int qt_batch_launches_per_run(const qt_batch *b);
  * batch order.  kernel_ctas picks the interpreter's register budget: the
  * variant compiled for 2 (128 registers a thread), 3 (80), 4 (64) or 5 (48)
  * resident CTAs per SM -- fewer registers, more warps to hide latency, some
- * spills; 0 takes 4 when the instances outnumber two CTAs per SM, else 2.
+ * spills -- or 1, the wide variant: 512 threads with 128 registers, one CTA
+ * per SM, for a few instances whose levels then take half the rounds; 0 takes
+ * 1 when there are no more instances than SMs, 4 when they outnumber two CTAs
+ * per SM, else 2.
  * The policy changes where data sits, which CTA runs an instance and how
  * registers are allocated, never the arithmetic: values are bit-identical
  * under every policy. */

@@ -484,7 +484,7 @@ static qt_status resident_start(qt_batch *b, uint32_t first_seq) {
     rl.idle_polls = (uint32_t) std::min(4.0e9, std::max(1.0, b->res_idle * 1.0e6));
     for (size_t j = 0; j < n; j++) __atomic_store_n(&b->h_mail[32 + j], 0u, __ATOMIC_RELAXED);   // no flag from a previous run
     __atomic_store_n(&b->h_mail[0], first_seq, __ATOMIC_RELEASE);
-    e = launch_resident(rl, b->res_stream);
+    e = launch_resident(rl, b->res_stream, b->variant);
     if (e != cudaSuccess) return cuda_error(ctx, e, "resident engine launch");
     ctx->launches++;
     b->res_starts++;
@@ -782,7 +782,8 @@ static qt_status batch_configure(qt_batch *b) {
     // cap, and the tile buffers when an instance has CTA-tiled steps; instances
     // beyond either region use the global slab / read in place
     // Defaults: a few instances (at most two CTAs per SM) get the 128-register
-    // interpreter and room to keep small workspaces and staged copies in shared
+    // interpreter -- the wide 512-thread form when one CTA per SM holds them
+    // all -- and room to keep small workspaces and staged copies in shared
     // memory; many instances are latency-bound and get the 64-register variant
     // with four CTAs per SM, which leaves room for small workspaces only.
     const qt_launch_policy &pol = b->policy;
@@ -813,7 +814,7 @@ static qt_status batch_configure(qt_batch *b) {
     const size_t smem = plan_header_bytes(b->header_steps) + 128 + b->ws_smem_bytes + b->stage_bytes + b->tile_bytes;
     if (n_grouped && smem > plan_smem_limit())
         return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "launch policy needs more shared memory than a CTA may have");
-    b->variant = pol.kernel_ctas ? pol.kernel_ctas : (many ? 4 : 2);
+    b->variant = pol.kernel_ctas ? pol.kernel_ctas : many ? 4 : n_grouped <= plan_num_sms() ? 1 : 2;
     b->grid = n_grouped ? std::min(n_grouped, plan_max_grid(smem, pol.ctas_per_sm, b->variant)) : 0;
     qt_status s = QT_OK;
     if (b->grid > 0 && !b->ws_in_smem) s = dev_alloc(ctx, b->ws_stride * b->grid, &b->d_ws);
@@ -1097,7 +1098,7 @@ qt_status qt_batch_use_resident(qt_batch *b, double idle_seconds) {
     if (!b->stepwise.empty() || b->inst_desc.empty())
         return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "resident evaluation needs every instance in the grouped launch");
     const size_t smem = plan_header_bytes(b->header_steps) + 128 + b->ws_smem_bytes + b->stage_bytes + b->tile_bytes;
-    if ((int) b->inst_desc.size() > b->grid || (int) b->inst_desc.size() > resident_capacity(smem))
+    if ((int) b->inst_desc.size() > b->grid || (int) b->inst_desc.size() > resident_capacity(smem, b->variant))
         return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "resident evaluation needs one resident CTA per instance");
     qt_status s = resident_stop(b);   // a new idle limit takes effect at the next start
     b->res_idle = std::min(idle_seconds, 3600.0);

@@ -20,6 +20,11 @@ namespace qtg {
 constexpr int kMaxWires = 24;      // rank limit of one operand (4^24 elements is far beyond HBM)
 constexpr uint8_t kNoWire = 0xff;
 constexpr int kPlanThreads = 256;              // threads of one interpreter CTA
+// threads of the wide interpreter variant: one CTA of 512 threads per SM (the
+// whole register file at 128 registers a thread) for launches with at most one
+// instance per SM, where a level's work items then take half the rounds
+constexpr int kPlanThreadsWide = 512;
+__host__ __device__ constexpr int plan_threads(int min_ctas) { return min_ctas == 1 ? kPlanThreadsWide : kPlanThreads; }
 constexpr int kPlanMaxSteps = 1024;            // steps of a plan the interpreter takes
 // per-step scale bookkeeping in shared memory: 8 bytes a step, for as many
 // steps as the largest plan of a launch has (rounded up to 128 bytes)

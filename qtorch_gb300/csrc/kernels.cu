@@ -582,7 +582,8 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, const HotStep *__
 // CTA-wide tiled step: the contraction as a product of the gathered matrices
 // A~(m, k) = A[oa(m) + ka(k)] and B~(k, n) = B[ob(n) + kb(k)], C[m + M n].
 // A tile of TM x TN outputs is split over 16 x 16 threads (MI x NJ outputs
-// each, rows tx + 16 i, columns ty + 16 j); the summed range runs in chunks
+// each, rows tx + 16 i, columns ty + 16 j; threads beyond 256, in the wide
+// interpreter, only help gather); the summed range runs in chunks
 // whose A~ and B~ slices are gathered into shared memory once and reused by
 // every thread of the tile.  Each output still accumulates over k in
 // increasing order, so the FP64 form keeps the reference's rounding.
@@ -635,7 +636,7 @@ __device__ float tiled_tiles(const StepDesc &d, const typename std::conditional<
                 Bs[kk * kCtaTileDim + n] = B[s_ob[n] + (uint32_t) scatter_digits(k0 + kk, d.posBs, (int) nSum)];
             }
             __syncthreads();
-            for (uint32_t kk = 0; kk < kc; kk++) {
+            for (uint32_t kk = 0; kk < kc && tid < 256u; kk++) {
                 V a[MI];
 #pragma unroll
                 for (int i = 0; i < MI; i++) a[i] = As[kk * kCtaTileDim + tx + 16 * i];
@@ -650,6 +651,7 @@ __device__ float tiled_tiles(const StepDesc &d, const typename std::conditional<
                 }
             }
         }
+        if (tid >= 256u) continue;   // (the next tile starts with a barrier every thread reaches)
 #pragma unroll
         for (int i = 0; i < MI; i++)
 #pragma unroll
@@ -928,9 +930,10 @@ __device__ __forceinline__ double2 plan_final_value(const PlanView &v, const cha
 
 // kMinCtas: the register budget -- the variant is compiled for that many
 // resident CTAs per SM (2: up to 128 registers a thread; 3: 80, 4: 64 and
-// 5: 48, with some spills), trading single-instance latency for warps per SM
+// 5: 48, with some spills), trading single-instance latency for warps per SM.
+// kMinCtas = 1 is the wide variant: 512 threads, 128 registers, one CTA per SM.
 template <bool kMixed, int kMinCtas>
-__global__ void __launch_bounds__(kPlanThreads, kMinCtas) plan_kernel(const PlanLaunch lp) {
+__global__ void __launch_bounds__(plan_threads(kMinCtas), kMinCtas) plan_kernel(const PlanLaunch lp) {
     extern __shared__ __align__(256) unsigned char smem_raw[];
     const uint32_t header_bytes = plan_header_bytes(lp.header_steps);
     PlanSmemHeader h{reinterpret_cast<uint32_t *>(smem_raw), reinterpret_cast<int32_t *>(smem_raw + 4u * lp.header_steps)};
@@ -1031,7 +1034,7 @@ __device__ __forceinline__ void st_release_sys(uint32_t *p, uint32_t v) {
 // poll gives up after idle_polls (the CTA leaves; the host relaunches it on the
 // next request) and the staging wait after about a second.
 template <int kMinCtas>
-__global__ void __launch_bounds__(kPlanThreads, kMinCtas) resident_kernel(const ResidentLaunch rl) {
+__global__ void __launch_bounds__(plan_threads(kMinCtas), kMinCtas) resident_kernel(const ResidentLaunch rl) {
     const PlanLaunch &lp = rl.lp;
     const int inst = blockIdx.x;
     if (inst >= lp.n_instances) return;
@@ -1150,11 +1153,23 @@ using PlanKernelFn = void (*)(const PlanLaunch);
 
 static PlanKernelFn plan_kernel_fn(bool mixed, int ctas) {
     switch (ctas) {
+    case 1: return mixed ? plan_kernel<true, 1> : plan_kernel<false, 1>;
     case 3: return mixed ? plan_kernel<true, 3> : plan_kernel<false, 3>;
     case 4: return mixed ? plan_kernel<true, 4> : plan_kernel<false, 4>;
     case 5: return mixed ? plan_kernel<true, 5> : plan_kernel<false, 5>;
     default: return mixed ? plan_kernel<true, 2> : plan_kernel<false, 2>;
     }
+}
+
+template <typename Fn>
+static cudaError_t raise_smem_limit(Fn fn, int dev);
+
+// the resident engine comes in the default (256 threads, 2 CTAs per SM) and
+// the wide (512 threads, 1 CTA per SM) form
+static int resident_variant(int variant) { return variant == 1 ? 1 : kPlanDefaultVariant; }
+using ResidentKernelFn = void (*)(const ResidentLaunch);
+static ResidentKernelFn resident_kernel_fn(int variant) {
+    return resident_variant(variant) == 1 ? resident_kernel<1> : resident_kernel<kPlanDefaultVariant>;
 }
 
 template <typename Fn>
@@ -1178,6 +1193,7 @@ static cudaError_t plan_attributes() {
         for (bool mixed : {true, false})
             if (e == cudaSuccess) e = raise_smem_limit(plan_kernel_fn(mixed, ctas), dev);
     if (e == cudaSuccess) e = raise_smem_limit(resident_kernel<kPlanDefaultVariant>, dev);
+    if (e == cudaSuccess) e = raise_smem_limit(resident_kernel<1>, dev);
     if (e == cudaSuccess && dev >= 0 && dev < 64) g_attr_done[dev] = true;
     return e;
 }
@@ -1216,7 +1232,8 @@ int plan_num_sms() { return num_sms(); }
 int plan_max_grid(size_t smem_bytes, int per_sm_cap, int variant) {
     int per_sm = 0;
     plan_attributes();
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, plan_kernel_fn(true, variant), kPlanThreads, smem_bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, plan_kernel_fn(true, variant), plan_threads(variant),
+                                                  smem_bytes);
     cudaGetLastError();
     if (per_sm_cap > 0) per_sm = std::min(per_sm, per_sm_cap);
     if (per_sm < 1) per_sm = 1;
@@ -1240,12 +1257,14 @@ size_t plan_smem_limit() {
             }
             static_max = std::max(static_max, fa.sharedSizeBytes);
         }
-    cudaFuncAttributes fr;
-    if (cudaFuncGetAttributes(&fr, resident_kernel<kPlanDefaultVariant>) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
+    for (ResidentKernelFn fn : {resident_kernel_fn(1), resident_kernel_fn(kPlanDefaultVariant)}) {
+        cudaFuncAttributes fr;
+        if (cudaFuncGetAttributes(&fr, fn) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        static_max = std::max(static_max, fr.sharedSizeBytes);
     }
-    static_max = std::max(static_max, fr.sharedSizeBytes);
     return (size_t) optin - static_max;
 }
 
@@ -1259,24 +1278,25 @@ cudaError_t launch_plan(const PlanLaunch &lp, bool mixed, int grid, cudaStream_t
     cudaError_t e = plan_attributes();
     if (e != cudaSuccess) return e;
     if (grid <= 0 || grid > lp.n_instances) grid = lp.n_instances;
-    plan_kernel_fn(mixed, variant)<<<grid, kPlanThreads, smem, stream>>>(lp);
+    plan_kernel_fn(mixed, variant)<<<grid, plan_threads(variant), smem, stream>>>(lp);
     return cudaGetLastError();
 }
 
-int resident_capacity(size_t smem_bytes) {
+int resident_capacity(size_t smem_bytes, int variant) {
     int per_sm = 0;
     plan_attributes();
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, resident_kernel<kPlanDefaultVariant>, kPlanThreads,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, resident_kernel_fn(variant), plan_threads(resident_variant(variant)),
                                                   smem_bytes);
     cudaGetLastError();
     return num_sms() * std::max(per_sm, 0);
 }
 
-cudaError_t launch_resident(const ResidentLaunch &rl, cudaStream_t stream) {
+cudaError_t launch_resident(const ResidentLaunch &rl, cudaStream_t stream, int variant) {
     if (rl.lp.n_instances <= 0) return cudaSuccess;
     cudaError_t e = plan_attributes();
     if (e != cudaSuccess) return e;
-    resident_kernel<kPlanDefaultVariant><<<rl.lp.n_instances, kPlanThreads, plan_smem_bytes(rl.lp), stream>>>(rl);
+    resident_kernel_fn(variant)<<<rl.lp.n_instances, plan_threads(resident_variant(variant)), plan_smem_bytes(rl.lp),
+                                  stream>>>(rl);
     return cudaGetLastError();
 }
 

@@ -37,8 +37,9 @@ cudaError_t launch_reduce_exact(const StepDesc &d, const double2 *A, const doubl
 // its shared memory (ws_in_smem; ws_stride bytes after the header) or
 // ws_base + blockIdx.x * ws_stride in global memory; with stage_bytes > 0 each
 // instance's plan block and leaf image are copied into shared memory first.
-// variant: the register budget, one of kPlanVariants (CTAs per SM it is built for)
-constexpr int kPlanVariants[] = {2, 3, 4, 5};
+// variant: the register budget, one of kPlanVariants (CTAs per SM it is built
+// for; 1 is the wide form, 512 threads a CTA)
+constexpr int kPlanVariants[] = {1, 2, 3, 4, 5};
 constexpr int kPlanDefaultVariant = 2;
 cudaError_t launch_plan(const PlanLaunch &lp, bool mixed, int grid, cudaStream_t stream,
                         int variant = kPlanDefaultVariant);
@@ -50,10 +51,10 @@ int plan_max_grid(size_t smem_bytes, int per_sm_cap = 0, int variant = kPlanDefa
 int plan_num_sms();
 // largest dynamic shared memory an interpreter CTA may have on this device
 size_t plan_smem_limit();
-// The resident engine (one CTA per instance, 128-register budget); returns
-// once launched.  resident_capacity: how many CTAs of that shared-memory size
-// are resident at once.
-cudaError_t launch_resident(const ResidentLaunch &rl, cudaStream_t stream);
-int resident_capacity(size_t smem_bytes);
+// The resident engine (one CTA per instance, 128-register budget; variant 1:
+// the wide 512-thread form, otherwise 256 threads); returns once launched.
+// resident_capacity: how many CTAs of that shared-memory size are resident at once.
+cudaError_t launch_resident(const ResidentLaunch &rl, cudaStream_t stream, int variant);
+int resident_capacity(size_t smem_bytes, int variant);
 
 }  // namespace qtg

@@ -41,6 +41,7 @@ POLICIES = [
     dict(kernel_ctas=4, ws_smem_cap=16 << 10),         # 64 registers a thread
     dict(kernel_ctas=3, stage_cap=0),
     dict(kernel_ctas=5, ws_smem_cap=0, stage_cap=0),   # 48 registers a thread
+    dict(kernel_ctas=1),                               # 512 threads a CTA, one CTA per SM
 ]
 
 
