@@ -19,6 +19,7 @@
 #include <thread>
 #include <unordered_map>
 
+#include "kernels.h"
 #include "plan.h"
 
 using namespace qtg;
@@ -99,7 +100,12 @@ static void lane_main(qt_server *s, int li) {
                                           vals.data());
         } else {
             st = qt_batch_create(lane.ctx, &b);
-            if (st == QT_OK) b->stepwise_macs = kLoneInstanceMaxMacs;   // waves are small: big plans take the whole GPU
+            if (st == QT_OK) {
+                b->stepwise_macs = kLoneInstanceMaxMacs;   // waves are small: big plans take the whole GPU
+                // the wide interpreter takes a whole SM per instance: a wave
+                // larger than its lanes' share of the SMs uses two CTAs per SM
+                if ((int) wave.size() * (int) s->lanes.size() > plan_num_sms()) b->policy.kernel_ctas = 2;
+            }
             for (auto &r : wave)
                 if (st == QT_OK) st = qt_batch_add(b, r.plan, r.leaves.empty() ? nullptr : r.leaves.data(), nullptr);
             if (st == QT_OK) st = qt_batch_execute(b, s->prec, vals.data());
