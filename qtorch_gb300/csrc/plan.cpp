@@ -64,8 +64,12 @@ private:
 };
 
 // A step runs CTA-wide as a tiled product when C's digits are A's free wires
-// followed by B's (the ContractNodes order), both sides give at least 16 rows
-// and the output has at least 4 elements per thread.
+// followed by B's (the ContractNodes order) and both sides give at least 16
+// rows (an output of at least one element per thread).  Its operand slices are
+// gathered once per chunk of the sum and reused across the tile, where work
+// items would each load their own operands: with workspaces in global memory
+// this took the 16-point batched QAOA step from 2.15 to 1.92 ms (requiring 4
+// elements per thread instead).
 static bool cta_tiled(const qtorch::StepRecord &r) {
     int fa = 0, fb = 0;
     for (size_t i = 0; i < r.freeIdx.size(); i++) {
@@ -76,7 +80,7 @@ static bool cta_tiled(const qtorch::StepRecord &r) {
             fb++;
         }
     }
-    return fa >= 2 && fb >= 2 && fa + fb >= 5 && !r.sumIdx.empty();
+    return fa >= 2 && fb >= 2 && !r.sumIdx.empty();
 }
 
 qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
