@@ -684,13 +684,14 @@ def run_reference(args):
     pool = mp.get_context("spawn").Pool(cores)
     times = []
     n_terms = len(seqs)
+    chunk = max(1, -(-n_terms // cores))   # one task per core and step: the least dispatch overhead
     for j in range(args.warmup + args.steps):
         pt = points[j % len(points)]
         t0 = time.perf_counter()
         # the reference's own per-step work: write each term's QASM text, parse it, contract it
         terms = qaoa_terms.all_terms(dgf, P, [pt[0], pt[1]])
         jobs = [(q, m, s) for (_, q, m), s in zip(terms, seqs)]
-        pool.map(_cpu_worker, jobs)
+        pool.map(_cpu_worker, jobs, chunksize=chunk)
         if j >= args.warmup:
             times.append(time.perf_counter() - t0)
     pool.close()
