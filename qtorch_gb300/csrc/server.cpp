@@ -10,8 +10,10 @@
 // slice.  Waves run on lanes, each lane with its own
 // CUDA stream, so a wave formed from requests that arrived while another wave
 // is on the GPU runs concurrently with it.  Lane 0 takes light waves only, so
-// light requests never queue behind a heavy one.  Each request's result is
-// independent of what it was batched with: an instance only ever touches its
+// light requests never queue behind a heavy one; it also leaves mid-size
+// grouped requests (more than 2^20 complex MACs) to the other lanes.  Each
+// request's result is independent of what it was batched with: an instance
+// only ever touches its
 // own leaves and its CTA's workspace.
 #include <algorithm>
 #include <condition_variable>
@@ -34,6 +36,7 @@ struct Request {
     std::chrono::steady_clock::time_point t_submit;
     uint64_t footprint;
     bool heavy;
+    bool small;   // lane 0 material: grouped and at most kLaneZeroMaxMacs
 };
 
 struct Result {
@@ -74,6 +77,11 @@ struct qt_server {
 
 // slicings are cached in the plans, which several servers may share
 static std::mutex g_slicing_lock;
+
+// Lane 0 serves small requests only (a QAOA term is 1e4-3e5 complex MACs):
+// a mid-size request (a 12-14 qubit circuit, 1e6-1.6e7 MACs) takes one CTA
+// for a millisecond or more and would hold up the small ones behind it.
+constexpr int64_t kLaneZeroMaxMacs = 1ll << 20;
 
 static uint64_t footprint(const qt_plan *p, qt_precision prec) {
     return p->ws_bytes[prec] + p->leaf_bytes[prec] + 4096;
@@ -147,18 +155,18 @@ static void dispatcher_main(qt_server *s) {
         s->cv.wait(g, [&] {
                 if (s->stop) return true;
             if (s->pending.empty()) return false;
-            bool any_light = false;
-            for (auto &r : s->pending) any_light = any_light || !r.heavy;
+            bool any_small = false;
+            for (auto &r : s->pending) any_small = any_small || r.small;
             for (size_t i = 0; i < s->lanes.size(); i++)
-                if (!s->lanes[i].busy && (i > 0 || any_light)) return true;
+                if (!s->lanes[i].busy && (i > 0 || any_small)) return true;
             return false;
         });
         if (s->stop) return;
-        bool any_light = false;
-        for (auto &r : s->pending) any_light = any_light || !r.heavy;
+        bool any_small = false;
+        for (auto &r : s->pending) any_small = any_small || r.small;
         int li = -1;
         for (int i = 0; i < (int) s->lanes.size(); i++)
-            if (!s->lanes[i].busy && (i > 0 || any_light)) {
+            if (!s->lanes[i].busy && (i > 0 || any_small)) {
                 li = i;
                 break;
             }
@@ -169,7 +177,7 @@ static void dispatcher_main(qt_server *s) {
         const uint64_t budget = s->ctx->memory_budget;
         const bool take_heavy = li > 0 && s->pending.front().heavy;
         for (auto it = s->pending.begin(); it != s->pending.end() && s->inflight < s->max_inflight;) {
-            if (it->heavy != take_heavy) {
+            if (it->heavy != take_heavy || (li == 0 && !it->small)) {
                 ++it;
                 continue;
             }
@@ -242,6 +250,7 @@ qt_status qt_server_submit(qt_server *s, qt_plan *plan, const double *leaves, in
     r.t_submit = std::chrono::steady_clock::now();
     r.footprint = footprint(plan, s->prec);
     r.heavy = !plan->grouped || plan->flops > kLoneInstanceMaxMacs;
+    r.small = !r.heavy && plan->flops <= kLaneZeroMaxMacs;
     const uint64_t budget = s->ctx->memory_budget;
     if (budget && r.footprint > budget) {
         // larger than the whole budget: sliced so that one slice fits, run alone
@@ -260,6 +269,7 @@ qt_status qt_server_submit(qt_server *s, qt_plan *plan, const double *leaves, in
         }
         r.footprint = qt_plan_workspace_bytes(qt_sliced_plan(r.sliced), s->prec) + fixed;
         r.heavy = true;
+        r.small = false;
     }
     {
         std::lock_guard<std::mutex> g(s->m);
