@@ -375,6 +375,69 @@ WalkCost walk_cost(const std::vector<int> &order, const std::vector<std::array<i
     return c;
 }
 
+// An order that builds the contraction tree in rounds: every round merges a
+// maximal set of disjoint pairs of the current nodes joined by a wire,
+// smallest merged rank first (then fewest MACs), and never a pair whose merge
+// would exceed `cap` wires unless no pair fits.  Each round adds at most one
+// level to the tree, so the height is about log2 of the node count when the
+// graph allows.
+std::vector<int> matching_order(const std::vector<std::array<int, 2>> &ends, int n_nodes, int cap) {
+    std::vector<int> parent(n_nodes);
+    std::vector<std::set<int>> wires(n_nodes);
+    for (int i = 0; i < n_nodes; i++) parent[i] = i;
+    for (size_t v = 0; v < ends.size(); v++) {
+        wires[ends[v][0]].insert((int) v);
+        wires[ends[v][1]].insert((int) v);
+    }
+    std::function<int(int)> find = [&](int x) { return parent[x] == x ? x : parent[x] = find(parent[x]); };
+    std::vector<int> order;
+    std::vector<char> placed(ends.size(), 0);
+    for (;;) {
+        struct Cand {
+            int merged, shared, v, a, b;
+        };
+        std::vector<Cand> cands;
+        std::set<std::pair<int, int>> seen;
+        for (size_t v = 0; v < ends.size(); v++) {
+            const int a = find(ends[v][0]), b = find(ends[v][1]);
+            if (a == b || !seen.insert({std::min(a, b), std::max(a, b)}).second) continue;
+            int shared = 0;
+            for (int w : wires[a]) shared += (int) wires[b].count(w);
+            const int merged = (int) (wires[a].size() + wires[b].size()) - 2 * shared;
+            cands.push_back({merged, shared, (int) v, a, b});
+        }
+        if (cands.empty()) break;
+        std::sort(cands.begin(), cands.end(), [](const Cand &x, const Cand &y) {
+            if (x.merged != y.merged) return x.merged < y.merged;
+            if (x.merged + x.shared != y.merged + y.shared) return x.merged + x.shared < y.merged + y.shared;
+            return x.v < y.v;
+        });
+        std::vector<char> used(n_nodes, 0);
+        std::vector<Cand> round;
+        for (const auto &c : cands) {
+            if (used[c.a] || used[c.b] || c.merged > cap) continue;
+            used[c.a] = used[c.b] = 1;
+            round.push_back(c);
+        }
+        if (round.empty()) round.push_back(cands.front());
+        for (const auto &c : round) {
+            order.push_back(c.v);
+            placed[c.v] = 1;
+            std::set<int> merged;
+            for (int w : wires[c.a])
+                if (!wires[c.b].count(w)) merged.insert(w);
+            for (int w : wires[c.b])
+                if (!wires[c.a].count(w)) merged.insert(w);
+            parent[c.a] = c.b;
+            wires[c.b].swap(merged);
+            wires[c.a].clear();
+        }
+    }
+    for (size_t v = 0; v < ends.size(); v++)   // wires already summed inside a node
+        if (!placed[v]) order.push_back((int) v);
+    return order;
+}
+
 }  // namespace
 
 const std::vector<int> &LineGraph::MinFillOrdering() {
@@ -406,7 +469,9 @@ const std::vector<int> &LineGraph::MinFillOrdering() {
     // the lowest estimated GPU time wins among those that create no larger
     // intermediate than classic min-fill: ~1.5 us per dependent level of the
     // interpreter plus the MACs at one CTA's ~2e9 complex MAC/s -- height decides
-    // for tiny networks, MACs for large ones.
+    // for tiny networks, MACs for large ones.  (Weighting MACs 5-25x lower, so
+    // that shallower trees with more MACs win, was measured slower everywhere:
+    // batched QAOA 1.90 -> 2.88 ms, config-3 terms 189 -> 195 us.)
     auto est = [](const WalkCost &c) { return 1.5e-6 * c.height + c.macs / 2e9; };
     std::vector<int> classic = min_fill_order(adj, ends, n_nodes, false);
     const WalkCost cc = walk_cost(classic, ends, n_nodes);
@@ -423,6 +488,20 @@ const std::vector<int> &LineGraph::MinFillOrdering() {
         if (est(c) < est(pc)) {
             pick = std::move(o);
             pc = c;
+        }
+    }
+    // trees built in rounds of disjoint merges (lowest height), for small
+    // graphs; where intermediates are tiny anyway (rank <= 6, 32 KB in
+    // complex64) they may grow by up to two wires over classic min-fill
+    if (n <= 400) {
+        const int allowed = std::max(cc.peak, std::min(cc.peak + 2, 6));
+        for (int cap = cc.peak; cap <= allowed; cap++) {
+            std::vector<int> o = matching_order(ends, n_nodes, cap);
+            const WalkCost c = walk_cost(o, ends, n_nodes);
+            if (c.peak <= allowed && est(c) < est(pc)) {
+                pick = std::move(o);
+                pc = c;
+            }
         }
     }
     for (int v : pick) mOrder.push_back(v + 1);
