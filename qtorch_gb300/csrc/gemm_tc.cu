@@ -46,12 +46,9 @@ constexpr int kGemmThreads = 128;
 constexpr uint32_t kAccBig = 3;
 constexpr uint32_t kTmemCols = 128 * (kAccBig + 1);
 
-__host__ __device__ inline uint64_t tiled_offset(uint64_t r, uint64_t k, uint64_t k_tiles) {
-    // tiles ordered [row tile][k tile]; canonical core-matrix layout inside a tile
-    const uint64_t tile = (r / kTileM) * k_tiles + k / kTileK;
-    const uint64_t rr = r % kTileM, kk = k % kTileK;
-    return tile * (kTileBytes / 4) + ((rr / 8) * 8 + kk / 4) * 32 + (rr % 8) * 4 + (kk % 4);
-}
+// Operand layout: tiles ordered [row tile][k tile], each kTileM x kTileK in the
+// canonical core-matrix order, element (rr, kk) of a tile at
+// ((rr / 8) * 8 + kk / 4) * 32 + (rr % 8) * 4 + kk % 4.
 
 // x -> hi + lo, both exact TF32 values (10 explicit mantissa bits), each rounded
 // to nearest (ties away from zero: add half an ulp of TF32, then clear the 13
@@ -67,40 +64,51 @@ __device__ __forceinline__ void split_tf32(float x, float &hi, float &lo) {
     lo = round_tf32(x - hi);   // x - hi is exact in FP32
 }
 
-// X: rows m < M, columns j < 2K; Y: rows i < 2N, columns j < 2K (see the file comment).
-__global__ void pack_operand(const float2 *__restrict__ src, const StepDesc d, int which, uint64_t rows,
-                             uint64_t rows_padded, uint64_t K, uint64_t k_tiles, float *__restrict__ hi,
-                             float *__restrict__ lo) {
-    const uint64_t cols_padded = k_tiles * kTileK;
-    const uint64_t total = rows_padded * cols_padded;
+// X: rows m < M, columns j < 2K; Y: rows i < 2N, columns j < 2K (see the file
+// comment).  One CTA per (row tile, k tile) of an operand: the tile's 128 row
+// offsets and 32 column offsets into the gathered operand are computed once
+// into shared memory, then its 4096 values are gathered, split hi/lo and
+// written in the tile's own canonical core-matrix order, so each warp's stores
+// are contiguous and no thread divides.
+__global__ void __launch_bounds__(256) pack_tiles(const float2 *__restrict__ src, const StepDesc d, int which,
+                                                  uint64_t rows, uint64_t K, uint64_t k_tiles,
+                                                  float *__restrict__ hi, float *__restrict__ lo) {
+    __shared__ uint64_t row_off[kTileM];
+    __shared__ uint64_t col_off[kTileK];
+    const uint64_t tk = blockIdx.x, tr = blockIdx.y;   // k tile, row tile
+    const uint32_t tid = threadIdx.x;
     const uint64_t M = 1ull << (2 * d.fA);
-    for (uint64_t t = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (uint64_t) gridDim.x * blockDim.x) {
-        const uint64_t r = t / cols_padded, j = t % cols_padded;
+    if (tid < (uint32_t) kTileM) {
+        const uint64_t r = tr * kTileM + tid;
+        uint64_t oa = 0, ob = 0;
+        // X row m: A's free digits; Y rows 2n, 2n+1: the B digits of output column n
+        if (r < rows) scatter_c(which == 0 ? r : (r >> 1) * M, d, oa, ob);
+        row_off[tid] = which == 0 ? oa : ob;
+    } else if (tid < (uint32_t) (kTileM + kTileK)) {
+        const uint64_t j = tk * kTileK + (tid - kTileM);
+        const uint64_t k = j < K ? j : j - K;
+        col_off[tid - kTileM] = j < 2 * K ? scatter_digits(k, which == 0 ? d.posAs : d.posBs, d.nSum) : 0;
+    }
+    __syncthreads();
+    float *const th = hi + (tr * k_tiles + tk) * (uint64_t) (kTileBytes / 4);
+    float *const tl = lo + (tr * k_tiles + tk) * (uint64_t) (kTileBytes / 4);
+    for (uint32_t p = tid; p < (uint32_t) (kTileM * kTileK); p += blockDim.x) {
+        // p = ((rr / 8) * 8 + kk / 4) * 32 + (rr % 8) * 4 + kk % 4 (tiled_offset inside a tile)
+        const uint32_t kk = (p & 3u) | (((p >> 5) & 7u) << 2);
+        const uint32_t rr = ((p >> 2) & 7u) | ((p >> 8) << 3);
+        const uint64_t r = tr * kTileM + rr, j = tk * kTileK + kk;
         float v = 0.f;
         if (r < rows && j < 2 * K) {
-            const uint64_t k = j < K ? j : j - K;
             const bool second = j >= K;
-            if (which == 0) {
-                // X row m: free digits of A, then the summed digits
-                uint64_t oa, ob;
-                scatter_c(r, d, oa, ob);   // r < M: only A digits are non-zero
-                const float2 a = src[oa + scatter_digits(k, d.posAs, d.nSum)];
-                v = second ? a.y : a.x;
-            } else {
-                const uint64_t n = r >> 1;
-                uint64_t oa, ob;
-                scatter_c(n * M, d, oa, ob);   // the B digits of output column n
-                const float2 b = src[ob + scatter_digits(k, d.posBs, d.nSum)];
-                if ((r & 1) == 0) v = second ? -b.y : b.x;
-                else v = second ? b.x : b.y;
-            }
+            const float2 x = src[row_off[rr] + col_off[kk]];
+            if (which == 0) v = second ? x.y : x.x;
+            else if ((r & 1) == 0) v = second ? -x.y : x.x;
+            else v = second ? x.x : x.y;
         }
         float h, l;
         split_tf32(v, h, l);
-        const uint64_t o = tiled_offset(r, j, k_tiles);
-        hi[o] = h;
-        lo[o] = l;
+        th[p] = h;
+        tl[p] = l;
     }
 }
 
@@ -297,12 +305,9 @@ cudaError_t launch_gemm_step(const StepDesc &d, const float2 *A, const float2 *B
                              int *error_flag, cudaStream_t stream) {
     const GemmSizes s = gemm_sizes(d);
     float *xh = scratch, *xl = xh + s.x_floats, *yh = xl + s.x_floats, *yl = yh + s.y_floats;
-    const int threads = 256;
-    const uint64_t xt = s.m_tiles * kTileM * s.k_tiles * kTileK, yt = s.n_tiles * kTileN * s.k_tiles * kTileK;
-    const unsigned gx = (unsigned) ((xt + threads - 1) / threads < 65535 * 8 ? (xt + threads - 1) / threads : 65535 * 8);
-    const unsigned gy = (unsigned) ((yt + threads - 1) / threads < 65535 * 8 ? (yt + threads - 1) / threads : 65535 * 8);
-    pack_operand<<<gx, threads, 0, stream>>>(A, d, 0, s.M, s.m_tiles * kTileM, s.K, s.k_tiles, xh, xl);
-    pack_operand<<<gy, threads, 0, stream>>>(B, d, 1, s.N2, s.n_tiles * kTileN, s.K, s.k_tiles, yh, yl);
+    if (s.m_tiles > 65535 || s.n_tiles > 65535 || s.k_tiles > 0x7fffffffull) return cudaErrorInvalidValue;
+    pack_tiles<<<dim3((unsigned) s.k_tiles, (unsigned) s.m_tiles), 256, 0, stream>>>(A, d, 0, s.M, s.K, s.k_tiles, xh, xl);
+    pack_tiles<<<dim3((unsigned) s.k_tiles, (unsigned) s.n_tiles), 256, 0, stream>>>(B, d, 1, s.N2, s.K, s.k_tiles, yh, yl);
     const size_t smem = gemm_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     if (e != cudaSuccess) return e;
