@@ -191,11 +191,24 @@ gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, cons
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
+    // Warp-specialised: lane 0 of warp 1 streams the operand tiles into the
+    // stage ring (waiting for the MMAs that read a stage before refilling it),
+    // thread 0 issues the MMAs as tiles land, so the tensor pipe always has the
+    // next k tile queued.  Every wait is bounded; a timeout stops both roles,
+    // the copies already issued are waited for, and the error flag is set.
+    __shared__ uint64_t s_issued, s_consumed;
     bool ok = true;
-    if (threadIdx.x == 0) {
+    auto stage_ptr = [&](int s, int plane) { return tiles + (s * 4 + plane) * kTileBytes; };
+    if (warp == 1 && lane == 0) {
         const uint64_t tile_floats = kTileBytes / 4;
-        auto stage_ptr = [&](int s, int plane) { return tiles + (s * 4 + plane) * kTileBytes; };
-        auto issue = [&](uint64_t kt, int s) {
+        uint32_t empty_phase[kStages] = {0, 0, 0};
+        uint64_t kt = 0;
+        for (; kt < k_tiles; kt++) {
+            const int s = (int) (kt % kStages);
+            if (kt >= (uint64_t) kStages) {
+                if (!mbar_wait(sm_addr(&bars[kStages + s]), empty_phase[s])) { ok = false; break; }
+                empty_phase[s] ^= 1u;
+            }
             const uint32_t full = sm_addr(&bars[s]);
             mbar_arrive_tx(full, 4 * kTileBytes);
             const uint64_t xt = (tm * k_tiles + kt) * tile_floats, yt = (tn * k_tiles + kt) * tile_floats;
@@ -203,10 +216,13 @@ gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, cons
             bulk_load(sm_addr(stage_ptr(s, 1)), x_lo + xt, kTileBytes, full);
             bulk_load(sm_addr(stage_ptr(s, 2)), y_hi + yt, kTileBytes, full);
             bulk_load(sm_addr(stage_ptr(s, 3)), y_lo + yt, kTileBytes, full);
-        };
-        uint32_t full_phase[kStages] = {0, 0, 0}, empty_phase[kStages] = {0, 0, 0};
-        for (uint64_t i = 0; i < (uint64_t) kStages && i < k_tiles; i++) issue(i, (int) i);
-        for (uint64_t kt = 0; kt < k_tiles && ok; kt++) {
+        }
+        s_issued = kt;
+    }
+    if (threadIdx.x == 0) {
+        uint32_t full_phase[kStages] = {0, 0, 0};
+        uint64_t kt = 0;
+        for (; kt < k_tiles; kt++) {
             const int s = (int) (kt % kStages);
             if (!mbar_wait(sm_addr(&bars[s]), full_phase[s])) { ok = false; break; }
             full_phase[s] ^= 1u;
@@ -223,20 +239,24 @@ gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, cons
                 mma_tf32(small, smem_desc(xh + o), smem_desc(yl + o), acc_small);
                 mma_tf32(small, smem_desc(xl + o), smem_desc(yh + o), 1u);
             }
-            mma_commit(sm_addr(&bars[kStages + s]));
-            const uint64_t next = kt + kStages;
-            if (next < k_tiles) {
-                if (!mbar_wait(sm_addr(&bars[kStages + s]), empty_phase[s])) { ok = false; break; }
-                empty_phase[s] ^= 1u;
-                issue(next, s);
-            }
+            mma_commit(sm_addr(&bars[kStages + s]));   // the stage is free once these MMAs have read it
         }
+        s_consumed = kt;
         mma_commit(sm_addr(&bars[2 * kStages]));
     }
     // every thread waits for the accumulator (bounded)
     ok = __syncthreads_and(ok) != 0;
-    bool done = ok && mbar_wait(sm_addr(&bars[2 * kStages]), 0);
-    done = __syncthreads_and(done) != 0;
+    if (!ok && warp == 1 && lane == 0) {
+        // after a timeout: the copies issued but never consumed land before the CTA leaves
+        for (uint64_t kt = s_consumed; kt < s_issued; kt++) {
+            const int s = (int) (kt % kStages);
+            mbar_wait(sm_addr(&bars[s]), (uint32_t) ((kt / kStages) & 1u));
+        }
+    }
+    // the MMAs issued so far (all of them, or those before a timeout) finish
+    // before the accumulator is read or released
+    bool done = mbar_wait(sm_addr(&bars[2 * kStages]), 0);
+    done = __syncthreads_and(ok && done) != 0;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (done) {
         const uint64_t m = tm * kTileM + (uint64_t) warp * 32 + lane;
