@@ -178,6 +178,10 @@ qt_status qt_plan_build(qt_ctx *ctx, const char *qasm_text, const char *measure_
                         qt_plan **out);
 qt_status qt_plan_free(qt_plan *plan);
 int qt_plan_num_steps(const qt_plan *plan);
+/* Work items of the mixed form that carry a host-prepared descriptor (0: the
+ * interpreter looks each item's step up instead; plans whose work-item steps
+ * all have offset tables and at most 8192 items carry them). */
+int64_t qt_plan_item_descriptors(const qt_plan *plan);
 int qt_plan_num_leaves(const qt_plan *plan);
 int qt_plan_peak_rank(const qt_plan *plan);
 uint64_t qt_plan_workspace_bytes(const qt_plan *plan, qt_precision prec);
@@ -331,8 +335,9 @@ int qt_batch_launches_per_run(const qt_batch *b);
  * staged copy of the plan block + leaf image of instances whose copy is at most
  * stage_cap bytes (larger ones are read in place).  Larger regions mean fewer
  * CTAs per SM.  Negative caps take the defaults (32 KiB; 64 KiB, 52 KiB when an
- * instance has CTA-tiled steps; 16 KiB and no staging when the instances
- * outnumber two CTAs per SM), 0 turns a region off.  ctas_per_sm = 0 runs as
+ * instance has CTA-tiled steps -- 144 KiB / 128 KiB for the wide variant; 16
+ * KiB and no staging when the instances outnumber two CTAs per SM), 0 turns a
+ * region off.  ctas_per_sm = 0 runs as
  * many CTAs as fit; static_schedule = 1 replaces the longest-first dynamic
  * schedule (used when there are more instances than CTAs) by a round robin in
  * batch order.  kernel_ctas picks the interpreter's register budget: the

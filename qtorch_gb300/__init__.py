@@ -442,6 +442,11 @@ class Plan(_Owned):
         return _lib().qt_plan_num_steps(self.handle)
 
     @property
+    def item_descriptors(self):
+        """work items of the mixed form with a host-prepared descriptor"""
+        return int(_lib().qt_plan_item_descriptors(self.handle))
+
+    @property
     def num_leaves(self):
         return _lib().qt_plan_num_leaves(self.handle)
 

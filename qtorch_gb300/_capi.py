@@ -75,6 +75,7 @@ SIGNATURES = [
                               P(c_void_p)]),
     ("qt_plan_free", c_int, [c_void_p]),
     ("qt_plan_num_steps", c_int, [c_void_p]),
+    ("qt_plan_item_descriptors", c_int64, [c_void_p]),
     ("qt_plan_num_leaves", c_int, [c_void_p]),
     ("qt_plan_peak_rank", c_int, [c_void_p]),
     ("qt_plan_workspace_bytes", c_uint64, [c_void_p, c_int]),

@@ -330,6 +330,7 @@ qt_status qt_plan_free(qt_plan *p) {
 }
 
 int qt_plan_num_steps(const qt_plan *p) { return p ? p->n_steps : -1; }
+int64_t qt_plan_item_descriptors(const qt_plan *p) { return p ? (int64_t) p->items[QT_PREC_MIXED].size() : -1; }
 int qt_plan_num_leaves(const qt_plan *p) { return p ? (int) p->leaf_rank.size() : -1; }
 int qt_plan_peak_rank(const qt_plan *p) { return p ? p->peak_rank : -1; }
 uint64_t qt_plan_workspace_bytes(const qt_plan *p, qt_precision prec) {
@@ -788,11 +789,13 @@ static qt_status batch_configure(qt_batch *b) {
     // with four CTAs per SM, which leaves room for small workspaces only.
     const qt_launch_policy &pol = b->policy;
     const bool many = n_grouped > 2 * plan_num_sms();
+    const bool wide = pol.kernel_ctas == 1 || (!pol.kernel_ctas && !many && n_grouped <= plan_num_sms());
     const uint64_t ws_cap = pol.ws_smem_cap >= 0 ? (uint64_t) pol.ws_smem_cap
                             : many                ? kSmemWorkspaceMaxMany
                                                   : kSmemWorkspaceMax;
     const uint64_t stage_cap = pol.stage_cap >= 0 ? (uint64_t) pol.stage_cap
                                : many             ? 0
+                               : wide             ? (any_tiled ? kSmemStageMaxWideTiled : kSmemStageMaxWide)
                                : any_tiled        ? kSmemStageMaxTiled
                                                   : kSmemStageMax;
     uint64_t ws_small = 0, stage_small = 0;
@@ -1250,7 +1253,7 @@ qt_status qt_batch_autotune(qt_batch *b, int reps, qt_launch_policy *chosen, dou
     // register budget and shared-memory regions together (they trade against
     // each other for CTAs per SM), then CTAs per SM and the schedule
     const int32_t ws_caps[] = {0, 8 << 10, 16 << 10, 32 << 10, 48 << 10, 64 << 10, 96 << 10};
-    const int32_t stage_caps[] = {0, 24 << 10, 52 << 10, 64 << 10, 96 << 10};
+    const int32_t stage_caps[] = {0, 24 << 10, 52 << 10, 64 << 10, 96 << 10, 144 << 10};
     const qt_launch_policy start = best;
     for (int32_t v : kPlanVariants)
         for (int32_t w : ws_caps)

@@ -83,6 +83,22 @@ struct HotStep {
 };
 static_assert(sizeof(HotStep) == 32, "HotStep layout");
 
+// One work item of the mixed form, prepared on the host (plans whose work-item
+// steps all have offset tables): the item's operand and output addresses are
+// final, so the interpreter reads one 16-byte descriptor instead of looking up
+// its step, unpacking the step's fields and reading the output's offsets.
+//   a, b  byte offsets of the item's first operand elements (leaf image or workspace)
+//   c     byte offset of its output element in the workspace
+//   meta  bits 0-15 first k-offset table entry, 16-18 lane-group log2, 19-22
+//         summed wires, 23/24 A/B in the leaf image, 25 compensated output
+//         (complex128 + complex64 copy), 26 a real output (0: alignment gap),
+//         27-30 the complex64 copy's distance from c in 8-byte units
+struct ItemDesc {
+    uint32_t a, b, c, meta;
+};
+static_assert(sizeof(ItemDesc) == 16, "ItemDesc layout");
+constexpr uint32_t kItemLeafA = 1u << 23, kItemLeafB = 1u << 24, kItemF64 = 1u << 25, kItemValid = 1u << 26;
+
 // One executable plan in device memory.
 struct PlanDesc {
     const StepDesc *steps;       // sorted by level
@@ -102,6 +118,8 @@ struct PlanDesc {
     // per level: bits 0-7 the largest lane-group log2 of its work items, bit 8
     // set when a compensated (FP64-class) step of it uses lane groups
     const uint32_t *level_meta;
+    // per work item, levels concatenated (mixed form; null: look items up)
+    const ItemDesc *items;
     int32_t n_steps;
     int32_t n_levels;
     int32_t n_rank0;

@@ -343,18 +343,24 @@ __device__ __forceinline__ void unscaled_check(float mag, float tmin, int si, Pl
 // (float values; the complex64 copy of a complex128 output).  Uniform across
 // the CTA: the flags were written before the barrier that precedes this.
 __device__ void unscaled_level_check(const StepDesc *__restrict__ steps, int s0, int s1, const char *ws,
-                                     const PlanSmemHeader &h, int *bad) {
+                                     const PlanSmemHeader &h, int *bad, bool all = false) {
     for (int s = s0; s < s1; s++) {
-        if (!(h.maxbits[s] & 1u)) continue;
+        // all: steps carry no flags (the descriptor path); every step of the
+        // level is scanned, and one holding a tiny magnitude but no normal one fails
+        if (!all && !(h.maxbits[s] & 1u)) continue;
         const StepDesc &d = steps[s];
         const uint32_t n_out = 1u << (2 * d.nFree);
         const float2 *v = reinterpret_cast<const float2 *>(ws + d.c_off + ((d.flags & kCF64) ? 16ull * n_out : 0ull));
-        int normal = 0;
+        int normal = 0, small = 0;
         for (uint32_t e = threadIdx.x; e < n_out; e += blockDim.x) {
             const float2 x = v[e];
-            normal |= fmaxf(fabsf(x.x), fabsf(x.y)) >= kUnscaledMin;
+            const float mag = fmaxf(fabsf(x.x), fabsf(x.y));
+            normal |= mag >= kUnscaledMin;
+            small |= mag > 0.f && mag < kUnscaledMin;
         }
-        if (!__syncthreads_or(normal) && threadIdx.x == 0) *bad = 1;
+        const bool any_normal = __syncthreads_or(normal) != 0;
+        const bool any_small = all ? __syncthreads_or(small) != 0 : true;
+        if (any_small && !any_normal && threadIdx.x == 0) *bad = 1;
     }
 }
 
@@ -575,6 +581,98 @@ __device__ void plan_level(const StepDesc *__restrict__ steps, const HotStep *__
             const uint32_t peers = __match_any_sync(0xffffffffu, key);
             const uint32_t wmax = __reduce_max_sync(peers, magbits);
             if (writer && (threadIdx.x & 31) == (uint32_t) (__ffs(peers) - 1)) atomicMax(&h.maxbits[si], wmax);
+        }
+    }
+}
+
+// The unscaled mixed pass over one level's work items from their host-prepared
+// descriptors (ItemDesc): the same arithmetic in the same order as the look-up
+// path of plan_level, without the step look-up, the field unpacking and the
+// output-offset table read.  A tiny magnitude only raises `tiny` (the level's
+// outputs are then checked as a whole, unscaled_level_check with all = true).
+__device__ void plan_level_items(const ItemDesc *__restrict__ items, uint32_t total, const char *leaves, char *ws,
+                                 const ushort2 *__restrict__ tables, int *bad, uint32_t meta, uint32_t &tiny) {
+    const uint32_t tid = threadIdx.x;
+    const uint32_t gmax = 1u << (meta & 0xffu);
+    const bool comp = (meta & 0x100u) != 0;
+    for (uint32_t base = 0; base < total; base += blockDim.x) {
+        if (base + (tid & ~31u) >= total) continue;   // warp-level collectives only below
+        const uint32_t item = base + tid;
+        uint4 w = make_uint4(0u, 0u, 0u, 0u);
+        if (item < total) w = reinterpret_cast<const uint4 *>(items)[item];
+        const uint32_t m = w.w;
+        const uint32_t g = 1u << ((m >> 16) & 7u);
+        const uint32_t K = 1u << (2 * ((m >> 19) & 15u));
+        const bool valid = (m & kItemValid) != 0;
+        const bool f64 = (m & kItemF64) != 0;
+        const uint32_t lane_k = item & (g - 1);
+        const float2 *A = reinterpret_cast<const float2 *>(((m & kItemLeafA) ? leaves : ws) + w.x);
+        const float2 *B = reinterpret_cast<const float2 *>(((m & kItemLeafB) ? leaves : ws) + w.y);
+        const ushort2 *ktab = tables + (m & 0xffffu);
+        float fre = 0.f, fim = 0.f, ere = 0.f, eim = 0.f;
+        if (valid) {
+            if (!f64) {
+                // four terms in flight, two accumulators to break the FMA chain
+                float r1 = 0.f, i1 = 0.f;
+                uint32_t k = lane_k;
+                for (; k + 3 * g < K; k += 4 * g) {
+                    float2 a[4], b[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const ushort2 kk = ktab[k + j * g];
+                        a[j] = A[kk.x];
+                        b[j] = B[kk.y];
+                    }
+                    cmac_f32(fre, fim, a[0], b[0]);
+                    cmac_f32(r1, i1, a[1], b[1]);
+                    cmac_f32(fre, fim, a[2], b[2]);
+                    cmac_f32(r1, i1, a[3], b[3]);
+                }
+                for (; k < K; k += g) {
+                    const ushort2 kk = ktab[k];
+                    cmac_f32(fre, fim, A[kk.x], B[kk.y]);
+                }
+                fre += r1;
+                fim += i1;
+            } else {
+                for (uint32_t k = lane_k; k < K; k += g) {
+                    const ushort2 kk = ktab[k];
+                    cmac_dot2(fre, ere, fim, eim, A[kk.x], B[kk.y]);
+                }
+            }
+        }
+        for (uint32_t off = gmax >> 1; off >= 1; off >>= 1) {
+            const float ore = __shfl_xor_sync(0xffffffffu, fre, (int) off);
+            const float oim = __shfl_xor_sync(0xffffffffu, fim, (int) off);
+            float oere = 0.f, oeim = 0.f;
+            if (comp) {
+                oere = __shfl_xor_sync(0xffffffffu, ere, (int) off);
+                oeim = __shfl_xor_sync(0xffffffffu, eim, (int) off);
+            }
+            if (off < g) {
+                if (f64) {
+                    dot2_merge(fre, ere, ore, oere);
+                    dot2_merge(fim, eim, oim, oeim);
+                } else {
+                    fre += ore;
+                    fim += oim;
+                }
+            }
+        }
+        if (valid && lane_k == 0) {
+            float mag;
+            if (f64) {
+                const double dre = (double) fre + (double) ere, dim = (double) fim + (double) eim;
+                *reinterpret_cast<double2 *>(ws + w.z) = make_double2(dre, dim);
+                const float2 f = make_float2((float) dre, (float) dim);
+                *reinterpret_cast<float2 *>(ws + w.z + 8u * ((m >> 27) & 15u)) = f;
+                mag = fmaxf(fabsf(f.x), fabsf(f.y));
+            } else {
+                *reinterpret_cast<float2 *>(ws + w.z) = make_float2(fre, fim);
+                mag = fmaxf(fabsf(fre), fabsf(fim));
+            }
+            if (!(mag <= kUnscaledMax)) *bad = 1;
+            else if (mag > 0.f && mag < kUnscaledMin) tiny = 1;
         }
     }
 }
@@ -833,6 +931,7 @@ struct PlanView {
     const uint8_t *item_step;
     const HotStep *hot;
     const ushort2 *tables;
+    const ItemDesc *items;   // null: the work items look their steps up
 };
 
 __device__ __forceinline__ PlanView plan_view(const PlanDesc *gplan, const unsigned char *stage) {
@@ -853,6 +952,7 @@ __device__ __forceinline__ PlanView plan_view(const PlanDesc *gplan, const unsig
     v.item_step = v.P.item_step ? reinterpret_cast<const uint8_t *>(at(v.P.item_step)) : nullptr;
     v.hot = reinterpret_cast<const HotStep *>(at(v.P.hot));
     v.level_meta = reinterpret_cast<const uint32_t *>(at(v.P.level_meta));
+    v.items = v.P.items ? reinterpret_cast<const ItemDesc *>(at(v.P.items)) : nullptr;
     return v;
 }
 
@@ -864,13 +964,18 @@ __device__ __forceinline__ void plan_levels(const PlanView &v, const char *leave
     uint32_t tiny = 0;   // this thread flagged a step of the level (unscaled pass)
     for (int L = 0; L < v.P.n_levels; L++) {
         const int sc = v.level_cta[L], s1 = v.level_start[L + 1];
-        plan_level<kMixed, kScaled>(v.steps, v.hot, v.level_start[L], sc, v.level_items[L], leaves, ws, h, v.tables,
-                                    v.item_step ? v.item_step + items_before : nullptr, bad, v.level_meta[L], tiny);
+        if (kMixed && !kScaled && v.items)
+            plan_level_items(v.items + items_before, v.level_items[L], leaves, ws, v.tables, bad, v.level_meta[L],
+                             tiny);
+        else
+            plan_level<kMixed, kScaled>(v.steps, v.hot, v.level_start[L], sc, v.level_items[L], leaves, ws, h,
+                                        v.tables, v.item_step ? v.item_step + items_before : nullptr, bad,
+                                        v.level_meta[L], tiny);
         items_before += v.level_items[L];
         for (int s = sc; s < s1; s++) run_tiled<kMixed, kScaled>(v.steps[s], s, leaves, ws, h, tile, bad, tiny);
         if constexpr (kMixed && !kScaled) {
             if (__syncthreads_or(tiny)) {
-                unscaled_level_check(v.steps, v.level_start[L], s1, ws, h, bad);
+                unscaled_level_check(v.steps, v.level_start[L], s1, ws, h, bad, v.items != nullptr);
                 tiny = 0;
             }
         } else {

@@ -372,6 +372,53 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
             hs.pad = 0;
         }
     }
+    // per-item descriptors of the mixed form: every work-item step tabled
+    {
+        const int prec = QT_PREC_MIXED;
+        const std::vector<StepDesc> &steps = p->steps[prec];
+        p->items[prec].clear();
+        uint64_t total = 0;
+        bool ok = !p->tables.empty();
+        for (int L0 = 0; L0 < n_levels && ok; L0++) {
+            total += p->level_items[prec][L0];
+            for (int i = p->level_start[L0]; i < p->level_cta[L0]; i++) ok = ok && steps[i].tab_off != kNoTable;
+        }
+        ok = ok && total <= kMaxItemDescs;
+        for (int L0 = 0; L0 < n_levels && ok; L0++) {
+            int si = p->level_start[L0];
+            for (uint32_t item = 0; item < p->level_items[prec][L0]; item++) {
+                while (si + 1 < p->level_cta[L0] && steps[si + 1].item_start <= item) si++;
+                const StepDesc &d = steps[si];
+                const uint32_t g = d.group ? d.group : 1, lg = (uint32_t) __builtin_ctz(g);
+                const uint32_t local = item - d.item_start, c = local >> lg;
+                const uint32_t n_out = 1u << (2 * d.nFree);
+                ItemDesc it{0, 0, 0, 0};
+                it.meta = (lg << 16) | ((uint32_t) d.nSum << 19);
+                if (d.flags & kALeaf) it.meta |= kItemLeafA;
+                if (d.flags & kBLeaf) it.meta |= kItemLeafB;
+                const bool f64 = (d.flags & kCF64) != 0;
+                if (f64) it.meta |= kItemF64;
+                if (item >= d.item_start && c < n_out) {
+                    const ushort2 o = p->tables[d.tab_off + c];
+                    const uint64_t a = (uint64_t) d.a_off + 8ull * o.x, b = (uint64_t) d.b_off + 8ull * o.y;
+                    const uint64_t cc = (uint64_t) d.c_off + (f64 ? 16ull : 8ull) * c;
+                    const uint64_t kt = (uint64_t) d.tab_off + n_out;
+                    // the complex64 copy of a compensated output: 16 n_out + 8 c bytes past its start
+                    const uint32_t delta = f64 ? 2 * n_out - c : 0;
+                    if (a > 0xffffffffull || b > 0xffffffffull || cc > 0xffffffffull || kt > 0xffffull || delta > 15) {
+                        ok = false;
+                        break;
+                    }
+                    it.a = (uint32_t) a;
+                    it.b = (uint32_t) b;
+                    it.c = (uint32_t) cc;
+                    it.meta |= (uint32_t) kt | kItemValid | (delta << 27);
+                }
+                p->items[prec].push_back(it);
+            }
+        }
+        if (!ok) p->items[prec].clear();
+    }
     p->n_steps = S;
     p->n_levels = n_levels;
     p->grouped = p->max_step_out <= kGroupedMaxRank && p->max_step_k <= kGroupedMaxSum &&
@@ -403,7 +450,9 @@ qt_status upload_plan(qt_plan *p, int prec) {
     const size_t off_hot = align_up(off_map + map_bytes, 16);
     const size_t meta_bytes = sizeof(uint32_t) * p->level_meta[prec].size();
     const size_t off_meta = align_up(off_hot + hot_bytes, 16);
-    const size_t off_tab = align_up(off_meta + meta_bytes, 256);
+    const size_t desc_bytes = sizeof(ItemDesc) * p->items[prec].size();
+    const size_t off_desc = align_up(off_meta + meta_bytes, 16);
+    const size_t off_tab = align_up(off_desc + desc_bytes, 256);
     const size_t total = off_tab + tab_bytes + 16;
     void *d = nullptr;
     qt_status s = dev_alloc(ctx, total, &d);
@@ -421,6 +470,8 @@ qt_status upload_plan(qt_plan *p, int prec) {
     pd.item_step = map_bytes ? reinterpret_cast<const uint8_t *>((char *) d + off_map) : nullptr;
     pd.hot = reinterpret_cast<const HotStep *>((char *) d + off_hot);
     pd.level_meta = reinterpret_cast<const uint32_t *>((char *) d + off_meta);
+    pd.items = desc_bytes ? reinterpret_cast<const ItemDesc *>((char *) d + off_desc) : nullptr;
+    if (desc_bytes) std::memcpy(host.data() + off_desc, p->items[prec].data(), desc_bytes);
     if (meta_bytes) std::memcpy(host.data() + off_meta, p->level_meta[prec].data(), meta_bytes);
     if (hot_bytes) std::memcpy(host.data() + off_hot, p->hot[prec].data(), hot_bytes);
     if (map_bytes) std::memcpy(host.data() + off_map, p->item_step[prec].data(), map_bytes);

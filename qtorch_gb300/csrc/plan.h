@@ -29,6 +29,10 @@ constexpr uint64_t kSmemWorkspaceMaxMany = 16ull << 10;
 constexpr uint64_t kSmemStageMax = 64ull << 10;
 // staging cap when the CTA also holds the tile buffers of CTA-tiled steps
 constexpr uint64_t kSmemStageMaxTiled = 52ull << 10;
+// staging cap of the wide interpreter (one CTA per SM): room for a plan block
+// with its per-item descriptors
+constexpr uint64_t kSmemStageMaxWide = 144ull << 10;
+constexpr uint64_t kSmemStageMaxWideTiled = 128ull << 10;
 inline uint64_t round16(uint64_t x) { return (x + 15) / 16 * 16; }
 // offset tables are built when they take at most this many bytes
 constexpr uint64_t kMaxTableBytes = 64ull << 10;
@@ -38,6 +42,8 @@ constexpr uint64_t kMaxTableBytes = 64ull << 10;
 constexpr int64_t kLoneInstanceMaxMacs = 1ll << 24;
 // plans with at most this many work items carry an item -> step map
 constexpr uint64_t kMaxItemMap = 8192;
+// plans with at most this many work items carry per-item descriptors (16 B each)
+constexpr uint64_t kMaxItemDescs = 8192;
 
 }  // namespace qtg
 
@@ -66,6 +72,7 @@ struct qt_plan {
     std::vector<uint32_t> level_items[2];             // interpreter work items per level, per precision
     std::vector<uint8_t> item_step[2];                // step of each work item (empty: none)
     std::vector<qtg::HotStep> hot[2];                 // packed per-step fields of the interpreter
+    std::vector<qtg::ItemDesc> items[2];              // per-item descriptors (mixed form; empty: none)
     std::vector<uint32_t> level_meta[2];              // per level: max lane-group log2, compensated groups
     std::vector<ushort2> tables;                      // interpreter offset tables (empty: none)
     std::vector<uint64_t> leaf_off[2];

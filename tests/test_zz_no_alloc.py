@@ -88,3 +88,46 @@ def test_static_entry_point_rejects_oversized_plans():
         assert "static scratch" in ctx.last_error
     finally:
         ctx.close()
+
+
+def test_item_descriptors_match_lookup_path_bit_for_bit():
+    """The mixed form's unscaled pass reads host-prepared per-item descriptors
+    when a plan carries them; the static entry point's copy of the plan block
+    has none, so it looks each item's step up.  Both must round the same
+    products in the same order: equal bit for bit, over the 60 terms of a
+    30-vertex p=1 objective (batched under two launch policies) and the p=2
+    terms of a 20-vertex graph."""
+    import torch
+    lib = qg._capi.load()
+    lib.qt_plan_execute_static.restype = ctypes.c_int
+    lib.qt_plan_execute_static.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.POINTER(ctypes.c_double)]
+    ctx = qg.Context(0)
+    try:
+        dgf = qg.random_regular_graph(30, 4, seed=1)
+        plans = [qg.Plan(*qg.qaoa_term_text(dgf, 1, [0.3, 0.7], e), ordering="linegraph", ctx=ctx)
+                 for e in range(60)]
+        plans += plans_under_test(ctx)[:4]
+        assert sum(p.item_descriptors > 0 for p in plans) >= 60
+        lookup = []
+        for plan in plans:
+            d_leaves = torch.from_numpy(plan.leaf_values().astype(np.complex64)).cuda()
+            out = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            assert static_call(lib, ctx, plan, qg.MIXED, d_leaves, out) == 0, ctx.last_error
+            ctx.synchronize()
+            v = out.cpu().numpy()
+            lookup.append(complex(v[0], v[1]))
+        for plan, want in zip(plans, lookup):
+            assert plan.execute(qg.MIXED) == want
+        for ctas in (1, 2):
+            batch = qg.Batch(ctx)
+            for plan in plans:
+                batch.add(plan)
+            batch.prepare(qg.MIXED)
+            batch.set_launch_policy(kernel_ctas=ctas)
+            got = batch.execute(qg.MIXED)
+            assert [complex(g) for g in got] == lookup
+            batch._release()
+    finally:
+        ctx.close()
