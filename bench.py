@@ -90,27 +90,34 @@ def build_terms(dgf, point):
 # CPU side (oracle port): the checker / baseline, never the product
 
 def _cpu_worker(job):
+    """One term on the oracle port: (value, parse seconds, contraction seconds)."""
     from oracle import port
     qasm, meas, seq = job
     t0 = time.perf_counter()
-    v, _ = port.replay_value(qasm, meas, seq)
-    return v, time.perf_counter() - t0
+    net = port.Net(qasm, meas)
+    t1 = time.perf_counter()
+    net.replay(seq)
+    return net.final_value, t1 - t0, time.perf_counter() - t1
 
 
 def cpu_terms_per_s(jobs, workers, min_seconds=0.0):
-    """Oracle port over (qasm, measure, sequence) jobs on `workers` processes (spawn)."""
+    """Oracle port over (qasm, measure, sequence) jobs on `workers` processes
+    (spawn): (terms/s, terms, seconds, share of the workers' time spent parsing)."""
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
+    parse_s = contract_s = 0.0
     with ctx.Pool(workers) as pool:
         pool.map(_cpu_worker, jobs[:workers])          # warm the workers
         done, t0 = 0, time.perf_counter()
         while True:
-            pool.map(_cpu_worker, jobs)
+            for _, tp, tc in pool.map(_cpu_worker, jobs):
+                parse_s += tp
+                contract_s += tc
             done += len(jobs)
             el = time.perf_counter() - t0
             if el >= min_seconds:
                 break
-    return done / el, done, el
+    return done / el, done, el, parse_s / max(parse_s + contract_s, 1e-30)
 
 
 def sequences_for(terms):
@@ -656,10 +663,13 @@ def run_engine(args):
         seqs = sequences_for(terms)
         jobs = [(q, m, s) for (q, m), s in zip(terms, seqs)]
         cores = os.cpu_count() or 1
-        rate, done, el = cpu_terms_per_s(jobs, cores, min_seconds=args.cpu_seconds)
+        rate, done, el, parse_share = cpu_terms_per_s(jobs, cores, min_seconds=args.cpu_seconds)
         line["cpu_baseline"] = {"value": rate, "unit": "terms/s", "cores": cores, "kind": "port",
                                 "sample": f"{done} terms ({done // n_terms} x the 60-term step) in {el:.1f} s, "
-                                          "QASM parse + recorded line-graph replay per term"}
+                                          "QASM parse + recorded line-graph replay per term",
+                                "parse_share": parse_share,
+                                "value_excluding_parse": rate / max(1.0 - parse_share, 1e-9),
+                                "ms_per_term_per_core": 1e3 * el * cores / done}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
