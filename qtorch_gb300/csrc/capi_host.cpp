@@ -396,7 +396,7 @@ qt_status qt_plan_leaf_values(const qt_plan *p, double *out, uint64_t cap) {
 
 qt_status qt_plan_execute(qt_ctx *ctx, qt_plan *p, qt_precision prec, double *v) {
     if (!ctx || !p || !p->ctx || !v || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return QT_ERR_INVALID_ARGUMENT;
-    if (!p->grouped || p->flops > kLoneInstanceMaxMacs) return execute_stepwise(p, prec, p->leaf_values.data(), v);
+    if (!p->grouped || p->flops > kLoneInstanceMaxMacs) return execute_stepwise(p, ctx, prec, p->leaf_values.data(), v);
     qt_batch *b = nullptr;
     qt_status s = qt_batch_create(ctx, &b);
     if (s != QT_OK) return s;
@@ -974,7 +974,7 @@ qt_status qt_batch_run(qt_batch *b) {
     // plans too large for one CTA run step by step
     for (int i : b->stepwise) {
         double v[2];
-        s = execute_stepwise(b->plans[i], b->prepared_prec, b->leaves[i].data(), v);
+        s = execute_stepwise(b->plans[i], ctx, b->prepared_prec, b->leaves[i].data(), v);
         if (s != QT_OK) return s;
         cudaMemcpyAsync((double *) b->d_values + 2 * i, v, 16, cudaMemcpyHostToDevice, ctx->stream);
     }

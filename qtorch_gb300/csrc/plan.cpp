@@ -428,6 +428,9 @@ qt_status lower_plan(qt_plan *p, const qtorch::Network &net) {
 }
 
 qt_status upload_plan(qt_plan *p, int prec) {
+    // uploaded once; later callers (batches on other contexts) do not take the
+    // owner's lock, which a long step-by-step run on that context may hold
+    if (p->dev_ready[prec].load(std::memory_order_acquire)) return QT_OK;
     qt_ctx *ctx = p->ctx;
     std::lock_guard<std::recursive_mutex> g(ctx->lock);
     if (p->dev[prec]) return QT_OK;
@@ -497,6 +500,7 @@ qt_status upload_plan(qt_plan *p, int prec) {
     }
     p->dev[prec] = d;
     p->dev_bytes[prec] = total;
+    p->dev_ready[prec].store(true, std::memory_order_release);
     return QT_OK;
 }
 
@@ -523,8 +527,7 @@ void pack_leaves(const qt_plan *p, int prec, const std::complex<double> *src, ch
 // Step-by-step execution with the whole-GPU pairwise kernel (plans whose
 // intermediates are too large for one CTA).  Mixed precision runs every step
 // in complex64 and reads the final value back as FP64.
-qt_status execute_stepwise(qt_plan *p, int prec, const std::complex<double> *leaves, double *value) {
-    qt_ctx *ctx = p->ctx;
+qt_status execute_stepwise(qt_plan *p, qt_ctx *ctx, int prec, const std::complex<double> *leaves, double *value) {
     const bool mixed = prec == QT_PREC_MIXED;
     const size_t es = mixed ? 8 : 16;
     std::lock_guard<std::recursive_mutex> g(ctx->lock);

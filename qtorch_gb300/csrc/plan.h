@@ -1,5 +1,6 @@
 // Host-side plan and batch objects of the C ABI.
 #pragma once
+#include <atomic>
 #include <complex>
 #include <string>
 #include <vector>
@@ -84,6 +85,8 @@ struct qt_plan {
     bool grouped = false;
     void *dev[2] = {nullptr, nullptr};
     size_t dev_bytes[2] = {0, 0};
+    // dev[prec] is published: readers on other contexts skip the owner's lock
+    std::atomic<bool> dev_ready[2]{};
     // slicings made for a workspace budget (per precision: budget, slicing), freed with the plan
     std::vector<std::pair<uint64_t, qt_sliced *>> slicings[2];
 };
@@ -150,5 +153,7 @@ void plan_collect_leaves(qt_plan *p, const qtorch::Network &net);
 qt_status plan_finish(qt_plan *p, const qtorch::Network &net);
 qt_status upload_plan(qt_plan *p, int prec);
 void pack_leaves(const qt_plan *p, int prec, const std::complex<double> *src, char *dst);
-qt_status execute_stepwise(qt_plan *p, int prec, const std::complex<double> *leaves, double *value);
+// runs on `ctx` (its stream, allocator and lock), which may differ from the
+// plan's own context: a server lane executes shared plans on its own stream
+qt_status execute_stepwise(qt_plan *p, qt_ctx *ctx, int prec, const std::complex<double> *leaves, double *value);
 }  // namespace qtg

@@ -110,3 +110,35 @@ def test_requests_above_the_budget_are_sliced(prec):
             srv.close()
     finally:
         c.close()
+
+
+def test_small_requests_pass_a_heavy_one():
+    """A heavy request runs step by step on its own lane's stream; small
+    requests submitted right after it are served on another lane meanwhile
+    (the shared plan's owner context is not held by the heavy run), so they
+    finish first, and their values are unchanged."""
+    from qtorch_gb300.circuits import qft_text
+    ctx = qg.Context(0)
+    try:
+        heavy = qg.Plan(qft_text(13, 4), "Z", ordering="linegraph", ctx=ctx)
+        dgf = qg.random_regular_graph(20, 3, seed=9)
+        small = [qg.Plan(*qg.qaoa_term_text(dgf, 1, [0.5, 1.2], e), ordering="linegraph", ctx=ctx)
+                 for e in range(8)]
+        alone = [p.execute(qg.MIXED) for p in small]
+        heavy_alone = heavy.execute(qg.MIXED)
+        srv = qg.Server(max_inflight=16, precision=qg.MIXED, ctx=ctx)
+        try:
+            for _ in range(2):   # the first round warms the lanes' caches
+                t_heavy = srv.submit(heavy)
+                tickets = [srv.submit(p) for p in small]
+                srv.drain()
+                v_heavy, l_heavy = srv.poll(t_heavy)
+                got = [srv.poll(t) for t in tickets]
+            assert abs(v_heavy - heavy_alone) <= 1e-6
+            for (v, lat), want in zip(got, alone):
+                assert abs(v - want) <= 1e-6
+                assert lat < l_heavy
+        finally:
+            srv.close()
+    finally:
+        ctx.close()
