@@ -208,7 +208,7 @@ qt_status qt_server_create(qt_ctx *ctx, int max_inflight, qt_precision prec, qt_
     ctx_retain(ctx);
     s->max_inflight = max_inflight;
     s->prec = prec;
-    const int n_lanes = 3;   // lane 0: light waves only
+    const int n_lanes = 4;   // lane 0: light waves only
     s->lanes.resize(n_lanes);
     for (int i = 0; i < n_lanes; i++) {
         // lane 0 (light waves) launches at the highest stream priority
