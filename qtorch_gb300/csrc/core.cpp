@@ -148,7 +148,8 @@ bool tensor_cores_enabled() {
     return on;
 }
 
-qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const void *B, void *C, bool f64) {
+qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const void *B, void *C, bool f64,
+                          int *gemm_flag) {
     // a long sum into a few outputs: the whole GPU on one sum.  In complex64
     // every such reduction (rank <= 2, >= 64 terms) takes the compensated kernel:
     // these are the expectation values where cancellation lives.
@@ -168,23 +169,25 @@ qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const v
         return cuda_error(ctx, e, "reduction launch");
     }
     if (!f64 && tensor_cores_enabled() && gemm_eligible(d)) {
-        void *scratch = nullptr, *flag = nullptr;
+        void *scratch = nullptr, *flag = gemm_flag;
         qt_status s = dev_alloc(ctx, sizeof(float) * gemm_scratch_floats(d), &scratch);
-        if (s == QT_OK) s = dev_alloc(ctx, 256, &flag);
+        if (s == QT_OK && !gemm_flag) s = dev_alloc(ctx, 256, &flag);
         if (s == QT_OK) {
-            cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream);
+            cudaError_t e = gemm_flag ? cudaSuccess : cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream);
             if (e == cudaSuccess)
                 e = launch_gemm_step(d, (const float2 *) A, (const float2 *) B, (float2 *) C, (float *) scratch,
                                      (int *) flag, ctx->stream);
-            ctx->launches += 3;
+            ctx->launches += gemm_flag ? 2 : 3;
             int h = 0;
-            if (e == cudaSuccess) e = cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+            if (!gemm_flag) {
+                if (e == cudaSuccess) e = cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+            }
             s = cuda_error(ctx, e, "tensor-core contraction");
             if (s == QT_OK && h) s = set_error(ctx, QT_ERR_CUDA, "tensor-core pipeline wait timed out");
         }
-        dev_free(ctx, scratch);
-        dev_free(ctx, flag);
+        dev_free(ctx, scratch);   // stream-ordered: the next user of the block runs after this step
+        if (!gemm_flag) dev_free(ctx, flag);
         return s;
     }
     if (tiled_shaped(d)) {

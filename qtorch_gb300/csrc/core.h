@@ -70,7 +70,11 @@ inline size_t elem_bytes(qt_dtype d) { return d == QT_C128 ? 16 : 8; }
 // One contraction step over the whole GPU: complex128 with the reference's
 // rounding, or complex64 -- through the tcgen05 tensor-core GEMM when the step
 // is GEMM-shaped and large (gemm_tc.cu), else the SIMT pair kernel.
-qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const void *B, void *C, bool f64);
+// gemm_flag: a zeroed device int the caller checks after its last step (the
+// tensor-core pipeline's timeout flag); null: checked here, with a stream
+// synchronisation after every tensor-core step
+qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const void *B, void *C, bool f64,
+                          int *gemm_flag = nullptr);
 // whether complex64 steps may use the tensor cores (QT_DISABLE_TCGEN05=1 turns it off)
 bool tensor_cores_enabled();
 

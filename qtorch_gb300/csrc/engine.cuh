@@ -69,6 +69,23 @@ struct StepDesc {
 };
 
 constexpr uint32_t kNoTable = 0xffffffffu;
+
+// A dependency level's small contractions, launched together when a plan runs
+// step by step (a kernel parameter: no copy).
+constexpr int kPairBatchMax = 32;
+constexpr int kPairBatchMaxLog2Macs = 22;   // steps of at most 2^22 complex MACs
+struct PairJob {
+    StepDesc d;
+    const void *A;
+    const void *B;
+    void *C;
+    uint64_t n_out, K;
+    uint32_t block_begin, pad;
+};
+struct PairBatch {
+    PairJob job[kPairBatchMax];
+    uint32_t n_jobs, pad;
+};
 static_assert(sizeof(StepDesc) % 8 == 0, "StepDesc alignment");
 
 // The fields a work item reads, packed into 32 bytes (two 16-byte loads):

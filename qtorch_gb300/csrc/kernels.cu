@@ -95,19 +95,21 @@ struct Vec2<double> { using type = double2; };
 template <>
 struct Vec2<float> { using type = float2; };
 
+// One contraction on CTAs blk = 0 .. nblk-1 of its launch.
 template <typename T>
-__global__ void __launch_bounds__(kPairThreads)
-pair_kernel(const typename Vec2<T>::type *__restrict__ A, const typename Vec2<T>::type *__restrict__ B,
-            typename Vec2<T>::type *__restrict__ C, const StepDesc d, uint64_t n_out, uint64_t K) {
+__device__ __forceinline__ void pair_body(const typename Vec2<T>::type *__restrict__ A,
+                                          const typename Vec2<T>::type *__restrict__ B,
+                                          typename Vec2<T>::type *__restrict__ C, const StepDesc &d, uint64_t n_out,
+                                          uint64_t K, uint32_t blk, uint32_t nblk) {
     using V = typename Vec2<T>::type;
     __shared__ uint64_t s_oa[kPairChunk];
     __shared__ uint64_t s_ob[kPairChunk];
-    const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+    const uint64_t stride = (uint64_t) nblk * blockDim.x;
     // every CTA walks the same number of outer iterations so that the
     // __syncthreads of the chunk loop stay uniform
     const uint64_t n_iter = (n_out + stride - 1) / stride;
     for (uint64_t it = 0; it < n_iter; it++) {
-        const uint64_t c = it * stride + (uint64_t) blockIdx.x * blockDim.x + threadIdx.x;
+        const uint64_t c = it * stride + (uint64_t) blk * blockDim.x + threadIdx.x;
         const bool valid = c < n_out;
         uint64_t oa0 = 0, ob0 = 0;
         if (valid) scatter_c(c, d, oa0, ob0);
@@ -136,6 +138,26 @@ pair_kernel(const typename Vec2<T>::type *__restrict__ A, const typename Vec2<T>
             C[c] = v;
         }
     }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPairThreads)
+pair_kernel(const typename Vec2<T>::type *__restrict__ A, const typename Vec2<T>::type *__restrict__ B,
+            typename Vec2<T>::type *__restrict__ C, const StepDesc d, uint64_t n_out, uint64_t K) {
+    pair_body<T>(A, B, C, d, n_out, K, blockIdx.x, gridDim.x);
+}
+
+// Several independent small contractions (one dependency level of a plan run
+// step by step) in one launch: job j owns CTAs [block_begin_j, block_begin_{j+1}).
+template <typename T>
+__global__ void __launch_bounds__(kPairThreads) pair_batch_kernel(const __grid_constant__ PairBatch pb) {
+    using V = typename Vec2<T>::type;
+    uint32_t j = 0;
+    while (j + 1 < pb.n_jobs && blockIdx.x >= pb.job[j + 1].block_begin) j++;
+    const PairJob &w = pb.job[j];
+    const uint32_t end = j + 1 < pb.n_jobs ? pb.job[j + 1].block_begin : gridDim.x;
+    pair_body<T>(reinterpret_cast<const V *>(w.A), reinterpret_cast<const V *>(w.B), reinterpret_cast<V *>(w.C), w.d,
+                 w.n_out, w.K, blockIdx.x - w.block_begin, end - w.block_begin);
 }
 
 // ---------------------------------------------------------------------------
@@ -1229,6 +1251,28 @@ static int num_sms() {
         if (g_num_sms <= 0) g_num_sms = 1;
     }
     return g_num_sms;
+}
+
+bool pair_batchable(const StepDesc &d, bool f64) {
+    if (2 * (d.nFree + d.nSum) > kPairBatchMaxLog2Macs) return false;
+    const bool small_out = (1ull << (2 * d.nFree)) <= kReduceMaxOut;
+    // the steps run_contraction would hand to the reduction kernels keep them
+    return !reduce_shaped(d) && (f64 || !small_out || d.nSum < 3);
+}
+
+cudaError_t launch_pair_batch(PairBatch &pb, bool f64, cudaStream_t stream) {
+    if (pb.n_jobs == 0) return cudaSuccess;
+    uint32_t blocks = 0;
+    for (uint32_t j = 0; j < pb.n_jobs; j++) {
+        PairJob &w = pb.job[j];
+        w.n_out = 1ull << (2 * w.d.nFree);
+        w.K = 1ull << (2 * w.d.nSum);
+        w.block_begin = blocks;
+        blocks += (uint32_t) ((w.n_out + kPairThreads - 1) / kPairThreads);
+    }
+    if (f64) pair_batch_kernel<double><<<blocks, kPairThreads, 0, stream>>>(pb);
+    else pair_batch_kernel<float><<<blocks, kPairThreads, 0, stream>>>(pb);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C, bool f64, cudaStream_t stream) {

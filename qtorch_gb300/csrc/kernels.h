@@ -8,6 +8,11 @@ namespace qtg {
 // One pairwise contraction over the whole GPU.  f64: complex128, reference
 // rounding; otherwise complex64 with FP32 FMA.
 cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C, bool f64, cudaStream_t stream);
+// a small step that run_contraction would give to a pair or tiled kernel: it
+// may join a PairBatch of its dependency level
+bool pair_batchable(const StepDesc &d, bool f64);
+// fills n_out, K and block_begin of every job and launches them together
+cudaError_t launch_pair_batch(PairBatch &pb, bool f64, cudaStream_t stream);
 
 // Wide steps (C = A~ B~ with both gathered sides >= 16 and >= 1024 outputs,
 // A's free wires first, ranks <= 15) as tiled products over the whole GPU;

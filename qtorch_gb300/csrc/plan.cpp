@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <new>
 
 #include "kernels.h"
@@ -570,26 +571,66 @@ qt_status execute_stepwise(qt_plan *p, qt_ctx *ctx, int prec, const std::complex
         if (d.b_step >= 0) uses[d.b_step]++;
     }
     s = QT_OK;
-    for (size_t i = 0; i < steps.size() && s == QT_OK; i++) {
+    // level by level (the steps are stored in level order and a level's steps
+    // are independent): the level's small steps go out as one batched launch,
+    // the others one launch each; the inputs a level consumed last are released
+    // once the level is on the stream
+    auto pb = std::make_unique<PairBatch>();
+    pb->n_jobs = 0;
+    // one timeout flag for every tensor-core step, read once at the end
+    void *gflag = nullptr;
+    s = dev_alloc(ctx, 256, &gflag);
+    if (s == QT_OK) s = cuda_error(ctx, cudaMemsetAsync(gflag, 0, sizeof(int), ctx->stream), "flag clear");
+    auto flush = [&]() -> qt_status {
+        const cudaError_t fe = launch_pair_batch(*pb, !mixed, ctx->stream);
+        if (pb->n_jobs) ctx->launches++;
+        pb->n_jobs = 0;
+        return cuda_error(ctx, fe, "batched pair launch");
+    };
+    const int n_levels = (int) p->level_start.size() - 1;
+    for (int L = 0; L < n_levels && s == QT_OK; L++) {
         if (deadline_passed(ctx)) {
             s = set_error(ctx, QT_ERR_DEADLINE, "deadline expired");
             break;
         }
-        const StepDesc &d = steps[i];
-        const void *A = (d.flags & kALeaf) ? (const char *) dleaf + leaf_off[p->a_leaf[i]] : outs[d.a_step];
-        const void *B = (d.flags & kBLeaf) ? (const char *) dleaf + leaf_off[p->b_leaf[i]] : outs[d.b_step];
-        s = dev_alloc(ctx, es << (2 * d.nFree), &outs[i]);
-        if (s != QT_OK) break;
-        s = run_contraction(ctx, d, A, B, outs[i], !mixed);
-        if (s != QT_OK) break;
-        if (d.a_step >= 0 && --uses[d.a_step] == 0 && !(steps[d.a_step].flags & kOutRank0)) {
-            dev_free(ctx, outs[d.a_step]);
-            outs[d.a_step] = nullptr;
+        const int i0 = p->level_start[L], i1 = p->level_start[L + 1];
+        for (int i = i0; i < i1 && s == QT_OK; i++) {
+            const StepDesc &d = steps[i];
+            const void *A = (d.flags & kALeaf) ? (const char *) dleaf + leaf_off[p->a_leaf[i]] : outs[d.a_step];
+            const void *B = (d.flags & kBLeaf) ? (const char *) dleaf + leaf_off[p->b_leaf[i]] : outs[d.b_step];
+            s = dev_alloc(ctx, es << (2 * d.nFree), &outs[i]);
+            if (s != QT_OK) break;
+            if (pair_batchable(d, !mixed)) {
+                PairJob &w = pb->job[pb->n_jobs++];
+                w.d = d;
+                w.A = A;
+                w.B = B;
+                w.C = outs[i];
+                if (pb->n_jobs == (uint32_t) kPairBatchMax) s = flush();
+            } else {
+                s = run_contraction(ctx, d, A, B, outs[i], !mixed, (int *) gflag);
+            }
         }
-        if (d.b_step >= 0 && --uses[d.b_step] == 0 && !(steps[d.b_step].flags & kOutRank0)) {
-            dev_free(ctx, outs[d.b_step]);
-            outs[d.b_step] = nullptr;
+        if (s == QT_OK) s = flush();
+        if (s != QT_OK) break;
+        for (int i = i0; i < i1; i++) {
+            const StepDesc &d = steps[i];
+            if (d.a_step >= 0 && --uses[d.a_step] == 0 && !(steps[d.a_step].flags & kOutRank0)) {
+                dev_free(ctx, outs[d.a_step]);
+                outs[d.a_step] = nullptr;
+            }
+            if (d.b_step >= 0 && --uses[d.b_step] == 0 && !(steps[d.b_step].flags & kOutRank0)) {
+                dev_free(ctx, outs[d.b_step]);
+                outs[d.b_step] = nullptr;
+            }
         }
+    }
+    if (s == QT_OK) {
+        int h = 0;
+        ce = cudaMemcpyAsync(&h, gflag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+        s = cuda_error(ctx, ce, "tensor-core contraction");
+        if (s == QT_OK && h) s = set_error(ctx, QT_ERR_CUDA, "tensor-core pipeline wait timed out");
     }
     if (s == QT_OK) {
         // final-value rule over the rank-0 outputs in contraction order (Network.h:961-965)
@@ -620,6 +661,7 @@ qt_status execute_stepwise(qt_plan *p, qt_ctx *ctx, int prec, const std::complex
     }
     for (void *o : outs) dev_free(ctx, o);
     dev_free(ctx, dleaf);
+    dev_free(ctx, gflag);
     return s;
 }
 
