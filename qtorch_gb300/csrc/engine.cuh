@@ -86,6 +86,8 @@ struct PairBatch {
     PairJob job[kPairBatchMax];
     uint32_t n_jobs, pad;
 };
+// passed by value as a kernel parameter (limit 32764 bytes)
+static_assert(sizeof(PairBatch) <= 32000, "PairBatch exceeds the kernel-parameter limit");
 static_assert(sizeof(StepDesc) % 8 == 0, "StepDesc alignment");
 
 // The fields a work item reads, packed into 32 bytes (two 16-byte loads):
