@@ -9,9 +9,10 @@
 // budget, which is sliced at submission (qt_plan_slice) and runs slice by
 // slice.  Waves run on lanes, each lane with its own
 // CUDA stream, so a wave formed from requests that arrived while another wave
-// is on the GPU runs concurrently with it.  Lane 0 takes light waves only, so
-// light requests never queue behind a heavy one; it also leaves mid-size
-// grouped requests (more than 2^20 complex MACs) to the other lanes.  Each
+// is on the GPU runs concurrently with it.  Lane 0 (highest stream priority)
+// takes the small requests (grouped, at most 2^20 complex MACs) and nothing
+// else, so they never queue behind a heavy one nor run on a low-priority
+// stream beside one; the other lanes take the rest.  Each
 // request's result is independent of what it was batched with: an instance
 // only ever touches its
 // own leaves and its CTA's workspace.
@@ -155,18 +156,22 @@ static void dispatcher_main(qt_server *s) {
         s->cv.wait(g, [&] {
                 if (s->stop) return true;
             if (s->pending.empty()) return false;
-            bool any_small = false;
-            for (auto &r : s->pending) any_small = any_small || r.small;
+            bool any_small = false, any_big = false;
+            for (auto &r : s->pending) (r.small ? any_small : any_big) = true;
             for (size_t i = 0; i < s->lanes.size(); i++)
-                if (!s->lanes[i].busy && (i > 0 || any_small)) return true;
+                if (!s->lanes[i].busy && (i > 0 ? any_big : any_small)) return true;
             return false;
         });
         if (s->stop) return;
-        bool any_small = false;
-        for (auto &r : s->pending) any_small = any_small || r.small;
+        bool any_small = false, any_big = false;
+        const Request *first_big = nullptr;
+        for (auto &r : s->pending) {
+            (r.small ? any_small : any_big) = true;
+            if (!r.small && !first_big) first_big = &r;
+        }
         int li = -1;
         for (int i = 0; i < (int) s->lanes.size(); i++)
-            if (!s->lanes[i].busy && (i > 0 || any_small)) {
+            if (!s->lanes[i].busy && (i > 0 ? any_big : any_small)) {
                 li = i;
                 break;
             }
@@ -175,9 +180,12 @@ static void dispatcher_main(qt_server *s) {
         // memory budget; a heavy request at the head of the queue goes alone
         std::vector<Request> wave;
         const uint64_t budget = s->ctx->memory_budget;
-        const bool take_heavy = li > 0 && s->pending.front().heavy;
+        // lane 0 serves the small requests, at the highest stream priority; the
+        // other lanes the rest (a heavy request alone), so that a small request
+        // never runs on a low-priority stream beside a heavy one
+        const bool take_heavy = li > 0 && first_big->heavy;
         for (auto it = s->pending.begin(); it != s->pending.end() && s->inflight < s->max_inflight;) {
-            if (it->heavy != take_heavy || (li == 0 && !it->small)) {
+            if (it->heavy != take_heavy || (li == 0) != it->small) {
                 ++it;
                 continue;
             }
