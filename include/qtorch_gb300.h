@@ -72,6 +72,13 @@ qt_status qt_ctx_set_memory_budget(qt_ctx *ctx, uint64_t bytes);
 qt_status qt_ctx_set_deadline(qt_ctx *ctx, double seconds_from_now);
 /* Number of kernels this library launched on the context (for accounting). */
 uint64_t qt_ctx_kernel_launches(const qt_ctx *ctx);
+/* Contraction steps of this context that ran on the tcgen05 tensor-core GEMM. */
+uint64_t qt_ctx_tensor_core_steps(const qt_ctx *ctx);
+/* The context's caching device allocator: bytes handed out, bytes cached for
+ * reuse, and how many cudaMalloc calls it has made since the context was
+ * created (any pointer may be NULL). */
+qt_status qt_ctx_memory_stats(qt_ctx *ctx, uint64_t *bytes_in_use, uint64_t *bytes_cached,
+                              uint64_t *device_allocations);
 
 /* ---- tensors ---------------------------------------------------------- */
 
@@ -218,8 +225,13 @@ qt_status qt_plan_execute(qt_ctx *ctx, qt_plan *plan, qt_precision prec, double 
  * a device looks the array's device address up, so make it before any stream
  * capture.  Every call shares the one array and overwrites what the previous
  * call left there: calls that overlap on the GPU (other streams, other
- * contexts of the same device) race.  The call returns after the launch; the
- * value is ready once the context stream reaches it. */
+ * contexts of the same device) race.
+ * Stream order: the descriptors are copied from host memory and the kernel is
+ * launched on the context's stream, without waiting for earlier work.  The
+ * leaves must therefore be complete in that stream's order -- create the
+ * context on the stream that writes them (qt_ctx_create's stream argument) or
+ * synchronise that stream first -- and value_device may be read once the
+ * context's stream has passed the launch. */
 qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *plan, qt_precision prec, const void *leaves_device,
                                  double *value_device);
 /* Parametrised rotation leaves (Rx, Ry, Rz, PHASE, CPHASE) of the plan, in leaf

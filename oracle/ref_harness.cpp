@@ -14,7 +14,19 @@
 //   gates                                   every gate tensor of Node.h for a fixed set of parameters
 //   pair   <in.bin> <out.bin>               one ContractIndices call (Network.h:876-971) on raw tensors
 //   qaoa   <dgf> <p> <b_1..b_p g_1..g_p>    per-edge light-cone QASM text exactly as maxcut.cpp:166-190 writes it
+//   bench  <dgf> <p> <seqfile> <anglesfile> <workers> <workdir>
+//                                           the reference's own QAOA objective per step (the F_p body,
+//                                           maxcut.cpp:166-196): for every edge term write the QASM and
+//                                           measurement files, parse them, contract them with
+//                                           ContractGivenSequence (ContractionTools.h:392-411) under a
+//                                           recorded ordering.  Terms go to `workers` forked processes
+//                                           (dynamic, one term at a time); one step per line of
+//                                           anglesfile ("b_1..b_p g_1..g_p"); prints "step <s> <f_p>"
+//                                           per step and "value <term> <re> <im>" for the first step
+#include <atomic>
+#include <chrono>
 #include <cstdio>
+#include <new>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
@@ -22,6 +34,10 @@
 #include <sstream>
 #include <vector>
 #include <string>
+
+#include <sys/mman.h>
+#include <sys/wait.h>
+#include <unistd.h>
 
 #include "maxcut.h"   // pulls in ContractionTools.h, Network.h, Node.h, LineGraph.h, preprocess.h
 
@@ -170,9 +186,175 @@ static int cmd_qaoa(int argc, char **argv) {
     return 0;
 }
 
+
+// ---- bench: the reference's objective evaluation on all host cores -------------
+
+namespace {
+
+// shared between the forked workers: the next term index of the current step
+// at offset 0, the values (re, im per term) from offset 64
+constexpr size_t kValuesOffset = 64;
+
+bool read_full(int fd, void *buf, size_t n) {
+    char *p = static_cast<char *>(buf);
+    while (n) {
+        ssize_t r = ::read(fd, p, n);
+        if (r <= 0) return false;
+        p += r;
+        n -= (size_t) r;
+    }
+    return true;
+}
+
+bool write_full(int fd, const void *buf, size_t n) {
+    const char *p = static_cast<const char *>(buf);
+    while (n) {
+        ssize_t r = ::write(fd, p, n);
+        if (r <= 0) return false;
+        p += r;
+        n -= (size_t) r;
+    }
+    return true;
+}
+
+// One term exactly as F_p handles it (maxcut.cpp:171-196), with the stochastic
+// contraction replaced by the replay of a recorded ordering.
+std::complex<double> bench_term(ExtraData &e, size_t k, const std::vector<double> &bg,
+                                const std::vector<std::pair<int, int>> &seq, const std::string &qasmPath,
+                                const std::string &measPath) {
+    std::ofstream q(qasmPath);
+    std::ofstream meas(measPath);
+    int numQubits = e.qubitsNeeded[k];
+    q << numQubits << std::endl;
+    outputInitialPlusStateToFile(q, numQubits);
+    applyU_CsThenU_Bs(e.realIterations[k], e.p, bg, numQubits, q);
+    for (int i = 0; i < numQubits; i++) meas << ((i == 0 || i == 1) ? "Z " : "T ");
+    meas.close();
+    q.close();
+    ContractionTools t(qasmPath, measPath, 1);
+    t.ContractGivenSequence(seq);
+    return t.GetFinalVal();
+}
+
+}  // namespace
+
+static int cmd_bench(char **argv) {
+    const char *dgf = argv[0];
+    int p = std::atoi(argv[1]);
+    const char *seqPath = argv[2], *anglesPath = argv[3];
+    int workers = std::max(1, std::atoi(argv[4]));
+    std::string workdir = argv[5];
+
+    ExtraData e(p, dgf);
+    size_t nTerms = e.pairs.size();
+    // seqfile: one line per term, "a b a b ..." (node-id pairs of GetAllNodes())
+    std::vector<std::vector<std::pair<int, int>>> seqs;
+    {
+        std::ifstream f(seqPath);
+        std::string line;
+        while (std::getline(f, line)) {
+            std::istringstream ls(line);
+            std::vector<std::pair<int, int>> s;
+            int a, b;
+            while (ls >> a >> b) s.push_back({a, b});
+            seqs.push_back(s);
+        }
+    }
+    if (seqs.size() != nTerms) {
+        std::fprintf(stderr, "bench: %zu sequences for %zu terms\n", seqs.size(), nTerms);
+        return 3;
+    }
+    std::vector<std::vector<double>> steps;
+    {
+        std::ifstream f(anglesPath);
+        std::string line;
+        while (std::getline(f, line)) {
+            std::istringstream ls(line);
+            std::vector<double> bg;
+            double x;
+            while (ls >> x) bg.push_back(x);
+            if ((int) bg.size() == 2 * p) steps.push_back(bg);
+        }
+    }
+
+    size_t shBytes = kValuesOffset + sizeof(double) * 2 * nTerms;
+    void *mem = mmap(nullptr, shBytes, PROT_READ | PROT_WRITE, MAP_SHARED | MAP_ANONYMOUS, -1, 0);
+    if (mem == MAP_FAILED) return 5;
+    std::atomic<long> *next = new (mem) std::atomic<long>(0);
+    double *values = reinterpret_cast<double *>(static_cast<char *>(mem) + kValuesOffset);
+
+    std::vector<int> toChild(workers), fromChild(workers);
+    std::vector<pid_t> pids(workers);
+    for (int w = 0; w < workers; w++) {
+        int a[2], b[2];
+        if (pipe(a) || pipe(b)) return 5;
+        pid_t pid = fork();
+        if (pid < 0) return 5;
+        if (pid == 0) {
+            ::close(a[1]);
+            ::close(b[0]);
+            std::string qp = workdir + "/tempMaxCut" + std::to_string(w) + ".qasm";
+            std::string mp = workdir + "/measureTest" + std::to_string(w) + ".txt";
+            int32_t s;
+            while (read_full(a[0], &s, sizeof s) && s >= 0) {
+                const std::vector<double> &bg = steps[(size_t) s];
+                int32_t ok = 1;
+                try {
+                    for (long k; (k = next->fetch_add(1)) < (long) nTerms;) {
+                        std::complex<double> v = bench_term(e, (size_t) k, bg, seqs[(size_t) k], qp, mp);
+                        values[2 * k] = v.real();
+                        values[2 * k + 1] = v.imag();
+                    }
+                } catch (std::exception &) {
+                    ok = 0;
+                }
+                if (!write_full(b[1], &ok, sizeof ok)) break;
+            }
+            std::remove(qp.c_str());
+            std::remove(mp.c_str());
+            _exit(0);
+        }
+        ::close(a[0]);
+        ::close(b[1]);
+        toChild[w] = a[1];
+        fromChild[w] = b[0];
+        pids[w] = pid;
+    }
+
+    int rc = 0;
+    for (size_t s = 0; s < steps.size() && rc == 0; s++) {
+        next->store(0);
+        auto t0 = std::chrono::steady_clock::now();
+        int32_t cmd = (int32_t) s;
+        for (int w = 0; w < workers; w++) write_full(toChild[w], &cmd, sizeof cmd);
+        for (int w = 0; w < workers; w++) {
+            int32_t ok = 0;
+            if (!read_full(fromChild[w], &ok, sizeof ok) || !ok) rc = 4;
+        }
+        double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        double fp = 0.0;   // F_p (maxcut.cpp:196)
+        for (size_t k = 0; k < nTerms; k++) fp += 0.5 * (1.0 - values[2 * k]);
+        std::printf("step %zu %.9f %.17g\n", s, sec, fp);
+        if (s == 0) {
+            for (size_t k = 0; k < nTerms; k++)
+                std::printf("value %zu %.17g %.17g\n", k, values[2 * k], values[2 * k + 1]);
+        }
+        std::fflush(stdout);
+    }
+    int32_t stop = -1;
+    for (int w = 0; w < workers; w++) {
+        write_full(toChild[w], &stop, sizeof stop);
+        ::close(toChild[w]);
+        ::close(fromChild[w]);
+    }
+    for (int w = 0; w < workers; w++) waitpid(pids[w], nullptr, 0);
+    munmap(mem, shBytes);
+    return rc;
+}
+
 int main(int argc, char **argv) {
     if (argc < 2) {
-        std::fprintf(stderr, "usage: %s stoch|seq|lg|lgwires|gates|pair|qaoa ...\n", argv[0]);
+        std::fprintf(stderr, "usage: %s stoch|seq|lg|lgwires|gates|pair|qaoa|bench ...\n", argv[0]);
         return 1;
     }
     g_null.open("/dev/null");
@@ -231,6 +413,8 @@ int main(int argc, char **argv) {
             rc = cmd_gates(argc >= 3 ? argv[2] : nullptr);
         } else if (cmd == "pair" && argc >= 4) {
             rc = cmd_pair(argv[2], argv[3]);
+        } else if (cmd == "bench" && argc >= 8) {
+            rc = cmd_bench(argv + 2);
         } else if (cmd == "qaoa" && argc >= 4) {
             rc = cmd_qaoa(argc - 2, argv + 2);
         } else {

@@ -166,6 +166,17 @@ class Context:
         return int(_lib().qt_ctx_kernel_launches(self.handle))
 
     @property
+    def tensor_core_steps(self):
+        """contraction steps that ran on the tcgen05 tensor-core GEMM"""
+        return int(_lib().qt_ctx_tensor_core_steps(self.handle))
+
+    def memory_stats(self):
+        """(bytes in use, bytes cached, cudaMalloc calls so far) of the context's allocator"""
+        a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        _check(_lib().qt_ctx_memory_stats(self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), self)
+        return int(a.value), int(b.value), int(c.value)
+
+    @property
     def last_error(self):
         buf = ctypes.create_string_buffer(512)
         _lib().qt_last_error(self.handle, buf, 512)

@@ -24,6 +24,14 @@ def qft_text(n, seed):
     return "\n".join(lines) + "\n"
 
 
+def qft_measure_text(n):
+    """<X> on the last qubit, traces elsewhere.  The QFT of a basis state |x> is
+    a product state: <Z> is 0 on every qubit and qubit 0 (after the reversal
+    swaps) carries the phase pi*x, so <X_0> = +-1; the last qubit carries
+    2 pi x / 2^n, a generic value."""
+    return " ".join(["T"] * (n - 1) + ["X"])
+
+
 def random_circuit_text(n, depth, seed):
     """Layers of seeded Rx/Ry/Rz on every qubit, then CZ on n/4 disjoint random pairs."""
     rng = np.random.default_rng(seed)

@@ -109,6 +109,7 @@ qt_status dev_alloc(qt_ctx *ctx, size_t bytes, void **out) {
     }
     ctx->block_size[p] = cls;
     ctx->bytes_in_use += cls;
+    ctx->device_allocs++;
     *out = p;
     return QT_OK;
 }
@@ -178,6 +179,7 @@ qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const v
                 e = launch_gemm_step(d, (const float2 *) A, (const float2 *) B, (float2 *) C, (float *) scratch,
                                      (int *) flag, ctx->stream);
             ctx->launches += gemm_flag ? 2 : 3;
+            ctx->tc_steps++;
             int h = 0;
             if (!gemm_flag) {
                 if (e == cudaSuccess) e = cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
@@ -346,6 +348,17 @@ qt_status qt_ctx_set_deadline(qt_ctx *ctx, double seconds) {
 }
 
 uint64_t qt_ctx_kernel_launches(const qt_ctx *ctx) { return ctx ? ctx->launches.load() : 0; }
+
+uint64_t qt_ctx_tensor_core_steps(const qt_ctx *ctx) { return ctx ? ctx->tc_steps.load() : 0; }
+
+qt_status qt_ctx_memory_stats(qt_ctx *ctx, uint64_t *bytes_in_use, uint64_t *bytes_cached, uint64_t *device_allocations) {
+    if (!ctx) return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    if (bytes_in_use) *bytes_in_use = ctx->bytes_in_use;
+    if (bytes_cached) *bytes_cached = ctx->bytes_cached;
+    if (device_allocations) *device_allocations = ctx->device_allocs.load();
+    return QT_OK;
+}
 
 qt_status qt_tensor_create(qt_ctx *ctx, int rank, qt_dtype dtype, qt_tensor **out) {
     if (!ctx || !out || rank < 0 || rank > kMaxWires || (dtype != QT_C128 && dtype != QT_C64)) return QT_ERR_INVALID_ARGUMENT;

@@ -31,6 +31,8 @@ struct qt_ctx {
     uint64_t bytes_cached = 0;
     uint64_t memory_budget = 0;          // 0 = unlimited
     std::atomic<uint64_t> launches{0};
+    std::atomic<uint64_t> device_allocs{0};   // cudaMalloc calls made by the caching allocator
+    std::atomic<uint64_t> tc_steps{0};        // contraction steps run on the tcgen05 GEMM
     bool has_deadline = false;
     std::chrono::steady_clock::time_point deadline;
     // pinned staging buffer for small host<->device transfers

@@ -141,8 +141,9 @@ extern "C" qt_status qt_plan_execute_static(qt_ctx *ctx, const qt_plan *p, qt_pr
         e = cudaMemcpyAsync(b + off_tab, p->tables.data(), tab_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(b + off_inst, &inst, sizeof inst, cudaMemcpyHostToDevice, ctx->stream);
-    // the stack copies above must not go out of scope before the transfers are done
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    // Copies from pageable host memory: each returns once its source has been
+    // staged by the driver, so pd and inst may go out of scope afterwards and
+    // the host never waits for earlier work on the stream.
     if (e != cudaSuccess) return cuda_error(ctx, e, "static scratch upload");
     PlanLaunch lp{};
     lp.instances = reinterpret_cast<const InstanceDesc *>(b + off_inst);

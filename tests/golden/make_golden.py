@@ -4,7 +4,7 @@ Runs only where the reference source tree exists (it builds oracle/_ref with
 ``make -C oracle ref``).  The fixtures it writes are committed, so the tests
 never need the reference at run time.
 
-    python tests/golden/make_golden.py [--ref-root /root/reference]
+    python tests/golden/make_golden.py --ref-root <reference checkout>   (or QT_REF_TREE=<checkout>)
 
 Fixtures:
   gates.json      every gate tensor the reference's Node classes build (src/Node.h:197-898)
@@ -227,7 +227,7 @@ def gen_reduce(ref_root, cwd):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default="/root/reference")
+    ap.add_argument("--ref-root", default=os.environ.get("QT_REF_TREE"), required="QT_REF_TREE" not in os.environ)
     ap.add_argument("--only", nargs="*", help="regenerate only these fixtures (the stochastic ones change every run)")
     args = ap.parse_args()
     src = os.path.join(args.ref_root, "src")

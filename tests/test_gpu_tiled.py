@@ -111,14 +111,18 @@ def test_mid_size_plans_alone_run_step_by_step(ctx, which):
     """A plan above 2^24 complex MACs evaluated alone runs step by step over the
     whole GPU (tiled, tensor-core and compensated reduction kernels); FP64 stays
     bit-exact with the oracle's replay, mixed within 1e-6."""
-    from qtorch_gb300.circuits import qft_text, random_circuit_text
+    from qtorch_gb300.circuits import qft_measure_text, qft_text, random_circuit_text
     text = {"qft10": qft_text(10, 4), "qft12": qft_text(12, 5), "rand12": random_circuit_text(12, 10, 1),
             "rand16": random_circuit_text(16, 12, 10)}[which]
-    plan = qg.Plan(text, "Z", ordering="linegraph", ctx=ctx)
+    # <Z> of a QFT'd basis state is 0 on every qubit; <X> of its last qubit is not
+    meas = qft_measure_text(int(which[3:])) if which.startswith("qft") else "Z"
+    plan = qg.Plan(text, meas, ordering="linegraph", ctx=ctx)
     assert plan.flops > 1 << 24
     v64 = plan.execute(qg.FP64)
+    if which.startswith("qft"):
+        assert abs(v64) > 1e-3
     if which in ("qft10", "rand12"):   # larger replays take too long on the host
-        v_or, _ = port.replay_value(text, "Z", plan.sequence())
+        v_or, _ = port.replay_value(text, meas, plan.sequence())
         assert v64 == v_or
     assert abs(plan.execute(qg.MIXED) - v64) <= MIXED_TOL
 

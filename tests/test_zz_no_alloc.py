@@ -6,8 +6,9 @@ cudaMalloc's implicit synchronisation.  They hand over inputs and outputs in
 device memory they already own, and the engine works in a statically reserved
 device array.  This test calls that entry point through the C ABI, twice in a
 row on the same static array, and checks it against qt_plan_execute: equal bit
-for bit in FP64, within 1e-6 in the mixed form.  It lives in a file of its own
-that pytest collects last."""
+for bit in FP64, within 1e-6 in the mixed form; across those calls neither the
+context's allocator nor the device's free memory may change.  It lives in a
+file of its own that pytest collects last."""
 import ctypes
 
 import numpy as np
@@ -53,12 +54,22 @@ def test_static_entry_point_matches_plan_execute(prec):
             if prec == qg.MIXED:
                 leaves = leaves.astype(np.complex64)
             d_leaves = torch.from_numpy(leaves).cuda()
+            outs = [torch.full((2,), float("nan"), dtype=torch.float64, device="cuda") for _ in range(2)]
+            # the leaves are written on torch's stream: complete them before the context's stream reads them
+            torch.cuda.synchronize()
+            stats0 = ctx.memory_stats()
+            # two calls in a row on the same static array; the device's free
+            # memory is compared around the second (the first launch of a kernel
+            # may let the driver grow its local-memory reservation)
+            assert static_call(lib, ctx, plan, prec, d_leaves, outs[0]) == 0, ctx.last_error
+            ctx.synchronize()
+            free0 = torch.cuda.mem_get_info()[0]
+            assert static_call(lib, ctx, plan, prec, d_leaves, outs[1]) == 0, ctx.last_error
+            ctx.synchronize()
+            assert torch.cuda.mem_get_info()[0] == free0  # no device memory allocated
+            assert ctx.memory_stats() == stats0          # no block taken from or added to the allocator
             got = []
-            for _ in range(2):   # two calls in a row on the same static array
-                out = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda")
-                torch.cuda.synchronize()
-                assert static_call(lib, ctx, plan, prec, d_leaves, out) == 0, ctx.last_error
-                ctx.synchronize()
+            for out in outs:
                 v = out.cpu().numpy()
                 got.append(complex(v[0], v[1]))
             for g in got:
