@@ -490,10 +490,10 @@ def run_config3(args):
         pl = qg.Plan(q, m, ordering="stochastic", seed=seed, ctx=ctx)
         if pl.peak_rank >= 13:
             plans.append(pl)
-    tc0 = ctx.tensor_core_steps
     v64 = [pl.execute(qg.FP64) for pl in plans]
+    tc0, st0 = ctx.tensor_core_steps, ctx.stream_steps
     vmx = [pl.execute(qg.MIXED) for pl in plans]
-    tc_steps = ctx.tensor_core_steps - tc0
+    tc_steps, st_steps = ctx.tensor_core_steps - tc0, ctx.stream_steps - st0
     ctx.synchronize()
 
     def timed(prec, reps):
@@ -519,7 +519,7 @@ def run_config3(args):
         "mixed_complex_macs_per_s": sum(p.flops for p in plans) / t_mx,
         "error_vs_fp64": {"max_abs": float(err.max()), "mean_abs": float(err.mean()), "bound": 1e-6},
         "value_fp64_abs": {"min": float(mag.min()), "max": float(mag.max())},
-        "tensor_core_steps_per_pass": tc_steps,
+        "tensor_core_steps_per_pass": tc_steps, "stream_steps_per_pass": st_steps,
         "timing": "host clock around Plan.execute per term (synchronous), best of 3 passes (FP64: 1)"}
     # --- every edge term under the line-graph ordering, one grouped launch
     lg = []
@@ -568,6 +568,78 @@ def run_config3(args):
     out["gemm_shaped"] = gemm
     ctx.close()
     return out
+
+
+def run_config3_mixed_only(args):
+    """The first --config3-terms terms of config 3's rank 13-14 set, mixed form
+    only, two passes (a small case for ncu launch lists and captures)."""
+    import qtorch_gb300 as qg
+    ctx = qg.Context(0)
+    dgf = qg.random_regular_graph(*CONFIG3_GRAPH[:2], seed=CONFIG3_GRAPH[2])
+    plans = []
+    for e, seed in CONFIG3_TERMS[:args.config3_terms]:
+        q, m = qg.qaoa_term_text(dgf, 2, CONFIG3_ANGLES, e)
+        plans.append(qg.Plan(q, m, ordering="stochastic", seed=seed, ctx=ctx))
+    out = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        vals = [pl.execute(qg.MIXED) for pl in plans]
+        out.append(time.perf_counter() - t0)
+    print(json.dumps({"terms": len(plans), "seconds_per_pass": out, "values": [[v.real, v.imag] for v in vals]}))
+    ctx.close()
+
+
+def run_stream_case(args):
+    """One complex64 contraction step of ranks (rA, rB) summed over K wires --
+    --stream-case rA,rB,K[,seed] -- with seeded random wires, through
+    qt_contract_pair on device tensors (C's free wires in ContractNodes order),
+    20 timed launches (CUDA events on the context stream, inputs larger than
+    L2): a small case for ncu captures of the step kernels.  Prints the step's
+    average time and algorithmic GB/s."""
+    import ctypes
+
+    import torch
+
+    import qtorch_gb300 as qg
+    f = [int(x) for x in args.stream_case.split(",")]
+    ra, rb, k = f[:3]
+    rng = np.random.default_rng(f[3] if len(f) > 3 else 1)
+    wa, wb = rng.permutation(ra), rng.permutation(rb)
+    sa, sb = [int(x) for x in wa[:k]], [int(x) for x in wb[:k]]
+    ffa = np.array([1] * (ra - k) + [0] * (rb - k), dtype=np.uint8)
+    fi = np.array([w for w in range(ra) if w not in sa] + [w for w in range(rb) if w not in sb], dtype=np.int32)
+    sa_a, sb_a = np.array(sa, dtype=np.int32), np.array(sb, dtype=np.int32)
+    stream = torch.cuda.Stream()
+    ctx = qg.Context(0, stream=stream.cuda_stream)
+    lib = qg._capi.load()
+    ta, tb = ctypes.c_void_p(), ctypes.c_void_p()
+    for r, t in ((ra, ta), (rb, tb)):
+        assert lib.qt_tensor_create(ctx.handle, r, 1, ctypes.byref(t)) == 0
+        host = rng.standard_normal(2 * 4 ** r).astype(np.float32)
+        assert lib.qt_tensor_upload(ctx.handle, t, host.ctypes.data_as(ctypes.c_void_p), host.nbytes) == 0
+    P8, P32 = ctypes.POINTER(ctypes.c_uint8), ctypes.POINTER(ctypes.c_int32)
+    ctx.synchronize()
+    n0 = (ctx.stream_steps, ctx.tensor_core_steps)
+    times = []
+    for i in range(23):
+        tc = ctypes.c_void_p()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        assert lib.qt_contract_pair(ctx.handle, ta, tb, len(fi), ffa.ctypes.data_as(P8), fi.ctypes.data_as(P32),
+                                    k, sa_a.ctypes.data_as(P32), sb_a.ctypes.data_as(P32), ctypes.byref(tc)) == 0
+        e1.record(stream)
+        e1.synchronize()
+        lib.qt_tensor_free(ctx.handle, tc)
+        if i >= 3:
+            times.append(e0.elapsed_time(e1) / 1e3)
+    lib.qt_tensor_free(ctx.handle, ta)
+    lib.qt_tensor_free(ctx.handle, tb)
+    t = sum(times) / len(times)
+    alg = 8 * (4 ** ra + 4 ** rb + 4 ** (ra + rb - 2 * k))
+    print(json.dumps({"step": [ra, rb, k], "sum_a": sa, "sum_b": sb, "us": 1e6 * t, "alg_bytes": alg,
+                      "gb_per_s": alg / t / 1e9, "stream_steps": ctx.stream_steps - n0[0],
+                      "tensor_core_steps": ctx.tensor_core_steps - n0[1]}))
+    ctx.close()
 
 
 def run_only_serving(args):
@@ -808,7 +880,8 @@ def bench_summary(line):
                                   "mixed_over_fp64": r(c["mixed_over_fp64"], 3),
                                   "max_err": r(c["error_vs_fp64"]["max_abs"], 2),
                                   "mean_err": r(c["error_vs_fp64"]["mean_abs"], 2),
-                                  "tensor_core_steps": c["tensor_core_steps_per_pass"]}
+                                  "tensor_core_steps": c["tensor_core_steps_per_pass"],
+                                  "stream_steps": c["stream_steps_per_pass"]}
     if "serving" in line:
         v = line["serving"]
         s["config5_serving"] = {"p50_ms": r(v["p50_ms"], 3), "p99_ms": r(v["p99_ms"], 3),
@@ -970,6 +1043,10 @@ def main():
     ap.add_argument("--serve-load", type=float, default=0.7)
     ap.add_argument("--no-config3", action="store_true", help="skip the p=2 50-vertex and GEMM-shaped cases")
     ap.add_argument("--only-config3", action="store_true", help="run only the config-3 cases (for profiling)")
+    ap.add_argument("--config3-terms", type=int, default=0,
+                    help="run only the first N rank 13-14 terms of config 3, mixed form (for profiling)")
+    ap.add_argument("--stream-case", default="",
+                    help="rA,rB,K[,seed]: time one complex64 step of these ranks (for profiling)")
     ap.add_argument("--rescan-config3", action="store_true",
                     help="print the (edge, seed) list of config 3's rank 13-14 terms and exit")
     ap.add_argument("--only-serving", action="store_true", help="run only the serving workload")
@@ -990,6 +1067,10 @@ def main():
     qbuild.build()
     if args.rescan_config3:
         print(config3_scan())
+    elif args.config3_terms > 0:
+        run_config3_mixed_only(args)
+    elif args.stream_case:
+        run_stream_case(args)
     elif args.only_batched:
         run_only_batched(args)
     elif args.only_config3:

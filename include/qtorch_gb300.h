@@ -74,6 +74,9 @@ qt_status qt_ctx_set_deadline(qt_ctx *ctx, double seconds_from_now);
 uint64_t qt_ctx_kernel_launches(const qt_ctx *ctx);
 /* Contraction steps of this context that ran on the tcgen05 tensor-core GEMM. */
 uint64_t qt_ctx_tensor_core_steps(const qt_ctx *ctx);
+/* Contraction steps of this context that ran on the streaming kernel (a small
+ * operand in shared memory, the large one read once by TMA bulk copies). */
+uint64_t qt_ctx_stream_steps(const qt_ctx *ctx);
 /* The context's caching device allocator: bytes handed out, bytes cached for
  * reuse, and how many cudaMalloc calls it has made since the context was
  * created (any pointer may be NULL). */

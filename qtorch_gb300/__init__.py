@@ -170,6 +170,11 @@ class Context:
         """contraction steps that ran on the tcgen05 tensor-core GEMM"""
         return int(_lib().qt_ctx_tensor_core_steps(self.handle))
 
+    @property
+    def stream_steps(self):
+        """contraction steps that ran on the streaming kernel (small operand in shared memory)"""
+        return int(_lib().qt_ctx_stream_steps(self.handle))
+
     def memory_stats(self):
         """(bytes in use, bytes cached, cudaMalloc calls so far) of the context's allocator"""
         a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()

@@ -37,6 +37,7 @@ SIGNATURES = [
     ("qt_ctx_set_deadline", c_int, [c_void_p, c_double]),
     ("qt_ctx_kernel_launches", c_uint64, [c_void_p]),
     ("qt_ctx_tensor_core_steps", c_uint64, [c_void_p]),
+    ("qt_ctx_stream_steps", c_uint64, [c_void_p]),
     ("qt_ctx_memory_stats", c_int, [c_void_p, P(c_uint64), P(c_uint64), P(c_uint64)]),
     ("qt_tensor_create", c_int, [c_void_p, c_int, c_int, P(c_void_p)]),
     ("qt_tensor_free", c_int, [c_void_p, c_void_p]),

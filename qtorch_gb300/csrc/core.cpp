@@ -9,6 +9,7 @@
 
 #include "gemm_tc.h"
 #include "kernels.h"
+#include "stream.h"
 
 namespace qtg {
 
@@ -149,8 +150,26 @@ bool tensor_cores_enabled() {
     return on;
 }
 
+bool stream_enabled() {
+    static const bool on = [] {
+        const char *v = std::getenv("QT_DISABLE_STREAM");
+        return !(v && v[0] == '1');
+    }();
+    return on;
+}
+
+// QT_STREAM_FIRST=1 offers every complex64 step to the streaming kernel before
+// the tensor-core and tiled kernels (for measuring one against the other)
+static bool stream_first() {
+    static const bool on = [] {
+        const char *v = std::getenv("QT_STREAM_FIRST");
+        return v && v[0] == '1';
+    }();
+    return on;
+}
+
 qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const void *B, void *C, bool f64,
-                          int *gemm_flag) {
+                          int *gemm_flag, const StepScaleRef &sc) {
     // a long sum into a few outputs: the whole GPU on one sum.  In complex64
     // every such reduction (rank <= 2, >= 64 terms) takes the compensated kernel:
     // these are the expectation values where cancellation lives.
@@ -164,40 +183,59 @@ qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const v
         void *scratch = nullptr;
         qt_status s = dev_alloc(ctx, reduce_scratch_bytes(d), &scratch);
         if (s != QT_OK) return s;
-        cudaError_t e = launch_reduce_f32(d, (const float2 *) A, (const float2 *) B, (float2 *) C, scratch, ctx->stream);
+        cudaError_t e = launch_reduce_f32(d, (const float2 *) A, (const float2 *) B, (float2 *) C, scratch, ctx->stream, sc);
         ctx->launches += 2;
         dev_free(ctx, scratch);   // stream-ordered: the next user of the block runs after these kernels
         return cuda_error(ctx, e, "reduction launch");
     }
-    if (!f64 && tensor_cores_enabled() && gemm_eligible(d)) {
+    // Dense steps of two large operands take the tensor cores (gemm_tc.cu),
+    // wide ones the tiled kernel; the other complex64 steps with one small
+    // operand stream the large one (stream.cu).  Both TMA-fed kernels report
+    // pipeline timeouts through a device flag: the caller's, read once after
+    // its last step, or one checked here.
+    StreamStep sp;
+    const bool first = stream_first();
+    const bool use_gemm = !f64 && tensor_cores_enabled() && gemm_eligible(d) && !(first && stream_plan(d, sp));
+    const bool use_stream =
+        !f64 && !use_gemm && (first || !tiled_shaped(d)) && stream_enabled() && stream_plan(d, sp);
+    if (use_stream || use_gemm) {
         void *scratch = nullptr, *flag = gemm_flag;
-        qt_status s = dev_alloc(ctx, sizeof(float) * gemm_scratch_floats(d), &scratch);
+        qt_status s = QT_OK;
+        if (use_gemm) s = dev_alloc(ctx, sizeof(float) * gemm_scratch_floats(d), &scratch);
         if (s == QT_OK && !gemm_flag) s = dev_alloc(ctx, 256, &flag);
         if (s == QT_OK) {
             cudaError_t e = gemm_flag ? cudaSuccess : cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream);
-            if (e == cudaSuccess)
-                e = launch_gemm_step(d, (const float2 *) A, (const float2 *) B, (float2 *) C, (float *) scratch,
-                                     (int *) flag, ctx->stream);
-            ctx->launches += gemm_flag ? 2 : 3;
-            ctx->tc_steps++;
+            if (e == cudaSuccess) {
+                if (use_stream) {
+                    e = launch_stream(sp, d, (const float2 *) A, (const float2 *) B, (float2 *) C, sc, (int *) flag,
+                                      ctx->stream);
+                    ctx->launches += 1;
+                    ctx->stream_steps++;
+                } else {
+                    e = launch_gemm_step(d, (const float2 *) A, (const float2 *) B, (float2 *) C, (float *) scratch,
+                                         (int *) flag, ctx->stream, sc);
+                    ctx->launches += 3;
+                    ctx->tc_steps++;
+                }
+            }
             int h = 0;
             if (!gemm_flag) {
                 if (e == cudaSuccess) e = cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
                 if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
             }
-            s = cuda_error(ctx, e, "tensor-core contraction");
-            if (s == QT_OK && h) s = set_error(ctx, QT_ERR_CUDA, "tensor-core pipeline wait timed out");
+            s = cuda_error(ctx, e, use_stream ? "streaming contraction" : "tensor-core contraction");
+            if (s == QT_OK && h) s = set_error(ctx, QT_ERR_CUDA, "TMA pipeline wait timed out");
         }
         dev_free(ctx, scratch);   // stream-ordered: the next user of the block runs after this step
         if (!gemm_flag) dev_free(ctx, flag);
         return s;
     }
     if (tiled_shaped(d)) {
-        cudaError_t e = launch_tiled_pair(d, A, B, C, f64, ctx->stream);
+        cudaError_t e = launch_tiled_pair(d, A, B, C, f64, ctx->stream, sc);
         ctx->launches++;
         return cuda_error(ctx, e, "tiled kernel launch");
     }
-    cudaError_t e = launch_pair(d, A, B, C, f64, ctx->stream);
+    cudaError_t e = launch_pair(d, A, B, C, f64, ctx->stream, sc);
     ctx->launches++;
     return cuda_error(ctx, e, "pair kernel launch");
 }
@@ -350,6 +388,8 @@ qt_status qt_ctx_set_deadline(qt_ctx *ctx, double seconds) {
 uint64_t qt_ctx_kernel_launches(const qt_ctx *ctx) { return ctx ? ctx->launches.load() : 0; }
 
 uint64_t qt_ctx_tensor_core_steps(const qt_ctx *ctx) { return ctx ? ctx->tc_steps.load() : 0; }
+
+uint64_t qt_ctx_stream_steps(const qt_ctx *ctx) { return ctx ? ctx->stream_steps.load() : 0; }
 
 qt_status qt_ctx_memory_stats(qt_ctx *ctx, uint64_t *bytes_in_use, uint64_t *bytes_cached, uint64_t *device_allocations) {
     if (!ctx) return QT_ERR_INVALID_ARGUMENT;

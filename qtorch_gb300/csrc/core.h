@@ -33,6 +33,7 @@ struct qt_ctx {
     std::atomic<uint64_t> launches{0};
     std::atomic<uint64_t> device_allocs{0};   // cudaMalloc calls made by the caching allocator
     std::atomic<uint64_t> tc_steps{0};        // contraction steps run on the tcgen05 GEMM
+    std::atomic<uint64_t> stream_steps{0};    // contraction steps run by the streaming kernel
     bool has_deadline = false;
     std::chrono::steady_clock::time_point deadline;
     // pinned staging buffer for small host<->device transfers
@@ -71,14 +72,20 @@ inline size_t elem_bytes(qt_dtype d) { return d == QT_C128 ? 16 : 8; }
 
 // One contraction step over the whole GPU: complex128 with the reference's
 // rounding, or complex64 -- through the tcgen05 tensor-core GEMM when the step
-// is GEMM-shaped and large (gemm_tc.cu), else the SIMT pair kernel.
+// is GEMM-shaped and large (gemm_tc.cu), the tiled kernel when both sides are
+// wide, the streaming kernel when one operand is small (stream.cu), else the
+// SIMT pair kernel.
 // gemm_flag: a zeroed device int the caller checks after its last step (the
 // tensor-core pipeline's timeout flag); null: checked here, with a stream
 // synchronisation after every tensor-core step
+// sc: the mixed form's per-tensor scale words of the step (scale.cuh); empty: no scaling
 qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const void *B, void *C, bool f64,
-                          int *gemm_flag = nullptr);
+                          int *gemm_flag = nullptr, const StepScaleRef &sc = StepScaleRef{});
 // whether complex64 steps may use the tensor cores (QT_DISABLE_TCGEN05=1 turns it off)
 bool tensor_cores_enabled();
+// whether complex64 steps with a small operand may use the streaming kernel
+// (QT_DISABLE_STREAM=1 turns it off)
+bool stream_enabled();
 
 // Fill a StepDesc from the reference's index lists (toNotSumOn, toSumOn).
 qt_status make_step(int rank_a, int rank_b, int n_free, const uint8_t *free_from_a, const int32_t *free_idx,

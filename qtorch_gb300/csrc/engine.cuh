@@ -15,6 +15,8 @@
 
 #include <cstdint>
 
+#include "scale.cuh"
+
 namespace qtg {
 
 constexpr int kMaxWires = 24;      // rank limit of one operand (4^24 elements is far beyond HBM)
@@ -79,6 +81,7 @@ struct PairJob {
     const void *A;
     const void *B;
     void *C;
+    StepScaleRef sc;             // complex64 jobs: the step's scale words (scale.cuh)
     uint64_t n_out, K;
     uint32_t block_begin, pad;
 };

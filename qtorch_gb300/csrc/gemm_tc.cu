@@ -168,7 +168,7 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
 __global__ void __launch_bounds__(kGemmThreads, 1)
 gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, const float *__restrict__ y_hi,
             const float *__restrict__ y_lo, uint64_t k_tiles, uint64_t M, uint64_t N2, float2 *__restrict__ C,
-            int *__restrict__ error_flag) {
+            int *__restrict__ error_flag, const StepScaleRef sc) {
     extern __shared__ __align__(1024) unsigned char smem[];
     // [stages x (x_hi, x_lo, y_hi, y_lo) tiles][full[stages], empty[stages], done][tmem address]
     unsigned char *tiles = smem;
@@ -246,6 +246,8 @@ gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, cons
     }
     // every thread waits for the accumulator (bounded)
     ok = __syncthreads_and(ok) != 0;
+    const int shift = scale_shift(sc);
+    uint32_t lmax = 0;
     if (!ok && warp == 1 && lane == 0) {
         // after a timeout: the copies issued but never consumed land before the CTA leaves
         for (uint64_t kt = s_consumed; kt < s_issued; kt++) {
@@ -281,13 +283,18 @@ gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, cons
 #pragma unroll
                 for (int j = 0; j < 16; j += 2) {
                     const uint64_t col = tn * kTileN + (uint64_t) (c0 + j);   // even: Re, odd: Im
-                    if (col + 1 < N2 + 1 && col < N2) C[m + M * (col >> 1)] = make_float2(v[j], v[j + 1]);
+                    if (col + 1 < N2 + 1 && col < N2) {
+                        const float2 out = make_float2(scale_pow2(v[j], shift), scale_pow2(v[j + 1], shift));
+                        lmax = max(lmax, mag_bits(out));
+                        C[m + M * (col >> 1)] = out;
+                    }
                 }
             }
         }
     } else if (threadIdx.x == 0) {
         atomicExch(error_flag, 1);
     }
+    scale_note(sc, lmax, shift, blockIdx.x == 0 && blockIdx.y == 0);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
@@ -322,7 +329,7 @@ GemmSizes gemm_sizes(const StepDesc &d) {
 size_t gemm_smem_bytes() { return (size_t) kStages * 4 * kTileBytes + (2 * kStages + 1) * 8 + 16; }
 
 cudaError_t launch_gemm_step(const StepDesc &d, const float2 *A, const float2 *B, float2 *C, float *scratch,
-                             int *error_flag, cudaStream_t stream) {
+                             int *error_flag, cudaStream_t stream, const StepScaleRef &sc) {
     const GemmSizes s = gemm_sizes(d);
     float *xh = scratch, *xl = xh + s.x_floats, *yh = xl + s.x_floats, *yl = yh + s.y_floats;
     if (s.m_tiles > 65535 || s.n_tiles > 65535 || s.k_tiles > 0x7fffffffull) return cudaErrorInvalidValue;
@@ -332,7 +339,7 @@ cudaError_t launch_gemm_step(const StepDesc &d, const float2 *A, const float2 *B
     cudaError_t e = cudaFuncSetAttribute(gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     if (e != cudaSuccess) return e;
     dim3 grid((unsigned) s.m_tiles, (unsigned) s.n_tiles);
-    gemm_tf32x3<<<grid, kGemmThreads, smem, stream>>>(xh, xl, yh, yl, s.k_tiles, s.M, s.N2, C, error_flag);
+    gemm_tf32x3<<<grid, kGemmThreads, smem, stream>>>(xh, xl, yh, yl, s.k_tiles, s.M, s.N2, C, error_flag, sc);
     return cudaGetLastError();
 }
 

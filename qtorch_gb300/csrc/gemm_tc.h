@@ -23,7 +23,8 @@ inline uint64_t gemm_scratch_floats(const StepDesc &d) {
 size_t gemm_smem_bytes();
 // pack X and Y (hi/lo TF32 planes) into scratch, then the tcgen05 GEMM writes C.
 // error_flag (device int, zero on entry) becomes 1 if a pipeline wait timed out.
+// sc: the mixed form's per-tensor scaling (scale.cuh), applied in the epilogue
 cudaError_t launch_gemm_step(const StepDesc &d, const float2 *A, const float2 *B, float2 *C, float *scratch,
-                             int *error_flag, cudaStream_t stream);
+                             int *error_flag, cudaStream_t stream, const StepScaleRef &sc = StepScaleRef{});
 
 }  // namespace qtg

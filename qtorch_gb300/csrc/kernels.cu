@@ -21,6 +21,7 @@
 
 #include "engine.cuh"
 #include "kernels.h"
+#include "scale.cuh"
 
 namespace qtg {
 
@@ -95,13 +96,16 @@ struct Vec2<double> { using type = double2; };
 template <>
 struct Vec2<float> { using type = float2; };
 
-// One contraction on CTAs blk = 0 .. nblk-1 of its launch.
+// One contraction on CTAs blk = 0 .. nblk-1 of its launch.  complex64: the
+// sums are scaled by 2^shift and the largest stored magnitude is returned
+// (mag_bits) for the step's scale word.
 template <typename T>
-__device__ __forceinline__ void pair_body(const typename Vec2<T>::type *__restrict__ A,
-                                          const typename Vec2<T>::type *__restrict__ B,
-                                          typename Vec2<T>::type *__restrict__ C, const StepDesc &d, uint64_t n_out,
-                                          uint64_t K, uint32_t blk, uint32_t nblk) {
+__device__ __forceinline__ uint32_t pair_body(const typename Vec2<T>::type *__restrict__ A,
+                                              const typename Vec2<T>::type *__restrict__ B,
+                                              typename Vec2<T>::type *__restrict__ C, const StepDesc &d,
+                                              uint64_t n_out, uint64_t K, uint32_t blk, uint32_t nblk, int shift) {
     using V = typename Vec2<T>::type;
+    uint32_t lmax = 0;
     __shared__ uint64_t s_oa[kPairChunk];
     __shared__ uint64_t s_ob[kPairChunk];
     const uint64_t stride = (uint64_t) nblk * blockDim.x;
@@ -133,18 +137,28 @@ __device__ __forceinline__ void pair_body(const typename Vec2<T>::type *__restri
         }
         if (valid) {
             V v;
-            v.x = cre;
-            v.y = cim;
+            if constexpr (sizeof(T) == 8) {
+                v.x = cre;
+                v.y = cim;
+            } else {
+                v.x = scale_pow2(cre, shift);
+                v.y = scale_pow2(cim, shift);
+                lmax = max(lmax, mag_bits(v));
+            }
             C[c] = v;
         }
     }
+    return lmax;
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kPairThreads)
 pair_kernel(const typename Vec2<T>::type *__restrict__ A, const typename Vec2<T>::type *__restrict__ B,
-            typename Vec2<T>::type *__restrict__ C, const StepDesc d, uint64_t n_out, uint64_t K) {
-    pair_body<T>(A, B, C, d, n_out, K, blockIdx.x, gridDim.x);
+            typename Vec2<T>::type *__restrict__ C, const StepDesc d, uint64_t n_out, uint64_t K,
+            const StepScaleRef sc) {
+    const int shift = sizeof(T) == 4 ? scale_shift(sc) : 0;
+    const uint32_t lmax = pair_body<T>(A, B, C, d, n_out, K, blockIdx.x, gridDim.x, shift);
+    if constexpr (sizeof(T) == 4) scale_note(sc, lmax, shift, blockIdx.x == 0);
 }
 
 // Several independent small contractions (one dependency level of a plan run
@@ -156,8 +170,11 @@ __global__ void __launch_bounds__(kPairThreads) pair_batch_kernel(const __grid_c
     while (j + 1 < pb.n_jobs && blockIdx.x >= pb.job[j + 1].block_begin) j++;
     const PairJob &w = pb.job[j];
     const uint32_t end = j + 1 < pb.n_jobs ? pb.job[j + 1].block_begin : gridDim.x;
-    pair_body<T>(reinterpret_cast<const V *>(w.A), reinterpret_cast<const V *>(w.B), reinterpret_cast<V *>(w.C), w.d,
-                 w.n_out, w.K, blockIdx.x - w.block_begin, end - w.block_begin);
+    const int shift = sizeof(T) == 4 ? scale_shift(w.sc) : 0;
+    const uint32_t lmax = pair_body<T>(reinterpret_cast<const V *>(w.A), reinterpret_cast<const V *>(w.B),
+                                       reinterpret_cast<V *>(w.C), w.d, w.n_out, w.K, blockIdx.x - w.block_begin,
+                                       end - w.block_begin, shift);
+    if constexpr (sizeof(T) == 4) scale_note(w.sc, lmax, shift, blockIdx.x == w.block_begin);
 }
 
 // ---------------------------------------------------------------------------
@@ -200,10 +217,12 @@ reduce_partial_f32(const float2 *__restrict__ A, const float2 *__restrict__ B, c
 }
 
 // one warp per output: merge the CTAs' partial sums, round once to complex64
+// (scaled by 2^shift of the step's producers)
 __global__ void reduce_final_f32(const float4 *__restrict__ partials, uint32_t n_parts, uint32_t n_out,
-                                 float2 *__restrict__ C) {
+                                 float2 *__restrict__ C, const StepScaleRef sc) {
     const uint32_t c = blockIdx.x;
     if (c >= n_out) return;
+    const int shift = scale_shift(sc);
     float pre = 0.f, sre = 0.f, pim = 0.f, sim = 0.f;
     for (uint32_t j = threadIdx.x; j < n_parts; j += 32) {
         const float4 t = partials[(uint64_t) c * n_parts + j];
@@ -216,7 +235,10 @@ __global__ void reduce_final_f32(const float4 *__restrict__ partials, uint32_t n
         dot2_merge(pre, sre, a, b);
         dot2_merge(pim, sim, e, f);
     }
-    if (threadIdx.x == 0) C[c] = make_float2((float) ((double) pre + (double) sre), (float) ((double) pim + (double) sim));
+    const float2 v = make_float2(scale_pow2((float) ((double) pre + (double) sre), shift),
+                                 scale_pow2((float) ((double) pim + (double) sim), shift));
+    if (threadIdx.x == 0) C[c] = v;
+    scale_note(sc, threadIdx.x == 0 ? mag_bits(v) : 0u, shift, c == 0);
 }
 
 // Exact complex128 reduction: one CTA per output.  The products of a chunk of
@@ -273,13 +295,13 @@ size_t reduce_scratch_bytes(const StepDesc &d) {
 }
 
 cudaError_t launch_reduce_f32(const StepDesc &d, const float2 *A, const float2 *B, float2 *C, void *scratch,
-                              cudaStream_t stream) {
+                              cudaStream_t stream, const StepScaleRef &sc) {
     const uint32_t n_out = (uint32_t) (1ull << (2 * d.nFree));
     const uint64_t K = 1ull << (2 * d.nSum);
     const uint32_t g = reduce_grid(d);
     float4 *parts = static_cast<float4 *>(scratch);
     reduce_partial_f32<<<g, kReduceThreads, 0, stream>>>(A, B, d, n_out, K, parts);
-    reduce_final_f32<<<n_out, 32, 0, stream>>>(parts, g, n_out, C);
+    reduce_final_f32<<<n_out, 32, 0, stream>>>(parts, g, n_out, C, sc);
     return cudaGetLastError();
 }
 
@@ -832,15 +854,19 @@ __device__ __forceinline__ void run_tiled(const StepDesc &d, int si, const char 
     else tiled_step<kMixed, kScaled, 1, 1>(d, si, leaves, ws, h, tile, bad, tiny);
 }
 
-// The same tiled product as a whole-GPU kernel for steps run one at a time
-// (no power-of-two scaling there): the CTAs stride over the output tiles.
+// The same tiled product as a whole-GPU kernel for steps run one at a time:
+// the CTAs stride over the output tiles; complex64 sums are scaled by the
+// step's producers (scale.cuh).
 template <bool kMixed, int MI, int NJ>
 __global__ void __launch_bounds__(kPlanThreads)
 tiled_pair_kernel(const typename std::conditional<kMixed, float2, double2>::type *A,
                   const typename std::conditional<kMixed, float2, double2>::type *B,
-                  typename std::conditional<kMixed, float2, double2>::type *C, const StepDesc d) {
+                  typename std::conditional<kMixed, float2, double2>::type *C, const StepDesc d,
+                  const StepScaleRef sc) {
     extern __shared__ __align__(16) unsigned char tile_smem[];
-    tiled_tiles<kMixed, MI, NJ>(d, A, B, C, 0, tile_smem, blockIdx.x, gridDim.x);
+    const int shift = kMixed ? scale_shift(sc) : 0;
+    const float tmax = tiled_tiles<kMixed, MI, NJ>(d, A, B, C, shift, tile_smem, blockIdx.x, gridDim.x);
+    if constexpr (kMixed) scale_note(sc, __float_as_uint(tmax), shift, blockIdx.x == 0);
 }
 
 // Rotation leaves rebuilt from an angle (mixed plans): the superoperators the
@@ -1275,7 +1301,8 @@ cudaError_t launch_pair_batch(PairBatch &pb, bool f64, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C, bool f64, cudaStream_t stream) {
+cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C, bool f64, cudaStream_t stream,
+                        const StepScaleRef &sc) {
     const uint64_t n_out = 1ull << (2 * d.nFree);
     const uint64_t K = 1ull << (2 * d.nSum);
     uint64_t blocks = (n_out + kPairThreads - 1) / kPairThreads;
@@ -1284,10 +1311,10 @@ cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C
     if (blocks < 1) blocks = 1;
     if (f64)
         pair_kernel<double><<<(unsigned) blocks, kPairThreads, 0, stream>>>(
-            (const double2 *) A, (const double2 *) B, (double2 *) C, d, n_out, K);
+            (const double2 *) A, (const double2 *) B, (double2 *) C, d, n_out, K, StepScaleRef{});
     else
         pair_kernel<float><<<(unsigned) blocks, kPairThreads, 0, stream>>>(
-            (const float2 *) A, (const float2 *) B, (float2 *) C, d, n_out, K);
+            (const float2 *) A, (const float2 *) B, (float2 *) C, d, n_out, K, sc);
     return cudaGetLastError();
 }
 
@@ -1354,7 +1381,8 @@ bool tiled_shaped(const StepDesc &d) {
 }
 
 template <bool kMixed>
-static cudaError_t launch_tiled_t(const StepDesc &d, const void *A, const void *B, void *C, cudaStream_t stream) {
+static cudaError_t launch_tiled_t(const StepDesc &d, const void *A, const void *B, void *C, cudaStream_t stream,
+                                  const StepScaleRef &sc) {
     using V = typename std::conditional<kMixed, float2, double2>::type;
     const bool wide_m = d.fA >= 3, wide_n = d.fB >= 3;
     const uint64_t tiles = (1ull << (2 * d.fA)) / (wide_m ? 64 : 16) * ((1ull << (2 * d.fB)) / (wide_n ? 64 : 16));
@@ -1365,15 +1393,15 @@ static cudaError_t launch_tiled_t(const StepDesc &d, const void *A, const void *
     const V *b = static_cast<const V *>(B);
     V *c = static_cast<V *>(C);
     const size_t smem = kCtaTileBytes;
-    if (wide_m && wide_n) tiled_pair_kernel<kMixed, 4, 4><<<(unsigned) grid, kPlanThreads, smem, stream>>>(a, b, c, d);
-    else if (wide_m) tiled_pair_kernel<kMixed, 4, 1><<<(unsigned) grid, kPlanThreads, smem, stream>>>(a, b, c, d);
-    else tiled_pair_kernel<kMixed, 1, 4><<<(unsigned) grid, kPlanThreads, smem, stream>>>(a, b, c, d);
+    if (wide_m && wide_n) tiled_pair_kernel<kMixed, 4, 4><<<(unsigned) grid, kPlanThreads, smem, stream>>>(a, b, c, d, sc);
+    else if (wide_m) tiled_pair_kernel<kMixed, 4, 1><<<(unsigned) grid, kPlanThreads, smem, stream>>>(a, b, c, d, sc);
+    else tiled_pair_kernel<kMixed, 1, 4><<<(unsigned) grid, kPlanThreads, smem, stream>>>(a, b, c, d, sc);
     return cudaGetLastError();
 }
 
 cudaError_t launch_tiled_pair(const StepDesc &d, const void *A, const void *B, void *C, bool f64,
-                              cudaStream_t stream) {
-    return f64 ? launch_tiled_t<false>(d, A, B, C, stream) : launch_tiled_t<true>(d, A, B, C, stream);
+                              cudaStream_t stream, const StepScaleRef &sc) {
+    return f64 ? launch_tiled_t<false>(d, A, B, C, stream, sc) : launch_tiled_t<true>(d, A, B, C, stream, sc);
 }
 
 int plan_num_sms() { return num_sms(); }

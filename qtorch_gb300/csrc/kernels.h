@@ -2,12 +2,15 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "engine.cuh"
+#include "scale.cuh"
 
 namespace qtg {
 
 // One pairwise contraction over the whole GPU.  f64: complex128, reference
 // rounding; otherwise complex64 with FP32 FMA.
-cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C, bool f64, cudaStream_t stream);
+// sc: the mixed form's per-tensor scaling (scale.cuh); empty: none
+cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C, bool f64, cudaStream_t stream,
+                        const StepScaleRef &sc = StepScaleRef{});
 // a small step that run_contraction would give to a pair or tiled kernel: it
 // may join a PairBatch of its dependency level
 bool pair_batchable(const StepDesc &d, bool f64);
@@ -19,7 +22,7 @@ cudaError_t launch_pair_batch(PairBatch &pb, bool f64, cudaStream_t stream);
 // each output sums over k in increasing order (FP64: the reference's rounding).
 bool tiled_shaped(const StepDesc &d);
 cudaError_t launch_tiled_pair(const StepDesc &d, const void *A, const void *B, void *C, bool f64,
-                              cudaStream_t stream);
+                              cudaStream_t stream, const StepScaleRef &sc = StepScaleRef{});
 
 // Steps with at most kReduceMaxOut outputs and a sum of at least kReduceMinK
 // terms (the final expectation values of large networks).
@@ -32,7 +35,7 @@ inline bool reduce_shaped(const StepDesc &d) {
 // merged in a second kernel; scratch holds reduce_scratch_bytes(d) bytes
 size_t reduce_scratch_bytes(const StepDesc &d);
 cudaError_t launch_reduce_f32(const StepDesc &d, const float2 *A, const float2 *B, float2 *C, void *scratch,
-                              cudaStream_t stream);
+                              cudaStream_t stream, const StepScaleRef &sc = StepScaleRef{});
 // complex128 with the reference's rounding: every thread of a CTA forms the
 // products of a chunk of k, one thread adds them in the reference's order
 cudaError_t launch_reduce_exact(const StepDesc &d, const double2 *A, const double2 *B, double2 *C,

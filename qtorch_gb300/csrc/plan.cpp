@@ -13,6 +13,7 @@
 #include "plan.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -527,7 +528,8 @@ void pack_leaves(const qt_plan *p, int prec, const std::complex<double> *src, ch
 
 // Step-by-step execution with the whole-GPU pairwise kernel (plans whose
 // intermediates are too large for one CTA).  Mixed precision runs every step
-// in complex64 and reads the final value back as FP64.
+// in complex64 with per-tensor power-of-two scaling (a scale word per step,
+// scale.cuh) and reads the final value back as FP64, times 2^E of its step.
 qt_status execute_stepwise(qt_plan *p, qt_ctx *ctx, int prec, const std::complex<double> *leaves, double *value) {
     const bool mixed = prec == QT_PREC_MIXED;
     const size_t es = mixed ? 8 : 16;
@@ -581,6 +583,13 @@ qt_status execute_stepwise(qt_plan *p, qt_ctx *ctx, int prec, const std::complex
     void *gflag = nullptr;
     s = dev_alloc(ctx, 256, &gflag);
     if (s == QT_OK) s = cuda_error(ctx, cudaMemsetAsync(gflag, 0, sizeof(int), ctx->stream), "flag clear");
+    // mixed form: the scale word of every step output, zeroed
+    ScaleWord *words = nullptr;
+    if (s == QT_OK && mixed) {
+        const size_t wb = sizeof(ScaleWord) * std::max<size_t>(steps.size(), 1);
+        s = dev_alloc(ctx, wb, reinterpret_cast<void **>(&words));
+        if (s == QT_OK) s = cuda_error(ctx, cudaMemsetAsync(words, 0, wb, ctx->stream), "scale words clear");
+    }
     auto flush = [&]() -> qt_status {
         const cudaError_t fe = launch_pair_batch(*pb, !mixed, ctx->stream);
         if (pb->n_jobs) ctx->launches++;
@@ -600,15 +609,22 @@ qt_status execute_stepwise(qt_plan *p, qt_ctx *ctx, int prec, const std::complex
             const void *B = (d.flags & kBLeaf) ? (const char *) dleaf + leaf_off[p->b_leaf[i]] : outs[d.b_step];
             s = dev_alloc(ctx, es << (2 * d.nFree), &outs[i]);
             if (s != QT_OK) break;
+            StepScaleRef sc;
+            if (mixed) {
+                sc.a = d.a_step >= 0 ? words + d.a_step : nullptr;
+                sc.b = d.b_step >= 0 ? words + d.b_step : nullptr;
+                sc.c = words + i;
+            }
             if (pair_batchable(d, !mixed)) {
                 PairJob &w = pb->job[pb->n_jobs++];
                 w.d = d;
                 w.A = A;
                 w.B = B;
                 w.C = outs[i];
+                w.sc = sc;
                 if (pb->n_jobs == (uint32_t) kPairBatchMax) s = flush();
             } else {
-                s = run_contraction(ctx, d, A, B, outs[i], !mixed, (int *) gflag);
+                s = run_contraction(ctx, d, A, B, outs[i], !mixed, (int *) gflag, sc);
             }
         }
         if (s == QT_OK) s = flush();
@@ -639,10 +655,12 @@ qt_status execute_stepwise(qt_plan *p, qt_ctx *ctx, int prec, const std::complex
             double v[2];
             if (mixed) {
                 float f[2];
+                ScaleWord w{};
                 ce = cudaMemcpyAsync(f, outs[r], 8, cudaMemcpyDeviceToHost, ctx->stream);
+                if (ce == cudaSuccess) ce = cudaMemcpyAsync(&w, words + r, sizeof w, cudaMemcpyDeviceToHost, ctx->stream);
                 if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
-                v[0] = f[0];
-                v[1] = f[1];
+                v[0] = std::ldexp((double) f[0], w.expo);
+                v[1] = std::ldexp((double) f[1], w.expo);
             } else {
                 ce = cudaMemcpyAsync(v, outs[r], 16, cudaMemcpyDeviceToHost, ctx->stream);
                 if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
@@ -662,6 +680,7 @@ qt_status execute_stepwise(qt_plan *p, qt_ctx *ctx, int prec, const std::complex
     for (void *o : outs) dev_free(ctx, o);
     dev_free(ctx, dleaf);
     dev_free(ctx, gflag);
+    dev_free(ctx, words);
     return s;
 }
 

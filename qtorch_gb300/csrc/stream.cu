@@ -1,0 +1,416 @@
+// Streaming contraction of complex64 steps with one small operand (see
+// stream.h).  One persistent CTA of 256 threads loops over tiles of the large
+// operand L:
+//
+//   * warp 0 issues the next tile's TMA bulk copies (cp.async.bulk, one per
+//     contiguous run, completion counted on an mbarrier) into the other half
+//     of a double buffer, so HBM reads of tile i+1 overlap the arithmetic of
+//     tile i;
+//   * thread t owns element t of every 256-element stretch of the tile (L's
+//     wires 0-3), so a warp's loads are consecutive and conflict-free; it
+//     loops over the tile's other digits, multiplies by S (in shared memory)
+//     for every free index of S, and adds into its own staging slots;
+//   * after a work item's last tile, the staged partial sums are reduced over
+//     the summed digits among wires 0-3 and written in C's digit order.
+//
+// HBM traffic is one read of L and S and one write of C: the step's
+// algorithmic bytes.  The mixed form's per-tensor power-of-two scaling
+// (scale.cuh) is applied to every stored value.  Every mbarrier wait is
+// bounded; on a timeout the CTA waits (bounded) for its copies in flight,
+// raises the error flag and leaves.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+#include "stream.h"
+
+namespace qtg {
+namespace {
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init1(uint32_t bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// at most 2^22 polls (tens of milliseconds with the back-off), then false
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t it = 0; it < (1u << 22); it++) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+        if (ok) return true;
+        if (it > 64) __nanosleep(32);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void cmac(float2 &c, float2 a, float2 b) {
+    c.x = fmaf(a.x, b.x, c.x);
+    c.x = fmaf(-a.y, b.y, c.x);
+    c.y = fmaf(a.x, b.y, c.y);
+    c.y = fmaf(a.y, b.x, c.y);
+}
+
+__host__ __device__ inline uint32_t round128(uint32_t x) { return (x + 127u) / 128u * 128u; }
+
+// byte offsets of the shared-memory regions (host and device agree)
+__host__ __device__ inline void stream_layout(const StreamStep &p, uint32_t off[6]) {
+    const uint32_t tile = 1u << (2 * (4 + p.go + p.ho));
+    const uint32_t stage = (uint32_t) kStreamThreads << (2 * (p.go + p.nsf));
+    off[0] = 0;                                    // tile buffer 0
+    off[1] = round128(8u * tile);                  // tile buffer 1
+    off[2] = off[1] + round128(8u * tile);         // staged partial sums
+    off[3] = off[2] + round128(8u * stage);        // S
+    off[4] = off[3] + round128(8u * p.s_elems);    // two mbarriers
+    off[5] = off[4] + 128u;                        // end
+}
+
+// warp 0: the bulk copies of (item, chunk) into tile buffer `dst`
+__device__ __forceinline__ void issue_tile(const StreamStep &p, float2 *dst, uint64_t *bar_ptr, uint32_t item,
+                                           uint32_t chunk, uint32_t lane) {
+    uint64_t lbase = 0;
+    for (uint32_t j = 0; j < p.n_item_d; j++) lbase += (uint64_t) ((item >> (2 * j)) & 3u) << (2 * p.item_lw[j]);
+    for (uint32_t j = 0; j < p.n_chunk_d; j++) lbase += (uint64_t) ((chunk >> (2 * j)) & 3u) << (2 * p.chunk_lw[j]);
+    const uint32_t bar = smem_u32(bar_ptr);
+    const uint32_t run_bytes = 8u * p.run_elems;
+    if (lane == 0) {
+        // the buffer's previous contents were read by ordinary loads before
+        // the CTA barrier that precedes this; order them before the async writes
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect(bar, run_bytes * p.n_runs);
+    }
+    __syncwarp();
+    for (uint32_t r = lane; r < p.n_runs; r += 32) {
+        uint64_t off = lbase;
+        for (uint32_t j = 0; j < p.n_run_d; j++) off += (uint64_t) ((r >> (2 * j)) & 3u) << (2 * p.run_lw[j]);
+        bulk_g2s(smem_u32(dst + (uint64_t) r * p.run_elems), p.L + off, run_bytes, bar);
+    }
+}
+
+template <int NSF>
+__global__ void __launch_bounds__(kStreamThreads, 2) stream_kernel(const __grid_constant__ StreamStep p) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint32_t off[6];
+    stream_layout(p, off);
+    float2 *const tile0 = reinterpret_cast<float2 *>(smem + off[0]);
+    float2 *const tile1 = reinterpret_cast<float2 *>(smem + off[1]);
+    float2 *const stage = reinterpret_cast<float2 *>(smem + off[2]);
+    float2 *const S = reinterpret_cast<float2 *>(smem + off[3]);
+    uint64_t *const bars = reinterpret_cast<uint64_t *>(smem + off[4]);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    const uint32_t G = 1u << (2 * p.go), H = 1u << (2 * p.ho);
+
+    for (uint32_t e = tid; e < p.s_elems; e += blockDim.x) S[e] = p.S[e];
+    // this thread's share of S's summed index (its summed digits among wires 0-3)
+    uint32_t s_lo = 0;
+    for (int w = 0; w < 4; w++)
+        if (p.lo_summed[w]) s_lo += ((tid >> (2 * w)) & 3u) << (2 * p.lo_other[w]);
+    uint32_t sfo[NSF];
+#pragma unroll
+    for (int f = 0; f < NSF; f++) {
+        uint32_t o = 0;
+        for (uint32_t j = 0; j < p.nsf; j++) o += (((uint32_t) f >> (2 * j)) & 3u) << (2 * p.sf_w[j]);
+        sfo[f] = o;
+    }
+    if (tid == 0) {
+        mbar_init1(smem_u32(&bars[0]));
+        mbar_init1(smem_u32(&bars[1]));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    const int shift = scale_shift(p.sc);
+    uint32_t lmax = 0;
+    uint32_t item = blockIdx.x, chunk = 0;
+    // per buffer: copies issued and not yet waited for, phases completed
+    bool pend0 = item < p.n_items, pend1 = false;
+    uint32_t waits0 = 0, waits1 = 0;
+    if (warp == 0 && item < p.n_items) issue_tile(p, tile0, &bars[0], item, 0, lane);
+    bool ok = true;
+    for (uint32_t it = 0; item < p.n_items; it++) {
+        const int buf = (int) (it & 1u);
+        // the tile after this one in this CTA's order
+        uint32_t n_item = item, n_chunk = chunk + 1;
+        if (n_chunk == p.n_chunks) {
+            n_chunk = 0;
+            n_item = item + gridDim.x;
+        }
+        if (n_item < p.n_items) {
+            if (warp == 0) issue_tile(p, buf ? tile0 : tile1, &bars[buf ^ 1], n_item, n_chunk, lane);
+            if (buf) pend0 = true;
+            else pend1 = true;
+        }
+        const bool got = mbar_wait(smem_u32(&bars[buf]), (buf ? waits1 : waits0) & 1u);
+        if (!__syncthreads_and(got)) {
+            ok = false;
+            break;
+        }
+        if (buf) {
+            waits1++;
+            pend1 = false;
+        } else {
+            waits0++;
+            pend0 = false;
+        }
+        const float2 *T = buf ? tile1 : tile0;
+
+        // S's share of the chunk's summed digits
+        uint32_t s_c = s_lo;
+        for (uint32_t j = 0; j < p.n_chunk_d; j++) s_c += ((chunk >> (2 * j)) & 3u) << (2 * p.chunk_sw[j]);
+        for (uint32_t g = 0; g < G; g++) {
+            uint32_t tg = tid;
+            for (uint32_t j = 0; j < p.go; j++) tg += ((g >> (2 * j)) & 3u) << (2 * p.g_pos[j]);
+            float2 acc[NSF];
+#pragma unroll
+            for (int f = 0; f < NSF; f++) acc[f] = make_float2(0.f, 0.f);
+            for (uint32_t h = 0; h < H; h++) {
+                uint32_t th = tg, sh = s_c;
+                for (uint32_t j = 0; j < p.ho; j++) {
+                    const uint32_t dg = (h >> (2 * j)) & 3u;
+                    th += dg << (2 * p.h_pos[j]);
+                    sh += dg << (2 * p.h_sw[j]);
+                }
+                const float2 x = T[th];
+#pragma unroll
+                for (int f = 0; f < NSF; f++) cmac(acc[f], x, S[sh + sfo[f]]);
+            }
+            float2 *st = stage + (uint64_t) g * NSF * kStreamThreads + tid;
+#pragma unroll
+            for (int f = 0; f < NSF; f++) {
+                if (chunk == 0) {
+                    st[f * kStreamThreads] = acc[f];
+                } else {
+                    const float2 o = st[f * kStreamThreads];
+                    st[f * kStreamThreads] = make_float2(o.x + acc[f].x, o.y + acc[f].y);
+                }
+            }
+        }
+        if (chunk + 1 == p.n_chunks) {
+            __syncthreads();
+            // the work item's outputs in C's digit order: reduce the staged
+            // partial sums over the summed digits among wires 0-3
+            uint64_t cbase = 0;
+            for (uint32_t j = 0; j < p.n_item_d; j++) cbase += (uint64_t) ((item >> (2 * j)) & 3u) << (2 * p.item_cd[j]);
+            const uint32_t n_out = 1u << (2 * p.n_dout), n_kl = 1u << (2 * p.n_klo);
+            for (uint32_t o = tid; o < n_out; o += blockDim.x) {
+                uint64_t coff = cbase;
+                uint32_t tf = 0, g = 0, f = 0;
+                for (uint32_t r = 0; r < p.n_dout; r++) {
+                    const uint32_t dg = (o >> (2 * r)) & 3u;
+                    coff += (uint64_t) dg << (2 * p.dout_cd[r]);
+                    const uint32_t sh = 2u * p.dout_idx[r];
+                    if (p.dout_kind[r] == 0) tf += dg << sh;
+                    else if (p.dout_kind[r] == 1) g += dg << sh;
+                    else f += dg << sh;
+                }
+                const float2 *st = stage + ((uint64_t) g * NSF + f) * kStreamThreads;
+                float vx = 0.f, vy = 0.f;
+                for (uint32_t kl = 0; kl < n_kl; kl++) {
+                    uint32_t t = tf, q = 0;
+                    for (int w = 0; w < 4; w++)
+                        if (p.lo_summed[w]) {
+                            t += ((kl >> (2 * q)) & 3u) << (2 * w);
+                            q++;
+                        }
+                    const float2 pv = st[t];
+                    vx += pv.x;
+                    vy += pv.y;
+                }
+                const float2 v = make_float2(scale_pow2(vx, shift), scale_pow2(vy, shift));
+                lmax = max(lmax, mag_bits(v));
+                p.C[coff] = v;
+            }
+        }
+        __syncthreads();   // the tile buffer (and the staging, after a write-back) are free again
+        if (++chunk == p.n_chunks) {
+            chunk = 0;
+            item += gridDim.x;
+        }
+    }
+    if (!ok) {
+        // copies still in flight land before the CTA leaves (bounded waits)
+        if (tid == 0) {
+            if (pend0) mbar_wait(smem_u32(&bars[0]), waits0 & 1u);
+            if (pend1) mbar_wait(smem_u32(&bars[1]), waits1 & 1u);
+            atomicExch(p.error_flag, 1);
+        }
+        __syncthreads();
+    }
+    scale_note(p.sc, lmax, shift, blockIdx.x == 0);
+}
+
+using StreamFn = void (*)(const StreamStep);
+
+StreamFn stream_fn(uint32_t nsf) {
+    if (nsf == 0) return stream_kernel<1>;
+    if (nsf == 1) return stream_kernel<4>;
+    return stream_kernel<16>;
+}
+
+std::mutex g_attr_lock;
+bool g_attr_done[64];
+
+cudaError_t stream_attributes() {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> g(g_attr_lock);
+    if (dev >= 0 && dev < 64 && g_attr_done[dev]) return cudaSuccess;
+    int optin = 0;
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    for (uint32_t nsf : {0u, 1u, 2u})
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(stream_fn(nsf), cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e == cudaSuccess && dev >= 0 && dev < 64) g_attr_done[dev] = true;
+    return e;
+}
+
+}  // namespace
+
+bool stream_plan(const StepDesc &d, StreamStep &p) {
+    std::memset(&p, 0, sizeof p);
+    const bool l_is_b = d.rB > d.rA;
+    const int rL = l_is_b ? d.rB : d.rA, rS = l_is_b ? d.rA : d.rB;
+    if (rS > kStreamMaxSmallRank || rL < 8 || d.nSum > kStreamMaxSmallRank) return false;
+    const uint8_t *cL = l_is_b ? d.cB : d.cA;
+    const uint8_t *cS = l_is_b ? d.cA : d.cB;
+    const uint8_t *posL = l_is_b ? d.posBs : d.posAs;
+    const uint8_t *posS = l_is_b ? d.posAs : d.posBs;
+    int pair_s[kMaxWires], cdig[kMaxWires];
+    bool summed[kMaxWires] = {false};
+    for (int w = 0; w < kMaxWires; w++) pair_s[w] = cdig[w] = -1;
+    for (int i = 0; i < d.nSum; i++) {
+        summed[posL[i]] = true;
+        pair_s[posL[i]] = posS[i];
+    }
+    int nsf = 0;
+    for (int i = 0; i < d.nFree; i++) {
+        if (cL[i] != kNoWire) cdig[cL[i]] = i;
+        else p.sf_w[nsf++] = cS[i];
+    }
+    if (nsf > 2) return false;   // at most 16 free indices of S per thread
+    p.l_is_b = l_is_b;
+    p.nsf = (uint32_t) nsf;
+    p.s_elems = 1u << (2 * rS);
+    // wires 0-3: the thread's own digits
+    int klo = 0;
+    for (int w = 0; w < 4; w++) {
+        p.lo_summed[w] = summed[w] ? 1 : 0;
+        p.lo_other[w] = (uint8_t) (summed[w] ? pair_s[w] : cdig[w]);
+        klo += summed[w];
+    }
+    p.n_klo = (uint32_t) klo;
+    int outer[kMaxWires], hi[kMaxWires], n_outer = 0, n_hi = 0;
+    for (int w = 4; w < rL; w++) {
+        if (summed[w]) hi[n_hi++] = w;
+        else outer[n_outer++] = w;
+    }
+    // loop digits of a tile: up to 16 elements per thread and 16 staged sums per thread
+    const int ho = std::min(n_hi, 2);
+    int go = std::min(n_outer, 2 - ho);
+    while (go > 0 && (1 << (2 * (go + nsf))) > (int) kStreamMaxStage) go--;
+    if (n_outer - go > 15 || n_hi - ho > 15) return false;
+    p.go = (uint32_t) go;
+    p.ho = (uint32_t) ho;
+    p.n_items = 1u << (2 * (n_outer - go));
+    p.n_chunks = 1u << (2 * (n_hi - ho));
+    p.n_item_d = (uint32_t) (n_outer - go);
+    p.n_chunk_d = (uint32_t) (n_hi - ho);
+    for (int j = go; j < n_outer; j++) {
+        p.item_lw[j - go] = (uint8_t) outer[j];
+        p.item_cd[j - go] = (uint8_t) cdig[outer[j]];
+    }
+    for (int j = ho; j < n_hi; j++) {
+        p.chunk_lw[j - ho] = (uint8_t) hi[j];
+        p.chunk_sw[j - ho] = (uint8_t) pair_s[hi[j]];
+    }
+    // in-tile wires in ascending order give the tile's local digits
+    bool in_tile[kMaxWires] = {false};
+    for (int w = 0; w < 4; w++) in_tile[w] = true;
+    for (int j = 0; j < go; j++) in_tile[outer[j]] = true;
+    for (int j = 0; j < ho; j++) in_tile[hi[j]] = true;
+    int tpos[kMaxWires], nt = 0;
+    for (int w = 0; w < rL; w++) tpos[w] = in_tile[w] ? nt++ : -1;
+    for (int j = 0; j < go; j++) {
+        p.g_pos[j] = (uint8_t) tpos[outer[j]];
+        p.g_cd[j] = (uint8_t) cdig[outer[j]];
+    }
+    for (int j = 0; j < ho; j++) {
+        p.h_pos[j] = (uint8_t) tpos[hi[j]];
+        p.h_sw[j] = (uint8_t) pair_s[hi[j]];
+    }
+    // bulk copies: runs along the lowest in-tile wires that follow each other from wire 0
+    int prefix = 0;
+    while (prefix < rL && in_tile[prefix]) prefix++;
+    p.run_elems = 1u << (2 * prefix);
+    p.n_runs = 1u << (2 * (nt - prefix));
+    int nr = 0;
+    for (int w = prefix; w < rL; w++)
+        if (in_tile[w]) p.run_lw[nr++] = (uint8_t) w;
+    p.n_run_d = (uint32_t) nr;
+    // outputs of a work item: the C digits of L's free wires 0-3, of the g
+    // digits and of S's free wires, ascending
+    int nd = 0;
+    for (int i = 0; i < d.nFree; i++) {
+        if (cL[i] != kNoWire) {
+            const int w = cL[i];
+            if (w < 4) {
+                p.dout_kind[nd] = 0;
+                p.dout_idx[nd] = (uint8_t) w;
+            } else {
+                int j = 0;
+                while (j < go && outer[j] != w) j++;
+                if (j == go) continue;   // a work-item digit
+                p.dout_kind[nd] = 1;
+                p.dout_idx[nd] = (uint8_t) j;
+            }
+        } else {
+            int j = 0;
+            while (j < nsf && p.sf_w[j] != cS[i]) j++;
+            p.dout_kind[nd] = 2;
+            p.dout_idx[nd] = (uint8_t) j;
+        }
+        p.dout_cd[nd++] = (uint8_t) i;
+    }
+    p.n_dout = (uint32_t) nd;
+    uint32_t off[6];
+    stream_layout(p, off);
+    p.smem_bytes = off[5];
+    return p.smem_bytes <= 200u * 1024u;
+}
+
+cudaError_t launch_stream(StreamStep &p, const StepDesc &d, const float2 *A, const float2 *B, float2 *C,
+                          const StepScaleRef &sc, int *error_flag, cudaStream_t stream) {
+    (void) d;
+    p.L = p.l_is_b ? B : A;
+    p.S = p.l_is_b ? A : B;
+    p.C = C;
+    p.sc = sc;
+    p.error_flag = error_flag;
+    cudaError_t e = stream_attributes();
+    if (e != cudaSuccess) return e;
+    const StreamFn fn = stream_fn(p.nsf);
+    int per_sm = 0, dev = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kStreamThreads, p.smem_bytes);
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const uint32_t grid = std::min<uint32_t>(p.n_items, (uint32_t) (sms * std::max(per_sm, 1)));
+    fn<<<grid, kStreamThreads, p.smem_bytes, stream>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace qtg

@@ -1,0 +1,76 @@
+// Streaming kernel for complex64 contraction steps with one small operand
+// (stream.cu).  These are the large steps of the QAOA light-cone networks
+// under stochastic orderings and of the serving heavy tail: a rank 12-14
+// tensor met by a gate-sized one.  They are bound by HBM bandwidth, so the
+// kernel reads the large operand L once in contiguous runs (TMA bulk copies)
+// and writes the output once in contiguous runs; the small operand S lives in
+// shared memory.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "engine.cuh"
+#include "scale.cuh"
+
+namespace qtg {
+
+// Work decomposition over L's wires (base-4 digits):
+//   wires 0-3            the thread's own digits: thread t of the CTA reads
+//                        element t of every 256-element run (conflict-free)
+//   "outer" free wires   (free wires >= 4) the lowest `go` of them are looped
+//                        over inside a tile (g); the rest number the work items
+//   summed wires >= 4    the lowest `ho` of them are looped over inside a tile
+//                        (h); the rest number the chunks of a work item, whose
+//                        partial sums accumulate in shared memory
+// A tile is (wires 0-3) x g x h: 4^(4 + go + ho) <= kStreamMaxTile elements,
+// copied as runs along L's lowest in-tile wires.  Partial sums are staged per
+// (g, S-free index, thread) and reduced over the summed digits among wires
+// 0-3 when a work item's last chunk is done.
+constexpr int kStreamMaxSmallRank = 6;       // S holds at most 4^6 elements (32 KB)
+constexpr uint32_t kStreamMaxTile = 4096;    // elements of one L tile (32 KB)
+constexpr uint32_t kStreamMaxStage = 16;     // g x S-free outputs a thread stages (256 threads x 16 x 8 B)
+constexpr int kStreamThreads = 256;          // = 4^4: one thread per combination of L's wires 0-3
+constexpr int kStreamMaxLoop = 6;            // digits looped over in a tile or chunk
+
+struct StreamStep {
+    const float2 *L;
+    const float2 *S;
+    float2 *C;
+    StepScaleRef sc;
+    int *error_flag;               // set when a TMA wait timed out (zero on entry)
+    uint32_t n_items;              // work items: combinations of the outer wires not looped in a tile
+    uint32_t n_chunks;             // tiles per work item: combinations of the summed wires >= 4 not in a tile
+    uint32_t run_elems;            // elements of one bulk copy (4^(lowest in-tile wires in a row))
+    uint32_t n_runs;               // bulk copies per tile
+    uint32_t s_elems;              // 4^rank(S)
+    uint32_t nsf;                  // free wires of S (NSF = 4^nsf outputs per thread and g)
+    uint32_t go, ho;               // outer / summed digits looped in a tile
+    uint32_t n_item_d, n_chunk_d;  // digits of the work-item and chunk indices
+    uint32_t n_run_d;              // in-tile digits above the run (bulk-copy index digits)
+    uint32_t n_dout, n_klo;        // output digits of a work item; summed wires among 0-3
+    uint32_t smem_bytes;
+    uint32_t l_is_b;               // the large operand is B (else A)
+    // work item digit j: L wire and C digit
+    uint8_t item_lw[kMaxWires], item_cd[kMaxWires];
+    // chunk digit j: L wire and S wire of the summed pair
+    uint8_t chunk_lw[kMaxWires], chunk_sw[kMaxWires];
+    // g digit j: tile-local digit and C digit; h digit j: tile-local digit and S wire
+    uint8_t g_pos[kStreamMaxLoop], g_cd[kStreamMaxLoop];
+    uint8_t h_pos[kStreamMaxLoop], h_sw[kStreamMaxLoop];
+    // bulk copy index digit j: L wire
+    uint8_t run_lw[kStreamMaxLoop];
+    // wires 0-3 of L: 1 when summed, then the S wire it is summed with (else its C digit)
+    uint8_t lo_summed[4], lo_other[4];
+    // S-free digit j: S wire
+    uint8_t sf_w[kStreamMaxSmallRank];
+    // output digit r of a work item (ascending C digits): its C digit, its kind
+    // (0: one of L's wires 0-3, 1: a g digit, 2: an S-free digit) and that digit's index
+    uint8_t dout_cd[kMaxWires], dout_kind[kMaxWires], dout_idx[kMaxWires];
+};
+
+// Plans the step (false: not a shape this kernel takes).
+bool stream_plan(const StepDesc &d, StreamStep &p);
+// Launches it on L = A or B as stream_plan chose (p.L, p.S, p.C filled here).
+cudaError_t launch_stream(StreamStep &p, const StepDesc &d, const float2 *A, const float2 *B, float2 *C,
+                          const StepScaleRef &sc, int *error_flag, cudaStream_t stream);
+
+}  // namespace qtg

@@ -3,10 +3,10 @@
 ParallelContract, src/ContractionTools.h:219-388, with a fixed seed) reaches a
 qTorch rank-13 or rank-14 intermediate -- 2^26 or 2^28 complex elements, the
 "rank 26-28" of dimension-2 legs.  Such plans exceed the grouped interpreter
-and run step by step; their GEMM-shaped complex64 steps take the tcgen05
-3xTF32 tensor-core GEMM.  FP64 must equal the oracle's replay of the same
-sequence bit for bit; the mixed form must stay within 1e-6 of FP64, on values
-far from zero."""
+and run step by step; their large complex64 steps, a rank 11-14 tensor met by
+a gate-sized one, take the HBM-streaming, tiled or tcgen05 tensor-core
+kernels.  FP64 must equal the oracle's replay of the same sequence bit for
+bit; the mixed form must stay within 1e-6 of FP64, on values far from zero."""
 import pytest
 
 import qtorch_gb300 as qg
@@ -23,14 +23,15 @@ def term(edge):
     return qg.qaoa_term_text(dgf, 2, ANGLES, edge)
 
 
-def test_rank13_term_fp64_bit_exact_and_mixed_on_tensor_cores(ctx):
+def test_rank13_term_fp64_bit_exact_and_mixed_within_tolerance(ctx):
     q, m = term(16)
     plan = qg.Plan(q, m, ordering="stochastic", seed=11, ctx=ctx)
     assert plan.peak_rank == 13
     v64 = plan.execute(qg.FP64)
-    tc0 = ctx.tensor_core_steps
+    tc0, st0 = ctx.tensor_core_steps, ctx.stream_steps
     vmx = plan.execute(qg.MIXED)
     assert ctx.tensor_core_steps > tc0, "no step of the rank-13 term ran on the tensor cores"
+    assert ctx.stream_steps > st0, "no step of the rank-13 term ran on the streaming kernel"
     v_or, flops = port.replay_value(q, m, plan.sequence())
     assert flops == plan.flops
     assert v64 == v_or
