@@ -7,11 +7,14 @@
 //     of a double buffer, so HBM reads of tile i+1 overlap the arithmetic of
 //     tile i;
 //   * thread t owns element t of every 256-element stretch of the tile (L's
-//     wires 0-3), so a warp's loads are consecutive and conflict-free; it
-//     loops over the tile's other digits, multiplies by S (in shared memory)
-//     for every free index of S, and adds into its own staging slots;
-//   * after a work item's last tile, the staged partial sums are reduced over
-//     the summed digits among wires 0-3 and written in C's digit order.
+//     wires 0-3), so a warp's loads are consecutive and conflict-free; its
+//     loop over the tile's other digits is unrolled at compile time (one
+//     instantiation per shape class: free indices of S, looped free and
+//     summed digits), with every element's tile and S offsets precomputed in
+//     registers, and its sums stay in registers across a work item's chunks;
+//   * after a work item's last tile, the summed digits among wires 0-3 are
+//     reduced by warp shuffles (wires 0-1) or through shared memory (wires
+//     2-3), and the sums are written to C.
 //
 // HBM traffic is one read of L and S and one write of C: the step's
 // algorithmic bytes.  The mixed form's per-tensor power-of-two scaling
@@ -70,10 +73,10 @@ __host__ __device__ inline uint32_t round128(uint32_t x) { return (x + 127u) / 1
 // byte offsets of the shared-memory regions (host and device agree)
 __host__ __device__ inline void stream_layout(const StreamStep &p, uint32_t off[6]) {
     const uint32_t tile = 1u << (2 * (4 + p.go + p.ho));
-    const uint32_t stage = (uint32_t) kStreamThreads << (2 * (p.go + p.nsf));
+    const uint32_t stage = p.klo_mode == 2 ? (uint32_t) kStreamThreads << (2 * (p.go + p.nsf)) : 0u;
     off[0] = 0;                                    // tile buffer 0
     off[1] = round128(8u * tile);                  // tile buffer 1
-    off[2] = off[1] + round128(8u * tile);         // staged partial sums
+    off[2] = off[1] + round128(8u * tile);         // staged sums (summed wires 2/3 only)
     off[3] = off[2] + round128(8u * stage);        // S
     off[4] = off[3] + round128(8u * p.s_elems);    // two mbarriers
     off[5] = off[4] + 128u;                        // end
@@ -101,8 +104,20 @@ __device__ __forceinline__ void issue_tile(const StreamStep &p, float2 *dst, uin
     }
 }
 
-template <int NSF>
+// C offset of output (g, f) of a work item, beyond the work item's base and
+// the thread's own free digits among wires 0-3
+__device__ __forceinline__ uint64_t out_offset(const StreamStep &p, uint32_t g, uint32_t f) {
+    uint64_t o = 0;
+    for (uint32_t j = 0; j < p.go; j++) o += (uint64_t) ((g >> (2 * j)) & 3u) << (2 * p.g_cd[j]);
+    for (uint32_t j = 0; j < p.nsf; j++) o += (uint64_t) ((f >> (2 * j)) & 3u) << (2 * p.sf_cd[j]);
+    return o;
+}
+
+// NSF free indices of S, G looped free and H looped summed combinations per
+// tile (E = G H elements per thread and tile)
+template <int NSF, int G, int H>
 __global__ void __launch_bounds__(kStreamThreads, 2) stream_kernel(const __grid_constant__ StreamStep p) {
+    constexpr int E = G * H;
     extern __shared__ __align__(128) unsigned char smem[];
     uint32_t off[6];
     stream_layout(p, off);
@@ -112,13 +127,34 @@ __global__ void __launch_bounds__(kStreamThreads, 2) stream_kernel(const __grid_
     float2 *const S = reinterpret_cast<float2 *>(smem + off[3]);
     uint64_t *const bars = reinterpret_cast<uint64_t *>(smem + off[4]);
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-    const uint32_t G = 1u << (2 * p.go), H = 1u << (2 * p.ho);
 
     for (uint32_t e = tid; e < p.s_elems; e += blockDim.x) S[e] = p.S[e];
-    // this thread's share of S's summed index (its summed digits among wires 0-3)
-    uint32_t s_lo = 0;
-    for (int w = 0; w < 4; w++)
-        if (p.lo_summed[w]) s_lo += ((tid >> (2 * w)) & 3u) << (2 * p.lo_other[w]);
+    // per thread: each element's tile offset and S offset (its summed digits
+    // among wires 0-3 and the h digits), the free-index offsets of S, and the
+    // C offset of its free digits among wires 0-3
+    uint32_t s_lo = 0, c_lo = 0;
+    for (int w = 0; w < 4; w++) {
+        const uint32_t dg = (tid >> (2 * w)) & 3u;
+        if (p.lo_summed[w]) s_lo += dg << (2 * p.lo_other[w]);
+        else c_lo += dg << (2 * p.lo_other[w]);
+    }
+    uint32_t eo[E], so[E];
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+        uint32_t tg = tid;
+        for (uint32_t j = 0; j < p.go; j++) tg += (((uint32_t) g >> (2 * j)) & 3u) << (2 * p.g_pos[j]);
+#pragma unroll
+        for (int h = 0; h < H; h++) {
+            uint32_t th = tg, sh = s_lo;
+            for (uint32_t j = 0; j < p.ho; j++) {
+                const uint32_t dg = ((uint32_t) h >> (2 * j)) & 3u;
+                th += dg << (2 * p.h_pos[j]);
+                sh += dg << (2 * p.h_sw[j]);
+            }
+            eo[g * H + h] = th;
+            so[g * H + h] = sh;
+        }
+    }
     uint32_t sfo[NSF];
 #pragma unroll
     for (int f = 0; f < NSF; f++) {
@@ -141,6 +177,7 @@ __global__ void __launch_bounds__(kStreamThreads, 2) stream_kernel(const __grid_
     uint32_t waits0 = 0, waits1 = 0;
     if (warp == 0 && item < p.n_items) issue_tile(p, tile0, &bars[0], item, 0, lane);
     bool ok = true;
+    float2 acc[G][NSF];
     for (uint32_t it = 0; item < p.n_items; it++) {
         const int buf = (int) (it & 1u);
         // the tile after this one in this CTA's order
@@ -168,71 +205,87 @@ __global__ void __launch_bounds__(kStreamThreads, 2) stream_kernel(const __grid_
         }
         const float2 *T = buf ? tile1 : tile0;
 
-        // S's share of the chunk's summed digits
-        uint32_t s_c = s_lo;
-        for (uint32_t j = 0; j < p.n_chunk_d; j++) s_c += ((chunk >> (2 * j)) & 3u) << (2 * p.chunk_sw[j]);
-        for (uint32_t g = 0; g < G; g++) {
-            uint32_t tg = tid;
-            for (uint32_t j = 0; j < p.go; j++) tg += ((g >> (2 * j)) & 3u) << (2 * p.g_pos[j]);
-            float2 acc[NSF];
+        if (chunk == 0) {
 #pragma unroll
-            for (int f = 0; f < NSF; f++) acc[f] = make_float2(0.f, 0.f);
-            for (uint32_t h = 0; h < H; h++) {
-                uint32_t th = tg, sh = s_c;
-                for (uint32_t j = 0; j < p.ho; j++) {
-                    const uint32_t dg = (h >> (2 * j)) & 3u;
-                    th += dg << (2 * p.h_pos[j]);
-                    sh += dg << (2 * p.h_sw[j]);
-                }
-                const float2 x = T[th];
+            for (int g = 0; g < G; g++)
 #pragma unroll
-                for (int f = 0; f < NSF; f++) cmac(acc[f], x, S[sh + sfo[f]]);
-            }
-            float2 *st = stage + (uint64_t) g * NSF * kStreamThreads + tid;
-#pragma unroll
-            for (int f = 0; f < NSF; f++) {
-                if (chunk == 0) {
-                    st[f * kStreamThreads] = acc[f];
-                } else {
-                    const float2 o = st[f * kStreamThreads];
-                    st[f * kStreamThreads] = make_float2(o.x + acc[f].x, o.y + acc[f].y);
-                }
-            }
+                for (int f = 0; f < NSF; f++) acc[g][f] = make_float2(0.f, 0.f);
         }
+        // S's share of the chunk's summed digits
+        uint32_t s_c = 0;
+        for (uint32_t j = 0; j < p.n_chunk_d; j++) s_c += ((chunk >> (2 * j)) & 3u) << (2 * p.chunk_sw[j]);
+        const float2 *Sc = S + s_c;
+#pragma unroll
+        for (int i = 0; i < E; i++) {
+            const float2 x = T[eo[i]];
+#pragma unroll
+            for (int f = 0; f < NSF; f++) cmac(acc[i / H][f], x, Sc[so[i] + sfo[f]]);
+        }
+
         if (chunk + 1 == p.n_chunks) {
-            __syncthreads();
-            // the work item's outputs in C's digit order: reduce the staged
-            // partial sums over the summed digits among wires 0-3
             uint64_t cbase = 0;
             for (uint32_t j = 0; j < p.n_item_d; j++) cbase += (uint64_t) ((item >> (2 * j)) & 3u) << (2 * p.item_cd[j]);
-            const uint32_t n_out = 1u << (2 * p.n_dout), n_kl = 1u << (2 * p.n_klo);
-            for (uint32_t o = tid; o < n_out; o += blockDim.x) {
-                uint64_t coff = cbase;
-                uint32_t tf = 0, g = 0, f = 0;
-                for (uint32_t r = 0; r < p.n_dout; r++) {
-                    const uint32_t dg = (o >> (2 * r)) & 3u;
-                    coff += (uint64_t) dg << (2 * p.dout_cd[r]);
-                    const uint32_t sh = 2u * p.dout_idx[r];
-                    if (p.dout_kind[r] == 0) tf += dg << sh;
-                    else if (p.dout_kind[r] == 1) g += dg << sh;
-                    else f += dg << sh;
+            if (p.klo_mode == 2) {
+                // summed wires 2/3 span warps: stage, then one thread per output
+#pragma unroll
+                for (int g = 0; g < G; g++)
+#pragma unroll
+                    for (int f = 0; f < NSF; f++) stage[((uint32_t) (g * NSF + f)) * kStreamThreads + tid] = acc[g][f];
+                __syncthreads();
+                const uint32_t n_out = 1u << (2 * p.n_dout), n_kl = 1u << (2 * p.n_klo);
+                for (uint32_t o = tid; o < n_out; o += blockDim.x) {
+                    uint64_t coff = cbase;
+                    uint32_t tf = 0, g = 0, f = 0;
+                    for (uint32_t r = 0; r < p.n_dout; r++) {
+                        const uint32_t dg = (o >> (2 * r)) & 3u;
+                        coff += (uint64_t) dg << (2 * p.dout_cd[r]);
+                        const uint32_t sh = 2u * p.dout_idx[r];
+                        if (p.dout_kind[r] == 0) tf += dg << sh;
+                        else if (p.dout_kind[r] == 1) g += dg << sh;
+                        else f += dg << sh;
+                    }
+                    const float2 *st = stage + ((uint64_t) g * NSF + f) * kStreamThreads;
+                    float vx = 0.f, vy = 0.f;
+                    for (uint32_t kl = 0; kl < n_kl; kl++) {
+                        uint32_t t = tf, q = 0;
+                        for (int w = 0; w < 4; w++)
+                            if (p.lo_summed[w]) {
+                                t += ((kl >> (2 * q)) & 3u) << (2 * w);
+                                q++;
+                            }
+                        const float2 pv = st[t];
+                        vx += pv.x;
+                        vy += pv.y;
+                    }
+                    const float2 v = make_float2(scale_pow2(vx, shift), scale_pow2(vy, shift));
+                    lmax = max(lmax, mag_bits(v));
+                    p.C[coff] = v;
                 }
-                const float2 *st = stage + ((uint64_t) g * NSF + f) * kStreamThreads;
-                float vx = 0.f, vy = 0.f;
-                for (uint32_t kl = 0; kl < n_kl; kl++) {
-                    uint32_t t = tf, q = 0;
-                    for (int w = 0; w < 4; w++)
-                        if (p.lo_summed[w]) {
-                            t += ((kl >> (2 * q)) & 3u) << (2 * w);
-                            q++;
+            } else {
+                // summed wires among 0/1 only: they are lane bits 0-3
+                bool writer = true;
+                for (int w = 0; w < 2; w++) {
+                    if (!p.lo_summed[w]) continue;
+                    writer = writer && ((tid >> (2 * w)) & 3u) == 0;
+#pragma unroll
+                    for (int g = 0; g < G; g++)
+#pragma unroll
+                        for (int f = 0; f < NSF; f++)
+                            for (uint32_t m = 1u << (2 * w); m <= (2u << (2 * w)); m <<= 1) {
+                                acc[g][f].x += __shfl_xor_sync(0xffffffffu, acc[g][f].x, m);
+                                acc[g][f].y += __shfl_xor_sync(0xffffffffu, acc[g][f].y, m);
+                            }
+                }
+                if (writer) {
+#pragma unroll
+                    for (int g = 0; g < G; g++)
+#pragma unroll
+                        for (int f = 0; f < NSF; f++) {
+                            const float2 v = make_float2(scale_pow2(acc[g][f].x, shift), scale_pow2(acc[g][f].y, shift));
+                            lmax = max(lmax, mag_bits(v));
+                            p.C[cbase + c_lo + out_offset(p, (uint32_t) g, (uint32_t) f)] = v;
                         }
-                    const float2 pv = st[t];
-                    vx += pv.x;
-                    vy += pv.y;
                 }
-                const float2 v = make_float2(scale_pow2(vx, shift), scale_pow2(vy, shift));
-                lmax = max(lmax, mag_bits(v));
-                p.C[coff] = v;
             }
         }
         __syncthreads();   // the tile buffer (and the staging, after a write-back) are free again
@@ -255,10 +308,20 @@ __global__ void __launch_bounds__(kStreamThreads, 2) stream_kernel(const __grid_
 
 using StreamFn = void (*)(const StreamStep);
 
-StreamFn stream_fn(uint32_t nsf) {
-    if (nsf == 0) return stream_kernel<1>;
-    if (nsf == 1) return stream_kernel<4>;
-    return stream_kernel<16>;
+// the instantiation of a plan's shape class (G x NSF <= 16, G x H <= 16)
+StreamFn stream_fn(uint32_t nsf, uint32_t go, uint32_t ho) {
+    const uint32_t key = nsf * 9 + go * 3 + ho;
+#define QT_STREAM_CASE(NS, GO, HO) \
+    case (NS) * 9 + (GO) * 3 + (HO): return stream_kernel<1 << (2 * (NS)), 1 << (2 * (GO)), 1 << (2 * (HO))>;
+    switch (key) {
+        QT_STREAM_CASE(0, 0, 0) QT_STREAM_CASE(0, 0, 1) QT_STREAM_CASE(0, 0, 2)
+        QT_STREAM_CASE(0, 1, 0) QT_STREAM_CASE(0, 1, 1) QT_STREAM_CASE(0, 2, 0)
+        QT_STREAM_CASE(1, 0, 0) QT_STREAM_CASE(1, 0, 1) QT_STREAM_CASE(1, 0, 2)
+        QT_STREAM_CASE(1, 1, 0) QT_STREAM_CASE(1, 1, 1)
+        QT_STREAM_CASE(2, 0, 0) QT_STREAM_CASE(2, 0, 1) QT_STREAM_CASE(2, 0, 2)
+    default: return nullptr;
+    }
+#undef QT_STREAM_CASE
 }
 
 std::mutex g_attr_lock;
@@ -272,8 +335,12 @@ cudaError_t stream_attributes() {
     if (dev >= 0 && dev < 64 && g_attr_done[dev]) return cudaSuccess;
     int optin = 0;
     e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    for (uint32_t nsf : {0u, 1u, 2u})
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(stream_fn(nsf), cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    for (uint32_t nsf = 0; nsf <= 2; nsf++)
+        for (uint32_t go = 0; go <= 2; go++)
+            for (uint32_t ho = 0; ho <= 2; ho++) {
+                const StreamFn fn = stream_fn(nsf, go, ho);
+                if (fn && e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            }
     if (e == cudaSuccess && dev >= 0 && dev < 64) g_attr_done[dev] = true;
     return e;
 }
@@ -298,8 +365,12 @@ bool stream_plan(const StepDesc &d, StreamStep &p) {
     }
     int nsf = 0;
     for (int i = 0; i < d.nFree; i++) {
-        if (cL[i] != kNoWire) cdig[cL[i]] = i;
-        else p.sf_w[nsf++] = cS[i];
+        if (cL[i] != kNoWire) {
+            cdig[cL[i]] = i;
+        } else {
+            p.sf_cd[nsf] = (uint8_t) i;
+            p.sf_w[nsf++] = cS[i];
+        }
     }
     if (nsf > 2) return false;   // at most 16 free indices of S per thread
     p.l_is_b = l_is_b;
@@ -313,6 +384,10 @@ bool stream_plan(const StepDesc &d, StreamStep &p) {
         klo += summed[w];
     }
     p.n_klo = (uint32_t) klo;
+    p.klo_mode = klo == 0 ? 0u : (summed[2] || summed[3]) ? 2u : 1u;
+    // a thread's C offset over its free digits among wires 0-3 is 32-bit
+    for (int w = 0; w < 4; w++)
+        if (!summed[w] && cdig[w] >= 16) return false;
     int outer[kMaxWires], hi[kMaxWires], n_outer = 0, n_hi = 0;
     for (int w = 4; w < rL; w++) {
         if (summed[w]) hi[n_hi++] = w;
@@ -389,7 +464,7 @@ bool stream_plan(const StepDesc &d, StreamStep &p) {
     uint32_t off[6];
     stream_layout(p, off);
     p.smem_bytes = off[5];
-    return p.smem_bytes <= 200u * 1024u;
+    return p.smem_bytes <= 200u * 1024u && stream_fn(p.nsf, p.go, p.ho) != nullptr;
 }
 
 cudaError_t launch_stream(StreamStep &p, const StepDesc &d, const float2 *A, const float2 *B, float2 *C,
@@ -402,7 +477,7 @@ cudaError_t launch_stream(StreamStep &p, const StepDesc &d, const float2 *A, con
     p.error_flag = error_flag;
     cudaError_t e = stream_attributes();
     if (e != cudaSuccess) return e;
-    const StreamFn fn = stream_fn(p.nsf);
+    const StreamFn fn = stream_fn(p.nsf, p.go, p.ho);
     int per_sm = 0, dev = 0, sms = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kStreamThreads, p.smem_bytes);
     if (e == cudaSuccess) e = cudaGetDevice(&dev);

@@ -19,12 +19,13 @@ namespace qtg {
 //   "outer" free wires   (free wires >= 4) the lowest `go` of them are looped
 //                        over inside a tile (g); the rest number the work items
 //   summed wires >= 4    the lowest `ho` of them are looped over inside a tile
-//                        (h); the rest number the chunks of a work item, whose
-//                        partial sums accumulate in shared memory
+//                        (h); the rest number the chunks of a work item
 // A tile is (wires 0-3) x g x h: 4^(4 + go + ho) <= kStreamMaxTile elements,
-// copied as runs along L's lowest in-tile wires.  Partial sums are staged per
-// (g, S-free index, thread) and reduced over the summed digits among wires
-// 0-3 when a work item's last chunk is done.
+// copied as runs along L's lowest in-tile wires.  A thread keeps one sum per
+// (g, S-free index) in registers across the chunks of a work item; the summed
+// digits among wires 0-3 are then reduced by warp shuffles (wires 0 and 1
+// lie within a warp) or through shared memory (wires 2 and 3), and the sums
+// are written straight to C.
 constexpr int kStreamMaxSmallRank = 6;       // S holds at most 4^6 elements (32 KB)
 constexpr uint32_t kStreamMaxTile = 4096;    // elements of one L tile (32 KB)
 constexpr uint32_t kStreamMaxStage = 16;     // g x S-free outputs a thread stages (256 threads x 16 x 8 B)
@@ -47,6 +48,7 @@ struct StreamStep {
     uint32_t n_item_d, n_chunk_d;  // digits of the work-item and chunk indices
     uint32_t n_run_d;              // in-tile digits above the run (bulk-copy index digits)
     uint32_t n_dout, n_klo;        // output digits of a work item; summed wires among 0-3
+    uint32_t klo_mode;             // 0: no summed wire among 0-3, 1: only wires 0/1 (shuffles), 2: staging
     uint32_t smem_bytes;
     uint32_t l_is_b;               // the large operand is B (else A)
     // work item digit j: L wire and C digit
@@ -60,8 +62,8 @@ struct StreamStep {
     uint8_t run_lw[kStreamMaxLoop];
     // wires 0-3 of L: 1 when summed, then the S wire it is summed with (else its C digit)
     uint8_t lo_summed[4], lo_other[4];
-    // S-free digit j: S wire
-    uint8_t sf_w[kStreamMaxSmallRank];
+    // S-free digit j: S wire and C digit
+    uint8_t sf_w[kStreamMaxSmallRank], sf_cd[kStreamMaxSmallRank];
     // output digit r of a work item (ascending C digits): its C digit, its kind
     // (0: one of L's wires 0-3, 1: a g digit, 2: an S-free digit) and that digit's index
     uint8_t dout_cd[kMaxWires], dout_kind[kMaxWires], dout_idx[kMaxWires];

@@ -2,8 +2,9 @@
 // host tests: for random contraction steps of the shapes the kernel takes, it
 // asks the library's stream_plan for the tiling and then walks every tile the
 // way the kernel's threads do -- the bulk-copy runs of the large operand, each
-// thread's loop over the tile with its staged partial sums, the reduction over
-// the summed low digits and the write-back in C's digit order -- checking every
+// thread's loop over its elements of the tile with its sums kept across the
+// chunks of a work item, the reduction over the summed digits among wires 0-3
+// (shuffles or staging) and the write-back to C -- checking every
 // index against its buffer, that every output is written exactly once, and
 // every output against a direct evaluation of the contraction.  No GPU.
 //
@@ -87,8 +88,9 @@ static std::string emulate(const StepDesc &d, const StreamStep &p, std::mt19937 
     if (tile_elems > kStreamMaxTile || G * NSF > kStreamMaxStage || p.s_elems != S.size()) return "region sizes";
     if (p.run_elems * p.n_runs != tile_elems || p.run_elems < 256) return "runs";
     std::vector<int> written(nC, 0);
-    std::vector<cf> tile(tile_elems), stage((uint64_t) T * G * NSF);
+    std::vector<cf> tile(tile_elems), acc((uint64_t) T * G * NSF);   // acc[(g * NSF + f) * T + tid]
     for (uint32_t item = 0; item < p.n_items; item++) {
+        std::fill(acc.begin(), acc.end(), cf(0.f, 0.f));
         for (uint32_t chunk = 0; chunk < p.n_chunks; chunk++) {
             // bulk copies
             uint64_t lbase = 0;
@@ -101,19 +103,18 @@ static std::string emulate(const StepDesc &d, const StreamStep &p, std::mt19937 
                 if (off + p.run_elems > L.size()) return "bulk copy beyond L";
                 for (uint32_t e = 0; e < p.run_elems; e++) tile[(uint64_t) r * p.run_elems + e] = L[off + e];
             }
-            // every thread's loop
+            // every thread's unrolled loop over its E = G H elements
+            uint32_t s_c = 0;
+            for (uint32_t j = 0; j < p.n_chunk_d; j++) s_c += ((chunk >> (2 * j)) & 3u) << (2 * p.chunk_sw[j]);
             for (uint32_t tid = 0; tid < T; tid++) {
                 uint32_t s_lo = 0;
                 for (int w = 0; w < 4; w++)
                     if (p.lo_summed[w]) s_lo += ((tid >> (2 * w)) & 3u) << (2 * p.lo_other[w]);
-                uint32_t s_c = s_lo;
-                for (uint32_t j = 0; j < p.n_chunk_d; j++) s_c += ((chunk >> (2 * j)) & 3u) << (2 * p.chunk_sw[j]);
                 for (uint32_t gg = 0; gg < G; gg++) {
                     uint32_t tg = tid;
                     for (uint32_t j = 0; j < p.go; j++) tg += ((gg >> (2 * j)) & 3u) << (2 * p.g_pos[j]);
-                    std::vector<cf> acc(NSF, cf(0.f, 0.f));
                     for (uint32_t h = 0; h < H; h++) {
-                        uint32_t th = tg, sh = s_c;
+                        uint32_t th = tg, sh = s_lo;
                         for (uint32_t j = 0; j < p.ho; j++) {
                             const uint32_t dg = (h >> (2 * j)) & 3u;
                             th += dg << (2 * p.h_pos[j]);
@@ -123,47 +124,79 @@ static std::string emulate(const StepDesc &d, const StreamStep &p, std::mt19937 
                         for (uint32_t f = 0; f < NSF; f++) {
                             uint32_t so = 0;
                             for (uint32_t j = 0; j < p.nsf; j++) so += ((f >> (2 * j)) & 3u) << (2 * p.sf_w[j]);
-                            if (sh + so >= S.size()) return "small operand index";
-                            acc[f] += tile[th] * S[sh + so];
+                            if (s_c + sh + so >= S.size()) return "small operand index";
+                            acc[((uint64_t) gg * NSF + f) * T + tid] += tile[th] * S[s_c + sh + so];
                         }
-                    }
-                    for (uint32_t f = 0; f < NSF; f++) {
-                        const uint64_t si = ((uint64_t) gg * NSF + f) * T + tid;
-                        stage[si] = chunk == 0 ? acc[f] : stage[si] + acc[f];
                     }
                 }
             }
         }
-        // reduction and write-back
         uint64_t cbase = 0;
         for (uint32_t j = 0; j < p.n_item_d; j++) cbase += (uint64_t) ((item >> (2 * j)) & 3u) << (2 * p.item_cd[j]);
-        const uint32_t n_out = 1u << (2 * p.n_dout), n_kl = 1u << (2 * p.n_klo);
-        for (uint32_t o = 0; o < n_out; o++) {
-            uint64_t coff = cbase;
-            uint32_t tf = 0, gg = 0, f = 0;
-            for (uint32_t r = 0; r < p.n_dout; r++) {
-                const uint32_t dg = (o >> (2 * r)) & 3u;
-                coff += (uint64_t) dg << (2 * p.dout_cd[r]);
-                const uint32_t sh = 2u * p.dout_idx[r];
-                if (p.dout_kind[r] == 0) tf += dg << sh;
-                else if (p.dout_kind[r] == 1) gg += dg << sh;
-                else f += dg << sh;
+        if (p.klo_mode == 2) {
+            // staged: one thread per output, decoded from C's digit order
+            const uint32_t n_out = 1u << (2 * p.n_dout), n_kl = 1u << (2 * p.n_klo);
+            for (uint32_t o = 0; o < n_out; o++) {
+                uint64_t coff = cbase;
+                uint32_t tf = 0, gg = 0, f = 0;
+                for (uint32_t r = 0; r < p.n_dout; r++) {
+                    const uint32_t dg = (o >> (2 * r)) & 3u;
+                    coff += (uint64_t) dg << (2 * p.dout_cd[r]);
+                    const uint32_t sh = 2u * p.dout_idx[r];
+                    if (p.dout_kind[r] == 0) tf += dg << sh;
+                    else if (p.dout_kind[r] == 1) gg += dg << sh;
+                    else f += dg << sh;
+                }
+                if (gg >= G || f >= NSF || tf >= T) return "output decode";
+                cf v(0.f, 0.f);
+                for (uint32_t kl = 0; kl < n_kl; kl++) {
+                    uint32_t t = tf, q = 0;
+                    for (int w = 0; w < 4; w++)
+                        if (p.lo_summed[w]) {
+                            t += ((kl >> (2 * q)) & 3u) << (2 * w);
+                            q++;
+                        }
+                    if (t >= T) return "staging index";
+                    v += acc[((uint64_t) gg * NSF + f) * T + t];
+                }
+                if (coff >= nC) return "C index";
+                written[coff]++;
+                C[coff] = v;
             }
-            if (gg >= G || f >= NSF || tf >= T) return "output decode";
-            cf v(0.f, 0.f);
-            for (uint32_t kl = 0; kl < n_kl; kl++) {
-                uint32_t t = tf, q = 0;
-                for (int w = 0; w < 4; w++)
-                    if (p.lo_summed[w]) {
-                        t += ((kl >> (2 * q)) & 3u) << (2 * w);
-                        q++;
+        } else {
+            // shuffles over the summed digits among wires 0/1 (lane bits 0-3):
+            // the lanes whose summed digits are 0 write their sums directly
+            if (p.klo_mode == 1 && (p.lo_summed[2] || p.lo_summed[3])) return "shuffle mode with wires 2/3";
+            for (uint32_t tid = 0; tid < T; tid++) {
+                bool writer = true;
+                uint32_t c_lo = 0;
+                for (int w = 0; w < 4; w++) {
+                    const uint32_t dg = (tid >> (2 * w)) & 3u;
+                    if (p.lo_summed[w]) writer = writer && dg == 0;
+                    else c_lo += dg << (2 * p.lo_other[w]);
+                }
+                if (!writer) continue;
+                const uint32_t n_kl = 1u << (2 * p.n_klo);
+                for (uint32_t gg = 0; gg < G; gg++)
+                    for (uint32_t f = 0; f < NSF; f++) {
+                        cf v(0.f, 0.f);
+                        for (uint32_t kl = 0; kl < n_kl; kl++) {
+                            uint32_t t = tid, q = 0;
+                            for (int w = 0; w < 2; w++)
+                                if (p.lo_summed[w]) {
+                                    t ^= ((kl >> (2 * q)) & 3u) << (2 * w);
+                                    q++;
+                                }
+                            v += acc[((uint64_t) gg * NSF + f) * T + t];
+                        }
+                        uint64_t coff = cbase + c_lo;
+                        for (uint32_t j = 0; j < p.go; j++) coff += (uint64_t) ((gg >> (2 * j)) & 3u) << (2 * p.g_cd[j]);
+                        for (uint32_t j = 0; j < p.nsf; j++) coff += (uint64_t) ((f >> (2 * j)) & 3u) << (2 * p.sf_cd[j]);
+                        if (coff >= nC) return "C index";
+                        written[coff]++;
+                        C[coff] = v;
                     }
-                if (t >= T) return "staging index";
-                v += stage[((uint64_t) gg * NSF + f) * T + t];
             }
-            if (coff >= nC) return "C index";
-            written[coff]++;
-            C[coff] = v;
         }
     }
     for (uint64_t c = 0; c < nC; c++)
