@@ -2,10 +2,12 @@
 // stream.h).  One persistent CTA of 256 threads loops over tiles of the large
 // operand L:
 //
-//   * warp 0 issues the next tile's TMA bulk copies (cp.async.bulk, one per
-//     contiguous run, completion counted on an mbarrier) into the other half
-//     of a double buffer, so HBM reads of tile i+1 overlap the arithmetic of
-//     tile i;
+//   * a producer warp streams the tiles into a ring of kStreamStages shared-
+//     memory stages with TMA bulk copies (cp.async.bulk, one per contiguous
+//     run, completion counted on the stage's "full" mbarrier); the eight
+//     consumer warps release a stage on its "empty" mbarrier once they have
+//     read it, so no block-wide barrier is needed in the steady state and up
+//     to kStreamStages tiles are in flight per CTA;
 //   * thread t owns element t of every 256-element stretch of the tile (L's
 //     wires 0-3), so a warp's loads are consecutive and conflict-free; its
 //     loop over the tile's other digits is unrolled at compile time (one
@@ -19,8 +21,8 @@
 // HBM traffic is one read of L and S and one write of C: the step's
 // algorithmic bytes.  The mixed form's per-tensor power-of-two scaling
 // (scale.cuh) is applied to every stored value.  Every mbarrier wait is
-// bounded; on a timeout the CTA waits (bounded) for its copies in flight,
-// raises the error flag and leaves.
+// bounded; after a timeout the warps stop, the CTA waits (bounded) for the
+// copies it issued, raises the error flag and leaves.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,12 +38,16 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ void mbar_init1(uint32_t bar) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
 }
 
 __device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 // at most 2^22 polls (tens of milliseconds with the back-off), then false
@@ -71,18 +77,17 @@ __device__ __forceinline__ void cmac(float2 &c, float2 a, float2 b) {
 __host__ __device__ inline uint32_t round128(uint32_t x) { return (x + 127u) / 128u * 128u; }
 
 // byte offsets of the shared-memory regions (host and device agree)
-__host__ __device__ inline void stream_layout(const StreamStep &p, uint32_t off[6]) {
+__host__ __device__ inline void stream_layout(const StreamStep &p, uint32_t off[5]) {
     const uint32_t tile = 1u << (2 * (4 + p.go + p.ho));
     const uint32_t stage = p.klo_mode == 2 ? (uint32_t) kStreamThreads << (2 * (p.go + p.nsf)) : 0u;
-    off[0] = 0;                                    // tile buffer 0
-    off[1] = round128(8u * tile);                  // tile buffer 1
-    off[2] = off[1] + round128(8u * tile);         // staged sums (summed wires 2/3 only)
-    off[3] = off[2] + round128(8u * stage);        // S
-    off[4] = off[3] + round128(8u * p.s_elems);    // two mbarriers
-    off[5] = off[4] + 128u;                        // end
+    off[0] = 0;                                                  // kStreamStages tile buffers
+    off[1] = kStreamStages * round128(8u * tile);                // staged sums (summed wires 2/3 only)
+    off[2] = off[1] + round128(8u * stage);                      // S
+    off[3] = off[2] + round128(8u * p.s_elems);                  // full[stages], empty[stages], issued count
+    off[4] = off[3] + round128(16u * kStreamStages + 8u);        // end
 }
 
-// warp 0: the bulk copies of (item, chunk) into tile buffer `dst`
+// producer warp: the bulk copies of (item, chunk) into tile buffer `dst`
 __device__ __forceinline__ void issue_tile(const StreamStep &p, float2 *dst, uint64_t *bar_ptr, uint32_t item,
                                            uint32_t chunk, uint32_t lane) {
     uint64_t lbase = 0;
@@ -114,126 +119,135 @@ __device__ __forceinline__ uint64_t out_offset(const StreamStep &p, uint32_t g, 
 }
 
 // NSF free indices of S, G looped free and H looped summed combinations per
-// tile (E = G H elements per thread and tile)
+// tile (E = G H elements per consumer thread and tile)
+// register-heavy classes (sums plus per-element offsets >= 64 registers)
+// run one CTA per SM instead of spilling at two
 template <int NSF, int G, int H>
-__global__ void __launch_bounds__(kStreamThreads, 2) stream_kernel(const __grid_constant__ StreamStep p) {
+constexpr int stream_min_ctas() { return 2 * NSF * G + 2 * G * H >= 64 ? 1 : 2; }
+
+template <int NSF, int G, int H>
+__global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
+    stream_kernel(const __grid_constant__ StreamStep p) {
     constexpr int E = G * H;
+    constexpr int NS = kStreamStages;
     extern __shared__ __align__(128) unsigned char smem[];
-    uint32_t off[6];
+    uint32_t off[5];
     stream_layout(p, off);
-    float2 *const tile0 = reinterpret_cast<float2 *>(smem + off[0]);
-    float2 *const tile1 = reinterpret_cast<float2 *>(smem + off[1]);
-    float2 *const stage = reinterpret_cast<float2 *>(smem + off[2]);
-    float2 *const S = reinterpret_cast<float2 *>(smem + off[3]);
-    uint64_t *const bars = reinterpret_cast<uint64_t *>(smem + off[4]);
+    const uint32_t tile_elems = 1u << (2 * (4 + p.go + p.ho));
+    const uint32_t tile_stride = round128(8u * tile_elems) / 8u;
+    float2 *const tiles = reinterpret_cast<float2 *>(smem + off[0]);
+    float2 *const stage = reinterpret_cast<float2 *>(smem + off[1]);
+    float2 *const S = reinterpret_cast<float2 *>(smem + off[2]);
+    uint64_t *const full = reinterpret_cast<uint64_t *>(smem + off[3]);
+    uint64_t *const empty = full + NS;
+    uint32_t *const issued_slot = reinterpret_cast<uint32_t *>(empty + NS);
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
 
     for (uint32_t e = tid; e < p.s_elems; e += blockDim.x) S[e] = p.S[e];
-    // per thread: each element's tile offset and S offset (its summed digits
-    // among wires 0-3 and the h digits), the free-index offsets of S, and the
-    // C offset of its free digits among wires 0-3
-    uint32_t s_lo = 0, c_lo = 0;
-    for (int w = 0; w < 4; w++) {
-        const uint32_t dg = (tid >> (2 * w)) & 3u;
-        if (p.lo_summed[w]) s_lo += dg << (2 * p.lo_other[w]);
-        else c_lo += dg << (2 * p.lo_other[w]);
-    }
-    uint32_t eo[E], so[E];
-#pragma unroll
-    for (int g = 0; g < G; g++) {
-        uint32_t tg = tid;
-        for (uint32_t j = 0; j < p.go; j++) tg += (((uint32_t) g >> (2 * j)) & 3u) << (2 * p.g_pos[j]);
-#pragma unroll
-        for (int h = 0; h < H; h++) {
-            uint32_t th = tg, sh = s_lo;
-            for (uint32_t j = 0; j < p.ho; j++) {
-                const uint32_t dg = ((uint32_t) h >> (2 * j)) & 3u;
-                th += dg << (2 * p.h_pos[j]);
-                sh += dg << (2 * p.h_sw[j]);
-            }
-            eo[g * H + h] = th;
-            so[g * H + h] = sh;
-        }
-    }
-    uint32_t sfo[NSF];
-#pragma unroll
-    for (int f = 0; f < NSF; f++) {
-        uint32_t o = 0;
-        for (uint32_t j = 0; j < p.nsf; j++) o += (((uint32_t) f >> (2 * j)) & 3u) << (2 * p.sf_w[j]);
-        sfo[f] = o;
-    }
     if (tid == 0) {
-        mbar_init1(smem_u32(&bars[0]));
-        mbar_init1(smem_u32(&bars[1]));
+        for (int s = 0; s < NS; s++) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), kStreamConsumerWarps);
+        }
+        *issued_slot = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
 
+    // this CTA's tiles: work items blockIdx.x, + gridDim.x, ..., each in n_chunks chunks
+    const uint32_t my_items = blockIdx.x < p.n_items ? (p.n_items - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const uint32_t n_t = my_items * p.n_chunks;
     const int shift = scale_shift(p.sc);
     uint32_t lmax = 0;
-    uint32_t item = blockIdx.x, chunk = 0;
-    // per buffer: copies issued and not yet waited for, phases completed
-    bool pend0 = item < p.n_items, pend1 = false;
-    uint32_t waits0 = 0, waits1 = 0;
-    if (warp == 0 && item < p.n_items) issue_tile(p, tile0, &bars[0], item, 0, lane);
     bool ok = true;
-    float2 acc[G][NSF];
-    for (uint32_t it = 0; item < p.n_items; it++) {
-        const int buf = (int) (it & 1u);
-        // the tile after this one in this CTA's order
-        uint32_t n_item = item, n_chunk = chunk + 1;
-        if (n_chunk == p.n_chunks) {
-            n_chunk = 0;
-            n_item = item + gridDim.x;
-        }
-        if (n_item < p.n_items) {
-            if (warp == 0) issue_tile(p, buf ? tile0 : tile1, &bars[buf ^ 1], n_item, n_chunk, lane);
-            if (buf) pend0 = true;
-            else pend1 = true;
-        }
-        const bool got = mbar_wait(smem_u32(&bars[buf]), (buf ? waits1 : waits0) & 1u);
-        if (!__syncthreads_and(got)) {
-            ok = false;
-            break;
-        }
-        if (buf) {
-            waits1++;
-            pend1 = false;
-        } else {
-            waits0++;
-            pend0 = false;
-        }
-        const float2 *T = buf ? tile1 : tile0;
 
-        if (chunk == 0) {
-#pragma unroll
-            for (int g = 0; g < G; g++)
-#pragma unroll
-                for (int f = 0; f < NSF; f++) acc[g][f] = make_float2(0.f, 0.f);
+    if (warp == kStreamConsumerWarps) {
+        // producer: fill stage t % NS once its previous tile has been released
+        uint32_t t = 0;
+        for (; t < n_t; t++) {
+            const uint32_t s = t % NS;
+            if (t >= (uint32_t) NS && !mbar_wait(smem_u32(&empty[s]), ((t / NS) - 1) & 1u)) {
+                ok = false;
+                break;
+            }
+            const uint32_t item = blockIdx.x + (t / p.n_chunks) * gridDim.x, chunk = t % p.n_chunks;
+            issue_tile(p, tiles + (uint64_t) s * tile_stride, &full[s], item, chunk, lane);
         }
-        // S's share of the chunk's summed digits
-        uint32_t s_c = 0;
-        for (uint32_t j = 0; j < p.n_chunk_d; j++) s_c += ((chunk >> (2 * j)) & 3u) << (2 * p.chunk_sw[j]);
-        const float2 *Sc = S + s_c;
-#pragma unroll
-        for (int i = 0; i < E; i++) {
-            const float2 x = T[eo[i]];
-#pragma unroll
-            for (int f = 0; f < NSF; f++) cmac(acc[i / H][f], x, Sc[so[i] + sfo[f]]);
+        if (lane == 0) *issued_slot = t;
+    } else {
+        // consumers: thread tid owns element tid of every 256-element stretch
+        uint32_t s_lo = 0, c_lo = 0;
+        for (int w = 0; w < 4; w++) {
+            const uint32_t dg = (tid >> (2 * w)) & 3u;
+            if (p.lo_summed[w]) s_lo += dg << (2 * p.lo_other[w]);
+            else c_lo += dg << (2 * p.lo_other[w]);
         }
+        // each element's tile offset and S offset (its summed digits among
+        // wires 0-3 and the h digits), and the free-index offsets of S
+        uint32_t eo[E], so[E];
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            uint32_t tg = tid;
+            for (uint32_t j = 0; j < p.go; j++) tg += (((uint32_t) g >> (2 * j)) & 3u) << (2 * p.g_pos[j]);
+#pragma unroll
+            for (int h = 0; h < H; h++) {
+                uint32_t th = tg, sh = s_lo;
+                for (uint32_t j = 0; j < p.ho; j++) {
+                    const uint32_t dg = ((uint32_t) h >> (2 * j)) & 3u;
+                    th += dg << (2 * p.h_pos[j]);
+                    sh += dg << (2 * p.h_sw[j]);
+                }
+                eo[g * H + h] = th;
+                so[g * H + h] = sh;
+            }
+        }
+        uint32_t sfo[NSF];
+#pragma unroll
+        for (int f = 0; f < NSF; f++) {
+            uint32_t o = 0;
+            for (uint32_t j = 0; j < p.nsf; j++) o += (((uint32_t) f >> (2 * j)) & 3u) << (2 * p.sf_w[j]);
+            sfo[f] = o;
+        }
+        float2 acc[G][NSF];
+        for (uint32_t t = 0; t < n_t; t++) {
+            const uint32_t s = t % NS;
+            const uint32_t item = blockIdx.x + (t / p.n_chunks) * gridDim.x, chunk = t % p.n_chunks;
+            if (!mbar_wait(smem_u32(&full[s]), (t / NS) & 1u)) {
+                ok = false;
+                break;
+            }
+            const float2 *T = tiles + (uint64_t) s * tile_stride;
+            if (chunk == 0) {
+#pragma unroll
+                for (int g = 0; g < G; g++)
+#pragma unroll
+                    for (int f = 0; f < NSF; f++) acc[g][f] = make_float2(0.f, 0.f);
+            }
+            // S's share of the chunk's summed digits
+            uint32_t s_c = 0;
+            for (uint32_t j = 0; j < p.n_chunk_d; j++) s_c += ((chunk >> (2 * j)) & 3u) << (2 * p.chunk_sw[j]);
+            const float2 *Sc = S + s_c;
+#pragma unroll
+            for (int i = 0; i < E; i++) {
+                const float2 x = T[eo[i]];
+#pragma unroll
+                for (int f = 0; f < NSF; f++) cmac(acc[i / H][f], x, Sc[so[i] + sfo[f]]);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&empty[s]));   // this warp is done with the stage
 
-        if (chunk + 1 == p.n_chunks) {
+            if (chunk + 1 < p.n_chunks) continue;
             uint64_t cbase = 0;
             for (uint32_t j = 0; j < p.n_item_d; j++) cbase += (uint64_t) ((item >> (2 * j)) & 3u) << (2 * p.item_cd[j]);
             if (p.klo_mode == 2) {
-                // summed wires 2/3 span warps: stage, then one thread per output
+                // summed wires 2/3 span warps: stage (consumers only), then one thread per output
 #pragma unroll
                 for (int g = 0; g < G; g++)
 #pragma unroll
                     for (int f = 0; f < NSF; f++) stage[((uint32_t) (g * NSF + f)) * kStreamThreads + tid] = acc[g][f];
-                __syncthreads();
+                asm volatile("bar.sync 1, %0;" ::"r"(kStreamThreads) : "memory");
                 const uint32_t n_out = 1u << (2 * p.n_dout), n_kl = 1u << (2 * p.n_klo);
-                for (uint32_t o = tid; o < n_out; o += blockDim.x) {
+                for (uint32_t o = tid; o < n_out; o += kStreamThreads) {
                     uint64_t coff = cbase;
                     uint32_t tf = 0, g = 0, f = 0;
                     for (uint32_t r = 0; r < p.n_dout; r++) {
@@ -247,13 +261,13 @@ __global__ void __launch_bounds__(kStreamThreads, 2) stream_kernel(const __grid_
                     const float2 *st = stage + ((uint64_t) g * NSF + f) * kStreamThreads;
                     float vx = 0.f, vy = 0.f;
                     for (uint32_t kl = 0; kl < n_kl; kl++) {
-                        uint32_t t = tf, q = 0;
+                        uint32_t tt = tf, q = 0;
                         for (int w = 0; w < 4; w++)
                             if (p.lo_summed[w]) {
-                                t += ((kl >> (2 * q)) & 3u) << (2 * w);
+                                tt += ((kl >> (2 * q)) & 3u) << (2 * w);
                                 q++;
                             }
-                        const float2 pv = st[t];
+                        const float2 pv = st[tt];
                         vx += pv.x;
                         vy += pv.y;
                     }
@@ -261,6 +275,7 @@ __global__ void __launch_bounds__(kStreamThreads, 2) stream_kernel(const __grid_
                     lmax = max(lmax, mag_bits(v));
                     p.C[coff] = v;
                 }
+                asm volatile("bar.sync 1, %0;" ::"r"(kStreamThreads) : "memory");   // staging free again
             } else {
                 // summed wires among 0/1 only: they are lane bits 0-3
                 bool writer = true;
@@ -288,20 +303,18 @@ __global__ void __launch_bounds__(kStreamThreads, 2) stream_kernel(const __grid_
                 }
             }
         }
-        __syncthreads();   // the tile buffer (and the staging, after a write-back) are free again
-        if (++chunk == p.n_chunks) {
-            chunk = 0;
-            item += gridDim.x;
-        }
     }
-    if (!ok) {
-        // copies still in flight land before the CTA leaves (bounded waits)
-        if (tid == 0) {
-            if (pend0) mbar_wait(smem_u32(&bars[0]), waits0 & 1u);
-            if (pend1) mbar_wait(smem_u32(&bars[1]), waits1 & 1u);
-            atomicExch(p.error_flag, 1);
-        }
-        __syncthreads();
+    // every wait above is bounded, so every thread gets here
+    ok = __syncthreads_and(ok) != 0;
+    if (!ok && tid == 0) {
+        // the last copy issued into each stage lands before the CTA leaves
+        const uint32_t issued = *issued_slot;
+        for (uint32_t s = 0; s < (uint32_t) NS; s++)
+            if (issued > s) {
+                const uint32_t last = s + ((issued - 1 - s) / NS) * NS;
+                mbar_wait(smem_u32(&full[s]), (last / NS) & 1u);
+            }
+        atomicExch(p.error_flag, 1);
     }
     scale_note(p.sc, lmax, shift, blockIdx.x == 0);
 }
@@ -461,9 +474,9 @@ bool stream_plan(const StepDesc &d, StreamStep &p) {
         p.dout_cd[nd++] = (uint8_t) i;
     }
     p.n_dout = (uint32_t) nd;
-    uint32_t off[6];
+    uint32_t off[5];
     stream_layout(p, off);
-    p.smem_bytes = off[5];
+    p.smem_bytes = off[4];
     return p.smem_bytes <= 200u * 1024u && stream_fn(p.nsf, p.go, p.ho) != nullptr;
 }
 
@@ -479,12 +492,12 @@ cudaError_t launch_stream(StreamStep &p, const StepDesc &d, const float2 *A, con
     if (e != cudaSuccess) return e;
     const StreamFn fn = stream_fn(p.nsf, p.go, p.ho);
     int per_sm = 0, dev = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kStreamThreads, p.smem_bytes);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kStreamBlock, p.smem_bytes);
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     const uint32_t grid = std::min<uint32_t>(p.n_items, (uint32_t) (sms * std::max(per_sm, 1)));
-    fn<<<grid, kStreamThreads, p.smem_bytes, stream>>>(p);
+    fn<<<grid, kStreamBlock, p.smem_bytes, stream>>>(p);
     return cudaGetLastError();
 }
 

@@ -29,7 +29,10 @@ namespace qtg {
 constexpr int kStreamMaxSmallRank = 6;       // S holds at most 4^6 elements (32 KB)
 constexpr uint32_t kStreamMaxTile = 4096;    // elements of one L tile (32 KB)
 constexpr uint32_t kStreamMaxStage = 16;     // g x S-free outputs a thread stages (256 threads x 16 x 8 B)
-constexpr int kStreamThreads = 256;          // = 4^4: one thread per combination of L's wires 0-3
+constexpr int kStreamThreads = 256;          // = 4^4 consumer threads: one per combination of L's wires 0-3
+constexpr int kStreamConsumerWarps = kStreamThreads / 32;
+constexpr int kStreamBlock = kStreamThreads + 32;   // the consumers and one producer warp
+constexpr int kStreamStages = 3;             // tiles in flight per CTA
 constexpr int kStreamMaxLoop = 6;            // digits looped over in a tile or chunk
 
 struct StreamStep {
