@@ -120,10 +120,10 @@ __device__ __forceinline__ uint64_t out_offset(const StreamStep &p, uint32_t g, 
 
 // NSF free indices of S, G looped free and H looped summed combinations per
 // tile (E = G H elements per consumer thread and tile)
-// register-heavy classes (sums plus per-element offsets >= 64 registers)
-// run one CTA per SM instead of spilling at two
+// the register-heaviest classes (16 sums per thread over 4 or 16 summed
+// combinations) run one CTA per SM instead of spilling at two
 template <int NSF, int G, int H>
-constexpr int stream_min_ctas() { return 2 * NSF * G + 2 * G * H >= 64 ? 1 : 2; }
+constexpr int stream_min_ctas() { return NSF * G >= 16 && H >= 4 ? 1 : 2; }
 
 template <int NSF, int G, int H>
 __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
@@ -182,21 +182,24 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
             if (p.lo_summed[w]) s_lo += dg << (2 * p.lo_other[w]);
             else c_lo += dg << (2 * p.lo_other[w]);
         }
-        // each element's tile offset and S offset (its summed digits among
-        // wires 0-3 and the h digits), and the free-index offsets of S
+        // each element's tile offset and S offset beyond the thread's own
+        // (the g and h digits), and the free-index offsets of S: the same for
+        // every thread of the CTA, so they stay out of the per-thread registers
         uint32_t eo[E], so[E];
 #pragma unroll
         for (int g = 0; g < G; g++) {
-            uint32_t tg = tid;
-            for (uint32_t j = 0; j < p.go; j++) tg += (((uint32_t) g >> (2 * j)) & 3u) << (2 * p.g_pos[j]);
+            uint32_t tg = 0;
+            if (G > 1)
+                for (uint32_t j = 0; j < p.go; j++) tg += (((uint32_t) g >> (2 * j)) & 3u) << (2 * p.g_pos[j]);
 #pragma unroll
             for (int h = 0; h < H; h++) {
-                uint32_t th = tg, sh = s_lo;
-                for (uint32_t j = 0; j < p.ho; j++) {
-                    const uint32_t dg = ((uint32_t) h >> (2 * j)) & 3u;
-                    th += dg << (2 * p.h_pos[j]);
-                    sh += dg << (2 * p.h_sw[j]);
-                }
+                uint32_t th = tg, sh = 0;
+                if (H > 1)
+                    for (uint32_t j = 0; j < p.ho; j++) {
+                        const uint32_t dg = ((uint32_t) h >> (2 * j)) & 3u;
+                        th += dg << (2 * p.h_pos[j]);
+                        sh += dg << (2 * p.h_sw[j]);
+                    }
                 eo[g * H + h] = th;
                 so[g * H + h] = sh;
             }
@@ -205,7 +208,8 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
 #pragma unroll
         for (int f = 0; f < NSF; f++) {
             uint32_t o = 0;
-            for (uint32_t j = 0; j < p.nsf; j++) o += (((uint32_t) f >> (2 * j)) & 3u) << (2 * p.sf_w[j]);
+            if (NSF > 1)
+                for (uint32_t j = 0; j < p.nsf; j++) o += (((uint32_t) f >> (2 * j)) & 3u) << (2 * p.sf_w[j]);
             sfo[f] = o;
         }
         float2 acc[G][NSF];
@@ -216,7 +220,7 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
                 ok = false;
                 break;
             }
-            const float2 *T = tiles + (uint64_t) s * tile_stride;
+            const float2 *T = tiles + (uint64_t) s * tile_stride + tid;
             if (chunk == 0) {
 #pragma unroll
                 for (int g = 0; g < G; g++)
@@ -226,7 +230,7 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
             // S's share of the chunk's summed digits
             uint32_t s_c = 0;
             for (uint32_t j = 0; j < p.n_chunk_d; j++) s_c += ((chunk >> (2 * j)) & 3u) << (2 * p.chunk_sw[j]);
-            const float2 *Sc = S + s_c;
+            const float2 *Sc = S + s_c + s_lo;
 #pragma unroll
             for (int i = 0; i < E; i++) {
                 const float2 x = T[eo[i]];
