@@ -83,8 +83,9 @@ __host__ __device__ inline void stream_layout(const StreamStep &p, uint32_t off[
     off[0] = 0;                                                  // kStreamStages tile buffers
     off[1] = kStreamStages * round128(8u * tile);                // staged sums (summed wires 2/3 only)
     off[2] = off[1] + round128(8u * stage);                      // S
-    off[3] = off[2] + round128(8u * p.s_elems);                  // full[stages], empty[stages], issued count
-    off[4] = off[3] + round128(16u * kStreamStages + 8u);        // end
+    off[3] = off[2] + round128(8u * p.s_elems);                  // full[stages], empty[stages], issued count,
+                                                                 // C offsets of a thread's outputs (g, f)
+    off[4] = off[3] + round128(16u * kStreamStages + 8u + 8u * kStreamMaxStage);   // end
 }
 
 // producer warp: the bulk copies of (item, chunk) into tile buffer `dst`
@@ -141,9 +142,11 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
     uint64_t *const full = reinterpret_cast<uint64_t *>(smem + off[3]);
     uint64_t *const empty = full + NS;
     uint32_t *const issued_slot = reinterpret_cast<uint32_t *>(empty + NS);
+    uint64_t *const out_off = reinterpret_cast<uint64_t *>(empty + NS + 1);   // [G * NSF]
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
 
     for (uint32_t e = tid; e < p.s_elems; e += blockDim.x) S[e] = p.S[e];
+    if (tid < (uint32_t) (G * NSF)) out_off[tid] = out_offset(p, tid / NSF, tid % NSF);
     if (tid == 0) {
         for (int s = 0; s < NS; s++) {
             mbar_init(smem_u32(&full[s]), 1);
@@ -281,29 +284,55 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
                 }
                 asm volatile("bar.sync 1, %0;" ::"r"(kStreamThreads) : "memory");   // staging free again
             } else {
-                // summed wires among 0/1 only: they are lane bits 0-3
+                // Summed wires among 0/1 only: lane bits 0-3.  A butterfly
+                // reduce-scatter over those bits halves the sums a lane keeps at
+                // every step (one shuffle per sum handed over), so the lanes
+                // sharing a sum end up each holding a different part of the
+                // work item's outputs and all of them store; bits beyond
+                // log2(G NSF) finish as an all-reduce, the lanes whose summed
+                // digits are 0 storing.
+                constexpr int M = G * NSF;
+                constexpr int LM = M >= 16 ? 4 : M >= 4 ? 2 : 0;   // log2(M)
+                float2 *flat = &acc[0][0];
+                // the summed lane bits are consecutive: 0-1, 2-3 or 0-3
+                const uint32_t b0 = p.lo_summed[0] ? 0u : 2u;
+                const uint32_t nb = 2u * (p.lo_summed[0] + p.lo_summed[1]);
+                uint32_t base = 0;
+#pragma unroll
+                for (int k = 0; k < LM; k++) {
+                    if ((uint32_t) k >= nb) break;
+                    const uint32_t mask = 1u << (b0 + (uint32_t) k);
+                    const bool hi = (tid & mask) != 0;
+                    const int half = M >> (k + 1);
+#pragma unroll
+                    for (int i = 0; i < M / 2; i++) {
+                        if (i >= half) break;
+                        const float2 a = flat[i], c = flat[i + half];
+                        const float2 send = hi ? a : c;
+                        float2 keep = hi ? c : a;
+                        keep.x += __shfl_xor_sync(0xffffffffu, send.x, mask);
+                        keep.y += __shfl_xor_sync(0xffffffffu, send.y, mask);
+                        flat[i] = keep;
+                    }
+                    if (hi) base += (uint32_t) half;
+                }
+                const uint32_t m_left = (uint32_t) M >> (nb < (uint32_t) LM ? nb : (uint32_t) LM);
                 bool writer = true;
-                for (int w = 0; w < 2; w++) {
-                    if (!p.lo_summed[w]) continue;
-                    writer = writer && ((tid >> (2 * w)) & 3u) == 0;
-#pragma unroll
-                    for (int g = 0; g < G; g++)
-#pragma unroll
-                        for (int f = 0; f < NSF; f++)
-                            for (uint32_t m = 1u << (2 * w); m <= (2u << (2 * w)); m <<= 1) {
-                                acc[g][f].x += __shfl_xor_sync(0xffffffffu, acc[g][f].x, m);
-                                acc[g][f].y += __shfl_xor_sync(0xffffffffu, acc[g][f].y, m);
-                            }
+                for (uint32_t k = LM; k < nb; k++) {
+                    const uint32_t mask = 1u << (b0 + k);
+                    flat[0].x += __shfl_xor_sync(0xffffffffu, flat[0].x, mask);
+                    flat[0].y += __shfl_xor_sync(0xffffffffu, flat[0].y, mask);
+                    writer = writer && (tid & mask) == 0;
                 }
                 if (writer) {
+                    const uint64_t cb = cbase + c_lo;
 #pragma unroll
-                    for (int g = 0; g < G; g++)
-#pragma unroll
-                        for (int f = 0; f < NSF; f++) {
-                            const float2 v = make_float2(scale_pow2(acc[g][f].x, shift), scale_pow2(acc[g][f].y, shift));
-                            lmax = max(lmax, mag_bits(v));
-                            p.C[cbase + c_lo + out_offset(p, (uint32_t) g, (uint32_t) f)] = v;
-                        }
+                    for (int j = 0; j < M; j++) {
+                        if ((uint32_t) j >= m_left) break;
+                        const float2 v = make_float2(scale_pow2(flat[j].x, shift), scale_pow2(flat[j].y, shift));
+                        lmax = max(lmax, mag_bits(v));
+                        p.C[cb + out_off[base + j]] = v;
+                    }
                 }
             }
         }

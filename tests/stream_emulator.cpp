@@ -164,38 +164,57 @@ static std::string emulate(const StepDesc &d, const StreamStep &p, std::mt19937 
                 C[coff] = v;
             }
         } else {
-            // shuffles over the summed digits among wires 0/1 (lane bits 0-3):
-            // the lanes whose summed digits are 0 write their sums directly
+            // butterfly reduce-scatter over the summed lane bits (wires 0/1),
+            // then an all-reduce over the bits beyond log2(G NSF)
             if (p.klo_mode == 1 && (p.lo_summed[2] || p.lo_summed[3])) return "shuffle mode with wires 2/3";
-            for (uint32_t tid = 0; tid < T; tid++) {
-                bool writer = true;
-                uint32_t c_lo = 0;
-                for (int w = 0; w < 4; w++) {
-                    const uint32_t dg = (tid >> (2 * w)) & 3u;
-                    if (p.lo_summed[w]) writer = writer && dg == 0;
-                    else c_lo += dg << (2 * p.lo_other[w]);
-                }
-                if (!writer) continue;
-                const uint32_t n_kl = 1u << (2 * p.n_klo);
-                for (uint32_t gg = 0; gg < G; gg++)
-                    for (uint32_t f = 0; f < NSF; f++) {
-                        cf v(0.f, 0.f);
-                        for (uint32_t kl = 0; kl < n_kl; kl++) {
-                            uint32_t t = tid, q = 0;
-                            for (int w = 0; w < 2; w++)
-                                if (p.lo_summed[w]) {
-                                    t ^= ((kl >> (2 * q)) & 3u) << (2 * w);
-                                    q++;
-                                }
-                            v += acc[((uint64_t) gg * NSF + f) * T + t];
-                        }
-                        uint64_t coff = cbase + c_lo;
-                        for (uint32_t j = 0; j < p.go; j++) coff += (uint64_t) ((gg >> (2 * j)) & 3u) << (2 * p.g_cd[j]);
-                        for (uint32_t j = 0; j < p.nsf; j++) coff += (uint64_t) ((f >> (2 * j)) & 3u) << (2 * p.sf_cd[j]);
-                        if (coff >= nC) return "C index";
-                        written[coff]++;
-                        C[coff] = v;
+            const uint32_t M = G * NSF, LM = M >= 16 ? 4 : M >= 4 ? 2 : 0;
+            const uint32_t b0 = p.lo_summed[0] ? 0u : 2u, nb = 2u * (p.lo_summed[0] + p.lo_summed[1]);
+            std::vector<std::vector<cf>> flat(T, std::vector<cf>(M));
+            for (uint32_t tid = 0; tid < T; tid++)
+                for (uint32_t i = 0; i < M; i++) flat[tid][i] = acc[(uint64_t) i * T + tid];   // i = g NSF + f
+            std::vector<uint32_t> base(T, 0);
+            std::vector<bool> writer(T, true);
+            for (uint32_t k = 0; k < LM && k < nb; k++) {
+                const uint32_t mask = 1u << (b0 + k), half = M >> (k + 1);
+                if (mask >= 32) return "shuffle beyond a warp";
+                auto next = flat;
+                for (uint32_t tid = 0; tid < T; tid++) {
+                    const bool hi = (tid & mask) != 0, phi = !hi;
+                    const uint32_t q = tid ^ mask;
+                    for (uint32_t i = 0; i < half; i++) {
+                        const cf send_q = phi ? flat[q][i] : flat[q][i + half];
+                        next[tid][i] = (hi ? flat[tid][i + half] : flat[tid][i]) + send_q;
                     }
+                    if (hi) base[tid] += half;
+                }
+                flat = next;
+            }
+            const uint32_t m_left = M >> std::min(nb, LM);
+            for (uint32_t k = LM; k < nb; k++) {
+                const uint32_t mask = 1u << (b0 + k);
+                if (mask >= 32) return "shuffle beyond a warp";
+                auto next = flat;
+                for (uint32_t tid = 0; tid < T; tid++) {
+                    next[tid][0] = flat[tid][0] + flat[tid ^ mask][0];
+                    if (tid & mask) writer[tid] = false;
+                }
+                flat = next;
+            }
+            for (uint32_t tid = 0; tid < T; tid++) {
+                if (!writer[tid]) continue;
+                uint32_t c_lo = 0;
+                for (int w = 0; w < 4; w++)
+                    if (!p.lo_summed[w]) c_lo += ((tid >> (2 * w)) & 3u) << (2 * p.lo_other[w]);
+                for (uint32_t j = 0; j < m_left; j++) {
+                    const uint32_t idx = base[tid] + j, gg = idx / NSF, f = idx % NSF;
+                    if (idx >= M) return "reduce-scatter index";
+                    uint64_t coff = cbase + c_lo;
+                    for (uint32_t jj = 0; jj < p.go; jj++) coff += (uint64_t) ((gg >> (2 * jj)) & 3u) << (2 * p.g_cd[jj]);
+                    for (uint32_t jj = 0; jj < p.nsf; jj++) coff += (uint64_t) ((f >> (2 * jj)) & 3u) << (2 * p.sf_cd[jj]);
+                    if (coff >= nC) return "C index";
+                    written[coff]++;
+                    C[coff] = flat[tid][j];
+                }
             }
         }
     }
