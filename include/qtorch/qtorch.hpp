@@ -265,6 +265,26 @@ private:
     int mNumThreadsInNetwork{8};
 };
 
+// ---- preProcess (src/preprocess.h:28-52) ----------------------------------
+// The reference retries its randomly seeded stochastic ordering up to 100
+// times and keeps the first sequence whose contraction finishes under a time
+// limit.  This build scores each seeded try by what sets the GPU's time and
+// memory -- the rank of its largest intermediate, then its complex MACs --
+// over a symbolic copy of the network (no contraction is run) and keeps the
+// best of `tries` seeds (seed, seed + 1, ...); with maxMacs > 0 it stops at
+// the first try of at most that many MACs, as the reference stops at the
+// first fast enough.  The sequence is the mCreatedFrom walk of the reference
+// (preprocess.h:41-46), replayable with ContractGivenSequence.
+struct PreProcessResult {
+    uint64_t seed = 0;
+    int tries = 0;          // tries run
+    int peakRank = 0;
+    long long flops = 0;    // complex MACs (getNumFloatOps)
+    std::vector<std::pair<int, int>> sequence;
+};
+bool preProcess(const std::string &qasmText, const std::string &measureText, const std::string &gateDir,
+                uint64_t seed, int tries, long long maxMacs, PreProcessResult &best);
+
 // ---- LineGraph (src/LineGraph.h:28-85) -------------------------------------
 // The reference asks the closed QuickBB binary for an elimination order; this
 // build computes a min-fill elimination order of the line graph itself.

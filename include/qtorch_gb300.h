@@ -186,6 +186,16 @@ qt_status qt_run_inp(qt_ctx *ctx, const char *inp_path, double *value, int64_t *
 qt_status qt_plan_build(qt_ctx *ctx, const char *qasm_text, const char *measure_text, const char *gate_dir,
                         qt_ordering ordering, uint64_t seed, const int32_t *sequence_pairs, int n_pairs,
                         qt_plan **out);
+/* preProcess (src/preprocess.h:28-52): the reference retries its stochastic
+ * ordering up to 100 times and keeps the first sequence that finishes under a
+ * time limit.  Here `tries` seeded stochastic orderings (seeds seed, seed + 1,
+ * ...) run over a symbolic copy of the network and are scored by the rank of
+ * their largest intermediate, then by complex MACs; the best becomes the plan
+ * (recorded as a sequence).  max_macs > 0 stops at the first try of at most
+ * that many MACs.  *chosen_seed (may be NULL) receives the winning seed, which
+ * QT_ORDER_STOCHASTIC reproduces. */
+qt_status qt_plan_build_search(qt_ctx *ctx, const char *qasm_text, const char *measure_text, const char *gate_dir,
+                               uint64_t seed, int tries, int64_t max_macs, qt_plan **out, uint64_t *chosen_seed);
 qt_status qt_plan_free(qt_plan *plan);
 int qt_plan_num_steps(const qt_plan *plan);
 /* Work items of the mixed form that carry a host-prepared descriptor (0: the

@@ -441,15 +441,29 @@ class Plan(_Owned):
     _release_rank = 3
 
     def __init__(self, qasm_text, measure_text="", ordering="linegraph", seed=0, sequence=None, gate_dir=None,
-                 ctx=None, symbolic=False):
+                 ctx=None, symbolic=False, tries=100, max_macs=0):
+        """ordering: "linegraph", "stochastic" (seeded), "sequence" (recorded
+        node-id pairs) or "search" -- the preProcess-style search
+        (qt_plan_build_search): `tries` seeded stochastic orderings from `seed`,
+        the one with the smallest largest intermediate, then fewest MACs, kept
+        (its seed in `chosen_seed`)."""
         # symbolic plans need no device: they can be inspected but not executed
         self.ctx = None if symbolic else (ctx or default_context())
+        self.chosen_seed = None
         h = ctypes.c_void_p()
-        seq = np.ascontiguousarray(np.asarray(sequence if sequence is not None else [], dtype=np.int32).reshape(-1))
-        _check(_lib().qt_plan_build(self.ctx.handle if self.ctx else None, qasm_text.encode(),
-                                    (measure_text or "").encode(),
-                                    gate_dir.encode() if gate_dir else None, _ORDER_NAMES[ordering], int(seed),
-                                    _ip(seq) if seq.size else None, seq.size // 2, ctypes.byref(h)), self.ctx)
+        if ordering == "search":
+            cs = ctypes.c_uint64()
+            _check(_lib().qt_plan_build_search(self.ctx.handle if self.ctx else None, qasm_text.encode(),
+                                               (measure_text or "").encode(), gate_dir.encode() if gate_dir else None,
+                                               int(seed), int(tries), int(max_macs), ctypes.byref(h),
+                                               ctypes.byref(cs)), self.ctx)
+            self.chosen_seed = int(cs.value)
+        else:
+            seq = np.ascontiguousarray(np.asarray(sequence if sequence is not None else [], dtype=np.int32).reshape(-1))
+            _check(_lib().qt_plan_build(self.ctx.handle if self.ctx else None, qasm_text.encode(),
+                                        (measure_text or "").encode(),
+                                        gate_dir.encode() if gate_dir else None, _ORDER_NAMES[ordering], int(seed),
+                                        _ip(seq) if seq.size else None, seq.size // 2, ctypes.byref(h)), self.ctx)
         self.handle = h.value
         self._register(self.ctx)
 

@@ -76,6 +76,8 @@ SIGNATURES = [
     ("qt_run_inp", c_int, [c_void_p, c_char_p, P(c_double), P(c_int64)]),
     ("qt_plan_build", c_int, [c_void_p, c_char_p, c_char_p, c_char_p, c_int, c_uint64, P(c_int32), c_int,
                               P(c_void_p)]),
+    ("qt_plan_build_search", c_int, [c_void_p, c_char_p, c_char_p, c_char_p, c_uint64, c_int, c_int64, P(c_void_p),
+                                     P(c_uint64)]),
     ("qt_plan_free", c_int, [c_void_p]),
     ("qt_plan_num_steps", c_int, [c_void_p]),
     ("qt_plan_item_descriptors", c_int64, [c_void_p]),

@@ -319,6 +319,28 @@ qt_status qt_plan_build(qt_ctx *ctx, const char *qasm_text, const char *measure_
     });
 }
 
+qt_status qt_plan_build_search(qt_ctx *ctx, const char *qasm_text, const char *measure_text, const char *gate_dir,
+                               uint64_t seed, int tries, int64_t max_macs, qt_plan **out, uint64_t *chosen_seed) {
+    if (!qasm_text || !out || tries < 1) return QT_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    qtorch::PreProcessResult best;
+    qt_status s = guard(ctx, [&]() {
+        if (!qtorch::preProcess(qasm_text, measure_text ? measure_text : "", gate_dir ? gate_dir : "", seed, tries,
+                                (long long) max_macs, best))
+            return set_error(ctx, QT_ERR_CONTRACTION_FAILURE, "no stochastic try finished the network");
+        return QT_OK;
+    });
+    if (s != QT_OK) return s;
+    if (chosen_seed) *chosen_seed = best.seed;
+    std::vector<int32_t> pairs;
+    for (const auto &pr : best.sequence) {
+        pairs.push_back(pr.first);
+        pairs.push_back(pr.second);
+    }
+    return qt_plan_build(ctx, qasm_text, measure_text, gate_dir, QT_ORDER_SEQUENCE, 0, pairs.data(),
+                         (int) best.sequence.size(), out);
+}
+
 qt_status qt_plan_free(qt_plan *p) {
     if (!p) return QT_ERR_INVALID_ARGUMENT;
     for (auto &v : p->slicings)

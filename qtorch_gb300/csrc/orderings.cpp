@@ -618,4 +618,36 @@ void Network::ReduceCircuit() {
     mNodesByWire = std::move(next);
 }
 
+// ---- preProcess (src/preprocess.h:28-52) ----------------------------------
+
+bool preProcess(const std::string &qasmText, const std::string &measureText, const std::string &gateDir,
+                uint64_t seed, int tries, long long maxMacs, PreProcessResult &best) {
+    best = PreProcessResult{};
+    bool found = false;
+    for (int i = 0; i < tries; i++) {
+        auto net = Network::FromText(qasmText, measureText, gateDir, nullptr);   // symbolic
+        ContractionTools t(net);
+        t.Seed(seed + (uint64_t) i);
+        t.Contract(Stochastic);
+        if (!net->IsDone()) continue;
+        int peak = 0;
+        for (const auto &n : net->GetAllNodes()) peak = std::max(peak, n->mRank);
+        const long long macs = net->getNumFloatOps();
+        best.tries = i + 1;
+        if (!found || peak < best.peakRank || (peak == best.peakRank && macs < best.flops)) {
+            found = true;
+            best.seed = seed + (uint64_t) i;
+            best.peakRank = peak;
+            best.flops = macs;
+            best.sequence.clear();
+            // the walk of preprocess.h:41-46
+            for (const auto &n : net->GetAllNodes())
+                if (!(n->mCreatedFrom.first == 0 && n->mCreatedFrom.second == 0))
+                    best.sequence.push_back(n->mCreatedFrom);
+        }
+        if (maxMacs > 0 && macs <= maxMacs) break;
+    }
+    return found;
+}
+
 }  // namespace qtorch
