@@ -77,6 +77,14 @@ uint64_t qt_ctx_tensor_core_steps(const qt_ctx *ctx);
 /* Contraction steps of this context that ran on the streaming kernel (a small
  * operand in shared memory, the large one read once by TMA bulk copies). */
 uint64_t qt_ctx_stream_steps(const qt_ctx *ctx);
+/* Test hook of the failure path (no reference counterpart): with mode 1 the
+ * streaming kernel leaves the first tile of every CTA unissued, so its
+ * pipeline waits -- bounded by `polls` polls (0: the normal limit) -- run out;
+ * the kernel then waits for the copies it did issue, raises its error flag and
+ * returns, and the call reports QT_ERR_CUDA ("TMA pipeline wait timed out")
+ * with the context still usable.  mode 0 restores normal operation.  The
+ * setting is per device and process. */
+qt_status qt_debug_stream_fault(qt_ctx *ctx, int mode, uint32_t polls);
 /* The context's caching device allocator: bytes handed out, bytes cached for
  * reuse, and how many cudaMalloc calls it has made since the context was
  * created (any pointer may be NULL). */

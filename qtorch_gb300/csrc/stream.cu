@@ -50,9 +50,16 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-// at most 2^22 polls (tens of milliseconds with the back-off), then false
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    for (uint32_t it = 0; it < (1u << 22); it++) {
+// Test hook for the failure path (qt_debug_stream_fault): with mode 1 the
+// producer leaves the first tile of every CTA unissued -- a wait that nothing
+// will ever complete -- and the pipeline waits give up after `polls` polls.
+// Waits for copies that were issued always use the full limit.
+__device__ uint32_t g_stream_fault_mode = 0;
+__device__ uint32_t g_stream_fault_polls = 0;
+
+// at most `limit` polls (2^22: tens of milliseconds with the back-off), then false
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t limit = 1u << 22) {
+    for (uint32_t it = 0; it < limit; it++) {
         uint32_t ok;
         asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
                      : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
@@ -163,16 +170,19 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
     const int shift = scale_shift(p.sc);
     uint32_t lmax = 0;
     bool ok = true;
+    const bool skip_first = g_stream_fault_mode == 1;
+    const uint32_t limit = g_stream_fault_polls ? g_stream_fault_polls : (1u << 22);
 
     if (warp == kStreamConsumerWarps) {
         // producer: fill stage t % NS once its previous tile has been released
         uint32_t t = 0;
         for (; t < n_t; t++) {
             const uint32_t s = t % NS;
-            if (t >= (uint32_t) NS && !mbar_wait(smem_u32(&empty[s]), ((t / NS) - 1) & 1u)) {
+            if (t >= (uint32_t) NS && !mbar_wait(smem_u32(&empty[s]), ((t / NS) - 1) & 1u, limit)) {
                 ok = false;
                 break;
             }
+            if (t == 0 && skip_first) continue;   // test hook: this tile never arrives
             const uint32_t item = blockIdx.x + (t / p.n_chunks) * gridDim.x, chunk = t % p.n_chunks;
             issue_tile(p, tiles + (uint64_t) s * tile_stride, &full[s], item, chunk, lane);
         }
@@ -219,7 +229,7 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
         for (uint32_t t = 0; t < n_t; t++) {
             const uint32_t s = t % NS;
             const uint32_t item = blockIdx.x + (t / p.n_chunks) * gridDim.x, chunk = t % p.n_chunks;
-            if (!mbar_wait(smem_u32(&full[s]), (t / NS) & 1u)) {
+            if (!mbar_wait(smem_u32(&full[s]), (t / NS) & 1u, limit)) {
                 ok = false;
                 break;
             }
@@ -345,7 +355,7 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
         for (uint32_t s = 0; s < (uint32_t) NS; s++)
             if (issued > s) {
                 const uint32_t last = s + ((issued - 1 - s) / NS) * NS;
-                mbar_wait(smem_u32(&full[s]), (last / NS) & 1u);
+                if (!(last == 0 && skip_first)) mbar_wait(smem_u32(&full[s]), (last / NS) & 1u);
             }
         atomicExch(p.error_flag, 1);
     }
@@ -392,6 +402,13 @@ cudaError_t stream_attributes() {
 }
 
 }  // namespace
+
+cudaError_t stream_set_fault(int mode, uint32_t polls) {
+    const uint32_t m = (uint32_t) mode;
+    cudaError_t e = cudaMemcpyToSymbol(g_stream_fault_mode, &m, sizeof m);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_stream_fault_polls, &polls, sizeof polls);
+    return e;
+}
 
 bool stream_plan(const StepDesc &d, StreamStep &p) {
     std::memset(&p, 0, sizeof p);

@@ -72,6 +72,11 @@ struct StreamStep {
     uint8_t dout_cd[kMaxWires], dout_kind[kMaxWires], dout_idx[kMaxWires];
 };
 
+// Test hook of the failure path: mode 1 makes every CTA's first tile never
+// arrive, so the pipeline's waits run out after `polls` polls (0: the normal
+// limit) and the launch reports a timeout; mode 0 restores normal operation.
+cudaError_t stream_set_fault(int mode, uint32_t polls);
+
 // Plans the step (false: not a shape this kernel takes).
 bool stream_plan(const StepDesc &d, StreamStep &p);
 // Launches it on L = A or B as stream_plan chose (p.L, p.S, p.C filled here).

@@ -85,3 +85,30 @@ def test_step_by_step_plans_scale_every_tensor(ctx, tmp_path, scale):
     assert 1e-3 < abs(v64) / scale ** 10 < 1e3
     vmx = plan.execute(qg.MIXED)
     assert abs(vmx - v64) <= 1e-5 * abs(v64)
+
+
+def test_pipeline_wait_timeout_reports_an_error_and_the_context_recovers(ctx):
+    """Failure detection without a fault: the test hook leaves every CTA's
+    first tile unissued (a wait nothing completes), the bounded waits give up
+    after a few thousand polls, the kernel drains the copies it did issue and
+    raises its flag; the call returns QT_ERR_CUDA, and with the hook off the
+    same contraction on the same context succeeds."""
+    lib = qg._capi.load()
+    ra, rb, nsum = 12, 3, 2
+    rng = np.random.default_rng(5)
+    a = (rng.standard_normal(4 ** ra) + 1j * rng.standard_normal(4 ** ra)).astype(np.complex64)
+    b = (rng.standard_normal(4 ** rb) + 1j * rng.standard_normal(4 ** rb)).astype(np.complex64)
+    ffa, fi, sa, sb = random_maps(rng, ra, rb, nsum, False)
+    assert lib.qt_debug_stream_fault(ctx.handle, 1, 4096) == 0
+    try:
+        n0 = ctx.stream_steps
+        with pytest.raises(qg.QtError) as info:
+            qg.contract_pair_c64(a, b, ffa, fi, sa, sb, ctx=ctx)
+        assert info.value.status == 10   # QT_ERR_CUDA
+        assert "timed out" in str(info.value)
+        assert ctx.stream_steps == n0 + 1
+    finally:
+        assert lib.qt_debug_stream_fault(ctx.handle, 0, 0) == 0
+    got = qg.contract_pair_c64(a, b, ffa, fi, sa, sb, ctx=ctx)
+    want = reference(a, b, ra, rb, ffa, fi, sa, sb)
+    assert np.max(np.abs(got - want)) <= 2e-6 * 4 * 8
