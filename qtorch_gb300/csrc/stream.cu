@@ -69,6 +69,15 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_
     return false;
 }
 
+// the 256 consumer threads agree on v (named barrier 1 with an AND reduction),
+// so that none of them stops at a barrier the others have left
+__device__ __forceinline__ bool consumers_all(bool v) {
+    uint32_t r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.and.pred q, 1, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+                 : "=r"(r) : "r"((uint32_t) v), "r"(kStreamThreads) : "memory");
+    return r != 0;
+}
+
 __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                  ::"r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
@@ -86,13 +95,13 @@ __host__ __device__ inline uint32_t round128(uint32_t x) { return (x + 127u) / 1
 // byte offsets of the shared-memory regions (host and device agree)
 __host__ __device__ inline void stream_layout(const StreamStep &p, uint32_t off[5]) {
     const uint32_t tile = 1u << (2 * (4 + p.go + p.ho));
-    const uint32_t stage = p.klo_mode == 2 ? (uint32_t) kStreamThreads << (2 * (p.go + p.nsf)) : 0u;
+    const uint32_t staged = p.staged ? 1u << (2 * p.n_dout) : 0u;
     off[0] = 0;                                                  // kStreamStages tile buffers
-    off[1] = kStreamStages * round128(8u * tile);                // staged sums (summed wires 2/3 only)
-    off[2] = off[1] + round128(8u * stage);                      // S
+    off[1] = kStreamStages * round128(8u * tile);                // staged outputs of a pass
+    off[2] = off[1] + round128(8u * staged);                     // S
     off[3] = off[2] + round128(8u * p.s_elems);                  // full[stages], empty[stages], issued count,
-                                                                 // C offsets of a thread's outputs (g, f)
-    off[4] = off[3] + round128(16u * kStreamStages + 8u + 8u * kStreamMaxStage);   // end
+                                                                 // C offsets and staged indices of (g, f)
+    off[4] = off[3] + round128(16u * kStreamStages + 8u + 12u * kStreamMaxStage);   // end
 }
 
 // producer warp: the bulk copies of (item, chunk) into tile buffer `dst`
@@ -117,17 +126,23 @@ __device__ __forceinline__ void issue_tile(const StreamStep &p, float2 *dst, uin
     }
 }
 
-// C offset of output (g, f) of a work item, beyond the work item's base and
-// the thread's own free digits among wires 0-3
+// C offset of the in-pass sum (g, f) of a work item, beyond the work item's
+// and pass's bases and the thread's own free digits among wires 0-3
 __device__ __forceinline__ uint64_t out_offset(const StreamStep &p, uint32_t g, uint32_t f) {
     uint64_t o = 0;
     for (uint32_t j = 0; j < p.go; j++) o += (uint64_t) ((g >> (2 * j)) & 3u) << (2 * p.g_cd[j]);
-    for (uint32_t j = 0; j < p.nsf; j++) o += (uint64_t) ((f >> (2 * j)) & 3u) << (2 * p.sf_cd[j]);
+    for (uint32_t j = 0; j < p.nsfp; j++) o += (uint64_t) ((f >> (2 * j)) & 3u) << (2 * p.sf_cd[j]);
     return o;
 }
 
-// NSF free indices of S, G looped free and H looped summed combinations per
-// tile (E = G H elements per consumer thread and tile)
+// staged index of the in-pass sum (g, f)
+__device__ __forceinline__ uint32_t staged_index(const StreamStep &p, uint32_t g, uint32_t f) {
+    uint32_t o = 0;
+    for (uint32_t j = 0; j < p.go; j++) o += ((g >> (2 * j)) & 3u) << (2 * p.g_rank[j]);
+    for (uint32_t j = 0; j < p.nsfp; j++) o += ((f >> (2 * j)) & 3u) << (2 * p.sf_rank[j]);
+    return o;
+}
+
 // the register-heaviest classes (16 sums per thread over 4 or 16 summed
 // combinations) run one CTA per SM instead of spilling at two
 template <int NSF, int G, int H>
@@ -137,6 +152,7 @@ template <int NSF, int G, int H>
 __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
     stream_kernel(const __grid_constant__ StreamStep p) {
     constexpr int E = G * H;
+    constexpr int M = G * NSF;   // sums a thread keeps per pass
     constexpr int NS = kStreamStages;
     extern __shared__ __align__(128) unsigned char smem[];
     uint32_t off[5];
@@ -144,16 +160,23 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
     const uint32_t tile_elems = 1u << (2 * (4 + p.go + p.ho));
     const uint32_t tile_stride = round128(8u * tile_elems) / 8u;
     float2 *const tiles = reinterpret_cast<float2 *>(smem + off[0]);
-    float2 *const stage = reinterpret_cast<float2 *>(smem + off[1]);
+    float2 *const ostage = reinterpret_cast<float2 *>(smem + off[1]);
     float2 *const S = reinterpret_cast<float2 *>(smem + off[2]);
     uint64_t *const full = reinterpret_cast<uint64_t *>(smem + off[3]);
     uint64_t *const empty = full + NS;
     uint32_t *const issued_slot = reinterpret_cast<uint32_t *>(empty + NS);
-    uint64_t *const out_off = reinterpret_cast<uint64_t *>(empty + NS + 1);   // [G * NSF]
+    uint64_t *const out_off = reinterpret_cast<uint64_t *>(empty + NS + 1);      // [M]
+    uint32_t *const st_gf = reinterpret_cast<uint32_t *>(out_off + kStreamMaxStage);   // [M]
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    const uint32_t n_out = 1u << (2 * p.n_dout);
 
     for (uint32_t e = tid; e < p.s_elems; e += blockDim.x) S[e] = p.S[e];
-    if (tid < (uint32_t) (G * NSF)) out_off[tid] = out_offset(p, tid / NSF, tid % NSF);
+    if (tid < (uint32_t) M) {
+        out_off[tid] = out_offset(p, tid / NSF, tid % NSF);
+        st_gf[tid] = staged_index(p, tid / NSF, tid % NSF);
+    }
+    if (p.staged && p.klo_mode == 2)   // sums from several warps meet there by atomic adds
+        for (uint32_t u = tid; u < n_out; u += blockDim.x) ostage[u] = make_float2(0.f, 0.f);
     if (tid == 0) {
         for (int s = 0; s < NS; s++) {
             mbar_init(smem_u32(&full[s]), 1);
@@ -189,11 +212,15 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
         if (lane == 0) *issued_slot = t;
     } else {
         // consumers: thread tid owns element tid of every 256-element stretch
-        uint32_t s_lo = 0, c_lo = 0;
+        uint32_t s_lo = 0, c_lo = 0, st_lo = 0;
         for (int w = 0; w < 4; w++) {
             const uint32_t dg = (tid >> (2 * w)) & 3u;
-            if (p.lo_summed[w]) s_lo += dg << (2 * p.lo_other[w]);
-            else c_lo += dg << (2 * p.lo_other[w]);
+            if (p.lo_summed[w]) {
+                s_lo += dg << (2 * p.lo_other[w]);
+            } else {
+                c_lo += dg << (2 * p.lo_other[w]);
+                st_lo += dg << (2 * p.lo_rank[w]);
+            }
         }
         // each element's tile offset and S offset beyond the thread's own
         // (the g and h digits), and the free-index offsets of S: the same for
@@ -222,92 +249,67 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
         for (int f = 0; f < NSF; f++) {
             uint32_t o = 0;
             if (NSF > 1)
-                for (uint32_t j = 0; j < p.nsf; j++) o += (((uint32_t) f >> (2 * j)) & 3u) << (2 * p.sf_w[j]);
+                for (uint32_t j = 0; j < p.nsfp; j++) o += (((uint32_t) f >> (2 * j)) & 3u) << (2 * p.sf_w[j]);
             sfo[f] = o;
         }
+        // the summed lane bits among wires 0/1 are consecutive: 0-1, 2-3 or 0-3
+        const uint32_t b0 = p.lo_summed[0] ? 0u : 2u;
+        const uint32_t nb = 2u * (p.lo_summed[0] + p.lo_summed[1]);
+        constexpr int LM = M >= 16 ? 4 : M >= 4 ? 2 : 0;   // log2(M)
         float2 acc[G][NSF];
+        float2 *flat = &acc[0][0];
         for (uint32_t t = 0; t < n_t; t++) {
             const uint32_t s = t % NS;
             const uint32_t item = blockIdx.x + (t / p.n_chunks) * gridDim.x, chunk = t % p.n_chunks;
-            if (!mbar_wait(smem_u32(&full[s]), (t / NS) & 1u, limit)) {
+            bool got = mbar_wait(smem_u32(&full[s]), (t / NS) & 1u, limit);
+            // staged outputs use consumer barriers: all consumers leave together
+            if (p.staged) got = consumers_all(got);
+            if (!got) {
                 ok = false;
                 break;
             }
             const float2 *T = tiles + (uint64_t) s * tile_stride + tid;
-            if (chunk == 0) {
-#pragma unroll
-                for (int g = 0; g < G; g++)
-#pragma unroll
-                    for (int f = 0; f < NSF; f++) acc[g][f] = make_float2(0.f, 0.f);
-            }
             // S's share of the chunk's summed digits
             uint32_t s_c = 0;
             for (uint32_t j = 0; j < p.n_chunk_d; j++) s_c += ((chunk >> (2 * j)) & 3u) << (2 * p.chunk_sw[j]);
-            const float2 *Sc = S + s_c + s_lo;
-#pragma unroll
-            for (int i = 0; i < E; i++) {
-                const float2 x = T[eo[i]];
-#pragma unroll
-                for (int f = 0; f < NSF; f++) cmac(acc[i / H][f], x, Sc[so[i] + sfo[f]]);
-            }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(smem_u32(&empty[s]));   // this warp is done with the stage
-
-            if (chunk + 1 < p.n_chunks) continue;
             uint64_t cbase = 0;
             for (uint32_t j = 0; j < p.n_item_d; j++) cbase += (uint64_t) ((item >> (2 * j)) & 3u) << (2 * p.item_cd[j]);
-            if (p.klo_mode == 2) {
-                // summed wires 2/3 span warps: stage (consumers only), then one thread per output
-#pragma unroll
-                for (int g = 0; g < G; g++)
-#pragma unroll
-                    for (int f = 0; f < NSF; f++) stage[((uint32_t) (g * NSF + f)) * kStreamThreads + tid] = acc[g][f];
-                asm volatile("bar.sync 1, %0;" ::"r"(kStreamThreads) : "memory");
-                const uint32_t n_out = 1u << (2 * p.n_dout), n_kl = 1u << (2 * p.n_klo);
-                for (uint32_t o = tid; o < n_out; o += kStreamThreads) {
-                    uint64_t coff = cbase;
-                    uint32_t tf = 0, g = 0, f = 0;
-                    for (uint32_t r = 0; r < p.n_dout; r++) {
-                        const uint32_t dg = (o >> (2 * r)) & 3u;
-                        coff += (uint64_t) dg << (2 * p.dout_cd[r]);
-                        const uint32_t sh = 2u * p.dout_idx[r];
-                        if (p.dout_kind[r] == 0) tf += dg << sh;
-                        else if (p.dout_kind[r] == 1) g += dg << sh;
-                        else f += dg << sh;
-                    }
-                    const float2 *st = stage + ((uint64_t) g * NSF + f) * kStreamThreads;
-                    float vx = 0.f, vy = 0.f;
-                    for (uint32_t kl = 0; kl < n_kl; kl++) {
-                        uint32_t tt = tf, q = 0;
-                        for (int w = 0; w < 4; w++)
-                            if (p.lo_summed[w]) {
-                                tt += ((kl >> (2 * q)) & 3u) << (2 * w);
-                                q++;
-                            }
-                        const float2 pv = st[tt];
-                        vx += pv.x;
-                        vy += pv.y;
-                    }
-                    const float2 v = make_float2(scale_pow2(vx, shift), scale_pow2(vy, shift));
-                    lmax = max(lmax, mag_bits(v));
-                    p.C[coff] = v;
+            // a work item with several passes has one chunk (stream_plan), so
+            // the sums never outlive a pass
+            for (uint32_t pass = 0; pass < p.n_pass; pass++) {
+                uint32_t s_p = s_c + s_lo;
+                uint64_t cpass = cbase;
+                for (uint32_t j = p.nsfp; j < p.nsf; j++) {
+                    const uint32_t dg = (pass >> (2 * (j - p.nsfp))) & 3u;
+                    s_p += dg << (2 * p.sf_w[j]);
+                    cpass += (uint64_t) dg << (2 * p.sf_cd[j]);
                 }
-                asm volatile("bar.sync 1, %0;" ::"r"(kStreamThreads) : "memory");   // staging free again
-            } else {
-                // Summed wires among 0/1 only: lane bits 0-3.  A butterfly
-                // reduce-scatter over those bits halves the sums a lane keeps at
-                // every step (one shuffle per sum handed over), so the lanes
-                // sharing a sum end up each holding a different part of the
-                // work item's outputs and all of them store; bits beyond
-                // log2(G NSF) finish as an all-reduce, the lanes whose summed
-                // digits are 0 storing.
-                constexpr int M = G * NSF;
-                constexpr int LM = M >= 16 ? 4 : M >= 4 ? 2 : 0;   // log2(M)
-                float2 *flat = &acc[0][0];
-                // the summed lane bits are consecutive: 0-1, 2-3 or 0-3
-                const uint32_t b0 = p.lo_summed[0] ? 0u : 2u;
-                const uint32_t nb = 2u * (p.lo_summed[0] + p.lo_summed[1]);
+                if (chunk == 0) {
+#pragma unroll
+                    for (int g = 0; g < G; g++)
+#pragma unroll
+                        for (int f = 0; f < NSF; f++) acc[g][f] = make_float2(0.f, 0.f);
+                }
+                const float2 *Sp = S + s_p;
+#pragma unroll
+                for (int i = 0; i < E; i++) {
+                    const float2 x = T[eo[i]];
+#pragma unroll
+                    for (int f = 0; f < NSF; f++) cmac(acc[i / H][f], x, Sp[so[i] + sfo[f]]);
+                }
+                if (pass + 1 == p.n_pass) {
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(smem_u32(&empty[s]));   // this warp is done with the stage
+                }
+                if (chunk + 1 < p.n_chunks) continue;
+
+                // Summed wires among 0/1 (lane bits 0-3): a butterfly
+                // reduce-scatter halves the sums a lane keeps at every step, so
+                // the lanes sharing a sum each end up with a different part of
+                // the outputs; bits beyond log2(M) finish as an all-reduce, the
+                // lanes whose summed digits are 0 keeping the sum.
                 uint32_t base = 0;
+                bool owner = true;
 #pragma unroll
                 for (int k = 0; k < LM; k++) {
                     if ((uint32_t) k >= nb) break;
@@ -327,23 +329,67 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
                     if (hi) base += (uint32_t) half;
                 }
                 const uint32_t m_left = (uint32_t) M >> (nb < (uint32_t) LM ? nb : (uint32_t) LM);
-                bool writer = true;
                 for (uint32_t k = LM; k < nb; k++) {
                     const uint32_t mask = 1u << (b0 + k);
                     flat[0].x += __shfl_xor_sync(0xffffffffu, flat[0].x, mask);
                     flat[0].y += __shfl_xor_sync(0xffffffffu, flat[0].y, mask);
-                    writer = writer && (tid & mask) == 0;
+                    owner = owner && (tid & mask) == 0;
                 }
-                if (writer) {
-                    const uint64_t cb = cbase + c_lo;
+                if (!p.staged) {
+                    if (owner) {
+                        const uint64_t cb = cpass + c_lo;
+#pragma unroll
+                        for (int j = 0; j < M; j++) {
+                            if ((uint32_t) j >= m_left) break;
+                            const float2 v = make_float2(scale_pow2(flat[j].x, shift), scale_pow2(flat[j].y, shift));
+                            lmax = max(lmax, mag_bits(v));
+                            p.C[cb + out_off[base + j]] = v;
+                        }
+                    }
+                    continue;
+                }
+                // staged: every output of the pass into shared memory in C's
+                // digit order (added up there when summed wires 2/3 spread a
+                // sum over warps), then stored along C's contiguous runs
+                if (owner) {
 #pragma unroll
                     for (int j = 0; j < M; j++) {
                         if ((uint32_t) j >= m_left) break;
-                        const float2 v = make_float2(scale_pow2(flat[j].x, shift), scale_pow2(flat[j].y, shift));
-                        lmax = max(lmax, mag_bits(v));
-                        p.C[cb + out_off[base + j]] = v;
+                        float2 *dst = ostage + st_lo + st_gf[base + j];
+                        if (p.klo_mode == 2) {
+                            atomicAdd(&dst->x, flat[j].x);
+                            atomicAdd(&dst->y, flat[j].y);
+                        } else {
+                            *dst = flat[j];
+                        }
                     }
                 }
+                asm volatile("bar.sync 1, %0;" ::"r"(kStreamThreads) : "memory");
+                const uint32_t run_log2 = 2 * p.out_run, run_mask = (1u << run_log2) - 1u;
+                if (p.out_run >= 1) {
+                    for (uint32_t u = 2 * tid; u < n_out; u += 2 * kStreamThreads) {
+                        uint64_t coff = cpass + (u & run_mask);
+                        uint32_t hi = u >> run_log2;
+                        for (uint32_t r = p.out_run; r < p.n_dout; r++, hi >>= 2) coff += (uint64_t) (hi & 3u) << (2 * p.dout_cd[r]);
+                        const float4 w = *reinterpret_cast<const float4 *>(ostage + u);
+                        const float4 v = make_float4(scale_pow2(w.x, shift), scale_pow2(w.y, shift),
+                                                     scale_pow2(w.z, shift), scale_pow2(w.w, shift));
+                        lmax = max(lmax, max(mag_bits(make_float2(v.x, v.y)), mag_bits(make_float2(v.z, v.w))));
+                        *reinterpret_cast<float4 *>(p.C + coff) = v;
+                        if (p.klo_mode == 2) *reinterpret_cast<float4 *>(ostage + u) = make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+                } else {
+                    for (uint32_t u = tid; u < n_out; u += kStreamThreads) {
+                        uint64_t coff = cpass;
+                        uint32_t hi = u;
+                        for (uint32_t r = 0; r < p.n_dout; r++, hi >>= 2) coff += (uint64_t) (hi & 3u) << (2 * p.dout_cd[r]);
+                        const float2 v = make_float2(scale_pow2(ostage[u].x, shift), scale_pow2(ostage[u].y, shift));
+                        lmax = max(lmax, mag_bits(v));
+                        p.C[coff] = v;
+                        if (p.klo_mode == 2) ostage[u] = make_float2(0.f, 0.f);
+                    }
+                }
+                asm volatile("bar.sync 1, %0;" ::"r"(kStreamThreads) : "memory");   // staging free again
             }
         }
     }
@@ -435,9 +481,11 @@ bool stream_plan(const StepDesc &d, StreamStep &p) {
             p.sf_w[nsf++] = cS[i];
         }
     }
-    if (nsf > 2) return false;   // at most 16 free indices of S per thread
+    if (nsf > 3) return false;   // at most 64 free indices of S: 16 per pass
     p.l_is_b = l_is_b;
     p.nsf = (uint32_t) nsf;
+    p.nsfp = (uint32_t) std::min(nsf, 2);
+    p.n_pass = 1u << (2 * (nsf - (int) p.nsfp));
     p.s_elems = 1u << (2 * rS);
     // wires 0-3: the thread's own digits
     int klo = 0;
@@ -456,11 +504,12 @@ bool stream_plan(const StepDesc &d, StreamStep &p) {
         if (summed[w]) hi[n_hi++] = w;
         else outer[n_outer++] = w;
     }
-    // loop digits of a tile: up to 16 elements per thread and 16 staged sums per thread
+    // loop digits of a tile: up to 16 elements per thread and 16 sums per thread
     const int ho = std::min(n_hi, 2);
     int go = std::min(n_outer, 2 - ho);
-    while (go > 0 && (1 << (2 * (go + nsf))) > (int) kStreamMaxStage) go--;
+    while (go > 0 && (1 << (2 * (go + (int) p.nsfp))) > (int) kStreamMaxStage) go--;
     if (n_outer - go > 15 || n_hi - ho > 15) return false;
+    if (p.n_pass > 1 && n_hi > ho) return false;   // several passes keep no sums across chunks
     p.go = (uint32_t) go;
     p.ho = (uint32_t) ho;
     p.n_items = 1u << (2 * (n_outer - go));
@@ -499,35 +548,45 @@ bool stream_plan(const StepDesc &d, StreamStep &p) {
     for (int w = prefix; w < rL; w++)
         if (in_tile[w]) p.run_lw[nr++] = (uint8_t) w;
     p.n_run_d = (uint32_t) nr;
-    // outputs of a work item: the C digits of L's free wires 0-3, of the g
-    // digits and of S's free wires, ascending
+    // the outputs of a pass: C digits of L's free wires 0-3, of the g digits
+    // and of the in-pass free wires of S, ascending
     int nd = 0;
     for (int i = 0; i < d.nFree; i++) {
         if (cL[i] != kNoWire) {
             const int w = cL[i];
             if (w < 4) {
-                p.dout_kind[nd] = 0;
-                p.dout_idx[nd] = (uint8_t) w;
+                p.lo_rank[w] = (uint8_t) nd;
             } else {
                 int j = 0;
                 while (j < go && outer[j] != w) j++;
                 if (j == go) continue;   // a work-item digit
-                p.dout_kind[nd] = 1;
-                p.dout_idx[nd] = (uint8_t) j;
+                p.g_rank[j] = (uint8_t) nd;
             }
         } else {
             int j = 0;
-            while (j < nsf && p.sf_w[j] != cS[i]) j++;
-            p.dout_kind[nd] = 2;
-            p.dout_idx[nd] = (uint8_t) j;
+            while (j < nsf && p.sf_cd[j] != i) j++;
+            if (j >= (int) p.nsfp) continue;   // a pass digit
+            p.sf_rank[j] = (uint8_t) nd;
         }
         p.dout_cd[nd++] = (uint8_t) i;
     }
     p.n_dout = (uint32_t) nd;
+    uint32_t run = 0;
+    while ((int) run < nd && p.dout_cd[run] == run) run++;
+    p.out_run = run;
+    // Direct stores from the owning lanes coalesce when C's digit 0 is one of
+    // the free lane digits (wires 0/1): consecutive lanes then write
+    // consecutive elements.  Otherwise -- and whenever summed wires 2/3 spread
+    // a sum over warps -- the outputs go through shared memory.
+    bool lane_digit0 = false;
+    for (int w = 0; w < 2; w++)
+        if (!summed[w] && cdig[w] == 0) lane_digit0 = true;
+    p.staged = (p.klo_mode == 2 || !lane_digit0) ? 1u : 0u;
+    if (p.staged && (1u << (2 * nd)) > kStreamMaxOut) return false;
     uint32_t off[5];
     stream_layout(p, off);
     p.smem_bytes = off[4];
-    return p.smem_bytes <= 200u * 1024u && stream_fn(p.nsf, p.go, p.ho) != nullptr;
+    return p.smem_bytes <= 200u * 1024u && stream_fn((uint32_t) p.nsfp, p.go, p.ho) != nullptr;
 }
 
 cudaError_t launch_stream(StreamStep &p, const StepDesc &d, const float2 *A, const float2 *B, float2 *C,
@@ -540,7 +599,7 @@ cudaError_t launch_stream(StreamStep &p, const StepDesc &d, const float2 *A, con
     p.error_flag = error_flag;
     cudaError_t e = stream_attributes();
     if (e != cudaSuccess) return e;
-    const StreamFn fn = stream_fn(p.nsf, p.go, p.ho);
+    const StreamFn fn = stream_fn(p.nsfp, p.go, p.ho);
     int per_sm = 0, dev = 0, sms = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kStreamBlock, p.smem_bytes);
     if (e == cudaSuccess) e = cudaGetDevice(&dev);

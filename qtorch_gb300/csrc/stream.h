@@ -28,7 +28,8 @@ namespace qtg {
 // are written straight to C.
 constexpr int kStreamMaxSmallRank = 6;       // S holds at most 4^6 elements (32 KB)
 constexpr uint32_t kStreamMaxTile = 4096;    // elements of one L tile (32 KB)
-constexpr uint32_t kStreamMaxStage = 16;     // g x S-free outputs a thread stages (256 threads x 16 x 8 B)
+constexpr uint32_t kStreamMaxStage = 16;     // g x S-free sums a thread keeps in registers
+constexpr uint32_t kStreamMaxOut = 4096;     // staged outputs of one pass (32 KB)
 constexpr int kStreamThreads = 256;          // = 4^4 consumer threads: one per combination of L's wires 0-3
 constexpr int kStreamConsumerWarps = kStreamThreads / 32;
 constexpr int kStreamBlock = kStreamThreads + 32;   // the consumers and one producer warp
@@ -46,12 +47,17 @@ struct StreamStep {
     uint32_t run_elems;            // elements of one bulk copy (4^(lowest in-tile wires in a row))
     uint32_t n_runs;               // bulk copies per tile
     uint32_t s_elems;              // 4^rank(S)
-    uint32_t nsf;                  // free wires of S (NSF = 4^nsf outputs per thread and g)
+    uint32_t nsf;                  // free wires of S
+    uint32_t nsfp;                 // of which one pass covers (NSFP = 4^nsfp sums per thread and g)
+    uint32_t n_pass;               // passes over a tile: combinations of S's free wires beyond nsfp
     uint32_t go, ho;               // outer / summed digits looped in a tile
     uint32_t n_item_d, n_chunk_d;  // digits of the work-item and chunk indices
     uint32_t n_run_d;              // in-tile digits above the run (bulk-copy index digits)
-    uint32_t n_dout, n_klo;        // output digits of a work item; summed wires among 0-3
-    uint32_t klo_mode;             // 0: no summed wire among 0-3, 1: only wires 0/1 (shuffles), 2: staging
+    uint32_t n_dout, n_klo;        // output digits of a pass; summed wires among 0-3
+    uint32_t klo_mode;             // 0: no summed wire among 0-3, 1: only wires 0/1 (shuffles), 2: wires 2/3 too
+    uint32_t staged;               // 1: outputs go through shared memory (summed wires 2/3, or
+                                   // C's digit 0 not among a warp's lane digits), 0: stored directly
+    uint32_t out_run;              // low staged digits that are C's digits 0, 1, ... in order
     uint32_t smem_bytes;
     uint32_t l_is_b;               // the large operand is B (else A)
     // work item digit j: L wire and C digit
@@ -67,9 +73,10 @@ struct StreamStep {
     uint8_t lo_summed[4], lo_other[4];
     // S-free digit j: S wire and C digit
     uint8_t sf_w[kStreamMaxSmallRank], sf_cd[kStreamMaxSmallRank];
-    // output digit r of a work item (ascending C digits): its C digit, its kind
-    // (0: one of L's wires 0-3, 1: a g digit, 2: an S-free digit) and that digit's index
-    uint8_t dout_cd[kMaxWires], dout_kind[kMaxWires], dout_idx[kMaxWires];
+    // staged outputs of a pass, digits in ascending C order: C digit of staged digit r,
+    // and the staged digit of each free wire among 0-3, g digit and in-pass S-free digit
+    uint8_t dout_cd[kMaxWires];
+    uint8_t lo_rank[4], g_rank[kStreamMaxLoop], sf_rank[kStreamMaxSmallRank];
 };
 
 // Test hook of the failure path: mode 1 makes every CTA's first tile never

@@ -82,15 +82,28 @@ static std::string emulate(const StepDesc &d, const StreamStep &p, std::mt19937 
     for (auto &x : A) x = cf(u(g), u(g));
     for (auto &x : B) x = cf(u(g), u(g));
     const std::vector<cf> &L = p.l_is_b ? B : A, &S = p.l_is_b ? A : B;
-    const uint32_t NSF = 1u << (2 * p.nsf), G = 1u << (2 * p.go), H = 1u << (2 * p.ho);
+    const uint32_t NSF = 1u << (2 * p.nsfp), G = 1u << (2 * p.go), H = 1u << (2 * p.ho);
     const uint32_t tile_elems = 1u << (2 * (4 + p.go + p.ho));
-    const uint32_t T = kStreamThreads;
-    if (tile_elems > kStreamMaxTile || G * NSF > kStreamMaxStage || p.s_elems != S.size()) return "region sizes";
+    const uint32_t T = kStreamThreads, M = G * NSF;
+    if (tile_elems > kStreamMaxTile || M > kStreamMaxStage || p.s_elems != S.size()) return "region sizes";
     if (p.run_elems * p.n_runs != tile_elems || p.run_elems < 256) return "runs";
+    if (p.n_pass > 1 && p.n_chunks > 1) return "passes with chunks";
     std::vector<int> written(nC, 0);
-    std::vector<cf> tile(tile_elems), acc((uint64_t) T * G * NSF);   // acc[(g * NSF + f) * T + tid]
+    std::vector<cf> tile(tile_elems);
+    // acc[pass][tid][i], i = g NSF + f, kept across the chunks of a work item
+    std::vector<std::vector<std::vector<cf>>> acc(p.n_pass, std::vector<std::vector<cf>>(T, std::vector<cf>(M)));
+    auto pass_offsets = [&](uint32_t pass, uint32_t &s_p, uint64_t &c_p) {
+        s_p = 0;
+        c_p = 0;
+        for (uint32_t j = p.nsfp; j < p.nsf; j++) {
+            const uint32_t dg = (pass >> (2 * (j - p.nsfp))) & 3u;
+            s_p += dg << (2 * p.sf_w[j]);
+            c_p += (uint64_t) dg << (2 * p.sf_cd[j]);
+        }
+    };
     for (uint32_t item = 0; item < p.n_items; item++) {
-        std::fill(acc.begin(), acc.end(), cf(0.f, 0.f));
+        for (auto &a : acc)
+            for (auto &v : a) std::fill(v.begin(), v.end(), cf(0.f, 0.f));
         for (uint32_t chunk = 0; chunk < p.n_chunks; chunk++) {
             // bulk copies
             uint64_t lbase = 0;
@@ -103,29 +116,33 @@ static std::string emulate(const StepDesc &d, const StreamStep &p, std::mt19937 
                 if (off + p.run_elems > L.size()) return "bulk copy beyond L";
                 for (uint32_t e = 0; e < p.run_elems; e++) tile[(uint64_t) r * p.run_elems + e] = L[off + e];
             }
-            // every thread's unrolled loop over its E = G H elements
             uint32_t s_c = 0;
             for (uint32_t j = 0; j < p.n_chunk_d; j++) s_c += ((chunk >> (2 * j)) & 3u) << (2 * p.chunk_sw[j]);
-            for (uint32_t tid = 0; tid < T; tid++) {
-                uint32_t s_lo = 0;
-                for (int w = 0; w < 4; w++)
-                    if (p.lo_summed[w]) s_lo += ((tid >> (2 * w)) & 3u) << (2 * p.lo_other[w]);
-                for (uint32_t gg = 0; gg < G; gg++) {
-                    uint32_t tg = tid;
-                    for (uint32_t j = 0; j < p.go; j++) tg += ((gg >> (2 * j)) & 3u) << (2 * p.g_pos[j]);
-                    for (uint32_t h = 0; h < H; h++) {
-                        uint32_t th = tg, sh = s_lo;
-                        for (uint32_t j = 0; j < p.ho; j++) {
-                            const uint32_t dg = (h >> (2 * j)) & 3u;
-                            th += dg << (2 * p.h_pos[j]);
-                            sh += dg << (2 * p.h_sw[j]);
-                        }
-                        if (th >= tile_elems) return "tile index";
-                        for (uint32_t f = 0; f < NSF; f++) {
-                            uint32_t so = 0;
-                            for (uint32_t j = 0; j < p.nsf; j++) so += ((f >> (2 * j)) & 3u) << (2 * p.sf_w[j]);
-                            if (s_c + sh + so >= S.size()) return "small operand index";
-                            acc[((uint64_t) gg * NSF + f) * T + tid] += tile[th] * S[s_c + sh + so];
+            for (uint32_t pass = 0; pass < p.n_pass; pass++) {
+                uint32_t s_p;
+                uint64_t c_p;
+                pass_offsets(pass, s_p, c_p);
+                for (uint32_t tid = 0; tid < T; tid++) {
+                    uint32_t s_lo = 0;
+                    for (int w = 0; w < 4; w++)
+                        if (p.lo_summed[w]) s_lo += ((tid >> (2 * w)) & 3u) << (2 * p.lo_other[w]);
+                    for (uint32_t gg = 0; gg < G; gg++) {
+                        uint32_t tg = tid;
+                        for (uint32_t j = 0; j < p.go; j++) tg += ((gg >> (2 * j)) & 3u) << (2 * p.g_pos[j]);
+                        for (uint32_t h = 0; h < H; h++) {
+                            uint32_t th = tg, sh = s_c + s_p + s_lo;
+                            for (uint32_t j = 0; j < p.ho; j++) {
+                                const uint32_t dg = (h >> (2 * j)) & 3u;
+                                th += dg << (2 * p.h_pos[j]);
+                                sh += dg << (2 * p.h_sw[j]);
+                            }
+                            if (th >= tile_elems) return "tile index";
+                            for (uint32_t f = 0; f < NSF; f++) {
+                                uint32_t so = 0;
+                                for (uint32_t j = 0; j < p.nsfp; j++) so += ((f >> (2 * j)) & 3u) << (2 * p.sf_w[j]);
+                                if (sh + so >= S.size()) return "small operand index";
+                                acc[pass][tid][gg * NSF + f] += tile[th] * S[sh + so];
+                            }
                         }
                     }
                 }
@@ -133,56 +150,26 @@ static std::string emulate(const StepDesc &d, const StreamStep &p, std::mt19937 
         }
         uint64_t cbase = 0;
         for (uint32_t j = 0; j < p.n_item_d; j++) cbase += (uint64_t) ((item >> (2 * j)) & 3u) << (2 * p.item_cd[j]);
-        if (p.klo_mode == 2) {
-            // staged: one thread per output, decoded from C's digit order
-            const uint32_t n_out = 1u << (2 * p.n_dout), n_kl = 1u << (2 * p.n_klo);
-            for (uint32_t o = 0; o < n_out; o++) {
-                uint64_t coff = cbase;
-                uint32_t tf = 0, gg = 0, f = 0;
-                for (uint32_t r = 0; r < p.n_dout; r++) {
-                    const uint32_t dg = (o >> (2 * r)) & 3u;
-                    coff += (uint64_t) dg << (2 * p.dout_cd[r]);
-                    const uint32_t sh = 2u * p.dout_idx[r];
-                    if (p.dout_kind[r] == 0) tf += dg << sh;
-                    else if (p.dout_kind[r] == 1) gg += dg << sh;
-                    else f += dg << sh;
-                }
-                if (gg >= G || f >= NSF || tf >= T) return "output decode";
-                cf v(0.f, 0.f);
-                for (uint32_t kl = 0; kl < n_kl; kl++) {
-                    uint32_t t = tf, q = 0;
-                    for (int w = 0; w < 4; w++)
-                        if (p.lo_summed[w]) {
-                            t += ((kl >> (2 * q)) & 3u) << (2 * w);
-                            q++;
-                        }
-                    if (t >= T) return "staging index";
-                    v += acc[((uint64_t) gg * NSF + f) * T + t];
-                }
-                if (coff >= nC) return "C index";
-                written[coff]++;
-                C[coff] = v;
-            }
-        } else {
-            // butterfly reduce-scatter over the summed lane bits (wires 0/1),
-            // then an all-reduce over the bits beyond log2(G NSF)
-            if (p.klo_mode == 1 && (p.lo_summed[2] || p.lo_summed[3])) return "shuffle mode with wires 2/3";
-            const uint32_t M = G * NSF, LM = M >= 16 ? 4 : M >= 4 ? 2 : 0;
-            const uint32_t b0 = p.lo_summed[0] ? 0u : 2u, nb = 2u * (p.lo_summed[0] + p.lo_summed[1]);
-            std::vector<std::vector<cf>> flat(T, std::vector<cf>(M));
-            for (uint32_t tid = 0; tid < T; tid++)
-                for (uint32_t i = 0; i < M; i++) flat[tid][i] = acc[(uint64_t) i * T + tid];   // i = g NSF + f
+        const uint32_t LM = M >= 16 ? 4 : M >= 4 ? 2 : 0;
+        const uint32_t b0 = p.lo_summed[0] ? 0u : 2u, nb = 2u * (p.lo_summed[0] + p.lo_summed[1]);
+        for (uint32_t pass = 0; pass < p.n_pass; pass++) {
+            uint32_t s_p;
+            uint64_t cpass;
+            pass_offsets(pass, s_p, cpass);
+            cpass += cbase;
+            // butterfly reduce-scatter over the summed lane bits of wires 0/1, then all-reduce
+            auto flat = acc[pass];
             std::vector<uint32_t> base(T, 0);
-            std::vector<bool> writer(T, true);
+            std::vector<bool> owner(T, true);
             for (uint32_t k = 0; k < LM && k < nb; k++) {
                 const uint32_t mask = 1u << (b0 + k), half = M >> (k + 1);
                 if (mask >= 32) return "shuffle beyond a warp";
                 auto next = flat;
                 for (uint32_t tid = 0; tid < T; tid++) {
-                    const bool hi = (tid & mask) != 0, phi = !hi;
+                    const bool hi = (tid & mask) != 0;
                     const uint32_t q = tid ^ mask;
                     for (uint32_t i = 0; i < half; i++) {
-                        const cf send_q = phi ? flat[q][i] : flat[q][i + half];
+                        const cf send_q = !hi ? flat[q][i] : flat[q][i + half];
                         next[tid][i] = (hi ? flat[tid][i + half] : flat[tid][i]) + send_q;
                     }
                     if (hi) base[tid] += half;
@@ -196,24 +183,53 @@ static std::string emulate(const StepDesc &d, const StreamStep &p, std::mt19937 
                 auto next = flat;
                 for (uint32_t tid = 0; tid < T; tid++) {
                     next[tid][0] = flat[tid][0] + flat[tid ^ mask][0];
-                    if (tid & mask) writer[tid] = false;
+                    if (tid & mask) owner[tid] = false;
                 }
                 flat = next;
             }
+            const uint32_t n_out = 1u << (2 * p.n_dout);
+            std::vector<cf> ostage(p.staged ? n_out : 0, cf(0.f, 0.f));
+            std::vector<int> staged_hits(p.staged ? n_out : 0, 0);
             for (uint32_t tid = 0; tid < T; tid++) {
-                if (!writer[tid]) continue;
-                uint32_t c_lo = 0;
+                if (!owner[tid]) continue;
+                uint32_t c_lo = 0, st_lo = 0;
                 for (int w = 0; w < 4; w++)
-                    if (!p.lo_summed[w]) c_lo += ((tid >> (2 * w)) & 3u) << (2 * p.lo_other[w]);
+                    if (!p.lo_summed[w]) {
+                        const uint32_t dg = (tid >> (2 * w)) & 3u;
+                        c_lo += dg << (2 * p.lo_other[w]);
+                        st_lo += dg << (2 * p.lo_rank[w]);
+                    }
                 for (uint32_t j = 0; j < m_left; j++) {
                     const uint32_t idx = base[tid] + j, gg = idx / NSF, f = idx % NSF;
                     if (idx >= M) return "reduce-scatter index";
-                    uint64_t coff = cbase + c_lo;
-                    for (uint32_t jj = 0; jj < p.go; jj++) coff += (uint64_t) ((gg >> (2 * jj)) & 3u) << (2 * p.g_cd[jj]);
-                    for (uint32_t jj = 0; jj < p.nsf; jj++) coff += (uint64_t) ((f >> (2 * jj)) & 3u) << (2 * p.sf_cd[jj]);
+                    if (p.staged) {
+                        uint32_t u = st_lo;
+                        for (uint32_t jj = 0; jj < p.go; jj++) u += ((gg >> (2 * jj)) & 3u) << (2 * p.g_rank[jj]);
+                        for (uint32_t jj = 0; jj < p.nsfp; jj++) u += ((f >> (2 * jj)) & 3u) << (2 * p.sf_rank[jj]);
+                        if (u >= n_out) return "staging index";
+                        ostage[u] += flat[tid][j];
+                        staged_hits[u]++;
+                    } else {
+                        uint64_t coff = cpass + c_lo;
+                        for (uint32_t jj = 0; jj < p.go; jj++) coff += (uint64_t) ((gg >> (2 * jj)) & 3u) << (2 * p.g_cd[jj]);
+                        for (uint32_t jj = 0; jj < p.nsfp; jj++) coff += (uint64_t) ((f >> (2 * jj)) & 3u) << (2 * p.sf_cd[jj]);
+                        if (coff >= nC) return "C index";
+                        written[coff]++;
+                        C[coff] = flat[tid][j];
+                    }
+                }
+            }
+            if (p.staged) {
+                const uint32_t expect = p.klo_mode == 2 ? 1u << (2 * (p.n_klo - nb / 2)) : 1u;
+                for (uint32_t u = 0; u < n_out; u++)
+                    if ((uint32_t) staged_hits[u] != expect) return "staging coverage";
+                for (uint32_t u = 0; u < n_out; u++) {
+                    uint64_t coff = cpass;
+                    for (uint32_t r = 0; r < p.n_dout; r++) coff += (uint64_t) ((u >> (2 * r)) & 3u) << (2 * p.dout_cd[r]);
+                    if (p.out_run >= 1 && (u & 1u) == 0 && (coff & 1u)) return "16-byte store alignment";
                     if (coff >= nC) return "C index";
                     written[coff]++;
-                    C[coff] = flat[tid][j];
+                    C[coff] = ostage[u];
                 }
             }
         }

@@ -50,8 +50,16 @@ SHAPES = [(12, 3, 2), (3, 12, 2), (12, 4, 3), (4, 12, 3), (12, 1, 1), (1, 12, 1)
           (11, 5, 4), (10, 6, 5), (2, 12, 1)]
 
 
-@pytest.mark.parametrize("shape", SHAPES, ids=[f"{a}x{b}k{k}" for a, b, k in SHAPES])
-@pytest.mark.parametrize("shuffle_c", [False, True], ids=["contractnodes-order", "any-order"])
+# wide shapes whose ContractNodes order takes the tiled or tensor-core kernel;
+# with C's digits in another order they stream too -- among them small
+# operands with 16 or 64 free indices (several passes over a tile) and outputs
+# staged through shared memory
+SHAPES_ANY_ORDER = [(12, 5, 2), (3, 12, 1), (12, 4, 1), (4, 12, 2), (5, 11, 2), (11, 6, 3)]
+CASES = [(s, False) for s in SHAPES] + [(s, True) for s in SHAPES + SHAPES_ANY_ORDER]
+
+
+@pytest.mark.parametrize("shape,shuffle_c", CASES,
+                         ids=[f"{a}x{b}k{k}-{'any' if sh else 'cn'}" for (a, b, k), sh in CASES])
 def test_streaming_contraction_matches_complex128(ctx, shape, shuffle_c):
     ra, rb, nsum = shape
     rng = np.random.default_rng(ra * 100 + rb * 10 + nsum + (7 if shuffle_c else 0))
