@@ -188,16 +188,23 @@ qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const v
         dev_free(ctx, scratch);   // stream-ordered: the next user of the block runs after these kernels
         return cuda_error(ctx, e, "reduction launch");
     }
-    // Dense steps of two large operands take the tensor cores (gemm_tc.cu),
-    // wide ones the tiled kernel; the other complex64 steps with one small
-    // operand stream the large one (stream.cu).  Both TMA-fed kernels report
-    // pipeline timeouts through a device flag: the caller's, read once after
-    // its last step, or one checked here.
+    // Complex64 steps with one small operand stream the large one (stream.cu)
+    // unless the tiled or tensor-core kernel does better for the shape:
+    // measured per shape, the streaming kernel wins whenever it is the only
+    // candidate (1.5-5.7x the pair kernel), and among wide or GEMM-shaped steps
+    // when the large operand is A -- C's low digits are then its free wires and
+    // the owning lanes store consecutive elements -- except with exactly 16
+    // free indices of the small operand; when the large operand is B the
+    // tiled kernel's output tiles store better.  Dense steps of two large
+    // operands take the tensor cores (gemm_tc.cu), other wide ones the tiled
+    // kernel.  The TMA-fed kernels report pipeline timeouts through a device
+    // flag: the caller's, read once after its last step, or one checked here.
     StreamStep sp;
-    const bool first = stream_first();
-    const bool use_gemm = !f64 && tensor_cores_enabled() && gemm_eligible(d) && !(first && stream_plan(d, sp));
-    const bool use_stream =
-        !f64 && !use_gemm && (first || !tiled_shaped(d)) && stream_enabled() && stream_plan(d, sp);
+    const bool can_stream = !f64 && stream_enabled() && stream_plan(d, sp);
+    const bool gemm_ok = !f64 && tensor_cores_enabled() && gemm_eligible(d);
+    const bool use_stream = can_stream && (stream_first() || (!sp.l_is_b && sp.nsf != 2) ||
+                                           (!gemm_ok && !tiled_shaped(d)));
+    const bool use_gemm = !use_stream && gemm_ok;
     if (use_stream || use_gemm) {
         void *scratch = nullptr, *flag = gemm_flag;
         qt_status s = QT_OK;

@@ -574,14 +574,11 @@ bool stream_plan(const StepDesc &d, StreamStep &p) {
     uint32_t run = 0;
     while ((int) run < nd && p.dout_cd[run] == run) run++;
     p.out_run = run;
-    // Direct stores from the owning lanes coalesce when C's digit 0 is one of
-    // the free lane digits (wires 0/1): consecutive lanes then write
-    // consecutive elements.  Otherwise -- and whenever summed wires 2/3 spread
-    // a sum over warps -- the outputs go through shared memory.
-    bool lane_digit0 = false;
-    for (int w = 0; w < 2; w++)
-        if (!summed[w] && cdig[w] == 0) lane_digit0 = true;
-    p.staged = (p.klo_mode == 2 || !lane_digit0) ? 1u : 0u;
+    // Sums that summed wires 2/3 spread over warps meet in shared memory;
+    // every other output is stored by the lane that owns it (staging those
+    // too, for better-coalesced stores, measured slower: two consumer barriers
+    // per tile cost more than the partly coalesced stores save).
+    p.staged = p.klo_mode == 2 ? 1u : 0u;
     if (p.staged && (1u << (2 * nd)) > kStreamMaxOut) return false;
     uint32_t off[5];
     stream_layout(p, off);

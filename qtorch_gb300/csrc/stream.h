@@ -55,8 +55,8 @@ struct StreamStep {
     uint32_t n_run_d;              // in-tile digits above the run (bulk-copy index digits)
     uint32_t n_dout, n_klo;        // output digits of a pass; summed wires among 0-3
     uint32_t klo_mode;             // 0: no summed wire among 0-3, 1: only wires 0/1 (shuffles), 2: wires 2/3 too
-    uint32_t staged;               // 1: outputs go through shared memory (summed wires 2/3, or
-                                   // C's digit 0 not among a warp's lane digits), 0: stored directly
+    uint32_t staged;               // 1: outputs go through shared memory (summed wires 2/3), 0: stored
+                                   // by the owning lanes
     uint32_t out_run;              // low staged digits that are C's digits 0, 1, ... in order
     uint32_t smem_bytes;
     uint32_t l_is_b;               // the large operand is B (else A)
