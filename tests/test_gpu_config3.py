@@ -4,8 +4,8 @@ ParallelContract, src/ContractionTools.h:219-388, with a fixed seed) reaches a
 qTorch rank-13 or rank-14 intermediate -- 2^26 or 2^28 complex elements, the
 "rank 26-28" of dimension-2 legs.  Such plans exceed the grouped interpreter
 and run step by step; their large complex64 steps, a rank 11-14 tensor met by
-a gate-sized one, take the HBM-streaming, tiled or tcgen05 tensor-core
-kernels.  FP64 must equal the oracle's replay of the same sequence bit for
+a gate-sized one, are bound by HBM bandwidth and take the streaming kernel
+(or the tiled kernel).  FP64 must equal the oracle's replay of the same sequence bit for
 bit; the mixed form must stay within 1e-6 of FP64, on values far from zero."""
 import pytest
 
@@ -28,10 +28,9 @@ def test_rank13_term_fp64_bit_exact_and_mixed_within_tolerance(ctx):
     plan = qg.Plan(q, m, ordering="stochastic", seed=11, ctx=ctx)
     assert plan.peak_rank == 13
     v64 = plan.execute(qg.FP64)
-    tc0, st0 = ctx.tensor_core_steps, ctx.stream_steps
+    st0 = ctx.stream_steps
     vmx = plan.execute(qg.MIXED)
-    assert ctx.tensor_core_steps > tc0, "no step of the rank-13 term ran on the tensor cores"
-    assert ctx.stream_steps > st0, "no step of the rank-13 term ran on the streaming kernel"
+    assert ctx.stream_steps >= st0 + 3, "the rank 11-13 steps did not take the streaming kernel"
     v_or, flops = port.replay_value(q, m, plan.sequence())
     assert flops == plan.flops
     assert v64 == v_or
@@ -45,9 +44,9 @@ def test_rank14_terms_mixed_within_tolerance(ctx, edge, seed):
     plan = qg.Plan(q, m, ordering="stochastic", seed=seed, ctx=ctx)
     assert plan.peak_rank == 14
     v64 = plan.execute(qg.FP64)
-    tc0 = ctx.tensor_core_steps
+    st0 = ctx.stream_steps
     vmx = plan.execute(qg.MIXED)
-    assert ctx.tensor_core_steps > tc0
+    assert ctx.stream_steps >= st0 + 3
     assert abs(v64) > 1e-3
     assert abs(vmx - v64) <= MIXED_TOL
     # a second run gives the same value (no state left behind by the first)
