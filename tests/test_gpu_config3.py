@@ -46,7 +46,7 @@ def test_rank14_terms_mixed_within_tolerance(ctx, edge, seed):
     v64 = plan.execute(qg.FP64)
     st0 = ctx.stream_steps
     vmx = plan.execute(qg.MIXED)
-    assert ctx.stream_steps >= st0 + 3
+    assert ctx.stream_steps >= st0 + 2
     assert abs(v64) > 1e-3
     assert abs(vmx - v64) <= MIXED_TOL
     # a second run gives the same value (no state left behind by the first)
