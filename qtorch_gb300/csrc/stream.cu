@@ -101,7 +101,7 @@ __host__ __device__ inline void stream_layout(const StreamStep &p, uint32_t off[
     off[2] = off[1] + round128(8u * staged);                     // S
     off[3] = off[2] + round128(8u * p.s_elems);                  // full[stages], empty[stages], issued count,
                                                                  // C offsets and staged indices of (g, f)
-    off[4] = off[3] + round128(16u * kStreamStages + 8u + 12u * kStreamMaxStage);   // end
+    off[4] = off[3] + round128(16u * kStreamStages + 8u + 20u * kStreamMaxStage);   // end
 }
 
 // producer warp: the bulk copies of (item, chunk) into tile buffer `dst`
@@ -143,11 +143,12 @@ __device__ __forceinline__ uint32_t staged_index(const StreamStep &p, uint32_t g
     return o;
 }
 
-// the register-heaviest classes (16 sums per thread over 4 or 16 summed
-// combinations) run one CTA per SM instead of spilling at two
+// Two CTAs per SM for every class but 4 g x 4 S-free sums over 4 summed
+// combinations, which runs one CTA per SM instead of spilling (measured faster
+// than looping its g digit over work items at two); 16 S-free sums keep
+// their element loop rolled and fit two.
 template <int NSF, int G, int H>
-constexpr int stream_min_ctas() { return NSF * G >= 16 && H >= 4 ? 1 : 2; }
-
+constexpr int stream_min_ctas() { return NSF == 4 && G == 4 && H == 4 ? 1 : 2; }
 template <int NSF, int G, int H>
 __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
     stream_kernel(const __grid_constant__ StreamStep p) {
@@ -167,6 +168,8 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
     uint32_t *const issued_slot = reinterpret_cast<uint32_t *>(empty + NS);
     uint64_t *const out_off = reinterpret_cast<uint64_t *>(empty + NS + 1);      // [M]
     uint32_t *const st_gf = reinterpret_cast<uint32_t *>(out_off + kStreamMaxStage);   // [M]
+    uint32_t *const eo_s = st_gf + kStreamMaxStage;     // [E]: element offsets for the rolled loop
+    uint32_t *const so_s = eo_s + kStreamMaxStage;      // [E]
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
     const uint32_t n_out = 1u << (2 * p.n_dout);
 
@@ -252,6 +255,22 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
                 for (uint32_t j = 0; j < p.nsfp; j++) o += (((uint32_t) f >> (2 * j)) & 3u) << (2 * p.sf_w[j]);
             sfo[f] = o;
         }
+        // with 16 free indices of S the element loop stays rolled (its body
+        // is 64 FMAs already): the offsets then come from shared memory
+        // (G == 1 there, so element tid is h digit combination tid)
+        if constexpr (NSF >= 16) {
+            if (tid < (uint32_t) E) {
+                uint32_t th = 0, sh = 0;
+                for (uint32_t j = 0; j < p.ho; j++) {
+                    const uint32_t dg = (tid >> (2 * j)) & 3u;
+                    th += dg << (2 * p.h_pos[j]);
+                    sh += dg << (2 * p.h_sw[j]);
+                }
+                eo_s[tid] = th;
+                so_s[tid] = sh;
+            }
+            asm volatile("bar.sync 1, %0;" ::"r"(kStreamThreads) : "memory");
+        }
         // the summed lane bits among wires 0/1 are consecutive: 0-1, 2-3 or 0-3
         const uint32_t b0 = p.lo_summed[0] ? 0u : 2u;
         const uint32_t nb = 2u * (p.lo_summed[0] + p.lo_summed[1]);
@@ -291,11 +310,22 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
                         for (int f = 0; f < NSF; f++) acc[g][f] = make_float2(0.f, 0.f);
                 }
                 const float2 *Sp = S + s_p;
+                if constexpr (NSF >= 16) {
+                    // G == 1 here: every element adds into acc[0]
+#pragma unroll 1
+                    for (int i = 0; i < E; i++) {
+                        const float2 x = T[eo_s[i]];
+                        const float2 *Si = Sp + so_s[i];
 #pragma unroll
-                for (int i = 0; i < E; i++) {
-                    const float2 x = T[eo[i]];
+                        for (int f = 0; f < NSF; f++) cmac(acc[0][f], x, Si[sfo[f]]);
+                    }
+                } else {
 #pragma unroll
-                    for (int f = 0; f < NSF; f++) cmac(acc[i / H][f], x, Sp[so[i] + sfo[f]]);
+                    for (int i = 0; i < E; i++) {
+                        const float2 x = T[eo[i]];
+#pragma unroll
+                        for (int f = 0; f < NSF; f++) cmac(acc[i / H][f], x, Sp[so[i] + sfo[f]]);
+                    }
                 }
                 if (pass + 1 == p.n_pass) {
                     __syncwarp();
@@ -508,6 +538,9 @@ bool stream_plan(const StepDesc &d, StreamStep &p) {
     const int ho = std::min(n_hi, 2);
     int go = std::min(n_outer, 2 - ho);
     while (go > 0 && (1 << (2 * (go + (int) p.nsfp))) > (int) kStreamMaxStage) go--;
+    // 16 sums over 16 elements (free and summed looped digits together) need
+    // more registers than two CTAs per SM leave: loop the free digit over work
+    // items instead
     if (n_outer - go > 15 || n_hi - ho > 15) return false;
     if (p.n_pass > 1 && n_hi > ho) return false;   // several passes keep no sums across chunks
     p.go = (uint32_t) go;
