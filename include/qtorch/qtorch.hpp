@@ -113,6 +113,10 @@ public:
     bool mSelectedInCostContractionAlgorithm{false};
 
     explicit Node(int rank);
+    // a node whose values come later: a contraction's result, adopted from the
+    // device, or a node of a symbolic network (no host array of 4^rank values)
+    struct NoData {};
+    Node(int rank, NoData);
     virtual ~Node();
     Node(const Node &) = delete;
     Node &operator=(const Node &) = delete;
@@ -284,6 +288,29 @@ struct PreProcessResult {
 };
 bool preProcess(const std::string &qasmText, const std::string &measureText, const std::string &gateDir,
                 uint64_t seed, int tries, long long maxMacs, PreProcessResult &best);
+
+// ---- Size-greedy ordering (no reference counterpart) ------------------------
+// For networks too large for the line graph's min-fill walk (circuits of
+// 20-30 qubits and depth 8-20 make line graphs of 10^3-10^4 wires): pairs of
+// nodes that share a wire are merged in order of the size change the merge
+// causes, 4^rank(C) - 4^rank(A) - 4^rank(B), so merges that shrink the network
+// (a trace into the gate before it, a one-qubit gate into its neighbour) come
+// first and growth is postponed.  Try 0 is deterministic; tries 1.. add seeded
+// noise to the scores; the try with the smallest largest intermediate, then the
+// fewest MACs, is kept and replayed on `net` with ContractNodes.  Leftover
+// rank-0 nodes of unconnected groups are multiplied in list order, as
+// LGContract does.
+struct GreedyResult {
+    int peakRank = 0;
+    double macs = 0;        // complex MACs
+    int height = 0;         // height of the contraction tree
+    int tries = 0;
+};
+GreedyResult GreedyContract(Network &net, uint64_t seed, int tries);
+// The planner's default for requests of any size: the greedy walk, and for line
+// graphs of at most maxMinFillWires wires also the min-fill walk, the better by
+// largest intermediate and estimated GPU time.
+GreedyResult AutoContract(std::shared_ptr<Network> net, uint64_t seed, int tries, int maxMinFillWires);
 
 // ---- LineGraph (src/LineGraph.h:28-85) -------------------------------------
 // The reference asks the closed QuickBB binary for an elimination order; this

@@ -136,7 +136,11 @@ qt_status qt_contract_pair_host(qt_ctx *ctx, const double *a, int rank_a, const 
 typedef enum qt_ordering {
     QT_ORDER_STOCHASTIC = 0,   /* ContractionTools::ParallelContract (ContractionTools.h:219-388), seeded */
     QT_ORDER_LINEGRAPH = 1,    /* LineGraph + min-fill elimination order (LineGraph.h:92-171, 357-376) */
-    QT_ORDER_SEQUENCE = 2      /* ContractGivenSequence (ContractionTools.h:392-411) */
+    QT_ORDER_SEQUENCE = 2,     /* ContractGivenSequence (ContractionTools.h:392-411) */
+    QT_ORDER_GREEDY = 3,       /* size-greedy pairwise merges, best of 32 seeded tries (no reference
+                                  counterpart: networks too large for min-fill) */
+    QT_ORDER_AUTO = 4          /* QT_ORDER_GREEDY, or the line graph's min-fill walk where the line
+                                  graph has <= 1500 wires and that walk is better */
 } qt_ordering;
 
 /* Network(qasm, measure) from text (Network.h:148-151, 246-304).  gate_dir
@@ -281,7 +285,8 @@ int qt_plan_step_info(const qt_plan *plan, qt_precision prec, int32_t *out, int 
  * when max_cuts do not get there).  ctx may be NULL to inspect the slicing
  * only.  qt_sliced_execute sums the slices' values in assignment order
  * (complex128); instances above 2^24 complex MACs run step by step one at a
- * time, so the device holds one sliced workspace. */
+ * time, so the device holds one sliced workspace; more than 4096 slices run
+ * in chunks of 4096 (one batch each, built per call). */
 typedef struct qt_sliced qt_sliced;
 qt_status qt_plan_slice(qt_ctx *ctx, const qt_plan *plan, qt_precision prec, uint64_t max_workspace_bytes,
                         int max_cuts, qt_sliced **out);
@@ -457,11 +462,17 @@ int64_t qt_random_regular_graph(int num_nodes, int degree, uint64_t seed, char *
  * memory budget and a slot is free, and runs every admitted request in grouped
  * launches; requests that arrive while others run join the next launch.  A
  * request whose workspace exceeds the whole budget is sliced at submission
- * (qt_plan_slice, up to 8 cut wires, cached in the plan) so that one slice
- * fits, and runs alone, slice by slice; QT_ERR_OUT_OF_MEMORY when no such
- * slicing exists. */
+ * (qt_plan_slice, up to 16 cut wires, cached in the plan) so that one slice
+ * fits, and runs alone, slice by slice (in chunks of 4096 slices);
+ * QT_ERR_OUT_OF_MEMORY when no such slicing exists.  With a work cap
+ * (qt_server_set_max_macs) a request whose complex MACs -- over all its slices
+ * -- exceed the cap is refused at submission with QT_ERR_REFUSED. */
 qt_status qt_server_create(qt_ctx *ctx, int max_inflight, qt_precision prec, qt_server **out);
 qt_status qt_server_free(qt_server *s);
+/* The work cap of one request in complex MACs (0: none, the default). */
+qt_status qt_server_set_max_macs(qt_server *s, int64_t max_macs);
+/* Submissions refused so far (work cap, budget without a fitting slicing). */
+int64_t qt_server_refused(qt_server *s);
 /* Submit (non-blocking).  *ticket identifies the request. */
 qt_status qt_server_submit(qt_server *s, qt_plan *plan, const double *leaves, int64_t *ticket);
 /* Poll: 1 = done (value written), 0 = pending, <0 = error (status negated). */

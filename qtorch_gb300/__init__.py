@@ -31,7 +31,7 @@ __all__ = [
 FP64 = 0
 MIXED = 1
 Stochastic = 0
-ORDER_STOCHASTIC, ORDER_LINEGRAPH, ORDER_SEQUENCE = 0, 1, 2
+ORDER_STOCHASTIC, ORDER_LINEGRAPH, ORDER_SEQUENCE, ORDER_GREEDY, ORDER_AUTO = 0, 1, 2, 3, 4
 
 
 class QtError(RuntimeError):
@@ -431,7 +431,8 @@ class LineGraph:
         return True
 
 
-_ORDER_NAMES = {"stochastic": ORDER_STOCHASTIC, "linegraph": ORDER_LINEGRAPH, "sequence": ORDER_SEQUENCE}
+_ORDER_NAMES = {"stochastic": ORDER_STOCHASTIC, "linegraph": ORDER_LINEGRAPH, "sequence": ORDER_SEQUENCE,
+                "greedy": ORDER_GREEDY, "auto": ORDER_AUTO}
 
 
 class Plan(_Owned):
@@ -443,7 +444,9 @@ class Plan(_Owned):
     def __init__(self, qasm_text, measure_text="", ordering="linegraph", seed=0, sequence=None, gate_dir=None,
                  ctx=None, symbolic=False, tries=100, max_macs=0):
         """ordering: "linegraph", "stochastic" (seeded), "sequence" (recorded
-        node-id pairs) or "search" -- the preProcess-style search
+        node-id pairs), "greedy" (size-greedy merges, best of 32 seeded tries:
+        for networks too large for min-fill), "auto" (greedy, or min-fill where
+        the line graph is small and its walk is better) or "search" -- the preProcess-style search
         (qt_plan_build_search): `tries` seeded stochastic orderings from `seed`,
         the one with the smallest largest intermediate, then fewest MACs, kept
         (its seed in `chosen_seed`)."""
@@ -716,13 +719,20 @@ class Server(_Owned):
     _free_name = "qt_server_free"
     _release_rank = 0
 
-    def __init__(self, max_inflight=64, precision=FP64, ctx=None):
+    def __init__(self, max_inflight=64, precision=FP64, ctx=None, max_macs=0):
+        """max_macs > 0: requests of more complex MACs (over all slices) are
+        refused at submission (submit raises Refused)."""
         self.ctx = ctx or default_context()
         h = ctypes.c_void_p()
         _check(_lib().qt_server_create(self.ctx.handle, max_inflight, precision, ctypes.byref(h)), self.ctx)
         self.handle = h.value
         self._keep = []
         self._register(self.ctx)
+        if max_macs:
+            self.set_max_macs(max_macs)
+
+    def set_max_macs(self, max_macs):
+        _check(_lib().qt_server_set_max_macs(self.handle, int(max_macs)), self.ctx)
 
     def close(self):
         self._release()
@@ -757,7 +767,8 @@ class Server(_Owned):
         _check(_lib().qt_server_wave_stats(self.handle, ctypes.byref(waves), ctypes.byref(reqs), ctypes.byref(secs)),
                self.ctx)
         return {"p50_s": p50.value, "p99_s": p99.value, "completed": done.value, "launches": launches.value,
-                "waves": waves.value, "wave_requests": reqs.value, "lane_seconds": secs.value}
+                "waves": waves.value, "wave_requests": reqs.value, "lane_seconds": secs.value,
+                "refused": int(_lib().qt_server_refused(self.handle))}
 
 
 def qaoa_num_edges(dgf_text):

@@ -302,6 +302,10 @@ qt_status qt_plan_build(qt_ctx *ctx, const char *qasm_text, const char *measure_
         } else if (ordering == QT_ORDER_LINEGRAPH) {
             qtorch::LineGraph lg(net);
             lg.LGContract();
+        } else if (ordering == QT_ORDER_GREEDY) {
+            qtorch::GreedyContract(*net, seed, 32);
+        } else if (ordering == QT_ORDER_AUTO) {
+            qtorch::AutoContract(net, seed, 32, 1500);
         } else if (ordering == QT_ORDER_SEQUENCE) {
             if (n_pairs < 0 || (n_pairs && !pairs)) return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "sequence");
             std::vector<std::pair<int, int>> seq(n_pairs);

@@ -208,6 +208,11 @@ Node::Node(int rank) : mRank(rank) {
     mVals.assign((size_t) 1 << (2 * rank), std::complex<double>(0.0));
 }
 
+Node::Node(int rank, NoData) : mRank(rank) {
+    if (rank < 0 || rank > qtg::kMaxWires) throw InvalidFunctionInput();
+    mHostValid = false;
+}
+
 Node::~Node() {
     if (mDevice && mCtx) qt_tensor_free(mCtx, mDevice);
 }
@@ -594,7 +599,7 @@ std::shared_ptr<Node> Network::ContractNodes(std::shared_ptr<Node> nodeA, std::s
     std::vector<std::pair<int, int>> pairs(indicesA.size());
     for (size_t k = 0; k < indicesA.size(); k++) pairs[k] = {indicesA[k], indicesB[k]};
 
-    auto nodeC = std::make_shared<Node>((int) indicesC.size());
+    auto nodeC = std::make_shared<Node>((int) indicesC.size(), Node::NoData{});
     nodeC->mTensorId = mNextTensorId++;
     for (auto &w : remaining) {
         nodeC->GetWires().push_back(w);

@@ -20,6 +20,8 @@
 #include <fstream>
 #include <functional>
 #include <map>
+#include <queue>
+#include <random>
 #include <set>
 #include <sstream>
 
@@ -648,6 +650,243 @@ bool preProcess(const std::string &qasmText, const std::string &measureText, con
         if (maxMacs > 0 && macs <= maxMacs) break;
     }
     return found;
+}
+
+// ---- size-greedy ordering --------------------------------------------------
+
+namespace {
+
+struct GreedyWalk {
+    std::vector<std::pair<int, int>> merges;   // node indices: 0..n-1 the leaves, n+k the k-th merge
+    int peak = 0;
+    double macs = 0;
+    int height = 0;
+};
+
+// One greedy walk over the abstract network: wires of each node (sorted),
+// ends of each wire.  temperature 0: the plain size-change order; > 0: each
+// score gets seeded Gumbel noise scaled by the larger operand's size.
+GreedyWalk greedy_walk(std::vector<std::vector<int>> nw, std::vector<std::array<int, 2>> we, double temperature,
+                       uint64_t seed) {
+    const int n0 = (int) nw.size();
+    std::vector<int> height(n0, 0);
+    std::vector<char> alive(n0, 1);
+    std::mt19937_64 gen(seed);
+    std::uniform_real_distribution<double> uni(1e-12, 1.0);
+    auto p4 = [](int r) { return std::ldexp(1.0, 2 * r); };
+    struct Cand {
+        double key;
+        int a, b;
+        bool operator<(const Cand &o) const {   // min-heap on key, then indices
+            if (key != o.key) return key > o.key;
+            if (a != o.a) return a > o.a;
+            return b > o.b;
+        }
+    };
+    std::priority_queue<Cand> heap;
+    std::vector<int> scratch;
+    // rank of the merge of a and b: wires in exactly one of them
+    auto merged_rank = [&](int a, int b, int &shared) {
+        const auto &x = nw[a], &y = nw[b];
+        size_t i = 0, j = 0;
+        int common = 0;
+        while (i < x.size() && j < y.size()) {
+            if (x[i] == y[j]) {
+                common++;
+                i++;
+                j++;
+            } else if (x[i] < y[j]) {
+                i++;
+            } else {
+                j++;
+            }
+        }
+        shared = common;
+        return (int) (x.size() + y.size()) - 2 * common;
+    };
+    auto push = [&](int a, int b) {
+        if (a == b || !alive[a] || !alive[b]) return;
+        int shared = 0;
+        const int rc = merged_rank(a, b, shared);
+        const int ra = (int) nw[a].size(), rb = (int) nw[b].size();
+        double key = p4(rc) - p4(ra) - p4(rb);
+        if (temperature > 0) key -= temperature * p4(std::max(ra, rb)) * -std::log(-std::log(uni(gen)));
+        heap.push({key, std::min(a, b), std::max(a, b)});
+    };
+    for (size_t w = 0; w < we.size(); w++) push(we[w][0], we[w][1]);
+    GreedyWalk out;
+    while (!heap.empty()) {
+        const Cand c = heap.top();
+        heap.pop();
+        if (!alive[c.a] || !alive[c.b]) continue;
+        const int k = (int) nw.size();
+        scratch.clear();
+        int shared = 0;
+        {
+            const auto &x = nw[c.a], &y = nw[c.b];
+            size_t i = 0, j = 0;
+            while (i < x.size() || j < y.size()) {
+                if (j == y.size() || (i < x.size() && x[i] < y[j])) {
+                    scratch.push_back(x[i++]);
+                } else if (i == x.size() || y[j] < x[i]) {
+                    scratch.push_back(y[j++]);
+                } else {
+                    shared++;
+                    i++;
+                    j++;
+                }
+            }
+        }
+        nw.push_back(scratch);
+        alive.push_back(1);
+        alive[c.a] = alive[c.b] = 0;
+        height.push_back(std::max(height[c.a], height[c.b]) + 1);
+        for (int w : nw[k])
+            for (int s = 0; s < 2; s++)
+                if (we[w][s] == c.a || we[w][s] == c.b) we[w][s] = k;
+        out.merges.push_back({c.a, c.b});
+        out.peak = std::max(out.peak, (int) nw[k].size());
+        out.macs += p4((int) nw[k].size() + shared);
+        out.height = std::max(out.height, height[k]);
+        nw[c.a].clear();
+        nw[c.b].clear();
+        nw[c.a].shrink_to_fit();
+        nw[c.b].shrink_to_fit();
+        for (int w : nw[k]) {
+            const int other = we[w][0] == k ? we[w][1] : we[w][0];
+            push(k, other);
+        }
+    }
+    return out;
+}
+
+// The uncontracted nodes as an abstract graph: wires of each node (sorted
+// ids), the two nodes of each wire.  Wire ids are given in first-seen order
+// over the nodes and their wires, as LineGraph::Build numbers them.
+void abstract_network(const Network &net, std::vector<std::vector<int>> &nw, std::vector<std::array<int, 2>> &we) {
+    const auto &nodes = net.GetUncontractedNodes();
+    std::map<const Node *, int> index;
+    for (size_t i = 0; i < nodes.size(); i++) index[nodes[i].get()] = (int) i;
+    std::map<const Wire *, int> wire_id;
+    nw.assign(nodes.size(), {});
+    we.clear();
+    for (size_t i = 0; i < nodes.size(); i++) {
+        for (auto &w : nodes[i]->GetWires()) {
+            auto it = wire_id.find(w.get());
+            if (it == wire_id.end()) {
+                auto a = w->GetNodeA().lock(), b = w->GetNodeB().lock();
+                if (!a || !b || !index.count(a.get()) || !index.count(b.get())) throw ContractionFailure();
+                it = wire_id.emplace(w.get(), (int) we.size()).first;
+                we.push_back({index[a.get()], index[b.get()]});
+            }
+            nw[i].push_back(it->second);
+        }
+        std::sort(nw[i].begin(), nw[i].end());
+        nw[i].erase(std::unique(nw[i].begin(), nw[i].end()), nw[i].end());
+    }
+}
+
+GreedyWalk best_greedy_walk(const std::vector<std::vector<int>> &nw, const std::vector<std::array<int, 2>> &we,
+                            uint64_t seed, int tries) {
+    GreedyWalk best;
+    bool have = false;
+    for (int t = 0; t < tries; t++) {
+        // temperatures cycle over a few scales so that both small and large
+        // perturbations of the plain order are tried
+        static const double kTemps[4] = {0.02, 0.1, 0.3, 1.0};
+        const double temp = t == 0 ? 0.0 : kTemps[(t - 1) % 4];
+        GreedyWalk g = greedy_walk(nw, we, temp, seed * 0x9e3779b97f4a7c15ull + (uint64_t) t);
+        if (!have || g.peak < best.peak || (g.peak == best.peak && g.macs < best.macs)) {
+            best = std::move(g);
+            have = true;
+        }
+    }
+    return best;
+}
+
+// Replays merges (indices as in GreedyWalk) on the network, then multiplies
+// leftover rank-0 nodes of unconnected groups in list order.
+void replay_merges(Network &net, const std::vector<std::pair<int, int>> &merges) {
+    std::vector<std::shared_ptr<Node>> nodes = net.GetUncontractedNodes();
+    for (const auto &m : merges) {
+        auto c = net.ContractNodes(nodes[m.first], nodes[m.second], 100);
+        if (!c) {
+            if (net.IsDone()) return;   // the merge that finished the network
+            throw ContractionFailure();
+        }
+        nodes.push_back(c);
+    }
+    while (net.GetUncontractedNodes().size() > 1) {
+        const auto &rem = net.GetUncontractedNodes();
+        bool all_scalar = true;
+        for (const auto &x : rem) all_scalar = all_scalar && x->mRank == 0;
+        if (!all_scalar) throw ContractionFailure();
+        net.ContractNodes(rem[0], rem[1], 100);
+    }
+}
+
+// The LGContract walk of a 1-based wire order over the abstract graph.
+GreedyWalk order_walk(const std::vector<int> &order1, const std::vector<std::vector<int>> &nw,
+                      const std::vector<std::array<int, 2>> &we) {
+    std::vector<std::array<int, 2>> ends(we.size());
+    for (size_t v = 0; v < we.size(); v++) ends[v] = we[v];
+    std::vector<int> order0;
+    for (int v : order1) order0.push_back(v - 1);
+    const WalkCost c = walk_cost(order0, ends, (int) nw.size());
+    GreedyWalk g;
+    g.peak = c.peak;
+    g.macs = c.macs;
+    g.height = c.height;
+    return g;
+}
+
+}  // namespace
+
+GreedyResult GreedyContract(Network &net, uint64_t seed, int tries) {
+    if (tries < 1) throw InvalidFunctionInput();
+    std::vector<std::vector<int>> nw;
+    std::vector<std::array<int, 2>> we;
+    abstract_network(net, nw, we);
+    GreedyWalk best = best_greedy_walk(nw, we, seed, tries);
+    GreedyResult r;
+    r.tries = tries;
+    r.peakRank = best.peak;
+    r.macs = best.macs;
+    r.height = best.height;
+    replay_merges(net, best.merges);
+    return r;
+}
+
+GreedyResult AutoContract(std::shared_ptr<Network> net, uint64_t seed, int tries, int maxMinFillWires) {
+    std::vector<std::vector<int>> nw;
+    std::vector<std::array<int, 2>> we;
+    abstract_network(*net, nw, we);
+    GreedyWalk g = best_greedy_walk(nw, we, seed, tries);
+    GreedyResult r;
+    r.tries = tries;
+    if ((int) we.size() <= maxMinFillWires) {
+        LineGraph lg(net);
+        const std::vector<int> order = lg.MinFillOrdering();
+        const GreedyWalk m = order_walk(order, nw, we);
+        // the GPU time estimate of the min-fill walk (1.5 us per dependent
+        // level, MACs at ~2e9 a second per CTA) decides unless the greedy walk
+        // keeps a smaller largest intermediate
+        auto est = [](const GreedyWalk &w) { return 1.5e-6 * w.height + w.macs / 2e9; };
+        const bool take_minfill = m.peak < g.peak || (m.peak == g.peak && est(m) <= est(g)) ||
+                                  (m.peak == g.peak + 1 && est(m) * 2 <= est(g));
+        if (take_minfill) {
+            r.peakRank = m.peak;
+            r.macs = m.macs;
+            r.height = m.height;
+            lg.LGContract(order);
+            return r;
+        }
+    }
+    r.peakRank = g.peak;
+    r.macs = g.macs;
+    r.height = g.height;
+    replay_merges(*net, g.merges);
+    return r;
 }
 
 }  // namespace qtorch

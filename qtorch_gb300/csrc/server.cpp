@@ -17,6 +17,7 @@
 // only ever touches its
 // own leaves and its CTA's workspace.
 #include <algorithm>
+#include <cmath>
 #include <condition_variable>
 #include <deque>
 #include <thread>
@@ -52,6 +53,8 @@ struct qt_server {
     qt_ctx *ctx = nullptr;                 // the caller's context (device, budget)
     int max_inflight = 64;
     qt_precision prec = QT_PREC_FP64;
+    int64_t max_macs = 0;                  // work cap of one request (complex MACs, all slices); 0: none
+    int64_t refused = 0;                   // submissions refused by the work cap or the budget
     std::mutex m;
     std::condition_variable cv;            // new work or a lane became free
     std::condition_variable done_cv;       // a request finished
@@ -78,6 +81,9 @@ struct qt_server {
 
 // slicings are cached in the plans, which several servers may share
 static std::mutex g_slicing_lock;
+// cut wires a request may be sliced over to fit the budget (4^16 slices, run
+// in chunks; the work cap bounds what that costs)
+constexpr int kServerMaxCuts = 16;
 
 // Lane 0 serves small requests only (a QAOA term is 1e4-3e5 complex MACs):
 // a mid-size request (a 12-14 qubit circuit, 1e6-1.6e7 MACs) takes one CTA
@@ -259,23 +265,39 @@ qt_status qt_server_submit(qt_server *s, qt_plan *plan, const double *leaves, in
     r.footprint = footprint(plan, s->prec);
     r.heavy = !plan->grouped || plan->flops > kLoneInstanceMaxMacs;
     r.small = !r.heavy && plan->flops <= kLaneZeroMaxMacs;
+    auto refuse = [&](qt_status st, const char *why) {
+        std::lock_guard<std::mutex> g(s->m);
+        s->refused++;
+        return set_error(s->ctx, st, why);
+    };
+    if (s->max_macs > 0 && plan->flops > s->max_macs) return refuse(QT_ERR_REFUSED, "request over the work cap");
     const uint64_t budget = s->ctx->memory_budget;
     if (budget && r.footprint > budget) {
         // larger than the whole budget: sliced so that one slice fits, run alone
         const uint64_t fixed = plan->leaf_bytes[s->prec] + 4096;
-        if (budget <= fixed) return set_error(s->ctx, QT_ERR_OUT_OF_MEMORY, "request larger than the budget");
+        if (budget <= fixed) return refuse(QT_ERR_OUT_OF_MEMORY, "request larger than the budget");
         const uint64_t target = budget - fixed;
-        std::lock_guard<std::mutex> g(g_slicing_lock);
-        for (auto &e : plan->slicings[s->prec])
-            if (e.first == target) r.sliced = e.second;
-        if (!r.sliced) {
-            qt_sliced *sl = nullptr;
-            qt_status st = qt_plan_slice(s->ctx, plan, s->prec, target, 8, &sl);
-            if (st != QT_OK) return set_error(s->ctx, st, "request larger than the budget, and no slicing fits it");
-            plan->slicings[s->prec].push_back({target, sl});
-            r.sliced = sl;
+        {
+            std::lock_guard<std::mutex> g(g_slicing_lock);
+            for (auto &e : plan->slicings[s->prec])
+                if (e.first == target) r.sliced = e.second;
+            if (!r.sliced) {
+                qt_sliced *sl = nullptr;
+                qt_status st = qt_plan_slice(s->ctx, plan, s->prec, target, kServerMaxCuts, &sl);
+                if (st != QT_OK) {
+                    std::lock_guard<std::mutex> g2(s->m);
+                    s->refused++;
+                    return set_error(s->ctx, st, "request larger than the budget, and no slicing fits it");
+                }
+                plan->slicings[s->prec].push_back({target, sl});
+                r.sliced = sl;
+            }
         }
-        r.footprint = qt_plan_workspace_bytes(qt_sliced_plan(r.sliced), s->prec) + fixed;
+        const qt_plan *sp = qt_sliced_plan(r.sliced);
+        const double total = (double) sp->flops * std::ldexp(1.0, 2 * qt_sliced_num_cuts(r.sliced));
+        if (s->max_macs > 0 && total > (double) s->max_macs)
+            return refuse(QT_ERR_REFUSED, "sliced request over the work cap");
+        r.footprint = qt_plan_workspace_bytes(sp, s->prec) + fixed;
         r.heavy = true;
         r.small = false;
     }
@@ -319,6 +341,19 @@ qt_status qt_server_wave_stats(qt_server *s, int64_t *waves, int64_t *requests, 
     if (requests) *requests = s->wave_requests;
     if (lane_seconds) *lane_seconds = s->wave_seconds;
     return QT_OK;
+}
+
+qt_status qt_server_set_max_macs(qt_server *s, int64_t max_macs) {
+    if (!s || max_macs < 0) return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->m);
+    s->max_macs = max_macs;
+    return QT_OK;
+}
+
+int64_t qt_server_refused(qt_server *s) {
+    if (!s) return -1;
+    std::lock_guard<std::mutex> g(s->m);
+    return s->refused;
 }
 
 qt_status qt_server_stats(qt_server *s, double *p50, double *p99, int64_t *completed, int64_t *launches) {

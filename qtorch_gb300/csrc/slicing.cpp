@@ -237,17 +237,22 @@ qt_plan *qt_sliced_plan(const qt_sliced *s) { return s ? s->plan : nullptr; }
 
 namespace {
 
-// A batch of every slice of `s` built from the uncut leaves `orig` (the
+// Slices per batch: a sliced plan with more assignments runs them in chunks of
+// this many (each chunk one batch), so the host and device hold the leaves of
+// at most this many slices at a time.
+constexpr uint64_t kSliceChunk = 4096;
+
+// A batch of slices a0 .. a1-1 of `s` built from the uncut leaves `orig` (the
 // plan's leaf order), on ctx.  stepwise_macs: instances above it run step by
 // step, one at a time.
-qt_status slice_batch(qt_ctx *ctx, const qt_sliced *s, const C *orig, int64_t stepwise_macs, qt_batch **out) {
-    const uint64_t n = 1ull << (2 * s->cuts.size());
+qt_status slice_batch(qt_ctx *ctx, const qt_sliced *s, const C *orig, int64_t stepwise_macs, uint64_t a0,
+                      uint64_t a1, qt_batch **out) {
     qt_batch *b = nullptr;
     qt_status st = qt_batch_create(ctx, &b);
     if (st != QT_OK) return st;
     b->stepwise_macs = stepwise_macs;
     const size_t n_leaves = s->orig_rank.size();
-    for (uint64_t a = 0; a < n && st == QT_OK; a++) {
+    for (uint64_t a = a0; a < a1 && st == QT_OK; a++) {
         std::vector<std::vector<int>> pos, val;
         cut_positions(s->cuts, a, n_leaves, pos, val);
         std::vector<C> leaves;
@@ -274,19 +279,35 @@ qt_status slice_batch(qt_ctx *ctx, const qt_sliced *s, const C *orig, int64_t st
     return QT_OK;
 }
 
-// the slices' values summed in assignment order
-qt_status sum_slices(qt_batch *b, uint64_t n, double *re_im) {
+// the values of a batch of n slices added, in assignment order, to re_im
+qt_status add_slices(qt_batch *b, uint64_t n, double *re_im) {
     std::vector<double> v(2 * n);
     qt_status st = qt_batch_run(b);
     if (st == QT_OK) st = qt_batch_fetch(b, v.data());
     if (st != QT_OK) return st;
-    double re = 0, im = 0;
     for (uint64_t a = 0; a < n; a++) {
-        re += v[2 * a];
-        im += v[2 * a + 1];
+        re_im[0] += v[2 * a];
+        re_im[1] += v[2 * a + 1];
     }
-    re_im[0] = re;
-    re_im[1] = im;
+    return QT_OK;
+}
+
+// every slice, chunk by chunk, summed in assignment order
+qt_status run_chunks(qt_ctx *ctx, const qt_sliced *s, const C *orig, int64_t stepwise_macs, qt_precision prec,
+                     double *re_im) {
+    const uint64_t n = 1ull << (2 * s->cuts.size());
+    double acc[2] = {0.0, 0.0};
+    for (uint64_t a0 = 0; a0 < n; a0 += kSliceChunk) {
+        const uint64_t a1 = std::min(n, a0 + kSliceChunk);
+        qt_batch *b = nullptr;
+        qt_status st = slice_batch(ctx, s, orig, stepwise_macs, a0, a1, &b);
+        if (st == QT_OK) st = qt_batch_prepare(b, prec);
+        if (st == QT_OK) st = add_slices(b, a1 - a0, acc);
+        if (b) qt_batch_free(b);
+        if (st != QT_OK) return st;
+    }
+    re_im[0] = acc[0];
+    re_im[1] = acc[1];
     return QT_OK;
 }
 
@@ -297,28 +318,26 @@ extern "C" {
 qt_status qt_sliced_execute(qt_sliced *s, qt_precision prec, double *re_im) {
     if (!s || !re_im || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return QT_ERR_INVALID_ARGUMENT;
     if (!s->ctx) return QT_ERR_INVALID_ARGUMENT;   // built for inspection only
+    const uint64_t n = 1ull << (2 * s->cuts.size());
+    // instances that are large for one CTA run step by step, one at a time
+    if (n > kSliceChunk) return run_chunks(s->ctx, s, s->orig_vals.data(), qtg::kLoneInstanceMaxMacs, prec, re_im);
     if (!s->batch || s->batch_prec != (int) prec) {
         if (s->batch) qt_batch_free(s->batch);
         s->batch = nullptr;
-        // instances that are large for one CTA run step by step, one at a time
-        qt_status st = slice_batch(s->ctx, s, s->orig_vals.data(), qtg::kLoneInstanceMaxMacs, &s->batch);
+        qt_status st = slice_batch(s->ctx, s, s->orig_vals.data(), qtg::kLoneInstanceMaxMacs, 0, n, &s->batch);
         if (st == QT_OK) st = qt_batch_prepare(s->batch, prec);
         if (st != QT_OK) return st;
         s->batch_prec = (int) prec;
     }
-    return sum_slices(s->batch, 1ull << (2 * s->cuts.size()), re_im);
+    re_im[0] = re_im[1] = 0.0;
+    return add_slices(s->batch, n, re_im);
 }
 
 qt_status qt_sliced_execute_leaves(qt_ctx *ctx, const qt_sliced *s, qt_precision prec, const double *leaves,
                                    double *re_im) {
     if (!ctx || !s || !re_im || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return QT_ERR_INVALID_ARGUMENT;
     // every slice step by step, one at a time: the device holds one slice's workspace
-    qt_batch *b = nullptr;
-    qt_status st = slice_batch(ctx, s, leaves ? reinterpret_cast<const C *>(leaves) : s->orig_vals.data(), -1, &b);
-    if (st == QT_OK) st = qt_batch_prepare(b, prec);
-    if (st == QT_OK) st = sum_slices(b, 1ull << (2 * s->cuts.size()), re_im);
-    if (b) qt_batch_free(b);
-    return st;
+    return run_chunks(ctx, s, leaves ? reinterpret_cast<const C *>(leaves) : s->orig_vals.data(), -1, prec, re_im);
 }
 
 qt_status qt_sliced_free(qt_sliced *s) {
