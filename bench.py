@@ -324,60 +324,96 @@ def run_batched(ctx, args, stream, flush):
 
 
 SERVE_BUDGET = 150 << 30
+# Work cap of one request: ~2-3 s of the GPU at the ~1e13 complex MAC/s the
+# large steps run at.  Requests above it are refused at submission.
+SERVE_MAX_MACS = int(3e13)
+# Distinct requests whose FP64 value is computed for the error bound (FP64 runs
+# at ~4e10 complex MAC/s on this part: ~2.5 s at the limit)
+SERVE_FP64_CHECK_MACS = int(1e11)
+SERVE_RAND_QUBITS = (10, 14, 18, 22, 26, 30)
+SERVE_RAND_DEPTHS = (8, 12, 16, 20)
+SERVE_QFT_QUBITS = tuple(range(8, 25, 2))
+
+
+def zipf(n, a=1.2):
+    w = np.array([(i + 1.0) ** -a for i in range(n)])
+    return w / w.sum()
 
 
 def run_serving(args):
     """Config 5: Poisson arrivals of contraction requests against a 150 GB
-    device-memory budget; the mix is QAOA edge terms (p=1 and p=2), random
-    Rx/Ry/Rz + CZ circuits and QFT circuits on a random basis input, with
-    heavy-tailed sizes (smaller circuits more likely, 2^-i)."""
+    device-memory budget.  The mix: QAOA edge terms (p=1 and p=2), random
+    Rx/Ry/Rz + CZ circuits of 10-30 qubits and depth 8-20, QFT circuits of 8-24
+    qubits on a random basis input; within each class the sizes are drawn from
+    a Zipf distribution (exponent 1.2) over the class's circuits ordered by
+    complex MACs, so the largest are rare but present.  Every circuit is
+    planned with the automatic ordering; one whose largest intermediate is
+    beyond the engine (more than 24 wires) is refused at planning, one above
+    the work cap at submission, and both are counted."""
     import qtorch_gb300 as qg
     from qtorch_gb300.circuits import qft_measure_text, qft_text, random_circuit_text
     ctx = qg.Context(0)
     ctx.set_memory_budget(SERVE_BUDGET)
-    pool = []   # (class, plan)
+    qaoa = []
     dgf = qg.random_regular_graph(NODES, DEGREE, seed=args.graph_seed)
     for e in range(qg.qaoa_num_edges(dgf)):
         q, m = qg.qaoa_term_text(dgf, 1, [0.4, 1.1], e)
-        pool.append(("qaoa", qg.Plan(q, m, ordering="linegraph", ctx=ctx)))
+        qaoa.append(qg.Plan(q, m, ordering="linegraph", ctx=ctx))
     dgf2 = qg.random_regular_graph(30, 3, seed=5)
     for e in range(0, qg.qaoa_num_edges(dgf2), 3):
         q, m = qg.qaoa_term_text(dgf2, 2, [0.3, 0.8, 0.6, 0.2], e)
-        pool.append(("qaoa", qg.Plan(q, m, ordering="linegraph", ctx=ctx)))
-    rand_sizes = [(10, 8), (12, 10), (14, 10), (16, 12)]
-    qft_sizes = [8, 10, 12, 14]
-    rand_plans = [qg.Plan(random_circuit_text(n, d, 7 + i), "Z", ordering="linegraph", ctx=ctx)
-                  for i, (n, d) in enumerate(rand_sizes)]
-    # QFT of a basis state is a product state with <Z> = 0 on every qubit: <X> of the last qubit
-    qft_plans = [qg.Plan(qft_text(n, 3 + i), qft_measure_text(n), ordering="linegraph", ctx=ctx)
-                 for i, n in enumerate(qft_sizes)]
-    qaoa = [p for _, p in pool]
-    # FP64 value of every distinct request: the error bound of the served values
-    ref = {id(p): p.execute(qg.FP64) for p in qaoa + rand_plans + qft_plans}
+        qaoa.append(qg.Plan(q, m, ordering="linegraph", ctx=ctx))
+    t_plan = time.perf_counter()
+    plan_s = []
+
+    def build(name, text, meas):
+        """(name, plan or None, macs): None when planning refuses it"""
+        t0 = time.perf_counter()
+        try:
+            p = qg.Plan(text, meas, ordering="auto", ctx=ctx)
+            out = (name, p, p.flops)
+        except qg.InvalidFunctionInput:
+            out = (name, None, float("inf"))
+        plan_s.append(time.perf_counter() - t0)
+        return out
+
+    rand = [build(f"rand{n}x{d}", random_circuit_text(n, d, 7 + i), "Z")
+            for i, (n, d) in enumerate((n, d) for n in SERVE_RAND_QUBITS for d in SERVE_RAND_DEPTHS)]
+    qft = [build(f"qft{n}", qft_text(n, 3 + i), qft_measure_text(n)) for i, n in enumerate(SERVE_QFT_QUBITS)]
+    t_plan = time.perf_counter() - t_plan
+    rand.sort(key=lambda r: r[2])
+    qft.sort(key=lambda r: r[2])
+    # FP64 value of every distinct request up to the check size: the error bound
+    ref = {}
+    for p in qaoa + [r[1] for r in rand + qft if r[1] is not None and r[2] <= SERVE_FP64_CHECK_MACS]:
+        ref[id(p)] = p.execute(qg.FP64)
     rng = np.random.default_rng(2024)
-    tail = np.array([2.0 ** -i for i in range(4)])
-    tail /= tail.sum()
-    reqs = []
+    p_rand, p_qft = zipf(len(rand)), zipf(len(qft))
+    reqs = []   # (class, name, plan or None)
     for _ in range(args.serve_requests):
         u = rng.uniform()
         if u < 0.80:
-            reqs.append(("qaoa", qaoa[int(rng.integers(len(qaoa)))]))
+            reqs.append(("qaoa", "qaoa", qaoa[int(rng.integers(len(qaoa)))]))
         elif u < 0.92:
-            reqs.append(("random", rand_plans[int(rng.choice(4, p=tail))]))
+            r = rand[int(rng.choice(len(rand), p=p_rand))]
+            reqs.append(("random", r[0], r[1]))
         else:
-            reqs.append(("qft", qft_plans[int(rng.choice(4, p=tail))]))
+            r = qft[int(rng.choice(len(qft), p=p_qft))]
+            reqs.append(("qft", r[0], r[1]))
 
     # one server for both phases: the saturation phase also warms its lanes'
     # device and pinned-memory caches and the plans' device blocks
-    srv = qg.Server(max_inflight=256, precision=qg.MIXED, ctx=ctx)
+    srv = qg.Server(max_inflight=256, precision=qg.MIXED, ctx=ctx, max_macs=SERVE_MAX_MACS)
+    classes = ("qaoa", "random", "qft")
 
     def serve(gaps):
         """Submit every request at its arrival time (gaps None: all at once);
-        latencies by class, wall time, max error against FP64."""
+        latencies by class, wall time, max error against FP64, refusals."""
         tickets = []
+        refused = {k: {} for k in classes}
         t0 = time.perf_counter()
         t_next = t0
-        for k, (cls, plan) in enumerate(reqs):
+        for k, (cls, name, plan) in enumerate(reqs):
             if gaps is not None:
                 t_next += gaps[k]
                 while True:
@@ -385,17 +421,31 @@ def run_serving(args):
                     if now >= t_next:
                         break
                     time.sleep(min(t_next - now, 0.0005))
-            tickets.append(srv.submit(plan))
+            if plan is None:
+                refused[cls][name] = refused[cls].get(name, 0) + 1   # beyond the engine at planning
+                tickets.append(None)
+                continue
+            try:
+                tickets.append(srv.submit(plan))
+            except (qg.Refused, qg.OutOfMemory):
+                refused[cls][name] = refused[cls].get(name, 0) + 1
+                tickets.append(None)
         srv.drain()
         wall = time.perf_counter() - t0
-        lat = {"qaoa": [], "random": [], "qft": []}
-        err = {"qaoa": 0.0, "random": 0.0, "qft": 0.0}
-        for (cls, plan), t in zip(reqs, tickets):
+        lat = {k: [] for k in classes}
+        err = {k: 0.0 for k in classes}
+        checked = {k: 0 for k in classes}
+        served_names = {k: set() for k in classes}
+        for (cls, name, plan), t in zip(reqs, tickets):
+            if t is None:
+                continue
             v, l = srv.poll(t)
             lat[cls].append(l)
-            err[cls] = max(err[cls], abs(v - ref[id(plan)]))
-        done = len(tickets)
-        return lat, wall, err, done
+            served_names[cls].add(name)
+            if id(plan) in ref:
+                err[cls] = max(err[cls], abs(v - ref[id(plan)]))
+                checked[cls] += 1
+        return lat, wall, err, checked, refused, served_names
 
     def pct(xs, f):
         xs = sorted(xs)
@@ -403,35 +453,46 @@ def run_serving(args):
 
     # saturation: everything at once gives the server's throughput on this mix;
     # the measured stream then offers a stated fraction of it as Poisson arrivals
-    _, wall_sat, err_sat, _ = serve(None)
-    capacity = len(reqs) / wall_sat
+    _, wall_sat, err_sat, _, _, _ = serve(None)
+    n_served = sum(1 for r in reqs if r[2] is not None and r[2].flops <= SERVE_MAX_MACS)
+    capacity = n_served / wall_sat
     rate = args.serve_rate if args.serve_rate > 0 else args.serve_load * capacity
     gaps = rng.exponential(1.0 / rate, len(reqs))
     st0 = srv.stats()
-    lat, wall, err, done = serve(gaps)
+    lat, wall, err, checked, refused, served_names = serve(gaps)
     st1 = srv.stats()
     srv.close()
     waves = st1["waves"] - st0["waves"]
     wave_reqs = st1["wave_requests"] - st0["wave_requests"]
     wave_s = st1["lane_seconds"] - st0["lane_seconds"]
     all_lat = [x for v in lat.values() for x in v]
+    largest = {cls: max((r for r in pool if r[0] in served_names[cls]), key=lambda r: r[2], default=None)
+               for cls, pool in (("random", rand), ("qft", qft))}
     out = {
         "workload": f"{len(reqs)} requests, Poisson arrivals at {rate:.0f}/s ({rate / capacity:.2f} of the "
-                    f"saturation throughput): 80% QAOA edge terms "
-                    f"(30-vertex 4-regular p=1, 30-vertex 3-regular p=2), 12% random Rx/Ry/Rz+CZ circuits "
-                    f"{rand_sizes} (qubits, depth), 8% QFT {qft_sizes} qubits on a random basis input; "
-                    "sizes drawn 2^-i (heavy tail: 5e3 to 6e10 complex MACs per request); <Z_0> measured (<X> of the last qubit for QFT), "
-                    "line-graph ordering; plans built before the stream (requests carry a plan)",
-        "precision": "mixed", "memory_budget_bytes": SERVE_BUDGET,
+                    f"saturation throughput): 80% QAOA edge terms (30-vertex 4-regular p=1, 30-vertex 3-regular "
+                    f"p=2), 12% random Rx/Ry/Rz+CZ circuits of {SERVE_RAND_QUBITS} qubits x depth "
+                    f"{SERVE_RAND_DEPTHS}, 8% QFT of {SERVE_QFT_QUBITS} qubits on a random basis input; sizes "
+                    "Zipf(1.2) over each class's circuits ordered by complex MACs; <Z_0> measured (<X> of the "
+                    "last qubit for QFT); automatic ordering (greedy or min-fill), plans built before the stream "
+                    "(requests carry a plan); refused: beyond 24-wire intermediates at planning, above the work "
+                    "cap at submission",
+        "precision": "mixed", "memory_budget_bytes": SERVE_BUDGET, "work_cap_complex_macs": SERVE_MAX_MACS,
+        "planning_s": {"total": t_plan, "max": max(plan_s), "circuits": len(plan_s)},
         "saturation_requests_per_s": capacity, "arrival_rate_per_s": rate,
         "p50_ms": pct(all_lat, 0.50), "p99_ms": pct(all_lat, 0.99),
         "p50_ms_by_class": {k: pct(v, 0.50) for k, v in lat.items()},
         "p99_ms_by_class": {k: pct(v, 0.99) for k, v in lat.items()},
-        "requests_per_s": len(reqs) / wall, "completed": done,
+        "requests_per_s": len(all_lat) / wall, "completed": len(all_lat),
+        "refused": sum(sum(v.values()) for v in refused.values()), "refused_by_circuit": refused,
+        "largest_served": {k: (v[0], float(v[2])) if v else None for k, v in largest.items()},
         "waves": waves, "mean_requests_per_wave": wave_reqs / max(waves, 1),
         "mean_wave_ms": 1e3 * wave_s / max(waves, 1),
         "error_vs_fp64_max_abs": max(max(err.values()), max(err_sat.values())),
-        "error_vs_fp64_max_abs_by_class": {k: max(err[k], err_sat[k]) for k in err}, "error_bound": 1e-6,
+        "error_vs_fp64_max_abs_by_class": {k: max(err[k], err_sat[k]) for k in err},
+        "fp64_checked_requests": checked,
+        "fp64_check": f"every served request of at most {SERVE_FP64_CHECK_MACS:.0e} complex MACs",
+        "error_bound": 1e-6,
     }
     ctx.close()
     return out
@@ -587,6 +648,57 @@ def run_config3_mixed_only(args):
         out.append(time.perf_counter() - t0)
     print(json.dumps({"terms": len(plans), "seconds_per_pass": out, "values": [[v.real, v.imag] for v in vals]}))
     ctx.close()
+
+
+def measure_permute(rank=13, dtype=1, kinds=("reverse", "random", "identity"), launches=20):
+    """The tiled index permutation (qt_permute_device) on one tensor of `rank`
+    wires (complex64: 537 MB at rank 13, larger than L2): CUDA events around
+    each launch on the context stream, after 3 warm-up launches.  Algorithmic
+    bytes per launch: the tensor read once and written once."""
+    import ctypes
+
+    import torch
+
+    import qtorch_gb300 as qg
+    stream = torch.cuda.Stream()
+    ctx = qg.Context(0, stream=stream.cuda_stream)
+    lib = qg._capi.load()
+    elem = 8 if dtype == 1 else 16
+    n = 4 ** rank
+    x = torch.empty(n * elem // 4, dtype=torch.float32, device="cuda")
+    y = torch.empty_like(x)
+    x.normal_()
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(3)
+    out = {}
+    for kind in kinds:
+        perm = {"reverse": list(range(rank))[::-1], "identity": list(range(rank)),
+                "random": [int(v) for v in rng.permutation(rank)]}[kind]
+        pa = np.array(perm, dtype=np.int32)
+        pp = pa.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        times = []
+        for i in range(launches + 3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            assert lib.qt_permute_device(ctx.handle, ctypes.c_void_p(x.data_ptr()), rank, dtype, pp,
+                                         ctypes.c_void_p(y.data_ptr())) == 0
+            e1.record(stream)
+            e1.synchronize()
+            if i >= 3:
+                times.append(e0.elapsed_time(e1) / 1e3)
+        t = sum(times) / len(times)
+        alg = 2 * n * elem
+        out[kind] = {"perm": perm, "us": 1e6 * t, "alg_bytes": alg, "gb_per_s": alg / t / 1e9,
+                     "frac_of_hbm_peak": alg / t / 1e9 / measured_peaks()[0]}
+    ctx.close()
+    return {"tensor": f"rank {rank} {'complex64' if dtype == 1 else 'complex128'} ({n * elem / 1e6:.0f} MB)",
+            "launches_timed": launches, "cases": out}
+
+
+def run_permute_case(args):
+    """--permute-case rank[,dtype]: the permutation measurement alone (a case for ncu)."""
+    f = [int(x) for x in args.permute_case.split(",")]
+    print(json.dumps(measure_permute(f[0], f[1] if len(f) > 1 else 1)), flush=True)
 
 
 def run_stream_case(args):
@@ -823,6 +935,8 @@ def run_engine(args):
     if not args.no_batched:
         bm._release()
         line["batched"] = run_batched(ctx, args, stream, flush)
+    if not args.no_permute:
+        line["permute"] = measure_permute()
     if not args.no_serving:
         line["serving"] = run_serving(args)
     if not args.no_config3:
@@ -887,7 +1001,11 @@ def bench_summary(line):
         s["config5_serving"] = {"p50_ms": r(v["p50_ms"], 3), "p99_ms": r(v["p99_ms"], 3),
                                 "offered_per_s": r(v["arrival_rate_per_s"]),
                                 "saturation_per_s": r(v["saturation_requests_per_s"]),
-                                "max_err": r(v["error_vs_fp64_max_abs"], 2)}
+                                "max_err": r(v["error_vs_fp64_max_abs"], 2), "refused": v["refused"],
+                                "completed": v["completed"]}
+    if "permute" in line:
+        s["permute_rank13_c64"] = {k: {"gb_per_s": r(v["gb_per_s"]), "frac": r(v["frac_of_hbm_peak"], 3)}
+                                   for k, v in line["permute"]["cases"].items()}
     if "cpu_baseline" in line:
         c = line["cpu_baseline"]
         s["cpu"] = {"kind": c["kind"], "terms_per_s": r(c["value"]), "cores": c["cores"]}
@@ -1045,6 +1163,9 @@ def main():
     ap.add_argument("--only-config3", action="store_true", help="run only the config-3 cases (for profiling)")
     ap.add_argument("--config3-terms", type=int, default=0,
                     help="run only the first N rank 13-14 terms of config 3, mixed form (for profiling)")
+    ap.add_argument("--no-permute", action="store_true", help="skip the index-permutation measurement")
+    ap.add_argument("--permute-case", default="",
+                    help="rank[,dtype]: time the tiled index permutation on one tensor (dtype 1: complex64, 0: complex128)")
     ap.add_argument("--stream-case", default="",
                     help="rA,rB,K[,seed]: time one complex64 step of these ranks (for profiling)")
     ap.add_argument("--rescan-config3", action="store_true",
@@ -1071,6 +1192,8 @@ def main():
         run_config3_mixed_only(args)
     elif args.stream_case:
         run_stream_case(args)
+    elif args.permute_case:
+        run_permute_case(args)
     elif args.only_batched:
         run_only_batched(args)
     elif args.only_config3:

@@ -126,6 +126,20 @@ qt_status qt_contract_pair_device(qt_ctx *ctx, const void *a, int rank_a, const 
                                   int n_free, const uint8_t *free_from_a, const int32_t *free_idx,
                                   int n_sum, const int32_t *sum_a, const int32_t *sum_b, void *c);
 
+/* Index permutation of a tensor (the reference forms the index map of
+ * src/Network.h:912-916 per element inside ContractIndices; here a copy is a
+ * kernel of its own): digit i of the output's flat index is digit perm[i] of
+ * the input's, for a permutation perm of 0..rank-1.  The copy moves through
+ * shared memory in tiles read along the input's contiguous runs and written
+ * along the output's, so both sides are coalesced.  *out receives a new tensor
+ * of the same rank and dtype.  QT_ERR_INVALID_ARGUMENT when perm is not a
+ * permutation. */
+qt_status qt_tensor_permute(qt_ctx *ctx, const qt_tensor *in, const int32_t *perm, qt_tensor **out);
+/* The same on caller-owned device buffers of 4^rank elements of `dtype`,
+ * 16-byte aligned (QT_ERR_INVALID_ARGUMENT otherwise); asynchronous on the
+ * context stream.  in and out must not overlap. */
+qt_status qt_permute_device(qt_ctx *ctx, const void *in, int rank, qt_dtype dtype, const int32_t *perm, void *out);
+
 /* The same on host buffers: copies A and B in, contracts, copies C out (synchronous). */
 qt_status qt_contract_pair_host(qt_ctx *ctx, const double *a, int rank_a, const double *b, int rank_b,
                                 int n_free, const uint8_t *free_from_a, const int32_t *free_idx,

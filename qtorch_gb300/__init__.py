@@ -256,6 +256,29 @@ def contract_pair_c64(a, b, free_from_a, free_idx, sum_a, sum_b, ctx=None):
                 lib.qt_tensor_free(ctx.handle, t)
 
 
+def permute(x, perm, ctx=None):
+    """Index permutation of a host tensor on the GPU (qt_tensor_permute): digit
+    i of the result's flat index is digit perm[i] of x's.  complex64 stays
+    complex64; anything else runs as complex128."""
+    ctx = ctx or default_context()
+    lib = _lib()
+    c64 = np.asarray(x).dtype == np.complex64
+    x = np.ascontiguousarray(x, dtype=np.complex64 if c64 else np.complex128).reshape(-1)
+    pa = np.ascontiguousarray(np.asarray(perm, dtype=np.int32))
+    tx, ty = ctypes.c_void_p(), ctypes.c_void_p()
+    try:
+        _check(lib.qt_tensor_create(ctx.handle, _rank_of(x.size), 1 if c64 else 0, ctypes.byref(tx)), ctx)
+        _check(lib.qt_tensor_upload(ctx.handle, tx, x.ctypes.data_as(ctypes.c_void_p), x.nbytes), ctx)
+        _check(lib.qt_tensor_permute(ctx.handle, tx, _ip(pa) if pa.size else None, ctypes.byref(ty)), ctx)
+        y = np.empty_like(x)
+        _check(lib.qt_tensor_download(ctx.handle, ty, y.ctypes.data_as(ctypes.c_void_p), y.nbytes), ctx)
+        return y
+    finally:
+        for t in (tx, ty):
+            if t.value:
+                lib.qt_tensor_free(ctx.handle, t)
+
+
 def contract_pair_device(a_ptr, rank_a, b_ptr, rank_b, free_from_a, free_idx, sum_a, sum_b, c_ptr, ctx=None):
     """ContractIndices on caller-owned device buffers (complex128), asynchronous on ctx's stream."""
     ctx = ctx or default_context()

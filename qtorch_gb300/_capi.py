@@ -51,6 +51,8 @@ SIGNATURES = [
                                  P(c_int32), P(c_void_p)]),
     ("qt_contract_pair_device", c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_int, P(c_uint8), P(c_int32),
                                         c_int, P(c_int32), P(c_int32), c_void_p]),
+    ("qt_tensor_permute", c_int, [c_void_p, c_void_p, P(c_int32), P(c_void_p)]),
+    ("qt_permute_device", c_int, [c_void_p, c_void_p, c_int, c_int, P(c_int32), c_void_p]),
     ("qt_contract_pair_host", c_int, [c_void_p, P(c_double), c_int, P(c_double), c_int, c_int, P(c_uint8),
                                       P(c_int32), c_int, P(c_int32), P(c_int32), P(c_double)]),
     ("qt_network_create", c_int, [c_void_p, c_char_p, c_char_p, c_char_p, P(c_void_p)]),

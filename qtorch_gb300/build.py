@@ -24,10 +24,10 @@ CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-rel
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-sign-compare",
              "-I" + os.path.join(CUDA, "include")]
 
-CU_SOURCES = ["kernels.cu", "static_scratch.cu", "gemm_tc.cu", "stream.cu"]
-CXX_SOURCES = ["core.cpp", "network.cpp", "orderings.cpp", "plan.cpp", "capi_host.cpp", "qaoa.cpp", "server.cpp", "slicing.cpp",
+CU_SOURCES = ["kernels.cu", "static_scratch.cu", "gemm_tc.cu", "stream.cu", "permute.cu"]
+CXX_SOURCES = ["permute_plan.cpp", "core.cpp", "network.cpp", "orderings.cpp", "plan.cpp", "capi_host.cpp", "qaoa.cpp", "server.cpp", "slicing.cpp",
                "inp.cpp"]
-HEADERS = ["engine.cuh", "kernels.h", "core.h", "plan.h", "gemm_tc.h", "scale.cuh", "stream.h"]
+HEADERS = ["engine.cuh", "kernels.h", "core.h", "plan.h", "gemm_tc.h", "scale.cuh", "stream.h", "permute.h", "dot2.cuh"]
 
 
 def _deps():

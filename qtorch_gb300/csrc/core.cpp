@@ -9,6 +9,7 @@
 
 #include "gemm_tc.h"
 #include "kernels.h"
+#include "permute.h"
 #include "stream.h"
 
 namespace qtg {
@@ -179,6 +180,25 @@ qt_status run_contraction(qt_ctx *ctx, const StepDesc &d, const void *A, const v
             cudaError_t e = launch_reduce_exact(d, (const double2 *) A, (const double2 *) B, (double2 *) C, ctx->stream);
             ctx->launches++;
             return cuda_error(ctx, e, "reduction launch");
+        }
+        const bool aligned = ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15u) == 0;
+        if (d.nFree == 0 && d.rA == d.rB && d.nSum == d.rA && d.rA >= 4 && aligned) {
+            // a full contraction (the expectation value of a large network):
+            // tiles of A and B, each read along its own contiguous runs, meet in
+            // shared memory (permute.cu) instead of one side being gathered
+            int32_t perm[kPermMaxRank];
+            for (int j = 0; j < d.nSum; j++) perm[d.posBs[j]] = d.posAs[j];   // B digit <- A digit
+            PermutePlan pp;
+            if (permute_plan(d.rA, perm, 8, pp)) {
+                void *partials = nullptr;
+                qt_status s = dev_alloc(ctx, sizeof(float4) * (size_t) dot_grid(pp), &partials);
+                if (s != QT_OK) return s;
+                cudaError_t e = launch_permuted_dot(pp, (const float2 *) A, (const float2 *) B, (float2 *) C, partials, sc,
+                                                    ctx->stream);
+                ctx->launches += 2;
+                dev_free(ctx, partials);
+                return cuda_error(ctx, e, "reduction launch");
+            }
         }
         void *scratch = nullptr;
         qt_status s = dev_alloc(ctx, reduce_scratch_bytes(d), &scratch);
@@ -513,6 +533,43 @@ qt_status qt_contract_pair(qt_ctx *ctx, const qt_tensor *a, const qt_tensor *b, 
         return s;
     }
     *c_out = c;
+    return QT_OK;
+}
+
+qt_status qt_permute_device(qt_ctx *ctx, const void *in, int rank, qt_dtype dtype, const int32_t *perm, void *out) {
+    if (!ctx || !in || !out || (dtype != QT_C64 && dtype != QT_C128)) return QT_ERR_INVALID_ARGUMENT;
+    if ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u)
+        return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "buffers must be 16-byte aligned");
+    PermutePlan p;
+    if (!permute_plan(rank, perm, (uint32_t) elem_bytes(dtype), p))
+        return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "perm is not a permutation of the tensor's wires");
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    if (deadline_passed(ctx)) return set_error(ctx, QT_ERR_DEADLINE, "deadline expired");
+    cudaError_t e = launch_permute(p, in, out, ctx->stream);
+    ctx->launches++;
+    return cuda_error(ctx, e, "permute launch");
+}
+
+qt_status qt_tensor_permute(qt_ctx *ctx, const qt_tensor *in, const int32_t *perm, qt_tensor **out) {
+    if (!ctx || !in || !out) return QT_ERR_INVALID_ARGUMENT;
+    if (!in->ptr) return set_error(ctx, QT_ERR_INVALID_FUNCTION_INPUT, "tensor holds no data");
+    PermutePlan p;
+    if (!permute_plan(in->rank, perm, (uint32_t) elem_bytes(in->dtype), p))
+        return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "perm is not a permutation of the tensor's wires");
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    qt_tensor *t = new (std::nothrow) qt_tensor();
+    if (!t) return QT_ERR_OUT_OF_MEMORY;
+    t->rank = in->rank;
+    t->dtype = in->dtype;
+    t->bytes = in->bytes;
+    qt_status s = dev_alloc(ctx, t->bytes, &t->ptr);
+    if (s == QT_OK) s = qt_permute_device(ctx, in->ptr, in->rank, in->dtype, perm, t->ptr);
+    if (s != QT_OK) {
+        if (t->ptr) dev_free(ctx, t->ptr);
+        delete t;
+        return s;
+    }
+    *out = t;
     return QT_OK;
 }
 

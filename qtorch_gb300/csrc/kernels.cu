@@ -20,6 +20,7 @@
 #include <type_traits>
 
 #include "engine.cuh"
+#include "dot2.cuh"
 #include "kernels.h"
 #include "scale.cuh"
 
@@ -41,44 +42,6 @@ __device__ __forceinline__ void cmac_f32(float &cre, float &cim, float2 a, float
     cre = fmaf(-a.y, b.y, cre);
     cim = fmaf(a.x, b.y, cim);
     cim = fmaf(a.y, b.x, cim);
-}
-
-// Compensated FP32 dot product (Ogita, Rump and Oishi, "Accurate sum and dot
-// product", SIAM J. Sci. Comput. 26(6), 2005, algorithm Dot2): the running sum
-// is p + s, every product is split exactly into h + r with one FMA (TwoProduct)
-// and every addition into p + q (Knuth's TwoSum); the errors q + r are summed
-// in s.  The result is as accurate as an FP32 loop run in twice the working
-// precision, and it runs on the FP32 pipe, which on GB300 is many times wider
-// than the FP64 one.  The _rn intrinsics keep the compiler from fusing the
-// error-free transformations into FMAs.
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-    s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
-__device__ __forceinline__ void dot2_acc(float &p, float &s, float x, float y) {
-    const float h = __fmul_rn(x, y);
-    const float r = __fmaf_rn(x, y, -h);
-    float q, np;
-    two_sum(p, h, np, q);
-    p = np;
-    s = __fadd_rn(s, __fadd_rn(q, r));
-}
-
-__device__ __forceinline__ void cmac_dot2(float &pre, float &sre, float &pim, float &sim, float2 a, float2 b) {
-    dot2_acc(pre, sre, a.x, b.x);
-    dot2_acc(pre, sre, -a.y, b.y);
-    dot2_acc(pim, sim, a.x, b.y);
-    dot2_acc(pim, sim, a.y, b.x);
-}
-
-// (p1 + s1) += (p2 + s2)
-__device__ __forceinline__ void dot2_merge(float &p, float &s, float p2, float s2) {
-    float np, q;
-    two_sum(p, p2, np, q);
-    p = np;
-    s = __fadd_rn(s, __fadd_rn(s2, q));
 }
 
 // ---------------------------------------------------------------------------
@@ -279,12 +242,10 @@ reduce_exact(const double2 *__restrict__ A, const double2 *__restrict__ B, const
     if (threadIdx.x == 0) C[c] = make_double2(cre, cim);
 }
 
-static int num_sms();
-
 static uint32_t reduce_grid(const StepDesc &d) {
     const uint64_t K = 1ull << (2 * d.nSum);
     uint64_t g = K / (kReduceThreads * 64ull);   // >= 64 terms per thread
-    const uint64_t cap = (uint64_t) num_sms() * 4;
+    const uint64_t cap = (uint64_t) persistent_sms() * 4;
     if (g > cap) g = cap;
     if (g < 1) g = 1;
     return (uint32_t) g;
@@ -292,6 +253,12 @@ static uint32_t reduce_grid(const StepDesc &d) {
 
 size_t reduce_scratch_bytes(const StepDesc &d) {
     return sizeof(float4) * (size_t) reduce_grid(d) * (size_t) (1ull << (2 * d.nFree));
+}
+
+cudaError_t launch_reduce_final_f32(const float4 *partials, uint32_t n_parts, uint32_t n_out, float2 *C,
+                                    const StepScaleRef &sc, cudaStream_t stream) {
+    reduce_final_f32<<<n_out, 32, 0, stream>>>(partials, n_parts, n_out, C, sc);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_reduce_f32(const StepDesc &d, const float2 *A, const float2 *B, float2 *C, void *scratch,
@@ -1279,6 +1246,12 @@ static int num_sms() {
     return g_num_sms;
 }
 
+static thread_local int t_sm_reserve = 0;
+
+void set_thread_sm_reserve(int sms) { t_sm_reserve = sms > 0 ? sms : 0; }
+
+int persistent_sms() { return std::max(1, num_sms() - t_sm_reserve); }
+
 bool pair_batchable(const StepDesc &d, bool f64) {
     if (2 * (d.nFree + d.nSum) > kPairBatchMaxLog2Macs) return false;
     const bool small_out = (1ull << (2 * d.nFree)) <= kReduceMaxOut;
@@ -1306,7 +1279,7 @@ cudaError_t launch_pair(const StepDesc &d, const void *A, const void *B, void *C
     const uint64_t n_out = 1ull << (2 * d.nFree);
     const uint64_t K = 1ull << (2 * d.nSum);
     uint64_t blocks = (n_out + kPairThreads - 1) / kPairThreads;
-    const uint64_t cap = (uint64_t) num_sms() * 8;
+    const uint64_t cap = (uint64_t) persistent_sms() * 8;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
     if (f64)
@@ -1387,7 +1360,7 @@ static cudaError_t launch_tiled_t(const StepDesc &d, const void *A, const void *
     const bool wide_m = d.fA >= 3, wide_n = d.fB >= 3;
     const uint64_t tiles = (1ull << (2 * d.fA)) / (wide_m ? 64 : 16) * ((1ull << (2 * d.fB)) / (wide_n ? 64 : 16));
     uint64_t grid = tiles;
-    const uint64_t cap = (uint64_t) num_sms() * 4;
+    const uint64_t cap = (uint64_t) persistent_sms() * 4;
     if (grid > cap) grid = cap;
     const V *a = static_cast<const V *>(A);
     const V *b = static_cast<const V *>(B);

@@ -36,6 +36,10 @@ inline bool reduce_shaped(const StepDesc &d) {
 size_t reduce_scratch_bytes(const StepDesc &d);
 cudaError_t launch_reduce_f32(const StepDesc &d, const float2 *A, const float2 *B, float2 *C, void *scratch,
                               cudaStream_t stream, const StepScaleRef &sc = StepScaleRef{});
+// merges n_parts compensated partial sums per output (float4: p_re, s_re,
+// p_im, s_im; output-major) into n_out complex64 outputs
+cudaError_t launch_reduce_final_f32(const float4 *partials, uint32_t n_parts, uint32_t n_out, float2 *C,
+                                    const StepScaleRef &sc, cudaStream_t stream);
 // complex128 with the reference's rounding: every thread of a CTA forms the
 // products of a chunk of k, one thread adds them in the reference's order
 cudaError_t launch_reduce_exact(const StepDesc &d, const double2 *A, const double2 *B, double2 *C,
@@ -57,6 +61,14 @@ size_t plan_smem_bytes(const PlanLaunch &lp);
 // the CTAs of the variant that fit one SM, at most per_sm_cap when positive
 int plan_max_grid(size_t smem_bytes, int per_sm_cap = 0, int variant = kPlanDefaultVariant);
 int plan_num_sms();
+// SMs that the whole-GPU kernels launched from the calling host thread leave
+// free: the grids of the persistent ones (streaming, tiled, pair and
+// reduction kernels) are capped at the other SMs.  Running CTAs are not
+// preempted, so a serving lane that runs heavy requests sets this to keep SMs
+// for the light lane's kernels.
+void set_thread_sm_reserve(int sms);
+// SMs the calling thread's persistent kernels may fill
+int persistent_sms();
 // largest dynamic shared memory an interpreter CTA may have on this device
 size_t plan_smem_limit();
 // The resident engine (one CTA per instance, 128-register budget; variant 1:

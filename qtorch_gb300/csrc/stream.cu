@@ -29,6 +29,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "kernels.h"
 #include "stream.h"
 
 namespace qtg {
@@ -630,11 +631,10 @@ cudaError_t launch_stream(StreamStep &p, const StepDesc &d, const float2 *A, con
     cudaError_t e = stream_attributes();
     if (e != cudaSuccess) return e;
     const StreamFn fn = stream_fn(p.nsfp, p.go, p.ho);
-    int per_sm = 0, dev = 0, sms = 0;
+    int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kStreamBlock, p.smem_bytes);
-    if (e == cudaSuccess) e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
+    const int sms = persistent_sms();
     const uint32_t grid = std::min<uint32_t>(p.n_items, (uint32_t) (sms * std::max(per_sm, 1)));
     fn<<<grid, kStreamBlock, p.smem_bytes, stream>>>(p);
     return cudaGetLastError();
