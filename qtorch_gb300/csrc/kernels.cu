@@ -1246,11 +1246,7 @@ static int num_sms() {
     return g_num_sms;
 }
 
-static thread_local int t_sm_reserve = 0;
-
-void set_thread_sm_reserve(int sms) { t_sm_reserve = sms > 0 ? sms : 0; }
-
-int persistent_sms() { return std::max(1, num_sms() - t_sm_reserve); }
+int persistent_sms() { return num_sms(); }
 
 bool pair_batchable(const StepDesc &d, bool f64) {
     if (2 * (d.nFree + d.nSum) > kPairBatchMaxLog2Macs) return false;

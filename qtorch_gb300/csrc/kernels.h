@@ -61,13 +61,8 @@ size_t plan_smem_bytes(const PlanLaunch &lp);
 // the CTAs of the variant that fit one SM, at most per_sm_cap when positive
 int plan_max_grid(size_t smem_bytes, int per_sm_cap = 0, int variant = kPlanDefaultVariant);
 int plan_num_sms();
-// SMs that the whole-GPU kernels launched from the calling host thread leave
-// free: the grids of the persistent ones (streaming, tiled, pair and
-// reduction kernels) are capped at the other SMs.  Running CTAs are not
-// preempted, so a serving lane that runs heavy requests sets this to keep SMs
-// for the light lane's kernels.
-void set_thread_sm_reserve(int sms);
-// SMs the calling thread's persistent kernels may fill
+// SMs the persistent whole-GPU kernels (streaming, tiled, pair, reduction
+// and permutation kernels) size their grids by
 int persistent_sms();
 // largest dynamic shared memory an interpreter CTA may have on this device
 size_t plan_smem_limit();

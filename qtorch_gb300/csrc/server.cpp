@@ -89,10 +89,6 @@ constexpr int kServerMaxCuts = 16;
 // a mid-size request (a 12-14 qubit circuit, 1e6-1.6e7 MACs) takes one CTA
 // for a millisecond or more and would hold up the small ones behind it.
 constexpr int64_t kLaneZeroMaxMacs = 1ll << 20;
-// SMs the heavy lanes' persistent kernels leave to lane 0: a running CTA is
-// not preempted, so without them a light wave waits for a heavy step's
-// persistent kernel to end (tens of milliseconds for a rank-15 step)
-constexpr int kLightLaneSms = 16;
 
 static uint64_t footprint(const qt_plan *p, qt_precision prec) {
     return p->ws_bytes[prec] + p->leaf_bytes[prec] + 4096;
@@ -100,7 +96,6 @@ static uint64_t footprint(const qt_plan *p, qt_precision prec) {
 
 static void lane_main(qt_server *s, int li) {
     auto &lane = s->lanes[li];
-    if (li > 0) set_thread_sm_reserve(kLightLaneSms);
     for (;;) {
         std::vector<Request> wave;
         {
