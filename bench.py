@@ -631,6 +631,26 @@ def run_config3(args):
     return out
 
 
+def run_gemm_case(args):
+    """--gemm-case qft14|rand16: one GEMM-shaped circuit of config 3 (QFT-14,
+    <X_13>; random 16 qubits depth 12, <Z_0>), mixed form, executed three
+    times (a case for ncu launch lists and captures); prints the last time."""
+    import qtorch_gb300 as qg
+    from qtorch_gb300.circuits import qft_measure_text, qft_text, random_circuit_text
+    text, meas = {"qft14": (qft_text(14, 5), qft_measure_text(14)),
+                  "rand16": (random_circuit_text(16, 12, 1), "Z")}[args.gemm_case]
+    ctx = qg.Context(0)
+    pl = qg.Plan(text, meas, ordering="linegraph", ctx=ctx)
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        v = pl.execute(qg.MIXED)
+        ts.append(time.perf_counter() - t0)
+    print(json.dumps({"circuit": args.gemm_case, "mixed_s": ts, "value": [v.real, v.imag],
+                      "tensor_core_steps": ctx.tensor_core_steps, "stream_steps": ctx.stream_steps}), flush=True)
+    ctx.close()
+
+
 def run_config3_mixed_only(args):
     """The first --config3-terms terms of config 3's rank 13-14 set, mixed form
     only, two passes (a small case for ncu launch lists and captures)."""
@@ -1164,6 +1184,8 @@ def main():
     ap.add_argument("--config3-terms", type=int, default=0,
                     help="run only the first N rank 13-14 terms of config 3, mixed form (for profiling)")
     ap.add_argument("--no-permute", action="store_true", help="skip the index-permutation measurement")
+    ap.add_argument("--gemm-case", default="", choices=["", "qft14", "rand16"],
+                    help="run one GEMM-shaped circuit of config 3 three times (for profiling)")
     ap.add_argument("--permute-case", default="",
                     help="rank[,dtype]: time the tiled index permutation on one tensor (dtype 1: complex64, 0: complex128)")
     ap.add_argument("--stream-case", default="",
@@ -1194,6 +1216,8 @@ def main():
         run_stream_case(args)
     elif args.permute_case:
         run_permute_case(args)
+    elif args.gemm_case:
+        run_gemm_case(args)
     elif args.only_batched:
         run_only_batched(args)
     elif args.only_config3:
