@@ -631,6 +631,64 @@ def run_config3(args):
     return out
 
 
+CONFIG1_FIXTURE = os.path.join(HERE, "tests", "golden", "config1.json")
+
+
+def run_config1(args):
+    """Config 1: seeded 6-qubit depth-10 circuits (Rx(theta), theta ~ U[0, 2 pi),
+    on every qubit, then CZ on 2 random disjoint pairs, per layer), <Z_0> by
+    full contraction of the complex128 network under a fixed-seed stochastic
+    ordering.  The fixtures hold, per seed, the circuit, the recorded ordering
+    and the unmodified reference's value for it; the GPU runs the same
+    ordering (FP64: checked equal to the reference bit for bit; mixed), and
+    the reference itself (oracle/_ref, -O2 and as shipped) replays it on one
+    host core (parse + contraction per evaluation, its ContractGivenSequence)."""
+    import tempfile
+
+    import qtorch_gb300 as qg
+    with open(CONFIG1_FIXTURE) as f:
+        cases = json.load(f)
+    ctx = qg.Context(0)
+    rows = []
+    have_ref = ensure_reference_harness()
+    for c in cases:
+        plan = qg.Plan(c["qasm"], c["measure"], ordering="stochastic", seed=c["seed"], ctx=ctx)
+        assert [list(p) for p in plan.sequence()] == c["sequence"]
+        want = complex(*c["value"])
+        row = {"seed": c["seed"], "complex_macs": plan.flops}
+        for name, prec in (("fp64", qg.FP64), ("mixed", qg.MIXED)):
+            v = plan.execute(prec)
+            n, t0 = 0, time.perf_counter()
+            while time.perf_counter() - t0 < 0.2 or n < 20:
+                v = plan.execute(prec)
+                n += 1
+            row[f"gpu_{name}_us"] = 1e6 * (time.perf_counter() - t0) / n
+            row[f"{name}_value"] = [v.real, v.imag]
+        row["fp64_equals_reference"] = complex(*row["fp64_value"]) == want
+        row["mixed_error_abs"] = abs(complex(*row["mixed_value"]) - want)
+        if have_ref:
+            with tempfile.TemporaryDirectory(prefix="qt_c1_") as wd:
+                paths = [os.path.join(wd, x) for x in ("c.qasm", "c.meas", "c.seq")]
+                for p, text in zip(paths, (c["qasm"], c["measure"],
+                                           "\n".join(f"{a} {b}" for a, b in c["sequence"]) + "\n")):
+                    with open(p, "w") as f:
+                        f.write(text)
+                for key, exe in (("reference_O2_us", REF_HARNESS), ("reference_as_shipped_us", REF_HARNESS_G)):
+                    r = subprocess.run([exe, "seqtime", *paths, "1.0"], capture_output=True, text=True, timeout=600)
+                    kv = {ln.split()[0]: ln.split()[1:] for ln in r.stdout.splitlines() if ln.split()}
+                    row[key] = 1e6 * float(kv["seconds_per_rep"][0]) if r.returncode == 0 else None
+                    if r.returncode == 0:
+                        row[key.replace("_us", "_value_equal")] = complex(float(kv["value"][0]),
+                                                                          float(kv["value"][1])) == want
+        rows.append(row)
+    ctx.close()
+    return {"workload": "seeded 6-qubit depth-10 Rx + CZ(2 disjoint pairs) circuits, <Z_0>, this build's seeded "
+                        "stochastic ordering (recorded in tests/golden/config1.json with the reference's value); "
+                        "GPU: Plan.execute per evaluation (host wall clock, plan built once); reference: its "
+                        "ContractGivenSequence on one host core, parse + contraction per evaluation",
+            "reference_available": have_ref, "cases": rows}
+
+
 def run_gemm_case(args):
     """--gemm-case qft14|rand16: one GEMM-shaped circuit of config 3 (QFT-14,
     <X_13>; random 16 qubits depth 12, <Z_0>), mixed form, executed three
@@ -957,6 +1015,8 @@ def run_engine(args):
         line["batched"] = run_batched(ctx, args, stream, flush)
     if not args.no_permute:
         line["permute"] = measure_permute()
+    if not args.no_config1:
+        line["config1"] = run_config1(args)
     if not args.no_serving:
         line["serving"] = run_serving(args)
     if not args.no_config3:
@@ -1023,6 +1083,11 @@ def bench_summary(line):
                                 "saturation_per_s": r(v["saturation_requests_per_s"]),
                                 "max_err": r(v["error_vs_fp64_max_abs"], 2), "refused": v["refused"],
                                 "completed": v["completed"]}
+    if "config1" in line:
+        cs = line["config1"]["cases"]
+        s["config1"] = {"fp64_equals_reference": all(c["fp64_equals_reference"] for c in cs),
+                        "gpu_fp64_us": r(sum(c["gpu_fp64_us"] for c in cs) / len(cs), 3),
+                        "reference_O2_us": r(sum(c.get("reference_O2_us") or 0 for c in cs) / len(cs), 3)}
     if "permute" in line:
         s["permute_rank13_c64"] = {k: {"gb_per_s": r(v["gb_per_s"]), "frac": r(v["frac_of_hbm_peak"], 3)}
                                    for k, v in line["permute"]["cases"].items()}
@@ -1184,6 +1249,8 @@ def main():
     ap.add_argument("--config3-terms", type=int, default=0,
                     help="run only the first N rank 13-14 terms of config 3, mixed form (for profiling)")
     ap.add_argument("--no-permute", action="store_true", help="skip the index-permutation measurement")
+    ap.add_argument("--no-config1", action="store_true", help="skip the 6-qubit config-1 circuits")
+    ap.add_argument("--only-config1", action="store_true", help="run only the config-1 circuits")
     ap.add_argument("--gemm-case", default="", choices=["", "qft14", "rand16"],
                     help="run one GEMM-shaped circuit of config 3 three times (for profiling)")
     ap.add_argument("--permute-case", default="",
@@ -1218,6 +1285,8 @@ def main():
         run_permute_case(args)
     elif args.gemm_case:
         run_gemm_case(args)
+    elif args.only_config1:
+        print(json.dumps(run_config1(args)), flush=True)
     elif args.only_batched:
         run_only_batched(args)
     elif args.only_config3:

@@ -9,6 +9,10 @@
 //   stoch  <qasm> <measure> <threads>       stochastic contraction (ContractionTools.h:219-388)
 //                                           -> value, flop counter, recorded mCreatedFrom sequence
 //   seq    <qasm> <measure> <seqfile>       ContractGivenSequence replay (ContractionTools.h:392-411)
+//   seqtime <qasm> <measure> <seqfile> <seconds>
+//                                           the same replay repeated (parse + contraction each time, one
+//                                           thread) for at least `seconds`; prints the value, the
+//                                           repetitions and the seconds per repetition
 //   lg     <qasm> <measure> <qbbfile>       LineGraph::LGContract replay of a qbb.out ordering (LineGraph.h:357-376)
 //   lgwires <qasm> <measure>                wire ids assigned by the LineGraph constructor (LineGraph.h:92-171)
 //   gates                                   every gate tensor of Node.h for a fixed set of parameters
@@ -377,6 +381,25 @@ int main(int argc, char **argv) {
             auto net = t.ContractGivenSequence(seq);
             print_value(t.GetFinalVal());
             std::printf("flops %lld\n", net->getNumFloatOps());
+        } else if (cmd == "seqtime" && argc >= 6) {
+            std::vector<std::pair<int, int>> seq;
+            std::ifstream s(argv[4]);
+            int a, b;
+            while (s >> a >> b) seq.push_back({a, b});
+            const double budget = std::atof(argv[5]);
+            std::complex<double> v;
+            long reps = 0;
+            const auto t0 = std::chrono::steady_clock::now();
+            double el = 0;
+            do {
+                ContractionTools t(argv[2], argv[3], 1);
+                t.ContractGivenSequence(seq);
+                v = t.GetFinalVal();
+                reps++;
+                el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            } while (el < budget);
+            print_value(v);
+            std::printf("reps %ld\nseconds_per_rep %.9g\n", reps, el / (double) reps);
         } else if (cmd == "lg" && argc >= 5) {
             auto net = std::make_shared<Network>(argv[2], argv[3]);
             net->SetNumThreads(1);

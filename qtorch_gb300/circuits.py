@@ -32,6 +32,20 @@ def qft_measure_text(n):
     return " ".join(["T"] * (n - 1) + ["X"])
 
 
+def config1_circuit_text(seed, n=6, depth=10, cz_pairs=2):
+    """Each layer: Rx(theta), theta ~ U[0, 2 pi), on every qubit, then CZ on
+    `cz_pairs` random disjoint qubit pairs (seeded)."""
+    rng = np.random.default_rng(seed)
+    lines = [str(n)]
+    for _ in range(depth):
+        for q in range(n):
+            lines.append(f"Rx {rng.uniform(0, 2 * math.pi):.6f} {q}")
+        perm = rng.permutation(n)
+        for j in range(cz_pairs):
+            lines.append(f"CZ {perm[2 * j]} {perm[2 * j + 1]}")
+    return "\n".join(lines) + "\n"
+
+
 def random_circuit_text(n, depth, seed):
     """Layers of seeded Rx/Ry/Rz on every qubit, then CZ on n/4 disjoint random pairs."""
     rng = np.random.default_rng(seed)

@@ -14,6 +14,9 @@ Fixtures:
                   and the same ordering replayed through ContractGivenSequence
   qaoa.json       light-cone QASM text of the MaxCut term generator (src/maxcut.h:105-233)
   linegraph.json  wire numbering of the LineGraph constructor (src/LineGraph.h:92-171)
+  config1.json    seeded 6-qubit depth-10 Rx + CZ circuits, <Z_0>: this build's seeded
+                  stochastic ordering recorded, the reference's value and flop count for
+                  it (ContractGivenSequence, ContractionTools.h:392-411)
 """
 import argparse
 import hashlib
@@ -225,6 +228,33 @@ def gen_reduce(ref_root, cwd):
     return out
 
 
+CONFIG1_SEEDS = (1, 2, 3, 4, 5)
+
+
+def gen_config1(cwd):
+    sys.path.insert(0, REPO)
+    import qtorch_gb300 as qg
+    from qtorch_gb300.circuits import config1_circuit_text
+    out = []
+    for seed in CONFIG1_SEEDS:
+        qtext = config1_circuit_text(seed)
+        plan = qg.Plan(qtext, "Z", ordering="stochastic", seed=seed, symbolic=True)
+        pairs = [list(p) for p in plan.sequence()]
+        qpath, mpath, spath = (f"/tmp/qt_golden_c1_{seed}.{x}" for x in ("qasm", "meas", "seq"))
+        with open(qpath, "w") as f:
+            f.write(qtext)
+        with open(mpath, "w") as f:
+            f.write("Z")
+        with open(spath, "w") as f:
+            f.write("\n".join(f"{a} {b}" for a, b in pairs) + "\n")
+        r = parse_kv(run(["seq", qpath, mpath, spath], cwd))
+        if "exception" in r:
+            raise RuntimeError(f"config 1 seed {seed}: {r['exception']}")
+        out.append({"seed": seed, "qasm": qtext, "measure": "Z", "sequence": pairs,
+                    "value": [float(r["value"][0][0]), float(r["value"][0][1])], "flops": int(r["flops"][0][0])})
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-root", default=os.environ.get("QT_REF_TREE"), required="QT_REF_TREE" not in os.environ)
@@ -240,6 +270,7 @@ def main():
         "qaoa.json": lambda: gen_qaoa(args.ref_root, cwd),
         "linegraph.json": lambda: gen_linegraph(args.ref_root, cwd),
         "reduce.json": lambda: gen_reduce(args.ref_root, cwd),
+        "config1.json": lambda: gen_config1(cwd),
     }
     fixtures = {k: f() for k, f in makers.items() if not args.only or k in args.only}
     for name, data in fixtures.items():
