@@ -422,7 +422,8 @@ qt_status qt_plan_leaf_values(const qt_plan *p, double *out, uint64_t cap) {
 
 qt_status qt_plan_execute(qt_ctx *ctx, qt_plan *p, qt_precision prec, double *v) {
     if (!ctx || !p || !p->ctx || !v || (prec != QT_PREC_FP64 && prec != QT_PREC_MIXED)) return QT_ERR_INVALID_ARGUMENT;
-    if (!p->grouped || p->flops > kLoneInstanceMaxMacs) return execute_stepwise(p, ctx, prec, p->leaf_values.data(), v);
+    if (!p->grouped || p->flops > lone_instance_max_macs(prec))
+        return execute_stepwise(p, ctx, prec, p->leaf_values.data(), v);
     qt_batch *b = nullptr;
     qt_status s = qt_batch_create(ctx, &b);
     if (s != QT_OK) return s;

@@ -41,6 +41,12 @@ constexpr uint64_t kMaxTableBytes = 64ull << 10;
 // this many complex MACs that runs alone (qt_plan_execute) or in a server wave
 // goes step by step through the whole-GPU kernels instead.
 constexpr int64_t kLoneInstanceMaxMacs = 1ll << 24;
+// the same for the FP64 form, whose pipe is ~1/64 of FP32's on this part: one
+// CTA takes milliseconds for a 6-qubit depth-10 circuit (1e6 MACs)
+constexpr int64_t kLoneInstanceMaxMacsF64 = 1ll << 18;
+inline int64_t lone_instance_max_macs(int prec) {
+    return prec == 0 ? kLoneInstanceMaxMacsF64 : kLoneInstanceMaxMacs;   // 0: QT_PREC_FP64
+}
 // plans with at most this many work items carry an item -> step map
 constexpr uint64_t kMaxItemMap = 8192;
 // plans with at most this many work items carry per-item descriptors (16 B each)
