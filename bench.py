@@ -769,6 +769,8 @@ def measure_permute(rank=13, dtype=1, kinds=("reverse", "random", "identity"), l
         out[kind] = {"perm": perm, "us": 1e6 * t, "alg_bytes": alg, "gb_per_s": alg / t / 1e9,
                      "frac_of_hbm_peak": alg / t / 1e9 / measured_peaks()[0]}
     ctx.close()
+    del x, y
+    torch.cuda.empty_cache()
     return {"tensor": f"rank {rank} {'complex64' if dtype == 1 else 'complex128'} ({n * elem / 1e6:.0f} MB)",
             "launches_timed": launches, "cases": out}
 

@@ -3,6 +3,7 @@
 // src/Network.h:876-971).
 #include "core.h"
 
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -35,12 +36,33 @@ static size_t size_class(size_t bytes) {
     return c;
 }
 
+// every live context, for the allocator's last resort (dev_alloc)
+static std::mutex g_ctx_list_lock;
+static std::vector<qt_ctx *> g_ctx_list;
+
+// Frees a context's cached blocks (caller holds its alloc_lock).  cudaFree
+// waits for the device, so blocks that in-flight work on the owner's stream
+// released in stream order are idle by then.
+static void trim_cache(qt_ctx *c) {
+    for (auto &kv : c->free_blocks)
+        for (void *q : kv.second) {
+            cudaFree(q);
+            c->block_size.erase(q);
+        }
+    c->free_blocks.clear();
+    c->bytes_cached = 0;
+}
+
 void ctx_retain(qt_ctx *ctx) {
     if (ctx) ctx->refs.fetch_add(1);
 }
 
 void ctx_release(qt_ctx *ctx) {
     if (!ctx || ctx->refs.fetch_sub(1) != 1) return;
+    {
+        std::lock_guard<std::mutex> g(g_ctx_list_lock);
+        g_ctx_list.erase(std::remove(g_ctx_list.begin(), g_ctx_list.end(), ctx), g_ctx_list.end());
+    }
     cudaSetDevice(ctx->device);
     // a caller's stream may be gone by now; cudaFree waits for the device anyway
     if (ctx->own_stream) cudaStreamSynchronize(ctx->stream);
@@ -79,7 +101,7 @@ void host_free(qt_ctx *ctx, void *p) {
 }
 
 qt_status dev_alloc(qt_ctx *ctx, size_t bytes, void **out) {
-    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    std::unique_lock<std::mutex> g(ctx->alloc_lock);
     const size_t cls = size_class(bytes ? bytes : 1);
     auto it = ctx->free_blocks.find(cls);
     if (it != ctx->free_blocks.end() && !it->second.empty()) {
@@ -96,13 +118,24 @@ qt_status dev_alloc(qt_ctx *ctx, size_t bytes, void **out) {
     if (e == cudaErrorMemoryAllocation) {
         // give the cached blocks back and retry once
         cudaGetLastError();
-        for (auto &kv : ctx->free_blocks)
-            for (void *q : kv.second) {
-                cudaFree(q);
-                ctx->block_size.erase(q);
+        trim_cache(ctx);
+        e = cudaMalloc(&p, cls);
+    }
+    if (e == cudaErrorMemoryAllocation) {
+        // then the other contexts' caches on this device (the lanes of a
+        // server each keep their own): each is taken only if its allocator is
+        // free right now, so two contexts doing this at once cannot deadlock
+        cudaGetLastError();
+        g.unlock();
+        {
+            std::lock_guard<std::mutex> lg(g_ctx_list_lock);
+            for (qt_ctx *o : g_ctx_list) {
+                if (o == ctx || o->device != ctx->device) continue;
+                std::unique_lock<std::mutex> og(o->alloc_lock, std::try_to_lock);
+                if (og.owns_lock()) trim_cache(o);
             }
-        ctx->free_blocks.clear();
-        ctx->bytes_cached = 0;
+        }
+        g.lock();
         e = cudaMalloc(&p, cls);
     }
     if (e != cudaSuccess) {
@@ -118,7 +151,7 @@ qt_status dev_alloc(qt_ctx *ctx, size_t bytes, void **out) {
 
 void dev_free(qt_ctx *ctx, void *p) {
     if (!p) return;
-    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    std::lock_guard<std::mutex> g(ctx->alloc_lock);
     auto it = ctx->block_size.find(p);
     if (it == ctx->block_size.end()) return;
     ctx->free_blocks[it->second].push_back(p);
@@ -359,6 +392,10 @@ qt_status qt_ctx_create(int device, void *stream, qt_ctx **out) {
         }
         ctx->own_stream = true;
     }
+    {
+        std::lock_guard<std::mutex> g(g_ctx_list_lock);
+        g_ctx_list.push_back(ctx);
+    }
     *out = ctx;
     return QT_OK;
 }
@@ -429,7 +466,7 @@ qt_status qt_debug_stream_fault(qt_ctx *ctx, int mode, uint32_t polls) {
 
 qt_status qt_ctx_memory_stats(qt_ctx *ctx, uint64_t *bytes_in_use, uint64_t *bytes_cached, uint64_t *device_allocations) {
     if (!ctx) return QT_ERR_INVALID_ARGUMENT;
-    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    std::lock_guard<std::mutex> g(ctx->alloc_lock);
     if (bytes_in_use) *bytes_in_use = ctx->bytes_in_use;
     if (bytes_cached) *bytes_cached = ctx->bytes_cached;
     if (device_allocations) *device_allocations = ctx->device_allocs.load();

@@ -24,7 +24,11 @@ struct qt_ctx {
     std::recursive_mutex lock;
     std::string last_error;
     std::mutex err_lock;
-    // caching allocator: size class (bytes, power of two >= 256) -> free blocks
+    // caching allocator: size class (bytes, power of two >= 256) -> free blocks;
+    // its state has a lock of its own (held briefly), so that an allocation
+    // that runs out of device memory can empty other contexts' caches while
+    // their owners run
+    std::mutex alloc_lock;
     std::map<size_t, std::vector<void *>> free_blocks;
     std::map<void *, size_t> block_size;
     uint64_t bytes_in_use = 0;

@@ -23,6 +23,7 @@
 #include <thread>
 #include <unordered_map>
 
+#include "gemm_tc.h"
 #include "kernels.h"
 #include "plan.h"
 
@@ -94,6 +95,16 @@ static uint64_t footprint(const qt_plan *p, qt_precision prec) {
     return p->ws_bytes[prec] + p->leaf_bytes[prec] + 4096;
 }
 
+// a plan run step by step also holds, during its largest tensor-core step,
+// that step's packed operands (gemm_tc.h)
+static uint64_t stepwise_scratch(const qt_plan *p, qt_precision prec) {
+    if (prec != QT_PREC_MIXED) return 0;
+    uint64_t m = 0;
+    for (const auto &d : p->steps[prec])
+        if (gemm_eligible(d)) m = std::max<uint64_t>(m, sizeof(float) * gemm_scratch_floats(d));
+    return m;
+}
+
 static void lane_main(qt_server *s, int li) {
     auto &lane = s->lanes[li];
     for (;;) {
@@ -116,7 +127,7 @@ static void lane_main(qt_server *s, int li) {
         } else {
             st = qt_batch_create(lane.ctx, &b);
             if (st == QT_OK) {
-                b->stepwise_macs = kLoneInstanceMaxMacs;   // waves are small: big plans take the whole GPU
+                b->stepwise_macs = lone_instance_max_macs(s->prec);   // waves are small: big plans take the whole GPU
                 // the wide interpreter takes a whole SM per instance: a wave
                 // larger than its lanes' share of the SMs uses two CTAs per SM
                 if ((int) wave.size() * (int) s->lanes.size() > plan_num_sms()) b->policy.kernel_ctas = 2;
@@ -263,8 +274,9 @@ qt_status qt_server_submit(qt_server *s, qt_plan *plan, const double *leaves, in
     if (leaves) r.leaves.assign(leaves, leaves + 2 * plan->leaf_values.size());
     r.t_submit = std::chrono::steady_clock::now();
     r.footprint = footprint(plan, s->prec);
-    r.heavy = !plan->grouped || plan->flops > kLoneInstanceMaxMacs;
+    r.heavy = !plan->grouped || plan->flops > lone_instance_max_macs(s->prec);
     r.small = !r.heavy && plan->flops <= kLaneZeroMaxMacs;
+    if (r.heavy) r.footprint += stepwise_scratch(plan, s->prec);
     auto refuse = [&](qt_status st, const char *why) {
         std::lock_guard<std::mutex> g(s->m);
         s->refused++;
@@ -297,7 +309,7 @@ qt_status qt_server_submit(qt_server *s, qt_plan *plan, const double *leaves, in
         const double total = (double) sp->flops * std::ldexp(1.0, 2 * qt_sliced_num_cuts(r.sliced));
         if (s->max_macs > 0 && total > (double) s->max_macs)
             return refuse(QT_ERR_REFUSED, "sliced request over the work cap");
-        r.footprint = qt_plan_workspace_bytes(sp, s->prec) + fixed;
+        r.footprint = qt_plan_workspace_bytes(sp, s->prec) + fixed + stepwise_scratch(sp, s->prec);
         r.heavy = true;
         r.small = false;
     }
