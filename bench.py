@@ -439,7 +439,10 @@ def run_serving(args):
         for (cls, name, plan), t in zip(reqs, tickets):
             if t is None:
                 continue
-            v, l = srv.poll(t)
+            try:
+                v, l = srv.poll(t)
+            except qg.QtError as e:
+                raise RuntimeError(f"request {name} failed: {e}; {ctx.last_error()}") from e
             lat[cls].append(l)
             served_names[cls].add(name)
             if id(plan) in ref:

@@ -139,6 +139,15 @@ static void lane_main(qt_server *s, int li) {
             if (b) qt_batch_free(b);
         }
         const auto now = std::chrono::steady_clock::now();
+        if (st != QT_OK) {
+            // the lane's message goes to the server's context, where the caller reads it
+            std::string msg;
+            {
+                std::lock_guard<std::mutex> eg(lane.ctx->err_lock);
+                msg = lane.ctx->last_error;
+            }
+            set_error(s->ctx, st, "lane " + std::to_string(li) + ": " + msg);
+        }
         {
             std::lock_guard<std::mutex> g(s->m);
             for (size_t i = 0; i < wave.size(); i++) {
