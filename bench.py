@@ -490,6 +490,7 @@ def run_serving(args):
         "refused": sum(sum(v.values()) for v in refused.values()), "refused_by_circuit": refused,
         "largest_served": {k: (v[0], float(v[2])) if v else None for k, v in largest.items()},
         "waves": waves, "mean_requests_per_wave": wave_reqs / max(waves, 1),
+        "oom_retries": st1["oom_retries"],
         "mean_wave_ms": 1e3 * wave_s / max(waves, 1),
         "error_vs_fp64_max_abs": max(max(err.values()), max(err_sat.values())),
         "error_vs_fp64_max_abs_by_class": {k: max(err[k], err_sat[k]) for k in err},

@@ -487,6 +487,10 @@ qt_status qt_server_free(qt_server *s);
 qt_status qt_server_set_max_macs(qt_server *s, int64_t max_macs);
 /* Submissions refused so far (work cap, budget without a fitting slicing). */
 int64_t qt_server_refused(qt_server *s);
+/* Heavy requests that ran out of device memory beside others and were run
+ * again alone (each at most twice; the admission budget counts plans'
+ * workspaces, not the blocks the lanes' allocators keep). */
+int64_t qt_server_oom_retries(qt_server *s);
 /* Submit (non-blocking).  *ticket identifies the request. */
 qt_status qt_server_submit(qt_server *s, qt_plan *plan, const double *leaves, int64_t *ticket);
 /* Poll: 1 = done (value written), 0 = pending, <0 = error (status negated). */

@@ -791,7 +791,8 @@ class Server(_Owned):
                self.ctx)
         return {"p50_s": p50.value, "p99_s": p99.value, "completed": done.value, "launches": launches.value,
                 "waves": waves.value, "wave_requests": reqs.value, "lane_seconds": secs.value,
-                "refused": int(_lib().qt_server_refused(self.handle))}
+                "refused": int(_lib().qt_server_refused(self.handle)),
+                "oom_retries": int(_lib().qt_server_oom_retries(self.handle))}
 
 
 def qaoa_num_edges(dgf_text):

@@ -40,7 +40,14 @@ struct Request {
     uint64_t footprint;
     bool heavy;
     bool small;   // lane 0 material: grouped and at most kLaneZeroMaxMacs
+    int retries = 0;      // runs that ran out of device memory
+    bool alone = false;   // after one: admitted only when nothing else is in flight
 };
+
+// A heavy request that runs out of device memory while others hold it (the
+// budget counts plans' workspaces, not the blocks the lanes' allocators keep)
+// goes back to the head of the queue and runs again alone, up to this many times.
+constexpr int kMaxOomRetries = 2;
 
 struct Result {
     int state = 0;   // 0 pending, 1 done, <0 -status
@@ -56,6 +63,7 @@ struct qt_server {
     qt_precision prec = QT_PREC_FP64;
     int64_t max_macs = 0;                  // work cap of one request (complex MACs, all slices); 0: none
     int64_t refused = 0;                   // submissions refused by the work cap or the budget
+    int64_t oom_retries = 0;               // heavy runs repeated alone after running out of memory
     std::mutex m;
     std::condition_variable cv;            // new work or a lane became free
     std::condition_variable done_cv;       // a request finished
@@ -139,6 +147,19 @@ static void lane_main(qt_server *s, int li) {
             if (b) qt_batch_free(b);
         }
         const auto now = std::chrono::steady_clock::now();
+        if (st == QT_ERR_OUT_OF_MEMORY && wave.size() == 1 && wave[0].heavy && wave[0].retries < kMaxOomRetries) {
+            std::lock_guard<std::mutex> g(s->m);
+            Request r = std::move(wave[0]);
+            s->inflight--;
+            s->inflight_bytes -= r.footprint;
+            r.retries++;
+            r.alone = true;
+            s->oom_retries++;
+            s->pending.push_front(std::move(r));
+            lane.busy = false;
+            s->cv.notify_all();
+            continue;
+        }
         if (st != QT_OK) {
             // the lane's message goes to the server's context, where the caller reads it
             std::string msg;
@@ -216,6 +237,7 @@ static void dispatcher_main(qt_server *s) {
                 continue;
             }
             if (budget && s->inflight_bytes + it->footprint > budget && s->inflight > 0) break;
+            if (it->alone && s->inflight > 0) break;
             s->inflight++;
             s->inflight_bytes += it->footprint;
             wave.push_back(std::move(*it));
@@ -375,6 +397,12 @@ int64_t qt_server_refused(qt_server *s) {
     if (!s) return -1;
     std::lock_guard<std::mutex> g(s->m);
     return s->refused;
+}
+
+int64_t qt_server_oom_retries(qt_server *s) {
+    if (!s) return -1;
+    std::lock_guard<std::mutex> g(s->m);
+    return s->oom_retries;
 }
 
 qt_status qt_server_stats(qt_server *s, double *p50, double *p99, int64_t *completed, int64_t *launches) {
