@@ -85,6 +85,13 @@ uint64_t qt_ctx_stream_steps(const qt_ctx *ctx);
  * with the context still usable.  mode 0 restores normal operation.  The
  * setting is per device and process. */
 qt_status qt_debug_stream_fault(qt_ctx *ctx, int mode, uint32_t polls);
+/* The same for the tcgen05 GEMM's pipeline (mode 1: the first k tile of every
+ * CTA is never loaded; the step reports QT_ERR_CUDA "TMA pipeline wait timed
+ * out") and for the grouped interpreter's staging of plan blocks and leaves
+ * (mode 1: no staging copy is issued; batch calls report QT_ERR_CUDA "TMA
+ * staging wait timed out").  Test use only; mode 0 restores normal operation. */
+qt_status qt_debug_gemm_fault(qt_ctx *ctx, int mode, uint32_t polls);
+qt_status qt_debug_staging_fault(qt_ctx *ctx, int mode, uint32_t polls);
 /* The context's caching device allocator: bytes handed out, bytes cached for
  * reuse, and how many cudaMalloc calls it has made since the context was
  * created (any pointer may be NULL). */

@@ -39,6 +39,8 @@ SIGNATURES = [
     ("qt_ctx_tensor_core_steps", c_uint64, [c_void_p]),
     ("qt_ctx_stream_steps", c_uint64, [c_void_p]),
     ("qt_debug_stream_fault", c_int, [c_void_p, c_int, ctypes.c_uint32]),
+    ("qt_debug_gemm_fault", c_int, [c_void_p, c_int, ctypes.c_uint32]),
+    ("qt_debug_staging_fault", c_int, [c_void_p, c_int, ctypes.c_uint32]),
     ("qt_ctx_memory_stats", c_int, [c_void_p, P(c_uint64), P(c_uint64), P(c_uint64)]),
     ("qt_tensor_create", c_int, [c_void_p, c_int, c_int, P(c_void_p)]),
     ("qt_tensor_free", c_int, [c_void_p, c_void_p]),

@@ -1008,6 +1008,17 @@ qt_status qt_batch_run(qt_batch *b) {
     return QT_OK;
 }
 
+// An instance whose staging copies did not arrive in time reports a NaN with
+// the kStagingTimeoutBits payload: the call then fails instead of returning it.
+static qt_status staging_status(qt_ctx *ctx, const double *v, size_t n) {
+    for (size_t i = 0; i < n; i++) {
+        uint64_t bits;
+        std::memcpy(&bits, v + i, sizeof bits);
+        if (bits == kStagingTimeoutBits) return set_error(ctx, QT_ERR_CUDA, "TMA staging wait timed out");
+    }
+    return QT_OK;
+}
+
 qt_status qt_batch_evaluate(qt_batch *b, const double *angles, int64_t n_angles, double *values) {
     if (!b || !values || b->prepared_prec < 0) return QT_ERR_INVALID_ARGUMENT;
     qt_ctx *ctx = b->ctx;
@@ -1074,7 +1085,7 @@ qt_status qt_batch_evaluate(qt_batch *b, const double *angles, int64_t n_angles,
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_error(ctx, e, "evaluation graph");
     std::memcpy(values, b->h_values, sizeof(double) * 2 * b->plans.size());
-    return QT_OK;
+    return staging_status(ctx, values, 2 * b->plans.size());
 }
 
 qt_status qt_batch_fetch(qt_batch *b, double *values) {
@@ -1087,7 +1098,7 @@ qt_status qt_batch_fetch(qt_batch *b, double *values) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_error(ctx, e, "value download");
     std::memcpy(values, b->h_values, bytes);
-    return QT_OK;
+    return staging_status(ctx, values, 2 * b->plans.size());
 }
 
 qt_status qt_batch_execute(qt_batch *b, qt_precision prec, double *values) {

@@ -464,6 +464,24 @@ qt_status qt_debug_stream_fault(qt_ctx *ctx, int mode, uint32_t polls) {
     return cuda_error(ctx, e, "stream fault hook");
 }
 
+qt_status qt_debug_gemm_fault(qt_ctx *ctx, int mode, uint32_t polls) {
+    if (!ctx || mode < 0 || mode > 1) return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) e = gemm_set_fault(mode, polls);
+    return cuda_error(ctx, e, "GEMM fault hook");
+}
+
+qt_status qt_debug_staging_fault(qt_ctx *ctx, int mode, uint32_t polls) {
+    if (!ctx || mode < 0 || mode > 1) return QT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::recursive_mutex> g(ctx->lock);
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) e = plan_set_staging_fault(mode, polls);
+    return cuda_error(ctx, e, "staging fault hook");
+}
+
 qt_status qt_ctx_memory_stats(qt_ctx *ctx, uint64_t *bytes_in_use, uint64_t *bytes_cached, uint64_t *device_allocations) {
     if (!ctx) return QT_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> g(ctx->alloc_lock);

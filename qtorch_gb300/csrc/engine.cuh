@@ -169,6 +169,10 @@ struct InstanceDesc {
 // header, a workspace region of ws_smem_bytes, a staging region of stage_bytes.
 // An instance whose workspace or plan block + leaves do not fit there uses the
 // CTA's global workspace slab or reads in place.
+// The value an instance reports when its staging copies did not arrive in
+// time (a NaN with this payload; the host turns it into an error status).
+constexpr uint64_t kStagingTimeoutBits = 0x7ff8dead5ca1ab1eull;
+
 struct PlanLaunch {
     const InstanceDesc *instances;
     int n_instances;

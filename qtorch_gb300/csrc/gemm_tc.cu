@@ -125,8 +125,15 @@ __device__ __forceinline__ void mbar_arrive_tx(uint32_t mbar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-    for (uint32_t it = 0; it < (1u << 24); it++) {
+// Test hook of the pipeline's failure path (qt_debug_gemm_fault): with mode 1
+// the producer issues no copies for the first k tile, so the MMA thread's wait
+// for it (and the producer's for the stage it never frees) run out after
+// g_gemm_fault_polls polls.
+__device__ uint32_t g_gemm_fault_mode = 0;
+__device__ uint32_t g_gemm_fault_polls = 0;
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint32_t limit = 1u << 24) {
+    for (uint32_t it = 0; it < limit; it++) {
         uint32_t ok;
         asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
                      : "=r"(ok) : "r"(mbar), "r"(parity) : "memory");
@@ -197,6 +204,8 @@ gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, cons
     // next k tile queued.  Every wait is bounded; a timeout stops both roles,
     // the copies already issued are waited for, and the error flag is set.
     __shared__ uint64_t s_issued, s_consumed;
+    const bool hook = g_gemm_fault_mode == 1;
+    const uint32_t limit = hook ? g_gemm_fault_polls : 1u << 24;
     bool ok = true;
     auto stage_ptr = [&](int s, int plane) { return tiles + (s * 4 + plane) * kTileBytes; };
     if (warp == 1 && lane == 0) {
@@ -206,9 +215,10 @@ gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, cons
         for (; kt < k_tiles; kt++) {
             const int s = (int) (kt % kStages);
             if (kt >= (uint64_t) kStages) {
-                if (!mbar_wait(sm_addr(&bars[kStages + s]), empty_phase[s])) { ok = false; break; }
+                if (!mbar_wait(sm_addr(&bars[kStages + s]), empty_phase[s], limit)) { ok = false; break; }
                 empty_phase[s] ^= 1u;
             }
+            if (hook && kt == 0) continue;   // the test hook: this tile never arrives
             const uint32_t full = sm_addr(&bars[s]);
             mbar_arrive_tx(full, 4 * kTileBytes);
             const uint64_t xt = (tm * k_tiles + kt) * tile_floats, yt = (tn * k_tiles + kt) * tile_floats;
@@ -224,7 +234,7 @@ gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, cons
         uint64_t kt = 0;
         for (; kt < k_tiles; kt++) {
             const int s = (int) (kt % kStages);
-            if (!mbar_wait(sm_addr(&bars[s]), full_phase[s])) { ok = false; break; }
+            if (!mbar_wait(sm_addr(&bars[s]), full_phase[s], limit)) { ok = false; break; }
             full_phase[s] ^= 1u;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t xh = sm_addr(stage_ptr(s, 0)), xl = sm_addr(stage_ptr(s, 1));
@@ -251,6 +261,7 @@ gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, cons
     if (!ok && warp == 1 && lane == 0) {
         // after a timeout: the copies issued but never consumed land before the CTA leaves
         for (uint64_t kt = s_consumed; kt < s_issued; kt++) {
+            if (hook && kt == 0) continue;   // never issued
             const int s = (int) (kt % kStages);
             mbar_wait(sm_addr(&bars[s]), (uint32_t) ((kt / kStages) & 1u));
         }
@@ -324,6 +335,13 @@ GemmSizes gemm_sizes(const StepDesc &d) {
     s.x_floats = s.m_tiles * kTileM * s.k_tiles * kTileK;
     s.y_floats = s.n_tiles * kTileN * s.k_tiles * kTileK;
     return s;
+}
+
+cudaError_t gemm_set_fault(int mode, uint32_t polls) {
+    const uint32_t m = (uint32_t) mode, p = polls ? polls : 1u;
+    cudaError_t e = cudaMemcpyToSymbol(g_gemm_fault_mode, &m, sizeof m);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_gemm_fault_polls, &p, sizeof p);
+    return e;
 }
 
 size_t gemm_smem_bytes() { return (size_t) kStages * 4 * kTileBytes + (2 * kStages + 1) * 8 + 16; }

@@ -21,6 +21,8 @@ inline uint64_t gemm_scratch_floats(const StepDesc &d) {
     return 2 * (s.x_floats + s.y_floats);
 }
 size_t gemm_smem_bytes();
+// test hook of the pipeline's bounded waits (qt_debug_gemm_fault)
+cudaError_t gemm_set_fault(int mode, uint32_t polls);
 // pack X and Y (hi/lo TF32 planes) into scratch, then the tcgen05 GEMM writes C.
 // error_flag (device int, zero on entry) becomes 1 if a pipeline wait timed out.
 // sc: the mixed form's per-tensor scaling (scale.cuh), applied in the epilogue

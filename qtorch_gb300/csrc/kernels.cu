@@ -916,10 +916,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
     return ok != 0;
 }
 
+// Test hook of the staging failure path (qt_debug_staging_fault): with mode 1
+// thread 0 issues no staging copies, so the wait below runs out after
+// g_stage_fault_polls polls and the instances report the timeout value.
+__device__ uint32_t g_stage_fault_mode = 0;
+__device__ uint32_t g_stage_fault_polls = 0;
+
 // Bounded wait: a bulk copy finishes in microseconds; after ~1 s of polling the
-// wait gives up and the instance reports NaN instead of hanging the CTA.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
-    for (uint32_t it = 0; it < (1u << 22); it++) {
+// wait gives up and the instance reports kStagingTimeoutBits instead of
+// hanging the CTA.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity, uint32_t limit = 1u << 22) {
+    for (uint32_t it = 0; it < limit; it++) {
         if (mbar_try_wait(mbar, parity)) return true;
         if (it > 64) __nanosleep(256);
     }
@@ -1093,19 +1100,21 @@ __global__ void __launch_bounds__(plan_threads(kMinCtas), kMinCtas) plan_kernel(
         char *const ws = I.ws_bytes <= lp.ws_smem_bytes ? ws_smem : ws_global;
         const bool staged = lp.stage_bytes && I.plan_bytes && I.plan_bytes + I.leaf_bytes <= lp.stage_bytes;
         if (staged) {
-            if (threadIdx.x == 0) {
+            const bool hook = g_stage_fault_mode == 1;
+            if (threadIdx.x == 0 && !hook) {
                 // the previous instance's generic reads of this region are ordered before the async writes
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_expect_tx(mbar, I.plan_bytes + I.leaf_bytes);
                 bulk_copy_chunks(stage, reinterpret_cast<const char *>(I.plan), I.plan_bytes, mbar);
                 bulk_copy_chunks(stage + I.plan_bytes, I.leaves, I.leaf_bytes, mbar);
             }
-            const bool ok = mbar_wait_bounded(mbar, parity);
+            const bool ok = mbar_wait_bounded(mbar, parity, hook ? g_stage_fault_polls : 1u << 22);
             parity ^= 1u;
             if (__syncthreads_or(!ok)) {
-                // the copies never completed: this CTA's instances report NaN instead of hanging
+                // the copies never completed: this CTA's instances report the
+                // timeout value instead of hanging
                 if (threadIdx.x == 0) {
-                    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+                    const double nan = __longlong_as_double((long long) kStagingTimeoutBits);
                     I.value[0] = I.value[1] = nan;
                     if (lp.next) {
                         for (int j = (int) atomicAdd(lp.next, 1u); j < lp.n_instances; j = (int) atomicAdd(lp.next, 1u))
@@ -1374,6 +1383,13 @@ cudaError_t launch_tiled_pair(const StepDesc &d, const void *A, const void *B, v
 }
 
 int plan_num_sms() { return num_sms(); }
+
+cudaError_t plan_set_staging_fault(int mode, uint32_t polls) {
+    const uint32_t m = (uint32_t) mode, p = polls ? polls : 1u;
+    cudaError_t e = cudaMemcpyToSymbol(g_stage_fault_mode, &m, sizeof m);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_stage_fault_polls, &p, sizeof p);
+    return e;
+}
 
 int plan_max_grid(size_t smem_bytes, int per_sm_cap, int variant) {
     int per_sm = 0;

@@ -61,6 +61,8 @@ size_t plan_smem_bytes(const PlanLaunch &lp);
 // the CTAs of the variant that fit one SM, at most per_sm_cap when positive
 int plan_max_grid(size_t smem_bytes, int per_sm_cap = 0, int variant = kPlanDefaultVariant);
 int plan_num_sms();
+// test hook of the interpreter's staging waits (qt_debug_staging_fault)
+cudaError_t plan_set_staging_fault(int mode, uint32_t polls);
 // SMs the persistent whole-GPU kernels (streaming, tiled, pair, reduction
 // and permutation kernels) size their grids by
 int persistent_sms();
