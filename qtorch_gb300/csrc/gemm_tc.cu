@@ -36,6 +36,7 @@ constexpr int kTileN = 128;          // rows of Y per tile (UMMA N, real columns
 constexpr int kTileK = 32;           // tf32 elements of K per stage (128 bytes)
 constexpr int kTileBytes = kTileM * kTileK * 4;   // 16 KB, same for X and Y tiles
 constexpr int kStages = 3;
+constexpr uint64_t kGroupM = 8;      // row tiles per band of the CTA order
 constexpr int kGemmThreads = 128;
 // Accumulators in tensor memory (128 columns each): the hi*hi products rotate
 // over kAccBig regions by k tile and the small hi*lo + lo*hi products have one
@@ -182,7 +183,16 @@ gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, cons
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kStages * 4 * kTileBytes);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kStages + 1);
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const uint64_t tm = blockIdx.x, tn = blockIdx.y;
+    // Tile order for L2 reuse: CTAs run in bands of kGroupM row tiles, the
+    // column tiles fastest within a band, so the CTAs resident at once share
+    // the band's X tiles and the Y tiles they walk; X is read about once and Y
+    // once per band (row-major order read all of X once per wave of columns).
+    const uint64_t m_tiles = (M + kTileM - 1) / kTileM, n_tiles = (N2 + kTileN - 1) / kTileN;
+    const uint64_t lin = blockIdx.x;
+    const uint64_t band = lin / (kGroupM * n_tiles), first_m = band * kGroupM;
+    const uint64_t rows_in_band = m_tiles - first_m < kGroupM ? m_tiles - first_m : kGroupM;
+    const uint64_t within = lin - band * kGroupM * n_tiles;
+    const uint64_t tm = first_m + within % rows_in_band, tn = within / rows_in_band;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
@@ -305,7 +315,7 @@ gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, cons
     } else if (threadIdx.x == 0) {
         atomicExch(error_flag, 1);
     }
-    scale_note(sc, lmax, shift, blockIdx.x == 0 && blockIdx.y == 0);
+    scale_note(sc, lmax, shift, blockIdx.x == 0);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
@@ -356,8 +366,9 @@ cudaError_t launch_gemm_step(const StepDesc &d, const float2 *A, const float2 *B
     const size_t smem = gemm_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     if (e != cudaSuccess) return e;
-    dim3 grid((unsigned) s.m_tiles, (unsigned) s.n_tiles);
-    gemm_tf32x3<<<grid, kGemmThreads, smem, stream>>>(xh, xl, yh, yl, s.k_tiles, s.M, s.N2, C, error_flag, sc);
+    const uint64_t ctas = s.m_tiles * s.n_tiles;
+    if (ctas > 0x7fffffffull) return cudaErrorInvalidValue;
+    gemm_tf32x3<<<(unsigned) ctas, kGemmThreads, smem, stream>>>(xh, xl, yh, yl, s.k_tiles, s.M, s.N2, C, error_flag, sc);
     return cudaGetLastError();
 }
 
