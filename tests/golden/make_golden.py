@@ -229,6 +229,7 @@ def gen_reduce(ref_root, cwd):
 
 
 CONFIG1_SEEDS = (1, 2, 3, 4, 5)
+CONFIG1_MEASURE = "Z T T T T T"   # <Z_0>, the other qubits traced
 
 
 def gen_config1(cwd):
@@ -238,19 +239,19 @@ def gen_config1(cwd):
     out = []
     for seed in CONFIG1_SEEDS:
         qtext = config1_circuit_text(seed)
-        plan = qg.Plan(qtext, "Z", ordering="stochastic", seed=seed, symbolic=True)
+        plan = qg.Plan(qtext, CONFIG1_MEASURE, ordering="stochastic", seed=seed, symbolic=True)
         pairs = [list(p) for p in plan.sequence()]
         qpath, mpath, spath = (f"/tmp/qt_golden_c1_{seed}.{x}" for x in ("qasm", "meas", "seq"))
         with open(qpath, "w") as f:
             f.write(qtext)
         with open(mpath, "w") as f:
-            f.write("Z")
+            f.write(CONFIG1_MEASURE)
         with open(spath, "w") as f:
             f.write("\n".join(f"{a} {b}" for a, b in pairs) + "\n")
         r = parse_kv(run(["seq", qpath, mpath, spath], cwd))
         if "exception" in r:
             raise RuntimeError(f"config 1 seed {seed}: {r['exception']}")
-        out.append({"seed": seed, "qasm": qtext, "measure": "Z", "sequence": pairs,
+        out.append({"seed": seed, "qasm": qtext, "measure": CONFIG1_MEASURE, "sequence": pairs,
                     "value": [float(r["value"][0][0]), float(r["value"][0][1])], "flops": int(r["flops"][0][0])})
     return out
 
