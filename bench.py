@@ -1041,11 +1041,13 @@ def run_engine(args):
                 "parse_share": parse_share}
         if ensure_reference_harness():
             rate, n, el = reference_cpu_sample(args.cpu_seconds, cores)
+            share, rate_ex = reference_parse_split(REF_HARNESS, rate)
             line["cpu_baseline"] = {"value": rate, "unit": "terms/s", "cores": cores, "kind": "reference",
                                     "sample": f"{n} steps of 60 terms in {el:.1f} s: the unmodified reference "
                                               "(g++ -O2) writing, parsing and contracting every term "
                                               "(maxcut.cpp:166-196) under the recorded orderings, "
                                               f"{cores} forked workers",
+                                    "parse_share": share, "terms_per_s_excluding_parse": rate_ex,
                                     "port": port}
         else:
             line["cpu_baseline"] = port
@@ -1153,7 +1155,13 @@ def run_reference_harness(exe, steps, workers):
             times.append(float(t[2]))
         elif t and t[0] == "value":
             values[int(t[1])] = complex(float(t[2]), float(t[3]))
+        elif t and t[0] == "split":
+            # worker seconds writing + parsing the terms' files, and contracting them
+            REF_SPLIT[os.path.basename(exe)] = (float(t[1]), float(t[2]))
     return times, [values[k] for k in sorted(values)]
+
+
+REF_SPLIT = {}   # harness name -> (file write + parse seconds, contraction seconds) of its last run
 
 
 def ensure_reference_harness():
@@ -1174,6 +1182,16 @@ def reference_cpu_sample(seconds, workers):
     return 60 * len(t) / sum(t), len(t), sum(t)
 
 
+def reference_parse_split(exe, rate):
+    """(share of the workers' time spent writing and parsing the term files,
+    terms/s with that share taken out) of the harness's last run."""
+    prep, contract = REF_SPLIT.get(os.path.basename(exe), (0.0, 0.0))
+    if prep + contract <= 0:
+        return None, None
+    share = prep / (prep + contract)
+    return share, rate / max(1e-12, 1.0 - share)
+
+
 def run_reference(args):
     """--impl reference: the unmodified reference (oracle/_ref, built from its
     own headers) timed on all host cores, on the engine arm's workload.  This
@@ -1182,6 +1200,7 @@ def run_reference(args):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
+    parse_share = None
     if ensure_reference_harness():
         times, _ = run_reference_harness(REF_HARNESS, args.warmup + args.steps, cores)
         times = times[args.warmup:]
@@ -1191,10 +1210,14 @@ def run_reference(args):
                   "(Network.h:246-304), ContractGivenSequence (ContractionTools.h:392-411) over the recorded "
                   f"ordering -- unmodified reference headers built with g++ -O2, {cores} forked workers, one term "
                   "at a time")
+        parse_share, _ = reference_parse_split(REF_HARNESS, 1.0)
         gsteps = max(3, min(args.steps, 10))
         gt, _ = run_reference_harness(REF_HARNESS_G, 2 + gsteps, cores)
-        as_shipped = {"value": 60 * gsteps / sum(gt[2:]), "unit": "terms/s", "steps": gsteps,
-                      "build": "g++ -g -std=c++11 -pthread, no -O (the reference's Makefile:34)"}
+        g_rate = 60 * gsteps / sum(gt[2:])
+        g_share, g_ex = reference_parse_split(REF_HARNESS_G, g_rate)
+        as_shipped = {"value": g_rate, "unit": "terms/s", "steps": gsteps,
+                      "build": "g++ -g -std=c++11 -pthread, no -O (the reference's Makefile:34)",
+                      "parse_share": g_share, "terms_per_s_excluding_parse": g_ex}
     else:
         # no staged reference headers on this machine: the C restatement instead
         import multiprocessing as mp
@@ -1226,6 +1249,7 @@ def run_reference(args):
         "config": shared_config(args.graph_seed),
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "terms/s", "cores": cores, "kind": kind, "sample": sample},
+        "parse_share": parse_share if kind == "reference" else None,
         "e2e": {"value": value, "unit": "terms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     if as_shipped:

@@ -26,7 +26,9 @@
 //                                           recorded ordering.  Terms go to `workers` forked processes
 //                                           (dynamic, one term at a time); one step per line of
 //                                           anglesfile ("b_1..b_p g_1..g_p"); prints "step <s> <f_p>"
-//                                           per step and "value <term> <re> <im>" for the first step
+//                                           per step, "value <term> <re> <im>" for the first step, and
+//                                           "split <prep> <contract>": worker seconds spent writing and
+//                                           parsing the terms' files and contracting them
 #include <atomic>
 #include <chrono>
 #include <cstdio>
@@ -225,7 +227,8 @@ bool write_full(int fd, const void *buf, size_t n) {
 // contraction replaced by the replay of a recorded ordering.
 std::complex<double> bench_term(ExtraData &e, size_t k, const std::vector<double> &bg,
                                 const std::vector<std::pair<int, int>> &seq, const std::string &qasmPath,
-                                const std::string &measPath) {
+                                const std::string &measPath, double *split) {
+    const auto t0 = std::chrono::steady_clock::now();
     std::ofstream q(qasmPath);
     std::ofstream meas(measPath);
     int numQubits = e.qubitsNeeded[k];
@@ -236,8 +239,14 @@ std::complex<double> bench_term(ExtraData &e, size_t k, const std::vector<double
     meas.close();
     q.close();
     ContractionTools t(qasmPath, measPath, 1);
+    const auto t1 = std::chrono::steady_clock::now();
     t.ContractGivenSequence(seq);
-    return t.GetFinalVal();
+    const std::complex<double> v = t.GetFinalVal();
+    const auto t2 = std::chrono::steady_clock::now();
+    // [0]: writing and parsing the term's files, [1]: the contraction
+    split[0] += std::chrono::duration<double>(t1 - t0).count();
+    split[1] += std::chrono::duration<double>(t2 - t1).count();
+    return v;
 }
 
 }  // namespace
@@ -281,11 +290,12 @@ static int cmd_bench(char **argv) {
         }
     }
 
-    size_t shBytes = kValuesOffset + sizeof(double) * 2 * nTerms;
+    size_t shBytes = kValuesOffset + sizeof(double) * 2 * nTerms + sizeof(double) * 2 * (size_t) workers;
     void *mem = mmap(nullptr, shBytes, PROT_READ | PROT_WRITE, MAP_SHARED | MAP_ANONYMOUS, -1, 0);
     if (mem == MAP_FAILED) return 5;
     std::atomic<long> *next = new (mem) std::atomic<long>(0);
     double *values = reinterpret_cast<double *>(static_cast<char *>(mem) + kValuesOffset);
+    double *splits = values + 2 * nTerms;   // per worker: file write + parse seconds, contraction seconds
 
     std::vector<int> toChild(workers), fromChild(workers);
     std::vector<pid_t> pids(workers);
@@ -305,7 +315,7 @@ static int cmd_bench(char **argv) {
                 int32_t ok = 1;
                 try {
                     for (long k; (k = next->fetch_add(1)) < (long) nTerms;) {
-                        std::complex<double> v = bench_term(e, (size_t) k, bg, seqs[(size_t) k], qp, mp);
+                        std::complex<double> v = bench_term(e, (size_t) k, bg, seqs[(size_t) k], qp, mp, splits + 2 * w);
                         values[2 * k] = v.real();
                         values[2 * k + 1] = v.imag();
                     }
@@ -345,6 +355,12 @@ static int cmd_bench(char **argv) {
         }
         std::fflush(stdout);
     }
+    double prep = 0, contract = 0;
+    for (int w = 0; w < workers; w++) {
+        prep += splits[2 * w];
+        contract += splits[2 * w + 1];
+    }
+    std::printf("split %.9f %.9f\n", prep, contract);   // summed over the workers and steps
     int32_t stop = -1;
     for (int w = 0; w < workers; w++) {
         write_full(toChild[w], &stop, sizeof stop);
