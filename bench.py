@@ -335,6 +335,9 @@ SERVE_RAND_DEPTHS = (8, 12, 16, 20)
 SERVE_QFT_QUBITS = tuple(range(8, 25, 2))
 
 
+SERVE_QUEUED = {}   # per class: seconds each request of the last serve() waited before admission
+
+
 def zipf(n, a=1.2):
     w = np.array([(i + 1.0) ** -a for i in range(n)])
     return w / w.sum()
@@ -433,6 +436,7 @@ def run_serving(args):
         srv.drain()
         wall = time.perf_counter() - t0
         lat = {k: [] for k in classes}
+        queued = {k: [] for k in classes}
         err = {k: 0.0 for k in classes}
         checked = {k: 0 for k in classes}
         served_names = {k: set() for k in classes}
@@ -440,14 +444,17 @@ def run_serving(args):
             if t is None:
                 continue
             try:
-                v, l = srv.poll(t)
+                v, l, qd, _ = srv.poll_detail(t)
             except qg.QtError as e:
                 raise RuntimeError(f"request {name} failed: {e}; {ctx.last_error()}") from e
             lat[cls].append(l)
+            queued[cls].append(qd)
             served_names[cls].add(name)
             if id(plan) in ref:
                 err[cls] = max(err[cls], abs(v - ref[id(plan)]))
                 checked[cls] += 1
+        SERVE_QUEUED.clear()
+        SERVE_QUEUED.update(queued)
         return lat, wall, err, checked, refused, served_names
 
     def pct(xs, f):
@@ -486,6 +493,8 @@ def run_serving(args):
         "p50_ms": pct(all_lat, 0.50), "p99_ms": pct(all_lat, 0.99),
         "p50_ms_by_class": {k: pct(v, 0.50) for k, v in lat.items()},
         "p99_ms_by_class": {k: pct(v, 0.99) for k, v in lat.items()},
+        "queued_p50_ms_by_class": {k: pct(v, 0.50) for k, v in SERVE_QUEUED.items()},
+        "queued_p99_ms_by_class": {k: pct(v, 0.99) for k, v in SERVE_QUEUED.items()},
         "requests_per_s": len(all_lat) / wall, "completed": len(all_lat),
         "refused": sum(sum(v.values()) for v in refused.values()), "refused_by_circuit": refused,
         "largest_served": {k: (v[0], float(v[2])) if v else None for k, v in largest.items()},

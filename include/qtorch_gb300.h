@@ -502,6 +502,10 @@ int64_t qt_server_oom_retries(qt_server *s);
 qt_status qt_server_submit(qt_server *s, qt_plan *plan, const double *leaves, int64_t *ticket);
 /* Poll: 1 = done (value written), 0 = pending, <0 = error (status negated). */
 int qt_server_poll(qt_server *s, int64_t ticket, double *re_im, double *latency_s);
+/* The same, and where the latency went: seconds from submission to admission
+ * into a wave, and the lane (0: the light lane) that ran it. */
+int qt_server_poll_detail(qt_server *s, int64_t ticket, double *re_im, double *latency_s, double *queued_s,
+                          int *lane);
 /* Block until every submitted request has finished. */
 qt_status qt_server_drain(qt_server *s);
 /* p50/p99 latency in seconds and completed count since creation. */

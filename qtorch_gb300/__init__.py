@@ -778,6 +778,16 @@ class Server(_Owned):
             raise _ERRORS.get(-st, QtError)(-st)
         return (complex(v[0], v[1]), lat.value) if st == 1 else None
 
+    def poll_detail(self, ticket):
+        """(value, latency, seconds queued before admission, lane) or None while pending"""
+        v = np.zeros(2)
+        lat, q, lane = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_int(-1)
+        st = _lib().qt_server_poll_detail(self.handle, ticket, _dp(v), ctypes.byref(lat), ctypes.byref(q),
+                                          ctypes.byref(lane))
+        if st < 0:
+            raise _ERRORS.get(-st, QtError)(-st)
+        return (complex(v[0], v[1]), lat.value, q.value, lane.value) if st == 1 else None
+
     def drain(self):
         _check(_lib().qt_server_drain(self.handle), self.ctx)
 

@@ -139,6 +139,7 @@ SIGNATURES = [
     ("qt_server_free", c_int, [c_void_p]),
     ("qt_server_submit", c_int, [c_void_p, c_void_p, P(c_double), P(c_int64)]),
     ("qt_server_poll", c_int, [c_void_p, c_int64, P(c_double), P(c_double)]),
+    ("qt_server_poll_detail", c_int, [c_void_p, c_int64, P(c_double), P(c_double), P(c_double), P(c_int)]),
     ("qt_server_set_max_macs", c_int, [c_void_p, c_int64]),
     ("qt_server_refused", c_int64, [c_void_p]),
     ("qt_server_oom_retries", c_int64, [c_void_p]),

@@ -37,6 +37,7 @@ struct Request {
     const qt_sliced *sliced = nullptr;   // the plan sliced to fit the budget (runs alone, slice by slice)
     std::vector<double> leaves;
     std::chrono::steady_clock::time_point t_submit;
+    std::chrono::steady_clock::time_point t_admit;   // taken into a wave
     uint64_t footprint;
     bool heavy;
     bool small;   // lane 0 material: grouped and at most kLaneZeroMaxMacs
@@ -53,6 +54,8 @@ struct Result {
     int state = 0;   // 0 pending, 1 done, <0 -status
     double v[2] = {0, 0};
     double latency = 0;
+    double queued = 0;   // seconds from submission to admission into a wave
+    int lane = -1;
 };
 
 }  // namespace
@@ -64,6 +67,7 @@ struct qt_server {
     int64_t max_macs = 0;                  // work cap of one request (complex MACs, all slices); 0: none
     int64_t refused = 0;                   // submissions refused by the work cap or the budget
     int64_t oom_retries = 0;               // heavy runs repeated alone after running out of memory
+    uint64_t wave_ends = 0;                // waves finished (or returned for a retry) so far
     std::mutex m;
     std::condition_variable cv;            // new work or a lane became free
     std::condition_variable done_cv;       // a request finished
@@ -156,6 +160,7 @@ static void lane_main(qt_server *s, int li) {
             r.alone = true;
             s->oom_retries++;
             s->pending.push_front(std::move(r));
+            s->wave_ends++;
             lane.busy = false;
             s->cv.notify_all();
             continue;
@@ -181,6 +186,8 @@ static void lane_main(qt_server *s, int li) {
                     res.state = -(int) st;
                 }
                 res.latency = std::chrono::duration<double>(now - wave[i].t_submit).count();
+                res.queued = std::chrono::duration<double>(wave[i].t_admit - wave[i].t_submit).count();
+                res.lane = li;
                 s->latencies.push_back(res.latency);
                 s->completed++;
                 s->inflight--;
@@ -188,6 +195,7 @@ static void lane_main(qt_server *s, int li) {
             }
             s->launches += nl;
             s->waves++;
+            s->wave_ends++;
             s->wave_requests += (int64_t) wave.size();
             s->wave_seconds += std::chrono::duration<double>(now - t_wave).count();
             lane.busy = false;
@@ -240,13 +248,17 @@ static void dispatcher_main(qt_server *s) {
             if (it->alone && s->inflight > 0) break;
             s->inflight++;
             s->inflight_bytes += it->footprint;
+            it->t_admit = std::chrono::steady_clock::now();
             wave.push_back(std::move(*it));
             it = s->pending.erase(it);
             if (take_heavy) break;
         }
         if (wave.empty()) {
-            // nothing admissible until a running wave returns its memory
-            s->cv.wait(g, [&] { return s->stop || s->inflight == 0; });
+            // nothing admissible on this lane until a running wave returns its
+            // memory: wait for the next wave to end (not for every wave -- the
+            // light lane keeps being served while heavy requests wait)
+            const uint64_t seen = s->wave_ends;
+            s->cv.wait(g, [&] { return s->stop || s->wave_ends != seen; });
             continue;
         }
         s->lanes[li].wave = std::move(wave);
@@ -368,6 +380,16 @@ int qt_server_poll(qt_server *s, int64_t ticket, double *v, double *latency) {
         if (latency) *latency = it->second.latency;
     }
     return it->second.state;
+}
+
+int qt_server_poll_detail(qt_server *s, int64_t ticket, double *v, double *latency, double *queued, int *lane) {
+    const int st = qt_server_poll(s, ticket, v, latency);
+    if (st != 1) return st;
+    std::lock_guard<std::mutex> g(s->m);
+    const Result &r = s->results.at(ticket);
+    if (queued) *queued = r.queued;
+    if (lane) *lane = r.lane;
+    return st;
 }
 
 qt_status qt_server_drain(qt_server *s) {
