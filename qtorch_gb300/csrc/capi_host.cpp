@@ -884,9 +884,15 @@ static qt_status batch_configure(qt_batch *b) {
     if (inst.empty()) return QT_OK;
     s = dev_alloc(ctx, sizeof(InstanceDesc) * inst.size(), &b->d_inst);
     if (s != QT_OK) return s;
-    cudaError_t e = cudaMemcpyAsync(b->d_inst, inst.data(), sizeof(InstanceDesc) * inst.size(),
-                                    cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);   // the host copy may change again
+    // through the context's pinned staging buffer: a copy from pageable memory
+    // goes through the driver's shared staging and can wait behind other
+    // threads' large pageable copies
+    const size_t inst_bytes = sizeof(InstanceDesc) * inst.size();
+    s = ensure_pinned(ctx, inst_bytes);
+    if (s != QT_OK) return s;
+    std::memcpy(ctx->pinned, inst.data(), inst_bytes);
+    cudaError_t e = cudaMemcpyAsync(b->d_inst, ctx->pinned, inst_bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);   // the staging buffer is reused
     return cuda_error(ctx, e, "instance upload");
 }
 

@@ -30,6 +30,10 @@ qt_status cuda_error(qt_ctx *ctx, cudaError_t e, const char *what) {
     return set_error(ctx, QT_ERR_CUDA, msg);
 }
 
+// largest ratio of a cached block's class to the requested class that a
+// request may take instead of allocating (twice for blocks above 64 MB)
+static size_t cache_stretch(size_t cls) { return cls <= (64ull << 20) ? 4 : 2; }
+
 static size_t size_class(size_t bytes) {
     size_t c = 256;
     while (c < bytes) c <<= 1;
@@ -77,13 +81,15 @@ void ctx_release(qt_ctx *ctx) {
 
 qt_status host_alloc(qt_ctx *ctx, size_t bytes, void **out) {
     std::lock_guard<std::recursive_mutex> g(ctx->lock);
-    const size_t cls = size_class(bytes ? bytes : 1);
-    auto it = ctx->free_pinned.find(cls);
-    if (it != ctx->free_pinned.end() && !it->second.empty()) {
-        *out = it->second.back();
-        it->second.pop_back();
-        return QT_OK;
-    }
+    const size_t cls = size_class(std::max<size_t>(bytes, ctx->min_class));
+    // a cached block of this class, or of a somewhat larger class (cache_stretch)
+    for (auto it = ctx->free_pinned.lower_bound(cls); it != ctx->free_pinned.end() && it->first <= cls * cache_stretch(cls);
+         ++it)
+        if (!it->second.empty()) {
+            *out = it->second.back();
+            it->second.pop_back();
+            return QT_OK;
+        }
     void *p = nullptr;
     cudaError_t e = cudaMallocHost(&p, cls);
     if (e != cudaSuccess) return cuda_error(ctx, e, "cudaMallocHost");
@@ -102,15 +108,19 @@ void host_free(qt_ctx *ctx, void *p) {
 
 qt_status dev_alloc(qt_ctx *ctx, size_t bytes, void **out) {
     std::unique_lock<std::mutex> g(ctx->alloc_lock);
-    const size_t cls = size_class(bytes ? bytes : 1);
-    auto it = ctx->free_blocks.find(cls);
-    if (it != ctx->free_blocks.end() && !it->second.empty()) {
-        *out = it->second.back();
-        it->second.pop_back();
-        ctx->bytes_cached -= cls;
-        ctx->bytes_in_use += cls;
-        return QT_OK;
-    }
+    const size_t cls = size_class(std::max<size_t>(bytes, ctx->min_class));
+    // a cached block of this class, or of a somewhat larger class
+    // (cache_stretch): a cudaMalloc can wait tens of milliseconds behind other threads'
+    // large allocations, a somewhat larger block costs nothing
+    for (auto it = ctx->free_blocks.lower_bound(cls); it != ctx->free_blocks.end() && it->first <= cls * cache_stretch(cls);
+         ++it)
+        if (!it->second.empty()) {
+            *out = it->second.back();
+            it->second.pop_back();
+            ctx->bytes_cached -= it->first;
+            ctx->bytes_in_use += it->first;
+            return QT_OK;
+        }
     if (ctx->memory_budget && ctx->bytes_in_use + cls > ctx->memory_budget)
         return set_error(ctx, QT_ERR_OUT_OF_MEMORY, "device memory budget exceeded");
     void *p = nullptr;

@@ -29,6 +29,11 @@ struct qt_ctx {
     // that runs out of device memory can empty other contexts' caches while
     // their owners run
     std::mutex alloc_lock;
+    // smallest size class of both caching allocators: a context that serves
+    // many short batches of varying size (a server's light lane) rounds its
+    // blocks up so that every batch after the first finds them cached -- a
+    // cudaMalloc or cudaMallocHost can wait behind other threads' large ones
+    size_t min_class = 256;
     std::map<size_t, std::vector<void *>> free_blocks;
     std::map<void *, size_t> block_size;
     uint64_t bytes_in_use = 0;
