@@ -8,6 +8,7 @@
 #include <new>
 #include <set>
 #include <sstream>
+#include <tuple>
 
 #include "kernels.h"
 #include "plan.h"
@@ -774,6 +775,41 @@ static qt_status batch_pack(qt_batch *b) {
 // memory regions of a CTA, the grid, the schedule, the global workspace slab
 // and the instance descriptors.  Leaf images, values and plan blocks stay where
 // they are, so a policy change (and each autotuner candidate) only re-runs this.
+// The occupancy figures a batch sizes its launch by, computed once per shape:
+// the driver queries behind them can wait while other threads allocate.
+static std::mutex g_launch_shape_lock;
+static std::map<std::tuple<size_t, int, int, int>, int> g_max_grid;
+static std::map<int, size_t> g_smem_limit;
+
+static int cached_max_grid(size_t smem, int per_sm_cap, int variant) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const auto key = std::make_tuple(smem, per_sm_cap, variant, dev);
+    {
+        std::lock_guard<std::mutex> g(g_launch_shape_lock);
+        auto it = g_max_grid.find(key);
+        if (it != g_max_grid.end()) return it->second;
+    }
+    const int v = plan_max_grid(smem, per_sm_cap, variant);
+    std::lock_guard<std::mutex> g(g_launch_shape_lock);
+    g_max_grid[key] = v;
+    return v;
+}
+
+static size_t cached_smem_limit() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    {
+        std::lock_guard<std::mutex> g(g_launch_shape_lock);
+        auto it = g_smem_limit.find(dev);
+        if (it != g_smem_limit.end()) return it->second;
+    }
+    const size_t v = plan_smem_limit();
+    std::lock_guard<std::mutex> g(g_launch_shape_lock);
+    if (v) g_smem_limit[dev] = v;
+    return v;
+}
+
 static qt_status batch_configure(qt_batch *b) {
     qt_ctx *ctx = b->ctx;
     const int prec = b->prepared_prec;
@@ -842,10 +878,10 @@ static qt_status batch_configure(qt_batch *b) {
     b->tile_bytes = any_tiled ? kCtaTileBytes : 0;
     b->ws_in_smem = ws <= b->ws_smem_bytes;   // no global slab needed
     const size_t smem = plan_header_bytes(b->header_steps) + 128 + b->ws_smem_bytes + b->stage_bytes + b->tile_bytes;
-    if (n_grouped && smem > plan_smem_limit())
+    if (n_grouped && smem > cached_smem_limit())
         return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "launch policy needs more shared memory than a CTA may have");
     b->variant = pol.kernel_ctas ? pol.kernel_ctas : many ? 4 : n_grouped <= plan_num_sms() ? 1 : 2;
-    b->grid = n_grouped ? std::min(n_grouped, plan_max_grid(smem, pol.ctas_per_sm, b->variant)) : 0;
+    b->grid = n_grouped ? std::min(n_grouped, cached_max_grid(smem, pol.ctas_per_sm, b->variant)) : 0;
     qt_status s = QT_OK;
     if (b->grid > 0 && !b->ws_in_smem) s = dev_alloc(ctx, b->ws_stride * b->grid, &b->d_ws);
     // more instances than CTAs: a dynamic schedule over the instances sorted by
