@@ -100,7 +100,7 @@ __host__ __device__ inline void stream_layout(const StreamStep &p, uint32_t off[
     off[0] = 0;                                                  // kStreamStages tile buffers
     off[1] = kStreamStages * round128(8u * tile);                // staged outputs of a pass
     off[2] = off[1] + round128(8u * staged);                     // S
-    off[3] = off[2] + round128(8u * p.s_elems);                  // full[stages], empty[stages], issued count,
+    off[3] = off[2] + round128(8u * p.s_store);                  // full[stages], empty[stages], issued count,
                                                                  // C offsets and staged indices of (g, f)
     off[4] = off[3] + round128(16u * kStreamStages + 8u + 20u * kStreamMaxStage);   // end
 }
@@ -174,7 +174,11 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
     const uint32_t n_out = 1u << (2 * p.n_dout);
 
-    for (uint32_t e = tid; e < p.s_elems; e += blockDim.x) S[e] = p.S[e];
+    for (uint32_t e = tid; e < p.s_elems; e += blockDim.x) {
+        uint32_t dst = 0;
+        for (int w = 0; w < kStreamMaxSmallRank; w++) dst += ((e >> (2 * w)) & 3u) * p.s_unit[w];
+        S[dst] = p.S[e];
+    }
     if (tid < (uint32_t) M) {
         out_off[tid] = out_offset(p, tid / NSF, tid % NSF);
         st_gf[tid] = staged_index(p, tid / NSF, tid % NSF);
@@ -220,7 +224,7 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
         for (int w = 0; w < 4; w++) {
             const uint32_t dg = (tid >> (2 * w)) & 3u;
             if (p.lo_summed[w]) {
-                s_lo += dg << (2 * p.lo_other[w]);
+                s_lo += dg * p.s_unit[p.lo_other[w]];
             } else {
                 c_lo += dg << (2 * p.lo_other[w]);
                 st_lo += dg << (2 * p.lo_rank[w]);
@@ -242,19 +246,11 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
                     for (uint32_t j = 0; j < p.ho; j++) {
                         const uint32_t dg = ((uint32_t) h >> (2 * j)) & 3u;
                         th += dg << (2 * p.h_pos[j]);
-                        sh += dg << (2 * p.h_sw[j]);
+                        sh += dg * p.s_unit[p.h_sw[j]];
                     }
                 eo[g * H + h] = th;
                 so[g * H + h] = sh;
             }
-        }
-        uint32_t sfo[NSF];
-#pragma unroll
-        for (int f = 0; f < NSF; f++) {
-            uint32_t o = 0;
-            if (NSF > 1)
-                for (uint32_t j = 0; j < p.nsfp; j++) o += (((uint32_t) f >> (2 * j)) & 3u) << (2 * p.sf_w[j]);
-            sfo[f] = o;
         }
         // with 16 free indices of S the element loop stays rolled (its body
         // is 64 FMAs already): the offsets then come from shared memory
@@ -265,7 +261,7 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
                 for (uint32_t j = 0; j < p.ho; j++) {
                     const uint32_t dg = (tid >> (2 * j)) & 3u;
                     th += dg << (2 * p.h_pos[j]);
-                    sh += dg << (2 * p.h_sw[j]);
+                    sh += dg * p.s_unit[p.h_sw[j]];
                 }
                 eo_s[tid] = th;
                 so_s[tid] = sh;
@@ -291,7 +287,7 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
             const float2 *T = tiles + (uint64_t) s * tile_stride + tid;
             // S's share of the chunk's summed digits
             uint32_t s_c = 0;
-            for (uint32_t j = 0; j < p.n_chunk_d; j++) s_c += ((chunk >> (2 * j)) & 3u) << (2 * p.chunk_sw[j]);
+            for (uint32_t j = 0; j < p.n_chunk_d; j++) s_c += ((chunk >> (2 * j)) & 3u) * p.s_unit[p.chunk_sw[j]];
             uint64_t cbase = 0;
             for (uint32_t j = 0; j < p.n_item_d; j++) cbase += (uint64_t) ((item >> (2 * j)) & 3u) << (2 * p.item_cd[j]);
             // a work item with several passes has one chunk (stream_plan), so
@@ -301,7 +297,7 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
                 uint64_t cpass = cbase;
                 for (uint32_t j = p.nsfp; j < p.nsf; j++) {
                     const uint32_t dg = (pass >> (2 * (j - p.nsfp))) & 3u;
-                    s_p += dg << (2 * p.sf_w[j]);
+                    s_p += dg * p.s_unit[p.sf_w[j]];
                     cpass += (uint64_t) dg << (2 * p.sf_cd[j]);
                 }
                 if (chunk == 0) {
@@ -311,22 +307,37 @@ __global__ void __launch_bounds__(kStreamBlock, stream_min_ctas<NSF, G, H>())
                         for (int f = 0; f < NSF; f++) acc[g][f] = make_float2(0.f, 0.f);
                 }
                 const float2 *Sp = S + s_p;
+                // a block of S's image holds an element's NSF values side by
+                // side, 16-byte aligned (blocks are an even number of elements
+                // apart): pairs of them load as one float4
                 if constexpr (NSF >= 16) {
                     // G == 1 here: every element adds into acc[0]
 #pragma unroll 1
                     for (int i = 0; i < E; i++) {
                         const float2 x = T[eo_s[i]];
-                        const float2 *Si = Sp + so_s[i];
+                        const float4 *Si = reinterpret_cast<const float4 *>(Sp + so_s[i]);
 #pragma unroll
-                        for (int f = 0; f < NSF; f++) cmac(acc[0][f], x, Si[sfo[f]]);
+                        for (int f = 0; f < NSF; f += 2) {
+                            const float4 s2 = Si[f / 2];
+                            cmac(acc[0][f], x, make_float2(s2.x, s2.y));
+                            cmac(acc[0][f + 1], x, make_float2(s2.z, s2.w));
+                        }
                     }
-                } else {
+                } else if constexpr (NSF >= 4) {
 #pragma unroll
                     for (int i = 0; i < E; i++) {
                         const float2 x = T[eo[i]];
+                        const float4 *Si = reinterpret_cast<const float4 *>(Sp + so[i]);
 #pragma unroll
-                        for (int f = 0; f < NSF; f++) cmac(acc[i / H][f], x, Sp[so[i] + sfo[f]]);
+                        for (int f = 0; f < NSF; f += 2) {
+                            const float4 s2 = Si[f / 2];
+                            cmac(acc[i / H][f], x, make_float2(s2.x, s2.y));
+                            cmac(acc[i / H][f + 1], x, make_float2(s2.z, s2.w));
+                        }
                     }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < E; i++) cmac(acc[i / H][0], T[eo[i]], Sp[so[i]]);
                 }
                 if (pass + 1 == p.n_pass) {
                     __syncwarp();
@@ -518,6 +529,19 @@ bool stream_plan(const StepDesc &d, StreamStep &p) {
     p.nsfp = (uint32_t) std::min(nsf, 2);
     p.n_pass = 1u << (2 * (nsf - (int) p.nsfp));
     p.s_elems = 1u << (2 * rS);
+    {
+        const uint32_t nblk = 1u << (2 * p.nsfp);
+        const uint32_t bstride = nblk == 1 ? 1u : nblk + 2u;
+        bool in_blk[kStreamMaxSmallRank] = {false};
+        for (uint32_t j = 0; j < p.nsfp; j++) {
+            in_blk[p.sf_w[j]] = true;
+            p.s_unit[p.sf_w[j]] = 1u << (2 * j);
+        }
+        uint32_t rank = 0;
+        for (int w = 0; w < rS; w++)
+            if (!in_blk[w]) p.s_unit[w] = bstride << (2 * rank++);
+        p.s_store = bstride << (2 * rank);
+    }
     // wires 0-3: the thread's own digits
     int klo = 0;
     for (int w = 0; w < 4; w++) {

@@ -47,6 +47,13 @@ struct StreamStep {
     uint32_t run_elems;            // elements of one bulk copy (4^(lowest in-tile wires in a row))
     uint32_t n_runs;               // bulk copies per tile
     uint32_t s_elems;              // 4^rank(S)
+    uint32_t s_store;              // elements of S's shared-memory image (blocks with padding)
+    // S's image: the in-pass free indices of S are each block's elements, in
+    // order (so a thread's NSF values for one element lie side by side and load
+    // as 16-byte pairs), blocks NSF + 2 elements apart (NSF > 1; the pad turns
+    // the lanes' different blocks onto different banks), S's other wires number
+    // the blocks.  s_unit[w]: image offset of one step of S wire w
+    uint32_t s_unit[kStreamMaxSmallRank];
     uint32_t nsf;                  // free wires of S
     uint32_t nsfp;                 // of which one pass covers (NSFP = 4^nsfp sums per thread and g)
     uint32_t n_pass;               // passes over a tile: combinations of S's free wires beyond nsfp

@@ -88,6 +88,18 @@ static std::string emulate(const StepDesc &d, const StreamStep &p, std::mt19937 
     if (tile_elems > kStreamMaxTile || M > kStreamMaxStage || p.s_elems != S.size()) return "region sizes";
     if (p.run_elems * p.n_runs != tile_elems || p.run_elems < 256) return "runs";
     if (p.n_pass > 1 && p.n_chunks > 1) return "passes with chunks";
+    // S's shared-memory image: element e at sum of digit_w(e) * s_unit[w];
+    // every slot written at most once, in-pass blocks 16-byte aligned
+    if (p.s_store > 8192) return "S image size";
+    std::vector<cf> Simg(p.s_store, cf(NAN, NAN));
+    std::vector<int> s_hits(p.s_store, 0);
+    for (uint32_t e = 0; e < p.s_elems; e++) {
+        uint32_t dst = 0;
+        for (int w = 0; w < kStreamMaxSmallRank; w++) dst += ((e >> (2 * w)) & 3u) * p.s_unit[w];
+        if (dst >= p.s_store) return "S image index";
+        if (s_hits[dst]++) return "S image slot written twice";
+        Simg[dst] = S[e];
+    }
     std::vector<int> written(nC, 0);
     std::vector<cf> tile(tile_elems);
     // acc[pass][tid][i], i = g NSF + f, kept across the chunks of a work item
@@ -97,7 +109,7 @@ static std::string emulate(const StepDesc &d, const StreamStep &p, std::mt19937 
         c_p = 0;
         for (uint32_t j = p.nsfp; j < p.nsf; j++) {
             const uint32_t dg = (pass >> (2 * (j - p.nsfp))) & 3u;
-            s_p += dg << (2 * p.sf_w[j]);
+            s_p += dg * p.s_unit[p.sf_w[j]];
             c_p += (uint64_t) dg << (2 * p.sf_cd[j]);
         }
     };
@@ -117,7 +129,7 @@ static std::string emulate(const StepDesc &d, const StreamStep &p, std::mt19937 
                 for (uint32_t e = 0; e < p.run_elems; e++) tile[(uint64_t) r * p.run_elems + e] = L[off + e];
             }
             uint32_t s_c = 0;
-            for (uint32_t j = 0; j < p.n_chunk_d; j++) s_c += ((chunk >> (2 * j)) & 3u) << (2 * p.chunk_sw[j]);
+            for (uint32_t j = 0; j < p.n_chunk_d; j++) s_c += ((chunk >> (2 * j)) & 3u) * p.s_unit[p.chunk_sw[j]];
             for (uint32_t pass = 0; pass < p.n_pass; pass++) {
                 uint32_t s_p;
                 uint64_t c_p;
@@ -125,7 +137,7 @@ static std::string emulate(const StepDesc &d, const StreamStep &p, std::mt19937 
                 for (uint32_t tid = 0; tid < T; tid++) {
                     uint32_t s_lo = 0;
                     for (int w = 0; w < 4; w++)
-                        if (p.lo_summed[w]) s_lo += ((tid >> (2 * w)) & 3u) << (2 * p.lo_other[w]);
+                        if (p.lo_summed[w]) s_lo += ((tid >> (2 * w)) & 3u) * p.s_unit[p.lo_other[w]];
                     for (uint32_t gg = 0; gg < G; gg++) {
                         uint32_t tg = tid;
                         for (uint32_t j = 0; j < p.go; j++) tg += ((gg >> (2 * j)) & 3u) << (2 * p.g_pos[j]);
@@ -134,14 +146,14 @@ static std::string emulate(const StepDesc &d, const StreamStep &p, std::mt19937 
                             for (uint32_t j = 0; j < p.ho; j++) {
                                 const uint32_t dg = (h >> (2 * j)) & 3u;
                                 th += dg << (2 * p.h_pos[j]);
-                                sh += dg << (2 * p.h_sw[j]);
+                                sh += dg * p.s_unit[p.h_sw[j]];
                             }
                             if (th >= tile_elems) return "tile index";
+                            // the kernel loads the block's NSF values as 16-byte pairs
+                            if (NSF > 1 && (sh % 2)) return "S block not 16-byte aligned";
                             for (uint32_t f = 0; f < NSF; f++) {
-                                uint32_t so = 0;
-                                for (uint32_t j = 0; j < p.nsfp; j++) so += ((f >> (2 * j)) & 3u) << (2 * p.sf_w[j]);
-                                if (sh + so >= S.size()) return "small operand index";
-                                acc[pass][tid][gg * NSF + f] += tile[th] * S[sh + so];
+                                if (sh + f >= p.s_store || !s_hits[sh + f]) return "small operand index";
+                                acc[pass][tid][gg * NSF + f] += tile[th] * Simg[sh + f];
                             }
                         }
                     }
