@@ -66,19 +66,25 @@ __device__ __forceinline__ void split_tf32(float x, float &hi, float &lo) {
 }
 
 // X: rows m < M, columns j < 2K; Y: rows i < 2N, columns j < 2K (see the file
-// comment).  One CTA per (row tile, k tile) of an operand: the tile's 128 row
-// offsets and 32 column offsets into the gathered operand are computed once
-// into shared memory, then its 4096 values are gathered, split hi/lo and
-// written in the tile's own canonical core-matrix order, so each warp's stores
-// are contiguous and no thread divides.
+// comment).  One CTA per (row tile, k tile of the first half of the columns):
+// the tile's 128 row offsets and its column offsets into the gathered operand
+// are computed once into shared memory, then every complex element the CTA
+// covers is read once and written to all the places it goes -- X: (m, k) and
+// (m, K + k); Y: rows 2n and 2n + 1 at columns k and K + k -- split hi/lo, in
+// the tiles' canonical core-matrix order (contiguous stores per warp).  The
+// element-per-place version read X's elements twice and Y's four times.  With
+// K = 16 a single k tile holds both halves (columns 0-15 and 16-31).
 __global__ void __launch_bounds__(256) pack_tiles(const float2 *__restrict__ src, const StepDesc d, int which,
                                                   uint64_t rows, uint64_t K, uint64_t k_tiles,
                                                   float *__restrict__ hi, float *__restrict__ lo) {
     __shared__ uint64_t row_off[kTileM];
     __shared__ uint64_t col_off[kTileK];
-    const uint64_t tk = blockIdx.x, tr = blockIdx.y;   // k tile, row tile
+    const uint64_t tk = blockIdx.x, tr = blockIdx.y;   // k tile of the first half, row tile
     const uint32_t tid = threadIdx.x;
     const uint64_t M = 1ull << (2 * d.fA);
+    const bool one_tile = K < (uint64_t) kTileK;           // both halves in tile 0
+    const uint64_t half_tiles = one_tile ? 0 : K / kTileK;  // tile of column K + k: tk + half_tiles
+    const uint32_t kcols = one_tile ? (uint32_t) K : (uint32_t) kTileK;
     if (tid < (uint32_t) kTileM) {
         const uint64_t r = tr * kTileM + tid;
         uint64_t oa = 0, ob = 0;
@@ -86,30 +92,43 @@ __global__ void __launch_bounds__(256) pack_tiles(const float2 *__restrict__ src
         if (r < rows) scatter_c(which == 0 ? r : (r >> 1) * M, d, oa, ob);
         row_off[tid] = which == 0 ? oa : ob;
     } else if (tid < (uint32_t) (kTileM + kTileK)) {
-        const uint64_t j = tk * kTileK + (tid - kTileM);
-        const uint64_t k = j < K ? j : j - K;
-        col_off[tid - kTileM] = j < 2 * K ? scatter_digits(k, which == 0 ? d.posAs : d.posBs, d.nSum) : 0;
+        const uint32_t kk = tid - kTileM;
+        const uint64_t k = tk * kTileK + kk;
+        col_off[kk] = kk < kcols && k < K ? scatter_digits(k, which == 0 ? d.posAs : d.posBs, d.nSum) : 0;
     }
     __syncthreads();
-    float *const th = hi + (tr * k_tiles + tk) * (uint64_t) (kTileBytes / 4);
-    float *const tl = lo + (tr * k_tiles + tk) * (uint64_t) (kTileBytes / 4);
+    const uint64_t tile_floats = kTileBytes / 4;
+    float *const h0 = hi + (tr * k_tiles + tk) * tile_floats, *const l0 = lo + (tr * k_tiles + tk) * tile_floats;
+    float *const h1 = hi + (tr * k_tiles + tk + half_tiles) * tile_floats;
+    float *const l1 = lo + (tr * k_tiles + tk + half_tiles) * tile_floats;
+    auto put = [](float *h, float *l, uint32_t p, float v) {
+        float a, b;
+        split_tf32(v, a, b);
+        h[p] = a;
+        l[p] = b;
+    };
     for (uint32_t p = tid; p < (uint32_t) (kTileM * kTileK); p += blockDim.x) {
         // p = ((rr / 8) * 8 + kk / 4) * 32 + (rr % 8) * 4 + kk % 4 (tiled_offset inside a tile)
         const uint32_t kk = (p & 3u) | (((p >> 5) & 7u) << 2);
         const uint32_t rr = ((p >> 2) & 7u) | ((p >> 8) << 3);
-        const uint64_t r = tr * kTileM + rr, j = tk * kTileK + kk;
-        float v = 0.f;
-        if (r < rows && j < 2 * K) {
-            const bool second = j >= K;
-            const float2 x = src[row_off[rr] + col_off[kk]];
-            if (which == 0) v = second ? x.y : x.x;
-            else if ((r & 1) == 0) v = second ? -x.y : x.x;
-            else v = second ? x.x : x.y;
+        if (kk >= kcols) continue;             // the Im half of a one-tile operand: written below
+        if (which == 1 && (rr & 1u)) continue;   // Y's odd rows: written with the even one
+        const uint64_t r = tr * kTileM + rr;
+        float2 x = make_float2(0.f, 0.f);
+        if (r < rows && tk * kTileK + kk < K) x = src[row_off[rr] + col_off[kk]];
+        // the Im half's position: the same (rr, kk) in the second tile, or 16 columns on
+        const uint32_t q = one_tile ? p + 128u : p;
+        float *const hq = one_tile ? h0 : h1, *const lq = one_tile ? l0 : l1;
+        if (which == 0) {
+            put(h0, l0, p, x.x);
+            put(hq, lq, q, x.y);
+        } else {
+            // row 2n = [Br | -Bi], row 2n + 1 = [Bi | Br]; row rr + 1 sits 4 floats on
+            put(h0, l0, p, x.x);
+            put(hq, lq, q, -x.y);
+            put(h0, l0, p + 4u, x.y);
+            put(hq, lq, q + 4u, x.x);
         }
-        float h, l;
-        split_tf32(v, h, l);
-        th[p] = h;
-        tl[p] = l;
     }
 }
 
@@ -361,8 +380,11 @@ cudaError_t launch_gemm_step(const StepDesc &d, const float2 *A, const float2 *B
     const GemmSizes s = gemm_sizes(d);
     float *xh = scratch, *xl = xh + s.x_floats, *yh = xl + s.x_floats, *yl = yh + s.y_floats;
     if (s.m_tiles > 65535 || s.n_tiles > 65535 || s.k_tiles > 0x7fffffffull) return cudaErrorInvalidValue;
-    pack_tiles<<<dim3((unsigned) s.k_tiles, (unsigned) s.m_tiles), 256, 0, stream>>>(A, d, 0, s.M, s.K, s.k_tiles, xh, xl);
-    pack_tiles<<<dim3((unsigned) s.k_tiles, (unsigned) s.n_tiles), 256, 0, stream>>>(B, d, 1, s.N2, s.K, s.k_tiles, yh, yl);
+    // one CTA per k tile of the first half of the columns (the second half's
+    // tiles are written by the same CTAs)
+    const uint64_t kt_half = s.K < (uint64_t) kTileK ? 1 : s.K / kTileK;
+    pack_tiles<<<dim3((unsigned) kt_half, (unsigned) s.m_tiles), 256, 0, stream>>>(A, d, 0, s.M, s.K, s.k_tiles, xh, xl);
+    pack_tiles<<<dim3((unsigned) kt_half, (unsigned) s.n_tiles), 256, 0, stream>>>(B, d, 1, s.N2, s.K, s.k_tiles, yh, yl);
     const size_t smem = gemm_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     if (e != cudaSuccess) return e;
