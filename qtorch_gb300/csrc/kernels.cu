@@ -1146,6 +1146,18 @@ __global__ void __launch_bounds__(plan_threads(kMinCtas), kMinCtas) plan_kernel(
             I.value[1] = val.y;
         }
         __syncthreads();   // the next instance reuses the header, the workspace and s_next
+        if (ws == ws_global) {
+            // The instance's intermediates are dead.  Their L2 lines are
+            // dropped without being written back (discard is a weak write of
+            // an indeterminate value; every intermediate of the next instance
+            // is written before it is read), so a slab larger than L2 does not
+            // turn every finished instance into DRAM writes.  The slab's stride
+            // is a multiple of 256 bytes, so each line belongs to this CTA.
+            const uint32_t lines = (I.ws_bytes + 127u) >> 7;
+            for (uint32_t l = threadIdx.x; l < lines; l += blockDim.x)
+                asm volatile("discard.global.L2 [%0], 128;" ::"l"(ws + ((uint64_t) l << 7)) : "memory");
+            __syncthreads();   // ordered before the next instance's first writes
+        }
         if (!lp.next) inst += gridDim.x;
     }
 }
