@@ -477,8 +477,24 @@ static qt_status resident_start(qt_batch *b, uint32_t first_seq) {
         if (s != QT_OK) return s;
         b->h_angles = static_cast<double *>(ha);
     }
+    // Requests post tagged angle words when every instance's angles fit one per
+    // thread of its CTA (they are polled one per thread).
+    if (!b->d_inst_res) {
+        const int threads = plan_threads(b->variant);
+        b->res_tagged = b->n_angles > 0;
+        for (const qt_plan *p : b->plans)
+            if ((int) p->rot_kind.size() > threads) b->res_tagged = false;
+    }
+    if (b->res_tagged && !b->h_tagged) {
+        void *ht = nullptr;
+        s = host_alloc(ctx, sizeof(uint64_t) * b->n_angles, &ht);
+        if (s != QT_OK) return s;
+        b->h_tagged = static_cast<uint64_t *>(ht);
+        std::memset(b->h_tagged, 0, sizeof(uint64_t) * b->n_angles);   // request 0 is never posted
+    }
     void *ha = nullptr, *hv = nullptr, *hm = nullptr;
-    if (b->h_angles) e = cudaHostGetDevicePointer(&ha, b->h_angles, 0);
+    if (b->res_tagged) e = cudaHostGetDevicePointer(&ha, b->h_tagged, 0);
+    else if (b->h_angles) e = cudaHostGetDevicePointer(&ha, b->h_angles, 0);
     if (e == cudaSuccess) e = cudaHostGetDevicePointer(&hv, b->h_values, 0);
     if (e == cudaSuccess) e = cudaHostGetDevicePointer(&hm, b->h_mail, 0);
     if (e != cudaSuccess) return cuda_error(ctx, e, "mapped host buffers");
@@ -487,6 +503,7 @@ static qt_status resident_start(qt_batch *b, uint32_t first_seq) {
         std::vector<InstanceDesc> zc = b->inst_desc;
         for (size_t j = 0; j < n; j++) {
             const int i = b->inst_index[j];
+            // (tagged: the 64-bit words of h_tagged, one per angle, at the same offsets)
             zc[j].angles = b->plans[i]->rot_kind.empty() ? nullptr
                                                          : static_cast<const double *>(ha) + b->inst_angle_off[i];
             zc[j].value = static_cast<double *>(hv) + 2 * i;
@@ -511,6 +528,7 @@ static qt_status resident_start(qt_batch *b, uint32_t first_seq) {
     rl.done = static_cast<uint32_t *>(hm) + 32;
     rl.first_seq = first_seq;
     rl.idle_polls = (uint32_t) std::min(4.0e9, std::max(1.0, b->res_idle * 1.0e6));
+    rl.tagged = b->res_tagged ? 1u : 0u;
     for (size_t j = 0; j < n; j++) __atomic_store_n(&b->h_mail[32 + j], 0u, __ATOMIC_RELAXED);   // no flag from a previous run
     __atomic_store_n(&b->h_mail[0], first_seq, __ATOMIC_RELEASE);
     e = launch_resident(rl, b->res_stream, b->variant);
@@ -521,8 +539,12 @@ static qt_status resident_start(qt_batch *b, uint32_t first_seq) {
     return QT_OK;
 }
 
+// A value slot's contents while its answer has not arrived: a signalling NaN
+// (quiet bit clear, payload nonzero), which no arithmetic result can be.
+constexpr uint64_t kValuePending = 0x7ff4c0de0000d0e5ull;
+
 // One evaluation through the engine: angles into pinned memory, the request
-// number after them, then every CTA's done flag.
+// number after them, then every CTA's value.
 static qt_status resident_evaluate(qt_batch *b, const double *angles, int64_t n_angles, double *values) {
     qt_ctx *ctx = b->ctx;
     if (n_angles != b->n_angles) return set_error(ctx, QT_ERR_INVALID_ARGUMENT, "angle count does not match the batch");
@@ -530,23 +552,52 @@ static qt_status resident_evaluate(qt_batch *b, const double *angles, int64_t n_
     const size_t n = b->inst_desc.size();
     // (an engine whose CTAs left while idle shows it in their flags: the wait
     // below restarts it)
-    // the previous request is complete, so the pinned angles are free
-    if (b->res_running && n_angles) std::memcpy(b->h_angles, angles, sizeof(double) * n_angles);
     if (!b->res_running) {
         s = resident_start(b, b->res_seq);
         if (s != QT_OK) return s;
-        if (n_angles) std::memcpy(b->h_angles, angles, sizeof(double) * n_angles);
     }
-    uint32_t seq = b->res_seq + 1;
-    if (seq == 0 || seq >= kResidentLeft) seq = 1;
+    uint32_t seq = resident_next_request(b->res_seq);
     b->res_seq = seq;
+    // Every value slot holds a signalling-NaN pattern until its CTA writes the
+    // answer (arithmetic never produces a signalling NaN).  The host watches the
+    // values themselves: a CTA writes its value and only then, behind a
+    // system-scope release, its done flag, so the value is in host memory one
+    // CPU-GPU round trip before the flag.  The slots are reset before the
+    // request's angles and number are published (release), so no answer can be
+    // overwritten.
+    uint64_t *const hv = reinterpret_cast<uint64_t *>(b->h_values);
+    for (size_t j = 0; j < n; j++) {
+        const size_t i = (size_t) b->inst_index[j];
+        __atomic_store_n(hv + 2 * i, kValuePending, __ATOMIC_RELAXED);
+        __atomic_store_n(hv + 2 * i + 1, kValuePending, __ATOMIC_RELAXED);
+    }
+    if (b->res_tagged) {
+        // (request << 32) | the angle narrowed to float, as the device narrows it
+        __atomic_thread_fence(__ATOMIC_RELEASE);
+        for (int64_t r = 0; r < n_angles; r++) {
+            const float f = (float) angles[r];
+            uint32_t bits;
+            std::memcpy(&bits, &f, 4);
+            __atomic_store_n(b->h_tagged + r, ((uint64_t) seq << 32) | bits, __ATOMIC_RELAXED);
+        }
+    } else if (n_angles) {
+        // the previous request is complete, so the pinned angles are free
+        std::memcpy(b->h_angles, angles, sizeof(double) * n_angles);
+    }
     __atomic_store_n(&b->h_mail[0], seq, __ATOMIC_RELEASE);
-    // Wait for every CTA's flag.  The engine is asked about only after a
-    // millisecond without an answer (a stream query costs more than a request).
+    // Wait for every CTA's value (or flag).  The engine is asked about only
+    // after a millisecond without an answer (a stream query costs more than a
+    // request).
     const auto t0 = std::chrono::steady_clock::now();
     bool relaunched = false;
     uint64_t spins = 0;
     for (size_t j = 0; j < n;) {
+        const size_t i = (size_t) b->inst_index[j];
+        if (__atomic_load_n(hv + 2 * i, __ATOMIC_ACQUIRE) != kValuePending &&
+            __atomic_load_n(hv + 2 * i + 1, __ATOMIC_ACQUIRE) != kValuePending) {
+            j++;
+            continue;
+        }
         const uint32_t d = __atomic_load_n(&b->h_mail[32 + j], __ATOMIC_ACQUIRE);
         if (d == seq) {
             j++;
@@ -604,6 +655,9 @@ static void batch_release(qt_batch *b) {
     b->tile_bytes = 0;
     host_free(ctx, b->h_angles);
     b->h_angles = nullptr;
+    host_free(ctx, b->h_tagged);
+    b->h_tagged = nullptr;
+    b->res_tagged = false;
     if (b->angles_done) cudaEventDestroy(b->angles_done);
     b->angles_done = nullptr;
     b->dev_rot = false;

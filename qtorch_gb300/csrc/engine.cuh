@@ -200,7 +200,18 @@ struct ResidentLaunch {
     uint32_t *done;              // mapped host, one per instance: the last request it finished
     uint32_t first_seq;          // requests up to this number are served already
     uint32_t idle_polls;         // polls (about a microsecond apart) without a request before leaving
+    uint32_t tagged;             // 1: each instance's angles are 64-bit words, (request << 32) | the
+                                 // angle narrowed to float, so the poll that sees the request also
+                                 // brings its angles (instances with at most a CTA's threads of angles)
+    uint32_t pad;
 };
+
+// The request after `last` (the host's numbering skips 0 and the two reserved
+// values kResidentLeft, kResidentStop).
+__host__ __device__ inline uint32_t resident_next_request(uint32_t last) {
+    const uint32_t n = last + 1u;
+    return (n == 0u || n >= kResidentLeft) ? 1u : n;
+}
 
 __host__ __device__ inline uint64_t scatter_digits(uint64_t x, const uint8_t *pos, int n) {
     uint64_t off = 0;

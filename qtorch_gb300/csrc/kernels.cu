@@ -1167,6 +1167,16 @@ __device__ __forceinline__ uint32_t ld_acquire_sys(const uint32_t *p) {
     asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ uint32_t ld_relaxed_sys(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint64_t ld_acquire_sys_u64(const uint64_t *p) {
+    uint64_t v;
+    asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ void st_release_sys(uint32_t *p, uint32_t v) {
     asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -1212,9 +1222,48 @@ __global__ void __launch_bounds__(plan_threads(kMinCtas), kMinCtas) resident_ker
     const PlanView v = plan_view(I.plan, staged ? stage : nullptr);
     char *const leaves = staged ? reinterpret_cast<char *>(stage) + I.plan_bytes : const_cast<char *>(I.leaves);
     uint32_t last = rl.first_seq;
+    // Tagged angle words: each carries its request's number beside the angle,
+    // so the poll that sees a request also brings the angles (one CPU-GPU
+    // round trip instead of two).
+    const bool tagged = rl.tagged && I.angles && v.P.n_rot > 0;
+    const uint64_t *const words = reinterpret_cast<const uint64_t *>(I.angles);
+    if (tagged && v.P.n_rot > (int) blockDim.x) {
+        // one word per thread is the host's promise; without it, say so and leave
+        if (threadIdx.x == 0) st_release_sys(rl.done + inst, kResidentLeft);
+        return;
+    }
     for (;;) {
-        if (threadIdx.x == 0) {
-            uint32_t s = last;
+        uint32_t s = last;
+        float angle = 0.f;
+        if (tagged) {
+            // Every thread that owns an angle polls its word until the word
+            // carries the next request's number; thread 0 also reads the
+            // request word, which here only says whether to leave.  Both are
+            // agreed CTA-wide, so every thread leaves the loop together.
+            const uint32_t want = resident_next_request(last);
+            bool have = threadIdx.x >= (uint32_t) v.P.n_rot;
+            for (uint32_t it = 0; it < rl.idle_polls; it++) {
+                const bool stop = threadIdx.x == 0 && ld_relaxed_sys(rl.seq) == kResidentStop;
+                if (!have) {
+                    // acquire: the host reset the value slots before it wrote
+                    // this word, so the value written below lands after them
+                    const uint64_t w = ld_acquire_sys_u64(words + threadIdx.x);
+                    if ((uint32_t) (w >> 32) == want) {
+                        have = true;
+                        angle = __uint_as_float((uint32_t) w);
+                    }
+                }
+                if (__syncthreads_and(have)) {
+                    s = want;
+                    break;
+                }
+                if (__syncthreads_or(stop)) {
+                    s = kResidentStop;
+                    break;
+                }
+                __nanosleep(it < 1024 ? 100 : 1000);   // a short spin after a request, then back off
+            }
+        } else if (threadIdx.x == 0) {
             for (uint32_t it = 0; it < rl.idle_polls; it++) {
                 s = ld_acquire_sys(rl.seq);
                 if (s != last) break;
@@ -1228,17 +1277,22 @@ __global__ void __launch_bounds__(plan_threads(kMinCtas), kMinCtas) resident_ker
         }
         if (threadIdx.x == 0) s_bad = 0;
         __syncthreads();
-        const uint32_t s = s_seq;
+        if (!tagged) s = s_seq;
         if (s == kResidentStop) break;   // asked to leave
         if (s == last) {                 // idle for too long: tell the host, then leave
             if (threadIdx.x == 0) st_release_sys(rl.done + inst, kResidentLeft);
             break;
         }
         last = s;
-        // the request's angles, read through to host memory (never a stale cached copy)
         if (I.angles && v.P.n_rot) {
-            for (int r = threadIdx.x; r < v.P.n_rot; r += blockDim.x)
-                build_rotation(leaves, v.rotations[r], __ldcv(I.angles + r));
+            if (tagged) {
+                // the angle arrived narrowed to float, as build_rotation narrows it
+                if (threadIdx.x < (uint32_t) v.P.n_rot) build_rotation(leaves, v.rotations[threadIdx.x], (double) angle);
+            } else {
+                // the request's angles, read through to host memory (never a stale cached copy)
+                for (int r = threadIdx.x; r < v.P.n_rot; r += blockDim.x)
+                    build_rotation(leaves, v.rotations[r], __ldcv(I.angles + r));
+            }
             __syncthreads();
         }
         plan_contract<true>(v, leaves, ws, h, tile, &s_bad, I.n_steps);

@@ -150,6 +150,8 @@ struct qt_batch {
     void *d_inst_res = nullptr;                       // descriptors on the mapped host angles and values
     uint32_t res_seq = 0;                             // the last request posted
     bool res_running = false;
+    bool res_tagged = false;                          // requests post tagged angle words (h_tagged)
+    uint64_t *h_tagged = nullptr;                     // pinned: (request << 32) | float bits, one per angle
     uint64_t res_starts = 0;                          // engine launches so far
 };
 

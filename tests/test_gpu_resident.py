@@ -108,3 +108,32 @@ def test_resident_needs_a_mixed_batch_with_one_cta_per_instance(ctx):
     big.prepare(qg.MIXED)
     with pytest.raises(qg.QtError):
         big.use_resident(1.0)
+
+
+def test_resident_engine_with_more_angles_than_threads(ctx):
+    """Requests normally post each angle in a 64-bit word tagged with the
+    request's number, polled one word per thread.  A plan with more rotations
+    than a CTA has threads takes the other request path (the request word,
+    then the angles); both must equal the launched path bit for bit."""
+    rng = np.random.default_rng(21)
+    lines = ["2"]
+    for _ in range(150):
+        lines += [f"Rx {rng.uniform(0, 6.28):.6f} 0", f"Rx {rng.uniform(0, 6.28):.6f} 1", "CZ 0 1"]
+    qasm = "\n".join(lines) + "\n"
+    long_plan = qg.Plan(qasm, "Z T", ordering="linegraph", ctx=ctx)
+    assert long_plan.num_rotations == 300
+    plans, angles = qaoa_terms(ctx, 1, 20, 3, seed=8)
+    for group in ([long_plan], plans):
+        res = mixed_batch(ctx, group)
+        ref = mixed_batch(ctx, group)
+        res.use_resident(1.0)
+        for k in range(4):
+            if group is plans:
+                a = angles(0.3 + 0.2 * k, 0.8 - 0.1 * k)
+            else:
+                a = rng.uniform(0, 6.28, 300)
+            got = res.evaluate(a)
+            assert np.array_equal(got, ref.evaluate(a)), k
+            assert np.all(np.isfinite(got))
+        assert res.resident_starts == 1
+        res.use_resident(0)
