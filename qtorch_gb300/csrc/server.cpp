@@ -209,14 +209,23 @@ static void lane_main(qt_server *s, int li) {
 
 static void dispatcher_main(qt_server *s) {
     std::unique_lock<std::mutex> g(s->m);
+    // A lane class (0: the light lane, 1: the others) whose next request could
+    // not be admitted stays blocked until the next wave ends and returns its
+    // memory; the other class keeps being served meanwhile (a light request
+    // that arrives while the heavy lanes wait for memory is not held up).
+    uint64_t blocked_at[2] = {UINT64_MAX, UINT64_MAX};
+    auto lane_open = [&](int i, bool any_small, bool any_big) {
+        const int cls = i > 0 ? 1 : 0;
+        return !s->lanes[i].busy && (cls ? any_big : any_small) && blocked_at[cls] != s->wave_ends;
+    };
     for (;;) {
         s->cv.wait(g, [&] {
-                if (s->stop) return true;
+            if (s->stop) return true;
             if (s->pending.empty()) return false;
             bool any_small = false, any_big = false;
             for (auto &r : s->pending) (r.small ? any_small : any_big) = true;
-            for (size_t i = 0; i < s->lanes.size(); i++)
-                if (!s->lanes[i].busy && (i > 0 ? any_big : any_small)) return true;
+            for (int i = 0; i < (int) s->lanes.size(); i++)
+                if (lane_open(i, any_small, any_big)) return true;
             return false;
         });
         if (s->stop) return;
@@ -228,7 +237,7 @@ static void dispatcher_main(qt_server *s) {
         }
         int li = -1;
         for (int i = 0; i < (int) s->lanes.size(); i++)
-            if (!s->lanes[i].busy && (i > 0 ? any_big : any_small)) {
+            if (lane_open(i, any_small, any_big)) {
                 li = i;
                 break;
             }
@@ -256,11 +265,10 @@ static void dispatcher_main(qt_server *s) {
             if (take_heavy) break;
         }
         if (wave.empty()) {
-            // nothing admissible on this lane until a running wave returns its
-            // memory: wait for the next wave to end (not for every wave -- the
-            // light lane keeps being served while heavy requests wait)
-            const uint64_t seen = s->wave_ends;
-            s->cv.wait(g, [&] { return s->stop || s->wave_ends != seen; });
+            // nothing admissible on this lane class until a running wave
+            // returns its memory: the class waits for the next wave to end,
+            // the other class does not
+            blocked_at[li > 0 ? 1 : 0] = s->wave_ends;
             continue;
         }
         s->lanes[li].wave = std::move(wave);

@@ -142,3 +142,44 @@ def test_small_requests_pass_a_heavy_one():
             srv.close()
     finally:
         ctx.close()
+
+
+def test_light_requests_run_while_a_heavy_one_waits_for_memory():
+    """A budget that holds one heavy request: the second waits for memory
+    while the first runs.  Light requests submitted meanwhile are served on
+    the light lane at once -- the dispatcher blocks only the heavy lanes until
+    a wave ends -- so they finish long before the first heavy request."""
+    import time
+
+    from qtorch_gb300.circuits import random_circuit_text
+    ctx = qg.Context(0)
+    try:
+        heavy = qg.Plan(random_circuit_text(14, 12, 6), "Z", ordering="auto", ctx=ctx)   # 4e8 MACs
+        dgf = qg.random_regular_graph(20, 3, seed=9)
+        small = [qg.Plan(*qg.qaoa_term_text(dgf, 1, [0.5, 1.2], e), ordering="linegraph", ctx=ctx)
+                 for e in range(8)]
+        alone = [p.execute(qg.FP64) for p in small]
+        heavy_alone = heavy.execute(qg.FP64)
+        # the server's footprint of an FP64 request: workspace + leaves + 4 KB
+        fp = heavy.workspace_bytes(qg.FP64) + 16 * heavy.leaf_values().size + 4096
+        ctx.set_memory_budget(int(fp * 1.5))
+        srv = qg.Server(max_inflight=64, precision=qg.FP64, ctx=ctx)
+        try:
+            for _ in range(2):   # the first round warms the lanes' caches
+                t1, t2 = srv.submit(heavy), srv.submit(heavy)
+                time.sleep(0.001)   # the second heavy request is waiting for memory by now
+                tickets = [srv.submit(p) for p in small]
+                srv.drain()
+                v1, l1 = srv.poll(t1)
+                v2, l2 = srv.poll(t2)
+                got = [srv.poll(t) for t in tickets]
+            assert v1 == heavy_alone and v2 == heavy_alone
+            assert l2 > l1
+            for (v, lat), want in zip(got, alone):
+                assert v == want
+                assert lat < 0.5 * l1, (lat, l1)
+        finally:
+            srv.close()
+    finally:
+        ctx.set_memory_budget(0)
+        ctx.close()
