@@ -39,6 +39,10 @@ struct qt_ctx {
     uint64_t bytes_in_use = 0;
     uint64_t bytes_cached = 0;
     uint64_t memory_budget = 0;          // 0 = unlimited
+    // stream-ordered pool (null: the caching allocator above): blocks are
+    // taken with cudaMallocFromPoolAsync and returned with cudaFreeAsync, both
+    // on this context's stream (a server's heavy lanes; device_pool())
+    cudaMemPool_t pool = nullptr;
     std::atomic<uint64_t> launches{0};
     std::atomic<uint64_t> device_allocs{0};   // cudaMalloc calls made by the caching allocator
     std::atomic<uint64_t> tc_steps{0};        // contraction steps run on the tcgen05 GEMM
@@ -72,6 +76,9 @@ qt_status cuda_error(qt_ctx *ctx, cudaError_t e, const char *what);
 // allocate from the context cache (bytes rounded up to a size class)
 qt_status dev_alloc(qt_ctx *ctx, size_t bytes, void **out);
 void dev_free(qt_ctx *ctx, void *p);
+// The stream-ordered memory pool of a device, created on first use and kept
+// for the life of the process (see core.cpp).
+qt_status device_pool(int device, cudaMemPool_t *out);
 qt_status ensure_pinned(qt_ctx *ctx, size_t bytes);
 // pinned host memory from the context cache (bytes rounded up to a size class)
 qt_status host_alloc(qt_ctx *ctx, size_t bytes, void **out);

@@ -297,6 +297,12 @@ qt_status qt_server_create(qt_ctx *ctx, int max_inflight, qt_precision prec, qt_
             delete s;
             return st;
         }
+        // the heavy lanes share the device's stream-ordered pool: their blocks
+        // change size from request to request, and a pool neither keeps them
+        // apart per lane nor frees them with a device-wide cudaFree (without a
+        // pool they keep the caching allocator)
+        cudaMemPool_t pool = nullptr;
+        if (i > 0 && device_pool(ctx->device, &pool) == QT_OK) s->lanes[i].ctx->pool = pool;
     }
     // the light lane's batches: 1 MB size classes, a few blocks of each kind
     // cached from the start (its waves then never call cudaMalloc or
