@@ -102,8 +102,8 @@ constexpr int kServerMaxCuts = 16;
 // a mid-size request (a 12-14 qubit circuit, 1e6-1.6e7 MACs) takes one CTA
 // for a millisecond or more and would hold up the small ones behind it.
 constexpr int64_t kLaneZeroMaxMacs = 1ll << 20;
-constexpr size_t kLightLaneMinBlock = 1u << 20;
-constexpr int kLightLaneWarmBlocks = 8;
+constexpr size_t kLaneMinBlock = 1u << 20;
+constexpr int kLaneWarmBlocks = 8;
 
 static uint64_t footprint(const qt_plan *p, qt_precision prec) {
     return p->ws_bytes[prec] + p->leaf_bytes[prec] + 4096;
@@ -304,22 +304,24 @@ qt_status qt_server_create(qt_ctx *ctx, int max_inflight, qt_precision prec, qt_
         cudaMemPool_t pool = nullptr;
         if (i > 0 && device_pool(ctx->device, &pool) == QT_OK) s->lanes[i].ctx->pool = pool;
     }
-    // the light lane's batches: 1 MB size classes, a few blocks of each kind
-    // cached from the start (its waves then never call cudaMalloc or
-    // cudaMallocHost while heavy lanes allocate)
-    {
-        qt_ctx *l0 = s->lanes[0].ctx;
-        l0->min_class = kLightLaneMinBlock;
-        void *d[kLightLaneWarmBlocks] = {}, *h[kLightLaneWarmBlocks] = {};
-        for (int k = 0; k < kLightLaneWarmBlocks; k++) {
-            dev_alloc(l0, kLightLaneMinBlock, &d[k]);
-            host_alloc(l0, kLightLaneMinBlock, &h[k]);
+    // Every lane's batches: 1 MB size classes, a few blocks of each kind cached
+    // from the start, so that waves never call cudaMallocHost (nor, on the
+    // light lane, cudaMalloc) while other lanes run: a serving run measured
+    // single cudaMallocHost calls of up to 0.37 s on the heavy lanes.  The
+    // heavy lanes' device blocks come from the pool.
+    for (int i = 0; i < n_lanes; i++) {
+        qt_ctx *lc = s->lanes[i].ctx;
+        lc->min_class = kLaneMinBlock;
+        void *d[kLaneWarmBlocks] = {}, *h[kLaneWarmBlocks] = {};
+        for (int k = 0; k < kLaneWarmBlocks; k++) {
+            if (!lc->pool) dev_alloc(lc, kLaneMinBlock, &d[k]);
+            host_alloc(lc, kLaneMinBlock, &h[k]);
         }
-        for (int k = 0; k < kLightLaneWarmBlocks; k++) {
-            dev_free(l0, d[k]);
-            host_free(l0, h[k]);
+        for (int k = 0; k < kLaneWarmBlocks; k++) {
+            dev_free(lc, d[k]);
+            host_free(lc, h[k]);
         }
-        ensure_pinned(l0, kLightLaneMinBlock);
+        ensure_pinned(lc, kLaneMinBlock);
     }
     for (int i = 0; i < n_lanes; i++) s->lanes[i].th = std::thread(lane_main, s, i);
     s->dispatcher = std::thread(dispatcher_main, s);
