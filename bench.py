@@ -446,7 +446,7 @@ def run_serving(args):
             try:
                 v, l, qd, _ = srv.poll_detail(t)
             except qg.QtError as e:
-                raise RuntimeError(f"request {name} failed: {e}; {ctx.last_error()}") from e
+                raise RuntimeError(f"request {name} failed: {e}; {ctx.last_error}") from e
             lat[cls].append(l)
             queued[cls].append(qd)
             served_names[cls].add(name)

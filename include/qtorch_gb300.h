@@ -158,7 +158,7 @@ typedef enum qt_ordering {
     QT_ORDER_STOCHASTIC = 0,   /* ContractionTools::ParallelContract (ContractionTools.h:219-388), seeded */
     QT_ORDER_LINEGRAPH = 1,    /* LineGraph + min-fill elimination order (LineGraph.h:92-171, 357-376) */
     QT_ORDER_SEQUENCE = 2,     /* ContractGivenSequence (ContractionTools.h:392-411) */
-    QT_ORDER_GREEDY = 3,       /* size-greedy pairwise merges, best of 32 seeded tries (no reference
+    QT_ORDER_GREEDY = 3,       /* size-greedy pairwise merges, best of 4096 seeded tries (no reference
                                   counterpart: networks too large for min-fill) */
     QT_ORDER_AUTO = 4          /* QT_ORDER_GREEDY, or the line graph's min-fill walk where the line
                                   graph has <= 1500 wires and that walk is better */
@@ -487,12 +487,15 @@ int64_t qt_random_regular_graph(int num_nodes, int degree, uint64_t seed, char *
  * fits, and runs alone, slice by slice (in chunks of 4096 slices);
  * QT_ERR_OUT_OF_MEMORY when no such slicing exists.  With a work cap
  * (qt_server_set_max_macs) a request whose complex MACs -- over all its slices
- * -- exceed the cap is refused at submission with QT_ERR_REFUSED. */
+ * -- exceed the cap is refused at submission with QT_ERR_REFUSED, and so is one
+ * whose plan (or slice) has an intermediate above rank 15 (4^15 elements, the
+ * largest the step-by-step kernels take; qt_plan_execute reports such a plan as
+ * QT_ERR_INVALID_ARGUMENT). */
 qt_status qt_server_create(qt_ctx *ctx, int max_inflight, qt_precision prec, qt_server **out);
 qt_status qt_server_free(qt_server *s);
 /* The work cap of one request in complex MACs (0: none, the default). */
 qt_status qt_server_set_max_macs(qt_server *s, int64_t max_macs);
-/* Submissions refused so far (work cap, budget without a fitting slicing). */
+/* Submissions refused so far (work cap, rank limit, budget without a fitting slicing). */
 int64_t qt_server_refused(qt_server *s);
 /* Heavy requests that ran out of device memory beside others and were run
  * again alone (each at most twice; the admission budget counts plans'

@@ -467,7 +467,7 @@ class Plan(_Owned):
     def __init__(self, qasm_text, measure_text="", ordering="linegraph", seed=0, sequence=None, gate_dir=None,
                  ctx=None, symbolic=False, tries=100, max_macs=0):
         """ordering: "linegraph", "stochastic" (seeded), "sequence" (recorded
-        node-id pairs), "greedy" (size-greedy merges, best of 32 seeded tries:
+        node-id pairs), "greedy" (size-greedy merges, best of 4096 seeded tries:
         for networks too large for min-fill), "auto" (greedy, or min-fill where
         the line graph is small and its walk is better) or "search" -- the preProcess-style search
         (qt_plan_build_search): `tries` seeded stochastic orderings from `seed`,

@@ -79,11 +79,14 @@ __global__ void __launch_bounds__(256) pack_tiles(const float2 *__restrict__ src
                                                   float *__restrict__ hi, float *__restrict__ lo) {
     __shared__ uint64_t row_off[kTileM];
     __shared__ uint64_t col_off[kTileK];
-    const uint64_t tk = blockIdx.x, tr = blockIdx.y;   // k tile of the first half, row tile
     const uint32_t tid = threadIdx.x;
     const uint64_t M = 1ull << (2 * d.fA);
     const bool one_tile = K < (uint64_t) kTileK;           // both halves in tile 0
     const uint64_t half_tiles = one_tile ? 0 : K / kTileK;  // tile of column K + k: tk + half_tiles
+    // one-dimensional grid (a row-tile count can pass 65,535): k tile of the
+    // first half fastest, then the row tile
+    const uint64_t kt_half = one_tile ? 1 : half_tiles;
+    const uint64_t tk = blockIdx.x % kt_half, tr = blockIdx.x / kt_half;
     const uint32_t kcols = one_tile ? (uint32_t) K : (uint32_t) kTileK;
     if (tid < (uint32_t) kTileM) {
         const uint64_t r = tr * kTileM + tid;
@@ -379,12 +382,12 @@ cudaError_t launch_gemm_step(const StepDesc &d, const float2 *A, const float2 *B
                              int *error_flag, cudaStream_t stream, const StepScaleRef &sc) {
     const GemmSizes s = gemm_sizes(d);
     float *xh = scratch, *xl = xh + s.x_floats, *yh = xl + s.x_floats, *yl = yh + s.y_floats;
-    if (s.m_tiles > 65535 || s.n_tiles > 65535 || s.k_tiles > 0x7fffffffull) return cudaErrorInvalidValue;
-    // one CTA per k tile of the first half of the columns (the second half's
-    // tiles are written by the same CTAs)
+    // one CTA per k tile of the first half of the columns and row tile (the
+    // second half's tiles are written by the same CTAs)
     const uint64_t kt_half = s.K < (uint64_t) kTileK ? 1 : s.K / kTileK;
-    pack_tiles<<<dim3((unsigned) kt_half, (unsigned) s.m_tiles), 256, 0, stream>>>(A, d, 0, s.M, s.K, s.k_tiles, xh, xl);
-    pack_tiles<<<dim3((unsigned) kt_half, (unsigned) s.n_tiles), 256, 0, stream>>>(B, d, 1, s.N2, s.K, s.k_tiles, yh, yl);
+    if (kt_half * s.m_tiles > 0x7fffffffull || kt_half * s.n_tiles > 0x7fffffffull) return cudaErrorInvalidValue;
+    pack_tiles<<<(unsigned) (kt_half * s.m_tiles), 256, 0, stream>>>(A, d, 0, s.M, s.K, s.k_tiles, xh, xl);
+    pack_tiles<<<(unsigned) (kt_half * s.n_tiles), 256, 0, stream>>>(B, d, 1, s.N2, s.K, s.k_tiles, yh, yl);
     const size_t smem = gemm_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     if (e != cudaSuccess) return e;

@@ -24,6 +24,7 @@
 #include <random>
 #include <set>
 #include <sstream>
+#include <thread>
 
 #include "../../include/qtorch/qtorch.hpp"
 
@@ -786,22 +787,45 @@ void abstract_network(const Network &net, std::vector<std::vector<int>> &nw, std
     }
 }
 
+// The walks of `tries` seeded tries, spread over up to 16 host threads: the
+// kept one is the best by (largest intermediate, MACs, try number), so the
+// result does not depend on how many threads ran them.  A walk of a 400-500
+// node network takes about half a millisecond.
 GreedyWalk best_greedy_walk(const std::vector<std::vector<int>> &nw, const std::vector<std::array<int, 2>> &we,
                             uint64_t seed, int tries) {
-    GreedyWalk best;
-    bool have = false;
-    for (int t = 0; t < tries; t++) {
+    auto better = [](const GreedyWalk &a, int ta, const GreedyWalk &b, int tb) {
+        if (a.peak != b.peak) return a.peak < b.peak;
+        if (a.macs != b.macs) return a.macs < b.macs;
+        return ta < tb;
+    };
+    auto run = [&](int t) {
         // temperatures cycle over a few scales so that both small and large
         // perturbations of the plain order are tried
         static const double kTemps[4] = {0.02, 0.1, 0.3, 1.0};
         const double temp = t == 0 ? 0.0 : kTemps[(t - 1) % 4];
-        GreedyWalk g = greedy_walk(nw, we, temp, seed * 0x9e3779b97f4a7c15ull + (uint64_t) t);
-        if (!have || g.peak < best.peak || (g.peak == best.peak && g.macs < best.macs)) {
-            best = std::move(g);
-            have = true;
+        return greedy_walk(nw, we, temp, seed * 0x9e3779b97f4a7c15ull + (uint64_t) t);
+    };
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int n_threads = std::max(1, std::min({tries / 64, 16, (int) (hw ? hw : 1)}));
+    std::vector<GreedyWalk> best(n_threads);
+    std::vector<int> best_t(n_threads, -1);
+    auto worker = [&](int w) {
+        for (int t = w; t < tries; t += n_threads) {
+            GreedyWalk g = run(t);
+            if (best_t[w] < 0 || better(g, t, best[w], best_t[w])) {
+                best[w] = std::move(g);
+                best_t[w] = t;
+            }
         }
-    }
-    return best;
+    };
+    std::vector<std::thread> pool;
+    for (int w = 1; w < n_threads; w++) pool.emplace_back(worker, w);
+    worker(0);
+    for (auto &th : pool) th.join();
+    int k = 0;
+    for (int w = 1; w < n_threads; w++)
+        if (best_t[w] >= 0 && (best_t[k] < 0 || better(best[w], best_t[w], best[k], best_t[k]))) k = w;
+    return std::move(best[k]);
 }
 
 // Replays merges (indices as in GreedyWalk) on the network, then multiplies

@@ -531,6 +531,10 @@ void pack_leaves(const qt_plan *p, int prec, const std::complex<double> *src, ch
 // in complex64 with per-tensor power-of-two scaling (a scale word per step,
 // scale.cuh) and reads the final value back as FP64, times 2^E of its step.
 qt_status execute_stepwise(qt_plan *p, qt_ctx *ctx, int prec, const std::complex<double> *leaves, double *value) {
+    if (p->peak_rank > kMaxStepwiseRank)
+        return set_error(ctx, QT_ERR_INVALID_ARGUMENT,
+                         "plan has a rank-" + std::to_string(p->peak_rank) +
+                             " intermediate: above 4^15 elements, beyond the step kernels (slice it)");
     const bool mixed = prec == QT_PREC_MIXED;
     const size_t es = mixed ? 8 : 16;
     std::lock_guard<std::recursive_mutex> g(ctx->lock);

@@ -163,5 +163,11 @@ qt_status upload_plan(qt_plan *p, int prec);
 void pack_leaves(const qt_plan *p, int prec, const std::complex<double> *src, char *dst);
 // runs on `ctx` (its stream, allocator and lock), which may differ from the
 // plan's own context: a server lane executes shared plans on its own stream
+// Largest intermediate a plan run step by step may have: rank 15, 4^15 =
+// 2^30 elements (8.6 GB in complex64).  The step kernels count tiles, runs
+// and outputs in 32 bits and pack_tiles' grid caps a GEMM operand at 65,535
+// row tiles, so a rank-16 tensor (2^32 elements) is beyond them; such a plan
+// is rejected before any launch (the server refuses it at submission).
+constexpr int kMaxStepwiseRank = 15;
 qt_status execute_stepwise(qt_plan *p, qt_ctx *ctx, int prec, const std::complex<double> *leaves, double *value);
 }  // namespace qtg

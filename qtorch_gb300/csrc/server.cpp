@@ -391,6 +391,10 @@ qt_status qt_server_submit(qt_server *s, qt_plan *plan, const double *leaves, in
         r.heavy = true;
         r.small = false;
     }
+    // the plan that will run (a slice of it, when sliced) must stay within the
+    // step kernels' largest intermediate
+    if ((r.sliced ? qt_sliced_plan(r.sliced)->peak_rank : plan->peak_rank) > kMaxStepwiseRank)
+        return refuse(QT_ERR_REFUSED, "request with an intermediate above 4^15 elements");
     {
         std::lock_guard<std::mutex> g(s->m);
         r.ticket = s->next_ticket++;
