@@ -621,6 +621,8 @@ class Batch(_Owned):
         _check(_lib().qt_batch_create(self.ctx.handle, ctypes.byref(h)), self.ctx)
         self.handle = h.value
         self._plans = []
+        self._eval = None   # evaluate(): angle and value buffers with their addresses
+        self._eval_lock = threading.Lock()
         self._register(self.ctx)
 
     def add(self, plan, leaves=None):
@@ -664,17 +666,28 @@ class Batch(_Owned):
         """Values of every instance at new rotation angles in one call (gate
         tensors built on the device; the batch must be prepared for MIXED when
         angles are given)."""
-        out = np.empty(len(self._plans), dtype=np.complex128)
         if angles is None:
+            out = np.empty(len(self._plans), dtype=np.complex128)
             st = _lib().qt_batch_evaluate(self.handle, None, 0, out.ctypes.data)
-        else:
-            a = angles
-            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
-                a = np.ascontiguousarray(a, dtype=np.float64)
-            st = _lib().qt_batch_evaluate(self.handle, a.ctypes.data, a.size, out.ctypes.data)
-        if st:
-            _check(st, self.ctx)
-        return out
+            if st:
+                _check(st, self.ctx)
+            return out
+        # The call is short (~10 us through the resident engine), so the
+        # wrapper keeps one angle and one value buffer per batch and their
+        # addresses (reading an array's .ctypes address costs about a
+        # microsecond); the lock keeps concurrent callers off each other's buffers.
+        with self._eval_lock:
+            e = self._eval
+            n = np.size(angles)
+            if e is None or e[0].size != n or e[2].size != len(self._plans):
+                ang = np.empty(n, dtype=np.float64)
+                out = np.empty(len(self._plans), dtype=np.complex128)
+                e = self._eval = (ang, ang.ctypes.data, out, out.ctypes.data, _lib().qt_batch_evaluate)
+            e[0][:] = np.ravel(angles)
+            st = e[4](self.handle, e[1], n, e[3])
+            if st:
+                _check(st, self.ctx)
+            return e[2].copy()
 
     def set_rotations_device(self, angles):
         """New rotation angles whose gate tensors are built on the device at the
