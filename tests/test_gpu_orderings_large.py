@@ -64,3 +64,23 @@ def test_work_cap_refuses_and_serves_the_rest(ctx):
         assert abs(srv.poll(t)[0] - big.execute(qg.FP64)) <= 1e-6
     finally:
         srv.close()
+
+
+def test_rank_16_plans_are_rejected_before_any_launch(ctx):
+    """A plan whose largest intermediate is rank 16 (2^32 elements) is beyond
+    the step kernels' 32-bit tile, run and output counters: executing it fails
+    with InvalidFunctionInput before any launch, and the server refuses it at
+    submission; the context stays usable."""
+    big = qg.Plan(random_circuit_text(22, 16, 21), "Z", ordering="auto", ctx=ctx)
+    assert big.peak_rank == 16
+    with pytest.raises(qg.InvalidFunctionInput):
+        big.execute(qg.MIXED)
+    assert "rank-16" in ctx.last_error
+    srv = qg.Server(max_inflight=4, precision=qg.MIXED, ctx=ctx, max_macs=int(3e13))
+    try:
+        with pytest.raises(qg.Refused):
+            srv.submit(big)
+    finally:
+        srv.close()
+    small = qg.Plan(random_circuit_text(10, 8, 3), "Z", ordering="auto", ctx=ctx)
+    assert abs(small.execute(qg.MIXED) - small.execute(qg.FP64)) <= 1e-6
