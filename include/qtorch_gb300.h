@@ -490,7 +490,7 @@ int64_t qt_random_regular_graph(int num_nodes, int degree, uint64_t seed, char *
  * -- exceed the cap is refused at submission with QT_ERR_REFUSED, and so is one
  * whose plan (or slice) has an intermediate above rank 15 (4^15 elements, the
  * largest the step-by-step kernels take; qt_plan_execute reports such a plan as
- * QT_ERR_INVALID_ARGUMENT). */
+ * QT_ERR_INVALID_FUNCTION_INPUT). */
 qt_status qt_server_create(qt_ctx *ctx, int max_inflight, qt_precision prec, qt_server **out);
 qt_status qt_server_free(qt_server *s);
 /* The work cap of one request in complex MACs (0: none, the default). */

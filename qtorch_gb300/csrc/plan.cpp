@@ -532,7 +532,7 @@ void pack_leaves(const qt_plan *p, int prec, const std::complex<double> *src, ch
 // scale.cuh) and reads the final value back as FP64, times 2^E of its step.
 qt_status execute_stepwise(qt_plan *p, qt_ctx *ctx, int prec, const std::complex<double> *leaves, double *value) {
     if (p->peak_rank > kMaxStepwiseRank)
-        return set_error(ctx, QT_ERR_INVALID_ARGUMENT,
+        return set_error(ctx, QT_ERR_INVALID_FUNCTION_INPUT,
                          "plan has a rank-" + std::to_string(p->peak_rank) +
                              " intermediate: above 4^15 elements, beyond the step kernels (slice it)");
     const bool mixed = prec == QT_PREC_MIXED;
