@@ -128,7 +128,7 @@ def test_small_requests_pass_a_heavy_one():
         heavy_alone = heavy.execute(qg.MIXED)
         srv = qg.Server(max_inflight=16, precision=qg.MIXED, ctx=ctx)
         try:
-            for _ in range(2):   # the first round warms the lanes' caches
+            for _ in range(2):   # the first pass warms the lanes' caches
                 t_heavy = srv.submit(heavy)
                 tickets = [srv.submit(p) for p in small]
                 srv.drain()
@@ -165,7 +165,7 @@ def test_light_requests_run_while_a_heavy_one_waits_for_memory():
         ctx.set_memory_budget(int(fp * 1.5))
         srv = qg.Server(max_inflight=64, precision=qg.FP64, ctx=ctx)
         try:
-            for _ in range(2):   # the first round warms the lanes' caches
+            for _ in range(2):   # the first pass warms the lanes' caches
                 t1, t2 = srv.submit(heavy), srv.submit(heavy)
                 time.sleep(0.001)   # the second heavy request is waiting for memory by now
                 tickets = [srv.submit(p) for p in small]
