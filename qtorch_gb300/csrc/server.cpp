@@ -12,7 +12,8 @@
 // is on the GPU runs concurrently with it.  Lane 0 (highest stream priority)
 // takes the small requests (grouped, at most 2^20 complex MACs) and nothing
 // else, so they never queue behind a heavy one nor run on a low-priority
-// stream beside one; the other lanes take the rest.  Each
+// stream beside one; the other lanes take the rest, lane 1 the pending medium
+// requests (grouped, above the small bound) before any heavy one.  Each
 // request's result is independent of what it was batched with: an instance
 // only ever touches its
 // own leaves and its CTA's workspace.
@@ -249,7 +250,12 @@ static void dispatcher_main(qt_server *s) {
         // lane 0 serves the small requests, at the highest stream priority; the
         // other lanes the rest (a heavy request alone), so that a small request
         // never runs on a low-priority stream beside a heavy one
-        const bool take_heavy = li > 0 && first_big->heavy;
+        // lane 1 serves the pending medium requests (grouped, above the small
+        // bound) before any heavy one, the other lanes take them in arrival
+        // order: a medium request then rarely waits for a heavy one to finish
+        bool any_medium = false;
+        for (auto &r : s->pending) any_medium = any_medium || (!r.small && !r.heavy);
+        const bool take_heavy = li > 0 && (li == 1 ? !any_medium : first_big->heavy);
         for (auto it = s->pending.begin(); it != s->pending.end() && s->inflight < s->max_inflight;) {
             if (it->heavy != take_heavy || (li == 0) != it->small) {
                 ++it;
