@@ -5,6 +5,11 @@
 //   X (M x 2K)  = [Ar | Ai]                       row m, K contiguous
 //   Y (2N x 2K) row 2n   = [Br_n | -Bi_n]          -> D[m][2n]   = Re C
 //               row 2n+1 = [Bi_n |  Br_n]          -> D[m][2n+1] = Im C
+// or, when B has more free indices than A (N > M), the other way round, so
+// that the larger operand is packed twice instead of four times:
+//   X (2M x 2K) row 2m   = [Ar_m | -Ai_m]          -> D[2m][n]   = Re C
+//               row 2m+1 = [Ai_m |  Ar_m]          -> D[2m+1][n] = Im C
+//   Y (N x 2K)  = [Br | Bi]
 // computed with three TF32 products per term (x_hi y_hi + x_hi y_lo + x_lo y_hi,
 // FP32 accumulation in tensor memory); with both parts rounded to nearest the
 // dropped x_lo y_lo and the rounding of the lo parts leave ~2^-21 per product,
@@ -65,17 +70,18 @@ __device__ __forceinline__ void split_tf32(float x, float &hi, float &lo) {
     lo = round_tf32(x - hi);   // x - hi is exact in FP32
 }
 
-// X: rows m < M, columns j < 2K; Y: rows i < 2N, columns j < 2K (see the file
-// comment).  One CTA per (row tile, k tile of the first half of the columns):
+// One operand (which: 0 = A into X, 1 = B into Y), `rows` rows, columns
+// j < 2K (see the file comment); pairs: its rows come in (2e, 2e + 1) pairs.
+// One CTA per (row tile, k tile of the first half of the columns):
 // the tile's 128 row offsets and its column offsets into the gathered operand
 // are computed once into shared memory, then every complex element the CTA
-// covers is read once and written to all the places it goes -- X: (m, k) and
-// (m, K + k); Y: rows 2n and 2n + 1 at columns k and K + k -- split hi/lo, in
+// covers is read once and written to all the places it goes -- single rows:
+// (e, k) and (e, K + k); pairs: rows 2e and 2e + 1 at columns k and K + k -- split hi/lo, in
 // the tiles' canonical core-matrix order (contiguous stores per warp).  The
 // element-per-place version read X's elements twice and Y's four times.  With
 // K = 16 a single k tile holds both halves (columns 0-15 and 16-31).
 __global__ void __launch_bounds__(256) pack_tiles(const float2 *__restrict__ src, const StepDesc d, int which,
-                                                  uint64_t rows, uint64_t K, uint64_t k_tiles,
+                                                  int pairs, uint64_t rows, uint64_t K, uint64_t k_tiles,
                                                   float *__restrict__ hi, float *__restrict__ lo) {
     __shared__ uint64_t row_off[kTileM];
     __shared__ uint64_t col_off[kTileK];
@@ -92,7 +98,8 @@ __global__ void __launch_bounds__(256) pack_tiles(const float2 *__restrict__ src
         const uint64_t r = tr * kTileM + tid;
         uint64_t oa = 0, ob = 0;
         // X row m: A's free digits; Y rows 2n, 2n+1: the B digits of output column n
-        if (r < rows) scatter_c(which == 0 ? r : (r >> 1) * M, d, oa, ob);
+        const uint64_t e = pairs ? r >> 1 : r;   // the element's index along this operand's free digits
+        if (r < rows) scatter_c(which == 0 ? e : e * M, d, oa, ob);
         row_off[tid] = which == 0 ? oa : ob;
     } else if (tid < (uint32_t) (kTileM + kTileK)) {
         const uint32_t kk = tid - kTileM;
@@ -115,18 +122,18 @@ __global__ void __launch_bounds__(256) pack_tiles(const float2 *__restrict__ src
         const uint32_t kk = (p & 3u) | (((p >> 5) & 7u) << 2);
         const uint32_t rr = ((p >> 2) & 7u) | ((p >> 8) << 3);
         if (kk >= kcols) continue;             // the Im half of a one-tile operand: written below
-        if (which == 1 && (rr & 1u)) continue;   // Y's odd rows: written with the even one
+        if (pairs && (rr & 1u)) continue;   // odd rows of a pair: written with the even one
         const uint64_t r = tr * kTileM + rr;
         float2 x = make_float2(0.f, 0.f);
         if (r < rows && tk * kTileK + kk < K) x = src[row_off[rr] + col_off[kk]];
         // the Im half's position: the same (rr, kk) in the second tile, or 16 columns on
         const uint32_t q = one_tile ? p + 128u : p;
         float *const hq = one_tile ? h0 : h1, *const lq = one_tile ? l0 : l1;
-        if (which == 0) {
+        if (!pairs) {
             put(h0, l0, p, x.x);
             put(hq, lq, q, x.y);
         } else {
-            // row 2n = [Br | -Bi], row 2n + 1 = [Bi | Br]; row rr + 1 sits 4 floats on
+            // row 2e = [re | -im], row 2e + 1 = [im | re]; row rr + 1 sits 4 floats on
             put(h0, l0, p, x.x);
             put(hq, lq, q, -x.y);
             put(h0, l0, p + 4u, x.y);
@@ -197,8 +204,8 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
 
 __global__ void __launch_bounds__(kGemmThreads, 1)
 gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, const float *__restrict__ y_hi,
-            const float *__restrict__ y_lo, uint64_t k_tiles, uint64_t M, uint64_t N2, float2 *__restrict__ C,
-            int *__restrict__ error_flag, const StepScaleRef sc) {
+            const float *__restrict__ y_lo, uint64_t k_tiles, uint64_t M, uint64_t N2, int x_pairs,
+            float2 *__restrict__ C, int *__restrict__ error_flag, const StepScaleRef sc) {
     extern __shared__ __align__(1024) unsigned char smem[];
     // [stages x (x_hi, x_lo, y_hi, y_lo) tiles][full[stages], empty[stages], done][tmem address]
     unsigned char *tiles = smem;
@@ -304,7 +311,10 @@ gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, cons
     done = __syncthreads_and(ok && done) != 0;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (done) {
+        // row of D this thread holds (its TMEM lane); X's rows: M (single) or
+        // 2 x the complex rows (pairs: the even row Re, the odd row Im)
         const uint64_t m = tm * kTileM + (uint64_t) warp * 32 + lane;
+        const uint64_t Mc = x_pairs ? M >> 1 : M;   // complex rows of C
         const uint32_t n_big = k_tiles < kAccBig ? (uint32_t) k_tiles : kAccBig;
         for (int c0 = 0; c0 < kTileN; c0 += 16) {
             float v[16];
@@ -322,14 +332,35 @@ gemm_tf32x3(const float *__restrict__ x_hi, const float *__restrict__ x_lo, cons
 #pragma unroll
                 for (int j = 0; j < 16; j++) v[j] = reg == 0 ? __uint_as_float(r[j]) : v[j] + __uint_as_float(r[j]);
             }
-            if (m < M) {
+            if (x_pairs) {
+                // lanes 2i and 2i + 1 hold Re and Im of complex row m >> 1 for
+                // the same 16 columns: each takes its partner's values and
+                // stores half of the columns (the even lane the even ones)
+                float o[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) o[j] = __shfl_xor_sync(0xffffffffu, v[j], 1);
+                const uint32_t odd = (uint32_t) (m & 1u);
+                if (m < M) {
+#pragma unroll
+                    for (int j = 0; j < 16; j += 2) {
+                        // even lane: column j, (v, o); odd lane: column j + 1, (o, v)
+                        const uint64_t col = tn * kTileN + (uint64_t) (c0 + j) + odd;
+                        if (col < N2) {
+                            const float re = odd ? o[j + 1] : v[j], im = odd ? v[j + 1] : o[j];
+                            const float2 out = make_float2(scale_pow2(re, shift), scale_pow2(im, shift));
+                            lmax = max(lmax, mag_bits(out));
+                            C[(m >> 1) + Mc * col] = out;
+                        }
+                    }
+                }
+            } else if (m < M) {
 #pragma unroll
                 for (int j = 0; j < 16; j += 2) {
                     const uint64_t col = tn * kTileN + (uint64_t) (c0 + j);   // even: Re, odd: Im
                     if (col + 1 < N2 + 1 && col < N2) {
                         const float2 out = make_float2(scale_pow2(v[j], shift), scale_pow2(v[j + 1], shift));
                         lmax = max(lmax, mag_bits(out));
-                        C[m + M * (col >> 1)] = out;
+                        C[m + Mc * (col >> 1)] = out;
                     }
                 }
             }
@@ -358,8 +389,11 @@ bool gemm_eligible(const StepDesc &d) {
 
 GemmSizes gemm_sizes(const StepDesc &d) {
     GemmSizes s;
-    s.M = 1ull << (2 * d.fA);
-    s.N2 = 2ull << (2 * d.fB);
+    // the operand with more free indices is packed twice, the other four times
+    s.x_pairs = d.fB > d.fA;
+    const uint64_t Mc = 1ull << (2 * d.fA), Nc = 1ull << (2 * d.fB);
+    s.M = s.x_pairs ? 2 * Mc : Mc;
+    s.N2 = s.x_pairs ? Nc : 2 * Nc;
     s.K = 1ull << (2 * d.nSum);
     s.k_tiles = (2 * s.K + kTileK - 1) / kTileK;
     s.m_tiles = (s.M + kTileM - 1) / kTileM;
@@ -386,14 +420,17 @@ cudaError_t launch_gemm_step(const StepDesc &d, const float2 *A, const float2 *B
     // second half's tiles are written by the same CTAs)
     const uint64_t kt_half = s.K < (uint64_t) kTileK ? 1 : s.K / kTileK;
     if (kt_half * s.m_tiles > 0x7fffffffull || kt_half * s.n_tiles > 0x7fffffffull) return cudaErrorInvalidValue;
-    pack_tiles<<<(unsigned) (kt_half * s.m_tiles), 256, 0, stream>>>(A, d, 0, s.M, s.K, s.k_tiles, xh, xl);
-    pack_tiles<<<(unsigned) (kt_half * s.n_tiles), 256, 0, stream>>>(B, d, 1, s.N2, s.K, s.k_tiles, yh, yl);
+    pack_tiles<<<(unsigned) (kt_half * s.m_tiles), 256, 0, stream>>>(A, d, 0, s.x_pairs ? 1 : 0, s.M, s.K, s.k_tiles,
+                                                                      xh, xl);
+    pack_tiles<<<(unsigned) (kt_half * s.n_tiles), 256, 0, stream>>>(B, d, 1, s.x_pairs ? 0 : 1, s.N2, s.K, s.k_tiles,
+                                                                      yh, yl);
     const size_t smem = gemm_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     if (e != cudaSuccess) return e;
     const uint64_t ctas = s.m_tiles * s.n_tiles;
     if (ctas > 0x7fffffffull) return cudaErrorInvalidValue;
-    gemm_tf32x3<<<(unsigned) ctas, kGemmThreads, smem, stream>>>(xh, xl, yh, yl, s.k_tiles, s.M, s.N2, C, error_flag, sc);
+    gemm_tf32x3<<<(unsigned) ctas, kGemmThreads, smem, stream>>>(xh, xl, yh, yl, s.k_tiles, s.M, s.N2,
+                                                                 s.x_pairs ? 1 : 0, C, error_flag, sc);
     return cudaGetLastError();
 }
 

@@ -7,7 +7,8 @@
 namespace qtg {
 
 struct GemmSizes {
-    uint64_t M, N2, K;              // rows of X, rows of Y (2 x complex columns), summed range
+    bool x_pairs;                   // X's rows come in (Re, Im) pairs: B has more free indices than A
+    uint64_t M, N2, K;              // rows of X, rows of Y (the paired one: 2 x complex rows), summed range
     uint64_t k_tiles, m_tiles, n_tiles;
     uint64_t x_floats, y_floats;    // one plane of packed X / Y
 };
