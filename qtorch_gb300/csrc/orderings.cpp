@@ -17,6 +17,7 @@
 //    with --min-fill-ordering).
 #include <algorithm>
 #include <cmath>
+#include <exception>
 #include <fstream>
 #include <functional>
 #include <map>
@@ -814,17 +815,26 @@ GreedyWalk best_greedy_walk(const std::vector<std::vector<int>> &nw, const std::
     std::vector<double> macs(tries);
     const unsigned hw = std::thread::hardware_concurrency();
     const int n_threads = std::max(1, std::min({tries / 64, 16, (int) (hw ? hw : 1)}));
+    // an exception of a worker thread (a failed allocation) reaches the caller
+    // after every thread has joined, as it would from a single thread
+    std::vector<std::exception_ptr> failed(n_threads);
     auto worker = [&](int w) {
-        for (int t = w; t < tries; t += n_threads) {
-            const GreedyWalk g = run(t);
-            peak[t] = g.peak;
-            macs[t] = g.macs;
+        try {
+            for (int t = w; t < tries; t += n_threads) {
+                const GreedyWalk g = run(t);
+                peak[t] = g.peak;
+                macs[t] = g.macs;
+            }
+        } catch (...) {
+            failed[w] = std::current_exception();
         }
     };
     std::vector<std::thread> pool;
     for (int w = 1; w < n_threads; w++) pool.emplace_back(worker, w);
     worker(0);
     for (auto &th : pool) th.join();
+    for (auto &f : failed)
+        if (f) std::rethrow_exception(f);
     const int p_min = *std::min_element(peak.begin(), peak.end());
     auto fewest = [&](int max_peak, int exact) {
         int k = -1;
