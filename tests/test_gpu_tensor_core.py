@@ -13,7 +13,9 @@ def reference_step(a, b, ffa, fi, sa, sb):
     return port.contract_indices(a.astype(np.complex128), b.astype(np.complex128), ffa, fi, sa, sb)
 
 
-@pytest.mark.parametrize("ra,rb,ns", [(9, 7, 3), (8, 8, 4), (10, 6, 2), (7, 9, 3)])
+# (7, 9, 3), (6, 10, 2) and (7, 10, 3) have more free indices on B: X holds A as
+# (Re, Im) row pairs; (6, 10, 2) sums 16 terms, both halves in one k tile
+@pytest.mark.parametrize("ra,rb,ns", [(9, 7, 3), (8, 8, 4), (10, 6, 2), (7, 9, 3), (6, 10, 2), (7, 10, 3)])
 def test_gemm_step_matches_complex128(ctx, ra, rb, ns):
     rng = np.random.default_rng(ra * 100 + rb * 10 + ns)
     sa = list(rng.permutation(ra)[:ns])
