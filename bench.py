@@ -1098,6 +1098,8 @@ def bench_summary(line):
         s["config5_serving"] = {"p50_ms": r(v["p50_ms"], 3), "p99_ms": r(v["p99_ms"], 3),
                                 "offered_per_s": r(v["arrival_rate_per_s"]),
                                 "saturation_per_s": r(v["saturation_requests_per_s"]),
+                                "p99_ms_by_class": {k: r(x, 3) for k, x in v["p99_ms_by_class"].items()
+                                                    if x is not None},
                                 "max_err": r(v["error_vs_fp64_max_abs"], 2), "refused": v["refused"],
                                 "completed": v["completed"]}
     if "config1" in line:
